@@ -1,0 +1,164 @@
+/*
+ * realcaustics.h - C ABI of librealcaustics.so, the GB300 (sm_103a) vertex-merging
+ * caustics renderer.
+ *
+ * Two groups of entry points:
+ *
+ *  1. The two exports of the reference "Real Caustics.dll" that the Blender add-on
+ *     binds, with unchanged names, argument lists and struct layouts:
+ *        init()   replaces Real Caustics/src/DLL.h:15-34 (defined at src/main.cpp:89-143)
+ *        main()   replaces Real Caustics/src/DLL.h:14    (defined at src/main.cpp:148-223)
+ *     Semantics follow the reference: init() copies scalars, triangles, camera and
+ *     materials and BORROWS the light array and the Blender vertex arrays until main()
+ *     returns; main() builds the BVH, renders `samples` progressive iterations, writes
+ *     the FP32 RGB EXR (default file name "D:\caustics.exr" in the working directory,
+ *     as src/main.cpp:206) and releases the scene.  Unlike the reference, main()
+ *     returns a non-zero status instead of crashing on bad input (no scene, zero
+ *     photons, unsupported light), and rc_last_error() describes it.
+ *
+ *  2. Additive rc_* exports: configuration beyond the reference's hard-coded values,
+ *     in-memory image readback, timing, and the parity hooks (closest-hit on given
+ *     rays, KD-tree radius query on given photons) that tests use to compare the
+ *     GPU kernels with the reference algorithms.
+ *
+ * All functions are synchronous, not re-entrant (one global scene, as the reference),
+ * and return 0 on success or a negative RC_E* code.  No torch types cross this ABI.
+ */
+#ifndef REALCAUSTICS_H
+#define REALCAUSTICS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- reference by-value / by-pointer structs (x86-64 and aarch64 LP64 layouts) ---- */
+
+/* vec3: 3 x f32 (Real Caustics/src/vec3.h:13-19), passed by value */
+typedef struct rc_vec3 { float x, y, z; } rc_vec3;
+
+/* Debug_stuff (src/Vertex_Merging.h:13-19), 24 bytes, passed by value */
+typedef struct rc_debug_stuff { int number_of_points; rc_vec3 direction; float roughness; float specular; } rc_debug_stuff;
+
+/* PythonMatrix4x4 (src/matrix.h:151-170): 16 f32, row-major t00..t33 */
+typedef struct rc_matrix4x4 { float t[16]; } rc_matrix4x4;
+
+/* Python_Light (src/Lights.h:15-36), 64 bytes. type: 'S' sun, 'P' point, else area.
+ * rotation is in degrees for area lights, radians for sun lights. */
+typedef struct rc_python_light {
+    char type; float color[3]; rc_vec3 position; float width, height, spread;
+    rc_vec3 rotation; float power, angle, radius;
+} rc_python_light;
+
+/* Python_Material (src/materials.h:21-32), 28 bytes. type: 'P' plastic, 'G' glass,
+ * 'M' metal, anything else a white diffuse plastic.  Additive type 'R' (rough GGX
+ * dielectric: ior, roughness) has no counterpart in the reference. */
+typedef struct rc_python_material { char type; float ior, roughness, specular; float color[3]; } rc_python_material;
+
+/* Reference export `init` (src/DLL.h:15-34).  meshes_pointers[i] is the address of a
+ * Blender Mesh (DNA 2.9x: mpoly at byte 200, mloop at 208, mvert at 256). */
+void init(int samples, float base_radius, float radius_reduction,
+          long long* meshes_pointers, unsigned int number_of_meshes,
+          rc_matrix4x4* mesh_matrices, unsigned int* meshes_number_of_verts,
+          unsigned int* meshes_number_of_tris, unsigned int camera_x, unsigned int camera_y,
+          rc_vec3 camera_position, rc_vec3 camera_corner0, rc_vec3 camera_corner1,
+          rc_vec3 camera_corner2, rc_vec3 camera_corner3,
+          rc_python_light* lights, unsigned int number_of_lights,
+          rc_python_material* materials, unsigned int number_of_materials,
+          int** materials_indices, int debug_test, rc_debug_stuff debug_stuff);
+
+/* Reference export `main` (src/DLL.h:14): build, render, write EXR, release. */
+int main(void);
+
+/* ---- additive exports ---- */
+
+enum {
+    RC_OK = 0,
+    RC_E_NO_SCENE = -1,      /* init() was not called, or main() already released it */
+    RC_E_INVALID = -2,       /* bad argument (null pointer, zero size, bad index)    */
+    RC_E_CUDA = -3,          /* CUDA runtime error (message in rc_last_error)        */
+    RC_E_UNSUPPORTED = -4,   /* feature outside this build                           */
+    RC_E_CAPACITY = -5,      /* a fixed-size buffer or queue would overflow          */
+    RC_E_TIMEOUT = -6,       /* a bounded device-side wait expired                   */
+    RC_E_IO = -7             /* output file could not be written                     */
+};
+
+/* Photon-emission sampler. */
+enum { RC_SAMPLER_UNIFORM = 0,   /* plain vertex merging: independent uniform light paths */
+       RC_SAMPLER_HYBRID = 1,    /* reference scheme (src/Vertex_Merging.cpp:231-276):
+                                    large step, small step on an invisible path, adaptive
+                                    mutation size; run as many independent chains */
+       RC_SAMPLER_PSSMLT = 2 };  /* visibility-target primary-sample MLT, large-step
+                                    probability `large_step_prob`, many chains */
+
+/* Rendering configuration beyond the reference's hard-coded values.  rc_default_config
+ * fills the reference values (max_path_length 6, photons per iteration = pixels,
+ * hybrid sampler, all reference quirks on). */
+typedef struct rc_config {
+    int max_path_length;        /* src/main.cpp:112 hard-codes 6                         */
+    long long photons_per_iter; /* 0 = resX*resY as src/Vertex_Merging.cpp:201           */
+    int sampler;                /* RC_SAMPLER_*                                          */
+    int mlt_chains;             /* chains for HYBRID/PSSMLT (0 = 65536)                  */
+    float large_step_prob;      /* PSSMLT only                                           */
+    unsigned long long seed;    /* counter-based RNG seed                                */
+    int write_exr;              /* main(): 1 = write EXR (reference behaviour)           */
+    char exr_path[256];         /* main(): output file, default "D:\\caustics.exr"       */
+    int verbose;                /* 1 = print per-iteration JSON lines to stdout          */
+} rc_config;
+
+int rc_default_config(rc_config* cfg);
+int rc_set_config(const rc_config* cfg);
+
+/* Stage the scene: BVH build + upload + light conversion (the pre-render half of main,
+ * src/main.cpp:150-168).  Called implicitly by rc_render/main. */
+int rc_prepare(void);
+
+/* Render `iterations` more progressive iterations into the FP64 running mean. */
+int rc_render(int iterations);
+
+/* Copy the current image (mean over rendered iterations) as FP32 RGB, rows in the
+ * reference's buffer order (the order SaveEXR receives, src/main.cpp:192-206). */
+int rc_read_image(float* rgb, int width, int height);
+
+/* Release the scene (what main() does at its end). */
+int rc_release(void);
+
+/* Last error message (static storage, valid until the next call). */
+const char* rc_last_error(void);
+
+/* Per-iteration statistics of the last rc_render call.
+ * out[0] light paths, [1] stored photons, [2] merge queries, [3] photons merged,
+ * [4] light-pass ms, [5] KD-build ms, [6] camera-pass ms, [7] gather ms,
+ * [8] accumulate ms, [9] total device ms, [10] iterations rendered so far,
+ * [11] scene radius, [12] current merge radius, [13] gather kernel launches. */
+int rc_get_stats(double* out, int n);
+
+/* ---- parity hooks (device kernels on caller-chosen inputs) ---- */
+
+/* Closest hit of n rays (origins/directions: 3 floats each, host memory) through the
+ * prepared scene, by the GPU traversal kernel (Scene::hit, src/Scene.cpp:154-189,
+ * including its world-leaf overwrite).  out: 8 words per ray:
+ * [hit(0/1), t, u, v (float bits), triangle id (global, ingest order), material,
+ *  mesh index, reserved]. */
+int rc_trace_rays(int n, const float* origins, const float* directions, float tmin, unsigned* out);
+
+/* Same closest hit, with the full hit record as floats (16 per ray, same layout as the
+ * oracle): [hit, t, u, v, Ng xyz, Ns xyz, position xyz, front_face, material, tri]. */
+int rc_trace_rays_full(int n, const float* origins, const float* directions, float tmin, float* out);
+
+/* Build the photon KD-tree on the GPU over n photon positions (3 floats each) and
+ * answer q radius queries (squared radius r2): counts[j] = number of photons with
+ * ((dx*dx + dy*dy) + dz*dz) < r2 (KD_Tree::find_closest_in_radius, src/KD_Tree.cpp:217-280),
+ * indices (photon ids, unordered within a query) packed in query order into idx
+ * (capacity cap).  *total receives the total count (may exceed cap). */
+int rc_kd_query(int n, const float* positions, int q, const float* queries, float r2,
+                int* counts, int* idx, long long cap, long long* total);
+
+/* The GPU-built tree in the reference's node format (8-byte KDTreeNode, heap order,
+ * root at 1, src/KD_Tree.h:13-32) for n photon positions; returns the node count in
+ * *num_nodes and copies up to cap nodes as (index word, split bits) pairs. */
+int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes, long long cap, long long* num_nodes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* REALCAUSTICS_H */

@@ -1,0 +1,632 @@
+// GPU photon KD-tree build by parallel median splits (see kdtree.cuh for the tree).
+//
+// Levels whose nodes hold more than kSmemSeg photons are split with global passes,
+// one pass per step over all photons (SoA x/y/z/id, double buffered):
+//   bbox      per-node extent -> axis (largest extent)
+//   hist x4   8-bit radix select of the rank-count/2 key along the node's axis
+//   partition photons below / equal / above the median key to their halves
+// A CTA covers kChunk consecutive positions; because nodes on these levels hold more
+// than kChunk photons, a chunk meets at most two nodes (and one ancestor median
+// between them), so histograms and counters stay in shared memory and only their
+// totals go to global memory.
+// From the first level with at most kSmemSeg photons per node, one CTA per node
+// loads its photons into shared memory and finishes the whole subtree there with a
+// bitonic sort per level (key, then local index), writing nodes and final order.
+#include "kdtree.cuh"
+#include <cmath>
+#include <cstdio>
+
+namespace rc {
+
+namespace {
+
+constexpr int kSmemSeg = 2048;      // largest node finished in shared memory
+constexpr int kChunk = 2048;        // positions per CTA in the global passes
+constexpr int kThreads = 256;
+constexpr int kItems = kChunk / kThreads;
+constexpr int kSmemThreads = 512;
+constexpr float kSplitBias = 1.175494e-38f;   // src/KD_Tree.cpp:150
+
+__device__ __forceinline__ uint32_t f2key(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key2f(uint32_t k) {
+    uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+// order-preserving int encoding for atomicMin/Max on floats
+__device__ __forceinline__ int f2ord(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : (i ^ 0x7fffffff);
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : (i ^ 0x7fffffff)); }
+
+__device__ __forceinline__ uint32_t odd_mask(int axis) { return axis == 0 ? 0x90000000u : (axis == 1 ? 0xb0000000u : 0xf0000000u); }
+__device__ __forceinline__ uint32_t even_mask(int axis) { return axis == 0 ? 0x80000000u : (axis == 1 ? 0xa0000000u : 0xe0000000u); }
+
+// aproximate_biggest_axis's final choice (src/KD_Tree.cpp:90-94)
+__device__ __forceinline__ int biggest_axis(float ex, float ey, float ez) {
+    float b = fmaxf(fmaxf(ex, ey), ez);
+    return b == ex ? 0 : (b == ey ? 1 : 2);
+}
+
+// Node on `level` whose range holds position i; returns 0 if i is the median photon
+// of an ancestor.  *start receives the node's first position.
+__device__ __forceinline__ long long locate(long long i, int level, long long n, long long* start) {
+    long long e = 1, s = 0, c = n;
+    for (int j = 0; j < level; ++j) {
+        long long half = c >> 1, odd = c & 1;
+        if (i < s + half) { e = 2 * e; }
+        else if (odd && i == s + half) { *start = 0; return 0; }
+        else { e = 2 * e + 1; s += half + odd; }
+        c = half;
+    }
+    *start = s;
+    return e;
+}
+
+struct NodeSel {
+    uint32_t prefix;   // selected high bits of the median key
+    int krem;          // remaining rank inside the selected bin
+    int eq;            // photons whose key equals the median key
+    int axis;
+    int cnt[3];        // partition cursors (below / equal / above)
+};
+
+struct Buffers {
+    float* x[2]; float* y[2]; float* z[2]; uint32_t* id[2];
+};
+
+// Chunk -> at most two nodes A, B on `level`.
+struct ChunkNodes {
+    long long eA, sA, eB, sB, c;
+};
+
+__device__ __forceinline__ void chunk_nodes(long long a, int level, long long n, ChunkNodes& cn) {
+    long long c = n >> level;
+    long long s;
+    long long e = locate(a, level, n, &s);
+    if (e == 0) e = locate(a + 1, level, n, &s);
+    cn.eA = e; cn.sA = s; cn.c = c;
+    long long endA = s + c;
+    cn.eB = 0; cn.sB = -1;
+    if (endA < a + kChunk && endA < n) {
+        long long s2;
+        long long e2 = locate(endA, level, n, &s2);
+        if (e2 == 0 && endA + 1 < n) e2 = locate(endA + 1, level, n, &s2);
+        if (e2) { cn.eB = e2; cn.sB = s2; }
+    }
+}
+
+// 0 = node A, 1 = node B, -1 = not inside a node on this level
+__device__ __forceinline__ int which(long long i, const ChunkNodes& cn) {
+    if (i >= cn.sA && i < cn.sA + cn.c) return 0;
+    if (cn.eB && i >= cn.sB && i < cn.sB + cn.c) return 1;
+    return -1;
+}
+
+__global__ void k_level_init(int level, long long first, long long count, int* nbox, NodeSel* sel, long long n) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    int* b = nbox + 6 * t;
+    b[0] = b[1] = b[2] = 0x7fffffff;
+    b[3] = b[4] = b[5] = (int)0x80000000;
+    NodeSel& s = sel[t];
+    s.prefix = 0; s.krem = (int)((n >> level) >> 1); s.eq = 0; s.axis = 0;
+    s.cnt[0] = s.cnt[1] = s.cnt[2] = 0;
+}
+
+__global__ void __launch_bounds__(kThreads) k_bbox(Buffers B, int cur, int level, long long n, long long first, int* nbox) {
+    __shared__ ChunkNodes cn;
+    __shared__ int sb[2][6];
+    long long a = blockIdx.x * (long long)kChunk;
+    if (threadIdx.x == 0) chunk_nodes(a, level, n, cn);
+    if (threadIdx.x < 12) sb[threadIdx.x / 6][threadIdx.x % 6] = (threadIdx.x % 6) < 3 ? 0x7fffffff : (int)0x80000000;
+    __syncthreads();
+    int mn[2][3], mx[2][3];
+    for (int q = 0; q < 2; ++q) for (int k = 0; k < 3; ++k) { mn[q][k] = 0x7fffffff; mx[q][k] = (int)0x80000000; }
+    for (int it = 0; it < kItems; ++it) {
+        long long i = a + it * kThreads + threadIdx.x;
+        if (i >= n) break;
+        int w = which(i, cn);
+        if (w < 0) continue;
+        int vx = f2ord(B.x[cur][i]), vy = f2ord(B.y[cur][i]), vz = f2ord(B.z[cur][i]);
+        if (w == 0) {
+            mn[0][0] = min(mn[0][0], vx); mn[0][1] = min(mn[0][1], vy); mn[0][2] = min(mn[0][2], vz);
+            mx[0][0] = max(mx[0][0], vx); mx[0][1] = max(mx[0][1], vy); mx[0][2] = max(mx[0][2], vz);
+        } else {
+            mn[1][0] = min(mn[1][0], vx); mn[1][1] = min(mn[1][1], vy); mn[1][2] = min(mn[1][2], vz);
+            mx[1][0] = max(mx[1][0], vx); mx[1][1] = max(mx[1][1], vy); mx[1][2] = max(mx[1][2], vz);
+        }
+    }
+    for (int q = 0; q < 2; ++q)
+        for (int k = 0; k < 3; ++k) {
+            int v = mn[q][k], u = mx[q][k];
+            for (int o = 16; o > 0; o >>= 1) {
+                v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+                u = max(u, __shfl_xor_sync(0xffffffffu, u, o));
+            }
+            if ((threadIdx.x & 31) == 0) { atomicMin(&sb[q][k], v); atomicMax(&sb[q][3 + k], u); }
+        }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        int q = threadIdx.x / 6, k = threadIdx.x % 6;
+        long long e = q == 0 ? cn.eA : cn.eB;
+        if (e) {
+            int* dst = nbox + 6 * (e - first) + k;
+            if (k < 3) atomicMin(dst, sb[q][k]); else atomicMax(dst, sb[q][k]);
+        }
+    }
+}
+
+__device__ __forceinline__ int node_axis(const int* nbox, long long t) {
+    const int* b = nbox + 6 * t;
+    float ex = ord2f(b[3]) - ord2f(b[0]);
+    float ey = ord2f(b[4]) - ord2f(b[1]);
+    float ez = ord2f(b[5]) - ord2f(b[2]);
+    return biggest_axis(ex, ey, ez);
+}
+
+__global__ void k_axis(long long count, const int* nbox, NodeSel* sel) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    sel[t].axis = node_axis(nbox, t);
+}
+
+__device__ __forceinline__ float coord(const Buffers& B, int cur, long long i, int axis) {
+    return axis == 0 ? B.x[cur][i] : (axis == 1 ? B.y[cur][i] : B.z[cur][i]);
+}
+
+__global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level, long long n, long long first,
+                                                   const NodeSel* sel, uint32_t* hist, int pass) {
+    __shared__ ChunkNodes cn;
+    __shared__ uint32_t sh[2][256];
+    __shared__ uint32_t pre[2];
+    __shared__ int ax[2];
+    long long a = blockIdx.x * (long long)kChunk;
+    if (threadIdx.x == 0) {
+        chunk_nodes(a, level, n, cn);
+        ax[0] = sel[cn.eA - first].axis; pre[0] = sel[cn.eA - first].prefix;
+        if (cn.eB) { ax[1] = sel[cn.eB - first].axis; pre[1] = sel[cn.eB - first].prefix; }
+    }
+    for (int k = threadIdx.x; k < 512; k += kThreads) (&sh[0][0])[k] = 0;
+    __syncthreads();
+    const int shift = 24 - 8 * pass;
+    for (int it = 0; it < kItems; ++it) {
+        long long i = a + it * kThreads + threadIdx.x;
+        if (i >= n) break;
+        int w = which(i, cn);
+        if (w < 0) continue;
+        uint32_t key = f2key(coord(B, cur, i, ax[w]));
+        if (pass > 0 && (key >> (shift + 8)) != (pre[w] >> (shift + 8))) continue;
+        atomicAdd(&sh[w][(key >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 512; k += kThreads) {
+        int q = k >> 8;
+        uint32_t v = (&sh[0][0])[k];
+        long long e = q == 0 ? cn.eA : cn.eB;
+        if (v && e) atomicAdd(&hist[(e - first) * 256 + (k & 255)], v);
+    }
+}
+
+// One warp per node: find the bin holding rank krem, narrow the prefix, clear the
+// histogram for the next pass.  After the last pass, write the node's split.
+__global__ void k_select(long long count, long long first, int level, long long n, NodeSel* sel, uint32_t* hist,
+                         int pass, uint2* nodes) {
+    long long t = blockIdx.x * (long long)(blockDim.x / 32) + threadIdx.x / 32;
+    int lane = threadIdx.x & 31;
+    if (t >= count) return;
+    uint32_t* h = hist + t * 256;
+    uint32_t v[8];
+    uint32_t sum = 0;
+    for (int k = 0; k < 8; ++k) { v[k] = h[lane * 8 + k]; sum += v[k]; h[lane * 8 + k] = 0; }
+    uint32_t incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    uint32_t excl = incl - sum;
+    int krem = sel[t].krem;
+    // lane whose range [excl, incl) contains krem
+    bool mine = (uint32_t)krem >= excl && (uint32_t)krem < incl;
+    unsigned bal = __ballot_sync(0xffffffffu, mine);
+    int owner = __ffs(bal) - 1;
+    if (lane == owner) {
+        uint32_t cum = excl;
+        int bin = 0;
+        for (int k = 0; k < 8; ++k) {
+            if ((uint32_t)krem < cum + v[k]) { bin = lane * 8 + k; break; }
+            cum += v[k];
+        }
+        NodeSel& s = sel[t];
+        s.krem = krem - (int)cum;
+        s.prefix |= (uint32_t)bin << (24 - 8 * pass);
+        if (pass == 3) {
+            s.eq = (int)v[bin - lane * 8];
+            long long c = n >> level;
+            float m = key2f(s.prefix);
+            long long e = first + t;
+            nodes[e].y = __float_as_uint((c & 1) ? m : m + kSplitBias);
+            if (!(c & 1)) nodes[e].x = even_mask(s.axis);
+        }
+    }
+}
+
+// Block-wide exclusive scan of 6 per-thread counters.
+__device__ __forceinline__ void block_scan6(int (&v)[6], int (&excl)[6], int (&total)[6]) {
+    __shared__ int warp_sums[kThreads / 32][6];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl[6];
+    for (int q = 0; q < 6; ++q) {
+        int x = v[q];
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        incl[q] = x;
+        if (lane == 31) warp_sums[wid][q] = x;
+    }
+    __syncthreads();
+    for (int q = 0; q < 6; ++q) {
+        int before = 0, tot = 0;
+        for (int w = 0; w < kThreads / 32; ++w) {
+            int s = warp_sums[w][q];
+            if (w < wid) before += s;
+            tot += s;
+        }
+        excl[q] = before + incl[q] - v[q];
+        total[q] = tot;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int level, long long n, long long first,
+                                                        NodeSel* sel, uint2* nodes) {
+    __shared__ ChunkNodes cn;
+    __shared__ int ax[2], krem[2], eq[2];
+    __shared__ uint32_t med[2];
+    __shared__ int base[6];
+    long long a = blockIdx.x * (long long)kChunk;
+    if (threadIdx.x == 0) {
+        chunk_nodes(a, level, n, cn);
+        NodeSel s = sel[cn.eA - first];
+        ax[0] = s.axis; krem[0] = s.krem; eq[0] = s.eq; med[0] = s.prefix;
+        if (cn.eB) {
+            s = sel[cn.eB - first];
+            ax[1] = s.axis; krem[1] = s.krem; eq[1] = s.eq; med[1] = s.prefix;
+        }
+    }
+    __syncthreads();
+    const int dst = cur ^ 1;
+    // each thread owns kItems consecutive positions (deterministic ranks inside the CTA)
+    long long my0 = a + (long long)threadIdx.x * kItems;
+    int cnt[6] = {0, 0, 0, 0, 0, 0};
+    int cls[kItems];
+    for (int it = 0; it < kItems; ++it) {
+        long long i = my0 + it;
+        cls[it] = -1;
+        if (i >= n) continue;
+        int w = which(i, cn);
+        if (w < 0) continue;
+        uint32_t key = f2key(coord(B, cur, i, ax[w]));
+        int c = key < med[w] ? 0 : (key == med[w] ? 1 : 2);
+        cls[it] = w * 3 + c;
+        cnt[w * 3 + c]++;
+    }
+    int excl[6], total[6];
+    block_scan6(cnt, excl, total);
+    if (threadIdx.x < 6) {
+        int q = threadIdx.x;
+        long long e = q < 3 ? cn.eA : cn.eB;
+        base[q] = (e && total[q]) ? atomicAdd(&sel[e - first].cnt[q % 3], total[q]) : 0;
+    }
+    __syncthreads();
+    const long long c = cn.c;
+    const long long k = c >> 1, odd = c & 1;
+    for (int it = 0; it < kItems; ++it) {
+        long long i = my0 + it;
+        if (i >= n) break;
+        int q = cls[it];
+        float xv = B.x[cur][i], yv = B.y[cur][i], zv = B.z[cur][i];
+        uint32_t idv = B.id[cur][i];
+        long long d;
+        if (q < 0) {
+            d = i;   // ancestor median: stays in place
+        } else {
+            int w = q / 3, cl = q % 3;
+            long long s = w == 0 ? cn.sA : cn.sB;
+            long long r = base[q] + excl[q]++;
+            long long kl = krem[w];
+            long long lt = k - kl;
+            if (cl == 0) d = s + r;
+            else if (cl == 1) {
+                if (r < kl) d = s + lt + r;
+                else if (odd && r == kl) {
+                    d = s + k;
+                    long long e = w == 0 ? cn.eA : cn.eB;
+                    nodes[e].x = idv | odd_mask(ax[w]);
+                } else d = s + k + odd + (r - kl - odd);
+            } else d = s + k + odd + (eq[w] - kl - odd) + r;
+        }
+        B.x[dst][d] = xv; B.y[dst][d] = yv; B.z[dst][d] = zv; B.id[dst][d] = idv;
+    }
+}
+
+__global__ void k_load(const float4* __restrict__ pos4, long long n, Buffers B) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos4[i];
+    B.x[0][i] = p.x; B.y[0][i] = p.y; B.z[0][i] = p.z; B.id[0][i] = (uint32_t)i;
+}
+
+// Copy the median photons of levels < level0 from buffer `src` to buffer 0.
+__global__ void k_copy_medians(Buffers B, int src, int level0, long long n) {
+    long long e = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (1LL << level0)) return;
+    int lv = 63 - __clzll(e);
+    long long c = n >> lv;
+    if (!(c & 1)) return;
+    long long p = kd_node_start(e, lv, n) + (c >> 1);
+    B.x[0][p] = B.x[src][p]; B.y[0][p] = B.y[src][p]; B.z[0][p] = B.z[src][p]; B.id[0][p] = B.id[src][p];
+}
+
+// Shared-memory subtree builder: one CTA per node on level0 (at most kSmemSeg photons).
+struct SmemLayout {
+    static constexpr size_t xs = 0;
+    static constexpr size_t ys = xs + 4 * kSmemSeg;
+    static constexpr size_t zs = ys + 4 * kSmemSeg;
+    static constexpr size_t ids = zs + 4 * kSmemSeg;
+    static constexpr size_t tx = ids + 4 * kSmemSeg;              // temp copies
+    static constexpr size_t ty = tx + 4 * kSmemSeg;
+    static constexpr size_t tz = ty + 4 * kSmemSeg;
+    static constexpr size_t tid = tz + 4 * kSmemSeg;
+    static constexpr size_t v = tid + 4 * kSmemSeg;               // 2*kSmemSeg uint64 keys
+    static constexpr size_t box = v + 8 * 2 * kSmemSeg;           // kSmemSeg/2 * 6 ints
+    static constexpr size_t segs = box + 4 * 6 * (kSmemSeg / 2);  // kSmemSeg/2 starts
+    static constexpr size_t axes = segs + 4 * (kSmemSeg / 2);     // kSmemSeg/2 axes
+    static constexpr size_t total = axes + 4 * (kSmemSeg / 2);
+};
+
+__global__ void __launch_bounds__(kSmemThreads) k_smem_build(Buffers B, int src, int level0, long long n, uint2* nodes) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* X = (float*)(smem + SmemLayout::xs);
+    float* Y = (float*)(smem + SmemLayout::ys);
+    float* Z = (float*)(smem + SmemLayout::zs);
+    uint32_t* I = (uint32_t*)(smem + SmemLayout::ids);
+    float* TX = (float*)(smem + SmemLayout::tx);
+    float* TY = (float*)(smem + SmemLayout::ty);
+    float* TZ = (float*)(smem + SmemLayout::tz);
+    uint32_t* TI = (uint32_t*)(smem + SmemLayout::tid);
+    unsigned long long* V = (unsigned long long*)(smem + SmemLayout::v);
+    int* box = (int*)(smem + SmemLayout::box);
+    int* segs = (int*)(smem + SmemLayout::segs);
+    int* axes = (int*)(smem + SmemLayout::axes);
+
+    const long long e0 = (1LL << level0) + blockIdx.x;
+    const long long s0 = kd_node_start(e0, level0, n);
+    const int c0 = (int)(n >> level0);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int i = tid; i < c0; i += nt) {
+        X[i] = B.x[src][s0 + i]; Y[i] = B.y[src][s0 + i]; Z[i] = B.z[src][s0 + i]; I[i] = B.id[src][s0 + i];
+    }
+    __syncthreads();
+    for (int j = 0;; ++j) {
+        const int c = c0 >> j;
+        const int nsub = 1 << j;
+        // sub-node starts (local)
+        for (int s = tid; s < nsub; s += nt) {
+            int st = 0, cc = c0;
+            for (int b = j - 1; b >= 0; --b) {
+                int half = cc >> 1;
+                if ((s >> b) & 1) st += half + (cc & 1);
+                cc = half;
+            }
+            segs[s] = st;
+        }
+        __syncthreads();
+        if (c <= 1) {
+            for (int s = tid; s < nsub; s += nt) {
+                long long e = (e0 << j) + s;
+                nodes[e] = make_uint2(I[segs[s]], 0u);
+            }
+            break;
+        }
+        // extents per sub-node: a warp per sub-node when nodes are wide, a thread
+        // per sub-node when they are narrower than a warp
+        {
+            const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+            if (c >= 32) {
+                for (int s = wid; s < nsub; s += nw) {
+                    int st = segs[s];
+                    int mn0 = 0x7fffffff, mn1 = 0x7fffffff, mn2 = 0x7fffffff;
+                    int mx0 = (int)0x80000000, mx1 = (int)0x80000000, mx2 = (int)0x80000000;
+                    for (int i = lane; i < c; i += 32) {
+                        int p = st + i;
+                        int a = f2ord(X[p]), b = f2ord(Y[p]), d = f2ord(Z[p]);
+                        mn0 = min(mn0, a); mn1 = min(mn1, b); mn2 = min(mn2, d);
+                        mx0 = max(mx0, a); mx1 = max(mx1, b); mx2 = max(mx2, d);
+                    }
+                    for (int o = 16; o > 0; o >>= 1) {
+                        mn0 = min(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
+                        mn1 = min(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
+                        mn2 = min(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
+                        mx0 = max(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
+                        mx1 = max(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
+                        mx2 = max(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
+                    }
+                    if (lane == 0) {
+                        int* b = box + 6 * s;
+                        b[0] = mn0; b[1] = mn1; b[2] = mn2; b[3] = mx0; b[4] = mx1; b[5] = mx2;
+                    }
+                }
+            } else {
+                for (int s = tid; s < nsub; s += nt) {
+                    int st = segs[s];
+                    int mn0 = 0x7fffffff, mn1 = 0x7fffffff, mn2 = 0x7fffffff;
+                    int mx0 = (int)0x80000000, mx1 = (int)0x80000000, mx2 = (int)0x80000000;
+                    for (int i = 0; i < c; ++i) {
+                        int p = st + i;
+                        int a = f2ord(X[p]), b = f2ord(Y[p]), d = f2ord(Z[p]);
+                        mn0 = min(mn0, a); mn1 = min(mn1, b); mn2 = min(mn2, d);
+                        mx0 = max(mx0, a); mx1 = max(mx1, b); mx2 = max(mx2, d);
+                    }
+                    int* b = box + 6 * s;
+                    b[0] = mn0; b[1] = mn1; b[2] = mn2; b[3] = mx0; b[4] = mx1; b[5] = mx2;
+                }
+            }
+        }
+        __syncthreads();
+        for (int s = tid; s < nsub; s += nt) {
+            const int* b = box + 6 * s;
+            axes[s] = biggest_axis(ord2f(b[3]) - ord2f(b[0]), ord2f(b[4]) - ord2f(b[1]), ord2f(b[5]) - ord2f(b[2]));
+        }
+        __syncthreads();
+        // keys into the padded virtual array: nsub blocks of pw entries
+        int pw = 1;
+        while (pw < c) pw <<= 1;
+        const int nv = nsub * pw;
+        for (int v = tid; v < nv; v += nt) {
+            int s = v / pw, off = v % pw;
+            unsigned long long key = ~0ull;
+            if (off < c) {
+                int p = segs[s] + off;
+                int a = axes[s];
+                float f = a == 0 ? X[p] : (a == 1 ? Y[p] : Z[p]);
+                key = ((unsigned long long)f2key(f) << 32) | (unsigned)p;
+            }
+            V[v] = key;
+        }
+        __syncthreads();
+        // bitonic sort of each pw block, ascending
+        for (int k = 2; k <= pw; k <<= 1) {
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                for (int i = tid; i < nv; i += nt) {
+                    int l = i ^ jj;
+                    if (l > i) {
+                        bool up = ((i & k) == 0) || (k == pw);
+                        unsigned long long a = V[i], b = V[l];
+                        if ((a > b) == up) { V[i] = b; V[l] = a; }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // node records (split from the rank-c/2 key) and the new order
+        for (int s = tid; s < nsub; s += nt) {
+            int k = c >> 1;
+            unsigned long long km = V[s * pw + k];
+            float m = key2f((uint32_t)(km >> 32));
+            long long e = (e0 << j) + s;
+            uint32_t p = (uint32_t)(km & 0xffffffffu);
+            if (c & 1) nodes[e] = make_uint2(I[p] | odd_mask(axes[s]), __float_as_uint(m));
+            else nodes[e] = make_uint2(even_mask(axes[s]), __float_as_uint(m + kSplitBias));
+        }
+        for (int i = tid; i < c0; i += nt) { TX[i] = X[i]; TY[i] = Y[i]; TZ[i] = Z[i]; TI[i] = I[i]; }
+        __syncthreads();
+        for (int v = tid; v < nv; v += nt) {
+            int s = v / pw, off = v % pw;
+            if (off < c) {
+                int p = segs[s] + off;
+                uint32_t q = (uint32_t)(V[v] & 0xffffffffu);
+                X[p] = TX[q]; Y[p] = TY[q]; Z[p] = TZ[q]; I[p] = TI[q];
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int i = tid; i < c0; i += nt) {
+        B.x[0][s0 + i] = X[i]; B.y[0][s0 + i] = Y[i]; B.z[0][s0 + i] = Z[i]; B.id[0][s0 + i] = I[i];
+    }
+}
+
+int first_smem_level(long long n) {
+    int l = 0;
+    while ((n >> l) > kSmemSeg) ++l;
+    return l;
+}
+
+}  // namespace
+
+long long kd_node_array_len(long long n) {
+    if (n <= 0) return 0;
+    // kdtree.resize(std::pow(2, (int)(std::log2f(size) + 1)))  (src/KD_Tree.cpp:186)
+    long long ref = (long long)std::pow(2.0, (int)(std::log2f((float)n) + 1));
+    int L = 63 - __builtin_clzll((unsigned long long)n);
+    long long need = 1LL << (L + 1);
+    return ref > need ? ref : need;
+}
+
+size_t kd_scratch_bytes(long long n) {
+    if (n <= 0) return 256;
+    int l0 = first_smem_level(n);
+    long long maxnodes = l0 > 0 ? (1LL << (l0 - 1)) : 1;
+    size_t b = 0;
+    b += 16 * (size_t)n;                      // second buffer x/y/z/id
+    b += 24 * (size_t)maxnodes;               // boxes
+    b += sizeof(NodeSel) * (size_t)maxnodes;  // selection state
+    b += 1024 * (size_t)maxnodes;             // histograms
+    return b + 1024;
+}
+
+int kd_build(const float4* pos4, long long n, KdTree& tree, void* scratch, size_t scratch_bytes,
+             cudaStream_t stream, int* launches) {
+    int nl = 0;
+    tree.n = n;
+    if (n <= 0) { tree.levels = 0; tree.num_nodes = 0; if (launches) *launches = 0; return 0; }
+    tree.levels = 63 - __builtin_clzll((unsigned long long)n);
+    tree.num_nodes = kd_node_array_len(n);
+    if (scratch_bytes < kd_scratch_bytes(n)) return -1;
+    int l0 = first_smem_level(n);
+    long long maxnodes = l0 > 0 ? (1LL << (l0 - 1)) : 1;
+    char* p = (char*)scratch;
+    Buffers B;
+    B.x[0] = tree.x; B.y[0] = tree.y; B.z[0] = tree.z; B.id[0] = tree.id;
+    B.x[1] = (float*)p; p += 4 * (size_t)n;
+    B.y[1] = (float*)p; p += 4 * (size_t)n;
+    B.z[1] = (float*)p; p += 4 * (size_t)n;
+    B.id[1] = (uint32_t*)p; p += 4 * (size_t)n;
+    p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
+    int* nbox = (int*)p; p += 24 * (size_t)maxnodes;
+    p = (char*)(((uintptr_t)p + 15) & ~(uintptr_t)15);
+    NodeSel* sel = (NodeSel*)p; p += sizeof(NodeSel) * (size_t)maxnodes;
+    p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
+    uint32_t* hist = (uint32_t*)p;
+
+    cudaMemsetAsync(tree.nodes, 0, sizeof(uint2) * (size_t)tree.num_nodes, stream);
+    k_load<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(pos4, n, B);
+    nl++;
+    if (l0 > 0) cudaMemsetAsync(hist, 0, 1024 * (size_t)maxnodes, stream);
+    int cur = 0;
+    const unsigned chunks = (unsigned)((n + kChunk - 1) / kChunk);
+    for (int l = 0; l < l0; ++l) {
+        long long first = 1LL << l, count = 1LL << l;
+        unsigned g = (unsigned)((count + 255) / 256);
+        k_level_init<<<g, 256, 0, stream>>>(l, first, count, nbox, sel, n);
+        k_bbox<<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, nbox);
+        k_axis<<<g, 256, 0, stream>>>(count, nbox, sel);
+        nl += 3;
+        for (int pass = 0; pass < 4; ++pass) {
+            k_hist<<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, sel, hist, pass);
+            k_select<<<(unsigned)((count + 7) / 8), 256, 0, stream>>>(count, first, l, n, sel, hist, pass, tree.nodes);
+            nl += 2;
+        }
+        k_partition<<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, sel, tree.nodes);
+        nl++;
+        cur ^= 1;
+    }
+    if (cur == 1 && l0 > 0) {
+        long long cnt = (1LL << l0) - 1;
+        k_copy_medians<<<(unsigned)((cnt + 255) / 256), 256, 0, stream>>>(B, 1, l0, n);
+        nl++;
+    }
+    size_t smem = SmemLayout::total;
+    cudaFuncSetAttribute(k_smem_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_smem_build<<<(unsigned)(1LL << l0), kSmemThreads, smem, stream>>>(B, cur, l0, n, tree.nodes);
+    nl++;
+    if (launches) *launches = nl;
+    return 0;
+}
+
+}  // namespace rc

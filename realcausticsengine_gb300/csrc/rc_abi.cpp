@@ -1,0 +1,656 @@
+// C ABI of librealcaustics.so: the reference's init()/main() plus the additive rc_*
+// entry points, over the host scene (host_scene.cpp) and the sm_103a kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "host_scene.h"
+#include "realcaustics.h"
+#include "vm.cuh"
+
+namespace rc {
+
+namespace {
+
+std::string g_err;
+std::unique_ptr<HostScene> g_scene;
+rc_config g_cfg;
+bool g_cfg_set = false;
+
+#define RC_CUDA(call)                                                                   \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            g_err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+            return RC_E_CUDA;                                                           \
+        }                                                                               \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t reserve(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr; n = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+struct DeviceState {
+    bool ready = false;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    // scene
+    DevBuf<float4> node_lo, node_hi, wnode_lo, wnode_hi, tri_v0, tri_e1, tri_e2, tri_n0, tri_n1, tri_n2;
+    DevBuf<int> world_mesh, mesh_root;
+    DevBuf<DevLight> lights;
+    DevBuf<float> cdf;
+    DevBuf<DevMaterial> materials;
+    SceneView view{};
+    // iteration buffers
+    DevBuf<float4> ph_pos, ph_dir;
+    DevBuf<float2> ph_tp;
+    DevBuf<uint32_t> ph_path;
+    DevBuf<float4> q0, q1, q2, q3, q4;
+    DevBuf<unsigned long long> counters;   // [0] photons, [1] queries
+    DevBuf<int> errors;
+    DevBuf<uint2> kd_nodes;
+    DevBuf<float> kd_x, kd_y, kd_z;
+    DevBuf<uint32_t> kd_id;
+    DevBuf<unsigned char> kd_scratch;
+    DevBuf<double> accum;
+    int iterations_done = 0;
+    double stats[16] = {};
+
+    void release() {
+        DevBuf<float4>* f4[] = {&node_lo, &node_hi, &wnode_lo, &wnode_hi, &tri_v0, &tri_e1, &tri_e2, &tri_n0,
+                                &tri_n1, &tri_n2, &ph_pos, &ph_dir, &q0, &q1, &q2, &q3, &q4};
+        for (auto* b : f4) b->release();
+        world_mesh.release(); mesh_root.release(); lights.release(); cdf.release(); materials.release();
+        ph_tp.release(); ph_path.release(); counters.release(); errors.release();
+        kd_nodes.release(); kd_x.release(); kd_y.release(); kd_z.release(); kd_id.release(); kd_scratch.release();
+        accum.release();
+        for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
+        if (stream) { cudaStreamDestroy(stream); stream = nullptr; }
+        ready = false;
+        iterations_done = 0;
+    }
+};
+
+DeviceState g_dev;
+
+void default_config(rc_config* c) {
+    std::memset(c, 0, sizeof(*c));
+    c->max_path_length = 6;
+    c->photons_per_iter = 0;
+    c->sampler = RC_SAMPLER_UNIFORM;
+    c->mlt_chains = 65536;
+    c->large_step_prob = 0.3f;
+    c->seed = 0;
+    c->write_exr = 1;
+    std::snprintf(c->exr_path, sizeof(c->exr_path), "%s", "D:\\caustics.exr");
+    c->verbose = 0;
+}
+
+const rc_config& cfg() {
+    if (!g_cfg_set) { default_config(&g_cfg); g_cfg_set = true; }
+    return g_cfg;
+}
+
+template <class T>
+int upload(DevBuf<T>& b, const std::vector<T>& v, cudaStream_t s) {
+    RC_CUDA(b.reserve(v.size()));
+    if (!v.empty()) RC_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return RC_OK;
+}
+
+inline float4 f4(float x, float y, float z, uint32_t w) {
+    float wf;
+    std::memcpy(&wf, &w, 4);
+    return make_float4(x, y, z, wf);
+}
+
+int upload_scene(HostScene& sc) {
+    DeviceState& d = g_dev;
+    if (!d.stream) {
+        RC_CUDA(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
+        for (auto& e : d.ev) RC_CUDA(cudaEventCreate(&e));
+    }
+    std::vector<float4> nlo, nhi, v0, e1, e2, n0, n1, n2;
+    std::vector<int> mesh_root;
+    uint32_t node_base = 0, tri_base = 0, tri_global = 0;
+    for (size_t m = 0; m < sc.meshes.size(); ++m) {
+        HostMesh& hm = sc.meshes[m];
+        mesh_root.push_back((int)node_base);
+        for (const BvhNode& nd : hm.bvh.nodes) {
+            uint32_t w0 = nd.w0, w1 = nd.w1;
+            if (w0 & 0x80000000u) w1 = tri_base + w1;
+            else { w0 += node_base; w1 += node_base; }
+            nlo.push_back(f4(nd.box.mn.x, nd.box.mn.y, nd.box.mn.z, w0));
+            nhi.push_back(f4(nd.box.mx.x, nd.box.mx.y, nd.box.mx.z, w1));
+        }
+        for (size_t k = 1; k < hm.bvh.index.size(); ++k) {
+            uint32_t t = (uint32_t)hm.bvh.index[k];
+            const V3& a = hm.wpos[hm.tri[3 * t]];
+            const V3& b = hm.wpos[hm.tri[3 * t + 1]];
+            const V3& c = hm.wpos[hm.tri[3 * t + 2]];
+            v0.push_back(f4(a.x, a.y, a.z, tri_global + t));
+            e1.push_back(f4(b.x - a.x, b.y - a.y, b.z - a.z, hm.mat[t]));
+            e2.push_back(f4(c.x - a.x, c.y - a.y, c.z - a.z, (uint32_t)m));
+            const V3& na = hm.wnrm[hm.tri[3 * t]];
+            const V3& nb = hm.wnrm[hm.tri[3 * t + 1]];
+            const V3& nc = hm.wnrm[hm.tri[3 * t + 2]];
+            n0.push_back(make_float4(na.x, na.y, na.z, 0.0f));
+            n1.push_back(make_float4(nb.x, nb.y, nb.z, 0.0f));
+            n2.push_back(make_float4(nc.x, nc.y, nc.z, 0.0f));
+        }
+        node_base += (uint32_t)hm.bvh.nodes.size();
+        tri_base += (uint32_t)(hm.bvh.index.size() - 1);
+        tri_global += hm.num_tris;
+    }
+    std::vector<float4> wlo, whi;
+    for (const BvhNode& nd : sc.world.nodes) {
+        wlo.push_back(f4(nd.box.mn.x, nd.box.mn.y, nd.box.mn.z, nd.w0));
+        whi.push_back(f4(nd.box.mx.x, nd.box.mx.y, nd.box.mx.z, nd.w1));
+    }
+    std::vector<int> wm(sc.world.index.begin() + 1, sc.world.index.end());
+    cudaStream_t s = d.stream;
+    int r;
+    if ((r = upload(d.node_lo, nlo, s)) || (r = upload(d.node_hi, nhi, s)) || (r = upload(d.wnode_lo, wlo, s)) ||
+        (r = upload(d.wnode_hi, whi, s)) || (r = upload(d.tri_v0, v0, s)) || (r = upload(d.tri_e1, e1, s)) ||
+        (r = upload(d.tri_e2, e2, s)) || (r = upload(d.tri_n0, n0, s)) || (r = upload(d.tri_n1, n1, s)) ||
+        (r = upload(d.tri_n2, n2, s)) || (r = upload(d.world_mesh, wm, s)) || (r = upload(d.mesh_root, mesh_root, s)) ||
+        (r = upload(d.lights, sc.lights, s)) || (r = upload(d.cdf, sc.light_cdf, s)) ||
+        (r = upload(d.materials, sc.materials, s)))
+        return r;
+    RC_CUDA(d.counters.reserve(4));
+    RC_CUDA(d.errors.reserve(ERR_COUNT));
+    RC_CUDA(cudaMemsetAsync(d.errors.p, 0, sizeof(int) * ERR_COUNT, s));
+    RC_CUDA(cudaStreamSynchronize(s));
+    SceneView& v = d.view;
+    v.node_lo = d.node_lo.p; v.node_hi = d.node_hi.p;
+    v.wnode_lo = d.wnode_lo.p; v.wnode_hi = d.wnode_hi.p;
+    v.world_mesh = d.world_mesh.p; v.mesh_root = d.mesh_root.p;
+    v.tri_v0 = d.tri_v0.p; v.tri_e1 = d.tri_e1.p; v.tri_e2 = d.tri_e2.p;
+    v.tri_n0 = d.tri_n0.p; v.tri_n1 = d.tri_n1.p; v.tri_n2 = d.tri_n2.p;
+    v.num_world_nodes = (int)sc.world.nodes.size();
+    v.num_meshes = (int)sc.meshes.size();
+    d.ready = true;
+    return RC_OK;
+}
+
+int prepare() {
+    if (!g_scene) { g_err = "no scene: init() was not called"; return RC_E_NO_SCENE; }
+    HostScene& sc = *g_scene;
+    if (sc.prepared) return RC_OK;
+    if (sc.meshes.empty()) { g_err = "scene has no meshes"; return RC_E_INVALID; }
+    // Scene::update_bvh (src/Scene.cpp:110-152)
+    for (HostMesh& m : sc.meshes) build_mesh_bvh(m);
+    build_world_bvh(sc);
+    // init_lights + update_pdf_distribution (src/main.cpp:160-163)
+    int r = convert_lights(sc, g_err);
+    if (r) return r;
+    convert_materials(sc);
+    // base_radius *= SceneRadius (src/main.cpp:166-168)
+    sc.base_radius *= sc.scene_radius;
+    r = upload_scene(sc);
+    if (r) return r;
+    sc.prepared = true;
+    return RC_OK;
+}
+
+int check_errors() {
+    int h[ERR_COUNT];
+    RC_CUDA(cudaMemcpy(h, g_dev.errors.p, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h[ERR_STACK]) { g_err = "BVH traversal stack overflow (depth > 64)"; return RC_E_CAPACITY; }
+    if (h[ERR_MATERIAL]) { g_err = "triangle material index out of range"; return RC_E_INVALID; }
+    return RC_OK;
+}
+
+VMParams make_params(const HostScene& sc, int iteration) {
+    VMParams p{};
+    p.scene = g_dev.view;
+    p.lights = LightsView{g_dev.lights.p, g_dev.cdf.p, (int)sc.lights.size(), sc.light_integral};
+    p.materials = g_dev.materials.p;
+    p.num_materials = (int)sc.materials.size();
+    const HostCamera& c = sc.camera;
+    p.camera.width = c.width; p.camera.height = c.height;
+    float* dst[4] = {p.camera.origin, p.camera.bottom_left, p.camera.horizontal, p.camera.vertical};
+    const V3* src[4] = {&c.origin, &c.bottom_left, &c.horizontal, &c.vertical};
+    for (int k = 0; k < 4; ++k) { dst[k][0] = src[k]->x; dst[k][1] = src[k]->y; dst[k][2] = src[k]->z; }
+    p.seed = cfg().seed;
+    p.iteration = (uint32_t)iteration;
+    long long npix = (long long)c.width * c.height;
+    p.num_light_paths = cfg().photons_per_iter > 0 ? cfg().photons_per_iter : npix;
+    p.max_path_length = cfg().max_path_length;
+    // src/Vertex_Merging.cpp:201-212
+    const float PI = 3.14159265359f;
+    float light_paths_count = (float)p.num_light_paths;
+    float radius = sc.base_radius;
+    radius /= std::pow(float(iteration + 1), 0.5f * (1.0f - sc.radius_alpha));
+    radius = std::max(radius, 1e-7f);
+    float radius_sqr = radius * radius;
+    p.radius_sqr = radius_sqr;
+    p.vm_norm = 1.0f / (PI * radius_sqr * light_paths_count);
+    p.error = g_dev.errors.p;
+    return p;
+}
+
+float ms_between(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+int render_iteration(HostScene& sc) {
+    DeviceState& d = g_dev;
+    cudaStream_t s = d.stream;
+    const int it = d.iterations_done;
+    VMParams p = make_params(sc, it);
+    const long long npix = (long long)sc.camera.width * sc.camera.height;
+    if (d.accum.n < (size_t)(3 * npix)) {
+        RC_CUDA(d.accum.reserve(3 * npix));
+        RC_CUDA(cudaMemsetAsync(d.accum.p, 0, sizeof(double) * 3 * npix, s));
+    }
+    // photon buffer: grow and re-trace the iteration if it overflowed (the RNG is
+    // counter based, so the re-trace produces the same photons)
+    long long cap = (long long)d.ph_pos.n;
+    if (cap < p.num_light_paths * 2) cap = p.num_light_paths * 2;
+    unsigned long long nph = 0;
+    float t_light = 0.0f;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        RC_CUDA(d.ph_pos.reserve(cap)); RC_CUDA(d.ph_dir.reserve(cap));
+        RC_CUDA(d.ph_tp.reserve(cap)); RC_CUDA(d.ph_path.reserve(cap));
+        RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
+        PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, cap, d.counters.p};
+        RC_CUDA(cudaEventRecord(d.ev[0], s));
+        launch_light_pass(p, ph, s);
+        RC_CUDA(cudaGetLastError());
+        RC_CUDA(cudaEventRecord(d.ev[1], s));
+        RC_CUDA(cudaMemcpyAsync(&nph, d.counters.p, sizeof(nph), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(cudaStreamSynchronize(s));
+        t_light = ms_between(d.ev[0], d.ev[1]);
+        if ((long long)nph <= cap) break;
+        cap = (long long)nph + nph / 8 + 1024;
+        if (attempt == 2) { g_err = "photon buffer overflow"; return RC_E_CAPACITY; }
+    }
+    int r = check_errors();
+    if (r) return r;
+    // KD tree over the stored photons
+    long long n = (long long)nph;
+    long long nn = kd_node_array_len(n);
+    RC_CUDA(d.kd_nodes.reserve(std::max<long long>(nn, 2)));
+    RC_CUDA(d.kd_x.reserve(std::max<long long>(n, 1))); RC_CUDA(d.kd_y.reserve(std::max<long long>(n, 1)));
+    RC_CUDA(d.kd_z.reserve(std::max<long long>(n, 1))); RC_CUDA(d.kd_id.reserve(std::max<long long>(n, 1)));
+    size_t sb = kd_scratch_bytes(n);
+    RC_CUDA(d.kd_scratch.reserve(sb));
+    KdTree tree;
+    tree.nodes = d.kd_nodes.p; tree.x = d.kd_x.p; tree.y = d.kd_y.p; tree.z = d.kd_z.p; tree.id = d.kd_id.p;
+    int kd_launches = 0;
+    RC_CUDA(cudaEventRecord(d.ev[2], s));
+    if (kd_build(d.ph_pos.p, n, tree, d.kd_scratch.p, d.kd_scratch.n, s, &kd_launches)) {
+        g_err = "KD scratch too small"; return RC_E_CAPACITY;
+    }
+    RC_CUDA(cudaGetLastError());
+    RC_CUDA(cudaEventRecord(d.ev[3], s));
+    // camera pass -> merge queries
+    long long qcap = (long long)d.q0.n;
+    if (qcap < npix * 2) qcap = npix * 2;
+    unsigned long long nq = 0;
+    float t_cam = 0.0f;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        RC_CUDA(d.q0.reserve(qcap)); RC_CUDA(d.q1.reserve(qcap)); RC_CUDA(d.q2.reserve(qcap));
+        RC_CUDA(d.q3.reserve(qcap)); RC_CUDA(d.q4.reserve(qcap));
+        RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s));
+        QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qcap, d.counters.p + 1};
+        RC_CUDA(cudaEventRecord(d.ev[4], s));
+        launch_camera_pass(p, qb, s);
+        RC_CUDA(cudaGetLastError());
+        RC_CUDA(cudaEventRecord(d.ev[5], s));
+        RC_CUDA(cudaMemcpyAsync(&nq, d.counters.p + 1, sizeof(nq), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(cudaStreamSynchronize(s));
+        t_cam = ms_between(d.ev[4], d.ev[5]);
+        if ((long long)nq <= qcap) break;
+        qcap = (long long)nq + nq / 8 + 1024;
+        if (attempt == 2) { g_err = "query buffer overflow"; return RC_E_CAPACITY; }
+    }
+    r = check_errors();
+    if (r) return r;
+    PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, (long long)d.ph_pos.n, d.counters.p};
+    QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, (long long)d.q0.n, d.counters.p + 1};
+    RC_CUDA(cudaEventRecord(d.ev[6], s));
+    launch_gather(p, tree, ph, qb, (long long)nq, d.accum.p, s);
+    RC_CUDA(cudaGetLastError());
+    RC_CUDA(cudaEventRecord(d.ev[7], s));
+    RC_CUDA(cudaStreamSynchronize(s));
+    d.iterations_done++;
+    double* st = d.stats;
+    st[0] = (double)p.num_light_paths;
+    st[1] = (double)nph;
+    st[2] = (double)nq;
+    st[3] = 0.0;
+    st[4] = t_light;
+    st[5] = ms_between(d.ev[2], d.ev[3]);
+    st[6] = t_cam;
+    st[7] = ms_between(d.ev[6], d.ev[7]);
+    st[8] = 0.0;
+    st[9] = st[4] + st[5] + st[6] + st[7];
+    st[10] = d.iterations_done;
+    st[11] = sc.scene_radius;
+    st[12] = std::sqrt(p.radius_sqr);
+    st[13] = kd_launches + 3;
+    if (cfg().verbose)
+        std::printf("{\"iteration\": %d, \"light_paths\": %lld, \"photons\": %llu, \"queries\": %llu, "
+                    "\"light_ms\": %.3f, \"kd_ms\": %.3f, \"camera_ms\": %.3f, \"gather_ms\": %.3f}\n",
+                    it, p.num_light_paths, nph, nq, st[4], st[5], st[6], st[7]);
+    return RC_OK;
+}
+
+// Minimal single-part scanline OpenEXR writer: FP32 RGB, no compression.
+int write_exr(const char* path, const float* rgb, int w, int h) {
+    FILE* f = std::fopen(path, "wb");
+    if (!f) { g_err = std::string("cannot open ") + path; return RC_E_IO; }
+    std::vector<unsigned char> hdr;
+    auto put = [&](const void* p, size_t n) { const unsigned char* c = (const unsigned char*)p; hdr.insert(hdr.end(), c, c + n); };
+    auto put_i32 = [&](int32_t v) { put(&v, 4); };
+    auto put_str = [&](const char* s) { put(s, std::strlen(s) + 1); };
+    auto attr = [&](const char* name, const char* type, int32_t size) { put_str(name); put_str(type); put_i32(size); };
+    const uint32_t magic = 20000630u;
+    put(&magic, 4);
+    put_i32(2);
+    attr("channels", "chlist", 3 * (2 + 16) + 1);
+    for (const char* ch : {"B", "G", "R"}) {
+        put_str(ch);
+        put_i32(2);                       // FLOAT
+        unsigned char lin[4] = {0, 0, 0, 0};
+        put(lin, 4);
+        put_i32(1); put_i32(1);           // sampling
+    }
+    unsigned char z = 0;
+    put(&z, 1);
+    attr("compression", "compression", 1); put(&z, 1);
+    attr("dataWindow", "box2i", 16); put_i32(0); put_i32(0); put_i32(w - 1); put_i32(h - 1);
+    attr("displayWindow", "box2i", 16); put_i32(0); put_i32(0); put_i32(w - 1); put_i32(h - 1);
+    attr("lineOrder", "lineOrder", 1); put(&z, 1);
+    float one = 1.0f, zero = 0.0f;
+    attr("pixelAspectRatio", "float", 4); put(&one, 4);
+    attr("screenWindowCenter", "v2f", 8); put(&zero, 4); put(&zero, 4);
+    attr("screenWindowWidth", "float", 4); put(&one, 4);
+    put(&z, 1);
+    const uint64_t line_bytes = 8 + 12ull * (uint64_t)w;
+    uint64_t off = hdr.size() + 8ull * (uint64_t)h;
+    for (int y = 0; y < h; ++y) { put(&off, 8); off += line_bytes; }
+    bool ok = std::fwrite(hdr.data(), 1, hdr.size(), f) == hdr.size();
+    std::vector<float> line(3 * (size_t)w);
+    for (int y = 0; y < h && ok; ++y) {
+        int32_t yy = y, sz = 12 * w;
+        for (int x = 0; x < w; ++x) {
+            line[x] = rgb[3 * ((size_t)y * w + x) + 2];
+            line[w + x] = rgb[3 * ((size_t)y * w + x) + 1];
+            line[2 * w + x] = rgb[3 * ((size_t)y * w + x) + 0];
+        }
+        ok = std::fwrite(&yy, 4, 1, f) == 1 && std::fwrite(&sz, 4, 1, f) == 1 &&
+             std::fwrite(line.data(), 4, line.size(), f) == line.size();
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) { g_err = std::string("write failed: ") + path; return RC_E_IO; }
+    return RC_OK;
+}
+
+int read_image(float* rgb, int w, int h) {
+    if (!g_scene) { g_err = "no scene"; return RC_E_NO_SCENE; }
+    if (!rgb || w != g_scene->camera.width || h != g_scene->camera.height) { g_err = "bad image buffer"; return RC_E_INVALID; }
+    size_t n = 3 * (size_t)w * h;
+    std::vector<double> acc(n, 0.0);
+    if (g_dev.accum.p && g_dev.accum.n >= n)
+        RC_CUDA(cudaMemcpy(acc.data(), g_dev.accum.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    int it = g_dev.iterations_done;
+    double sc = it > 0 ? 1.0 / it : 0.0;
+    for (size_t i = 0; i < n; ++i) rgb[i] = (float)(acc[i] * sc);
+    return RC_OK;
+}
+
+void release_all() {
+    g_dev.release();
+    g_scene.reset();
+}
+
+}  // namespace
+}  // namespace rc
+
+using namespace rc;
+
+extern "C" {
+
+void init(int samples, float base_radius, float radius_reduction, long long* meshes_pointers,
+          unsigned int number_of_meshes, rc_matrix4x4* mesh_matrices, unsigned int* meshes_number_of_verts,
+          unsigned int* meshes_number_of_tris, unsigned int camera_x, unsigned int camera_y, rc_vec3 camera_position,
+          rc_vec3 camera_corner0, rc_vec3 camera_corner1, rc_vec3 camera_corner2, rc_vec3 camera_corner3,
+          rc_python_light* lights, unsigned int number_of_lights, rc_python_material* materials,
+          unsigned int number_of_materials, int** materials_indices, int debug_test, rc_debug_stuff debug_stuff) {
+    (void)debug_stuff;
+    release_all();
+    g_err.clear();
+    auto sc = std::make_unique<HostScene>();
+    sc->samples = samples;
+    sc->base_radius = base_radius;
+    sc->radius_alpha = radius_reduction;
+    sc->debug_test = debug_test;
+    if (number_of_meshes && (!meshes_pointers || !mesh_matrices || !meshes_number_of_verts ||
+                             !meshes_number_of_tris || !materials_indices)) {
+        g_err = "init: null mesh arrays";
+        return;
+    }
+    sc->meshes.resize(number_of_meshes);
+    for (unsigned i = 0; i < number_of_meshes; ++i) {
+        int r = ingest_mesh(sc->meshes[i], (const void*)meshes_pointers[i], meshes_number_of_verts[i],
+                            meshes_number_of_tris[i], mesh_matrices[i], materials_indices[i], g_err);
+        if (r) return;
+    }
+    for (unsigned i = 0; i < number_of_meshes; ++i)
+        for (uint32_t m : sc->meshes[i].mat)
+            if (m >= number_of_materials) { g_err = "init: material index out of range"; return; }
+    // Camera(camera_x, camera_y, position, corners...) (src/Camera.h:21-26)
+    HostCamera& c = sc->camera;
+    c.width = (int)camera_x;
+    c.height = (int)camera_y;
+    c.origin = {camera_position.x, camera_position.y, camera_position.z};
+    c.bottom_left = {camera_corner2.x, camera_corner2.y, camera_corner2.z};
+    c.horizontal = {camera_corner1.x - camera_corner2.x, camera_corner1.y - camera_corner2.y, camera_corner1.z - camera_corner2.z};
+    c.vertical = {camera_corner3.x - camera_corner2.x, camera_corner3.y - camera_corner2.y, camera_corner3.z - camera_corner2.z};
+    sc->py_lights = lights;
+    sc->num_lights = number_of_lights;
+    if (number_of_materials && !materials) { g_err = "init: null materials"; return; }
+    sc->py_materials.assign(materials, materials + number_of_materials);
+    g_scene = std::move(sc);
+}
+
+int main(void) {
+    if (!g_scene) { g_err = "main: no scene (init was not called or failed: " + g_err + ")"; return RC_E_NO_SCENE; }
+    int r = prepare();
+    if (!r) {
+        int iters = g_scene->samples;
+        for (int i = 0; i < iters && !r; ++i) r = render_iteration(*g_scene);
+    }
+    if (!r && cfg().write_exr) {
+        int w = g_scene->camera.width, h = g_scene->camera.height;
+        std::vector<float> img(3 * (size_t)w * h);
+        r = read_image(img.data(), w, h);
+        if (!r) r = write_exr(cfg().exr_path, img.data(), w, h);
+    }
+    std::string keep = g_err;
+    release_all();
+    g_err = keep;
+    return r;
+}
+
+int rc_default_config(rc_config* c) {
+    if (!c) return RC_E_INVALID;
+    default_config(c);
+    return RC_OK;
+}
+
+int rc_set_config(const rc_config* c) {
+    if (!c) { g_err = "null config"; return RC_E_INVALID; }
+    if (c->max_path_length < 0 || c->max_path_length > 30) { g_err = "max_path_length out of range [0, 30]"; return RC_E_INVALID; }
+    if (c->photons_per_iter < 0) { g_err = "photons_per_iter < 0"; return RC_E_INVALID; }
+    if (c->sampler != RC_SAMPLER_UNIFORM) { g_err = "sampler not available in this build"; return RC_E_UNSUPPORTED; }
+    g_cfg = *c;
+    g_cfg.exr_path[sizeof(g_cfg.exr_path) - 1] = 0;
+    g_cfg_set = true;
+    return RC_OK;
+}
+
+int rc_prepare(void) { return prepare(); }
+
+int rc_render(int iterations) {
+    if (iterations < 0) { g_err = "iterations < 0"; return RC_E_INVALID; }
+    int r = prepare();
+    for (int i = 0; i < iterations && !r; ++i) r = render_iteration(*g_scene);
+    return r;
+}
+
+int rc_read_image(float* rgb, int width, int height) { return read_image(rgb, width, height); }
+
+int rc_release(void) {
+    release_all();
+    return RC_OK;
+}
+
+const char* rc_last_error(void) { return g_err.c_str(); }
+
+int rc_get_stats(double* out, int n) {
+    if (!out || n < 0) return RC_E_INVALID;
+    for (int i = 0; i < n && i < 16; ++i) out[i] = g_dev.stats[i];
+    return RC_OK;
+}
+
+int rc_trace_rays(int n, const float* origins, const float* directions, float tmin, unsigned* out) {
+    int r = prepare();
+    if (r) return r;
+    if (n < 0 || (n > 0 && (!origins || !directions || !out))) { g_err = "bad ray arrays"; return RC_E_INVALID; }
+    if (n == 0) return RC_OK;
+    cudaStream_t s = g_dev.stream;
+    DevBuf<float> o, d;
+    DevBuf<unsigned> w;
+    RC_CUDA(o.reserve(3 * (size_t)n)); RC_CUDA(d.reserve(3 * (size_t)n)); RC_CUDA(w.reserve(8 * (size_t)n));
+    RC_CUDA(cudaMemcpyAsync(o.p, origins, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
+    RC_CUDA(cudaMemcpyAsync(d.p, directions, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
+    launch_trace_rays(g_dev.view, n, o.p, d.p, tmin, nullptr, w.p, g_dev.errors.p, s);
+    RC_CUDA(cudaGetLastError());
+    RC_CUDA(cudaMemcpyAsync(out, w.p, 32 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    RC_CUDA(cudaStreamSynchronize(s));
+    o.release(); d.release(); w.release();
+    return check_errors();
+}
+
+int rc_trace_rays_full(int n, const float* origins, const float* directions, float tmin, float* out) {
+    int r = prepare();
+    if (r) return r;
+    if (n < 0 || (n > 0 && (!origins || !directions || !out))) { g_err = "bad ray arrays"; return RC_E_INVALID; }
+    if (n == 0) return RC_OK;
+    cudaStream_t s = g_dev.stream;
+    DevBuf<float> o, d, f;
+    RC_CUDA(o.reserve(3 * (size_t)n)); RC_CUDA(d.reserve(3 * (size_t)n)); RC_CUDA(f.reserve(16 * (size_t)n));
+    RC_CUDA(cudaMemcpyAsync(o.p, origins, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
+    RC_CUDA(cudaMemcpyAsync(d.p, directions, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
+    launch_trace_rays(g_dev.view, n, o.p, d.p, tmin, f.p, nullptr, g_dev.errors.p, s);
+    RC_CUDA(cudaGetLastError());
+    RC_CUDA(cudaMemcpyAsync(out, f.p, 64 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    RC_CUDA(cudaStreamSynchronize(s));
+    o.release(); d.release(); f.release();
+    return check_errors();
+}
+
+static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, DevBuf<uint2>& nodes, DevBuf<float>& x,
+                         DevBuf<float>& y, DevBuf<float>& z, DevBuf<uint32_t>& id, DevBuf<unsigned char>& scratch,
+                         KdTree& tree, cudaStream_t s) {
+    std::vector<float4> p4((size_t)n);
+    for (int i = 0; i < n; ++i) p4[i] = make_float4(positions[3 * i], positions[3 * i + 1], positions[3 * i + 2], 0.0f);
+    RC_CUDA(pos.reserve(std::max(n, 1)));
+    if (n) RC_CUDA(cudaMemcpyAsync(pos.p, p4.data(), 16 * (size_t)n, cudaMemcpyHostToDevice, s));
+    long long nn = kd_node_array_len(n);
+    RC_CUDA(nodes.reserve(std::max<long long>(nn, 2)));
+    RC_CUDA(x.reserve(std::max(n, 1))); RC_CUDA(y.reserve(std::max(n, 1)));
+    RC_CUDA(z.reserve(std::max(n, 1))); RC_CUDA(id.reserve(std::max(n, 1)));
+    RC_CUDA(scratch.reserve(kd_scratch_bytes(n)));
+    tree.nodes = nodes.p; tree.x = x.p; tree.y = y.p; tree.z = z.p; tree.id = id.p;
+    if (kd_build(pos.p, n, tree, scratch.p, scratch.n, s, nullptr)) { g_err = "KD scratch"; return RC_E_CAPACITY; }
+    RC_CUDA(cudaGetLastError());
+    return RC_OK;
+}
+
+int rc_kd_query(int n, const float* positions, int q, const float* queries, float r2, int* counts, int* idx,
+                long long cap, long long* total) {
+    if (n < 0 || q < 0 || (n > 0 && !positions) || (q > 0 && (!queries || !counts))) { g_err = "bad KD arrays"; return RC_E_INVALID; }
+    cudaStream_t s = nullptr;
+    RC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    DevBuf<float4> pos; DevBuf<uint2> nodes; DevBuf<float> x, y, z, qp; DevBuf<uint32_t> id;
+    DevBuf<unsigned char> scratch; DevBuf<int> cnt, out; DevBuf<long long> off;
+    KdTree tree;
+    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, tree, s);
+    if (!r && q > 0) {
+        do {
+            RC_CUDA(qp.reserve(3 * (size_t)q)); RC_CUDA(cnt.reserve(q)); RC_CUDA(off.reserve(q));
+            RC_CUDA(cudaMemcpyAsync(qp.p, queries, 12 * (size_t)q, cudaMemcpyHostToDevice, s));
+            launch_kd_query(tree, q, qp.p, r2, cnt.p, nullptr, nullptr, s);
+            RC_CUDA(cudaGetLastError());
+            RC_CUDA(cudaMemcpyAsync(counts, cnt.p, 4 * (size_t)q, cudaMemcpyDeviceToHost, s));
+            RC_CUDA(cudaStreamSynchronize(s));
+            std::vector<long long> offs(q);
+            long long t = 0;
+            for (int j = 0; j < q; ++j) { offs[j] = t; t += counts[j]; }
+            if (total) *total = t;
+            if (idx && t > 0 && t <= cap) {
+                RC_CUDA(out.reserve(t));
+                RC_CUDA(cudaMemcpyAsync(off.p, offs.data(), 8 * (size_t)q, cudaMemcpyHostToDevice, s));
+                launch_kd_query(tree, q, qp.p, r2, cnt.p, off.p, out.p, s);
+                RC_CUDA(cudaGetLastError());
+                RC_CUDA(cudaMemcpyAsync(idx, out.p, 4 * (size_t)t, cudaMemcpyDeviceToHost, s));
+                RC_CUDA(cudaStreamSynchronize(s));
+            }
+        } while (0);
+    } else if (!r && total) {
+        *total = 0;
+    }
+    pos.release(); nodes.release(); x.release(); y.release(); z.release(); id.release(); scratch.release();
+    cnt.release(); out.release(); off.release(); qp.release();
+    cudaStreamDestroy(s);
+    return r;
+}
+
+int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes_out, long long cap, long long* num_nodes) {
+    if (n < 0 || (n > 0 && !positions)) { g_err = "bad KD arrays"; return RC_E_INVALID; }
+    cudaStream_t s = nullptr;
+    RC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    DevBuf<float4> pos; DevBuf<uint2> nodes; DevBuf<float> x, y, z; DevBuf<uint32_t> id; DevBuf<unsigned char> scratch;
+    KdTree tree;
+    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, tree, s);
+    if (!r) {
+        long long nn = kd_node_array_len(n);
+        if (num_nodes) *num_nodes = nn;
+        if (nodes_out && nn > 0) {
+            long long m = std::min(nn, cap);
+            cudaError_t e = cudaMemcpyAsync(nodes_out, nodes.p, 8 * (size_t)m, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) { g_err = cudaGetErrorString(e); r = RC_E_CUDA; }
+        }
+    }
+    pos.release(); nodes.release(); x.release(); y.release(); z.release(); id.release(); scratch.release();
+    cudaStreamDestroy(s);
+    return r;
+}
+
+}  // extern "C"

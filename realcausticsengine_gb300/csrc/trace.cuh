@@ -1,0 +1,208 @@
+// Closest-hit traversal of the reference's two-level SAH BVH on sm_103a.
+//
+// Bit-exact restatement of Scene::hit (src/Scene.cpp:154-189) ->
+// CacheBVHNode_world::hit (src/BVH/BVH_world.cpp:267-283) -> Mesh::hit
+// (src/mesh.cpp:70-105) -> CacheBVHNode_mesh::hit (src/BVH/BVH_mesh.cpp:265-283) ->
+// aabb::hit (src/aabb.cpp:6-41) and Triangle::hit (src/Triangle.cpp:20-88):
+//  * stack DFS, right child pushed before left, so the left subtree is visited first;
+//  * every box is tested against the current closest distance of its own level;
+//  * a world leaf starts a fresh record (distance = inf) and, if any of its meshes is
+//    hit, OVERWRITES the running result - so the answer is the last hit world leaf's
+//    closest triangle, exactly as the reference returns it;
+//  * ties keep the first triangle found (strict t < closest).
+// Vertices are pre-transformed on upload with the reference's operation order, which
+// gives the same floats the reference recomputes per test.
+#pragma once
+#include "dev_math.cuh"
+
+namespace rc {
+
+// Device view of the scene.  Nodes: two float4 per node (min.xyz|w0, max.xyz|w1).
+// Mesh-level inner nodes hold global child indices; mesh-level leaves hold
+// (0x80000000|count, first triangle slot).  World leaves hold
+// (0x80000000|count, first slot in world_mesh).  Triangles are stored in leaf order.
+struct SceneView {
+    const float4* __restrict__ node_lo;
+    const float4* __restrict__ node_hi;
+    const float4* __restrict__ wnode_lo;
+    const float4* __restrict__ wnode_hi;
+    const int* __restrict__ world_mesh;     // mesh id per world-leaf slot
+    const int* __restrict__ mesh_root;      // global root node per mesh
+    const float4* __restrict__ tri_v0;      // v0.xyz | global triangle id
+    const float4* __restrict__ tri_e1;      // (v1 - v0).xyz | material
+    const float4* __restrict__ tri_e2;      // (v2 - v0).xyz | mesh id
+    const float4* __restrict__ tri_n0;      // vertex normals (normalised, world space)
+    const float4* __restrict__ tri_n1;
+    const float4* __restrict__ tri_n2;
+    int num_world_nodes;
+    int num_meshes;
+};
+
+constexpr int kStackSize = 64;   // BVH_STACK_SIZE in the reference
+
+struct HitRec {
+    float t, u, v;
+    int slot;       // triangle slot (leaf order) of the reported hit, -1 if none
+};
+
+// aabb::hit with the per-ray reciprocals (1/d computed once: the same division the
+// reference repeats per box).  NaN and -0 behaviour follows the ternaries as written.
+__device__ __forceinline__ bool box_hit(float4 lo, float4 hi, F3 o, F3 inv, float tmin, float tmax) {
+    float t0 = (lo.x - o.x) * inv.x, t1 = (hi.x - o.x) * inv.x;
+    if (inv.x < 0) { float s = t0; t0 = t1; t1 = s; }
+    tmin = t0 > tmin ? t0 : tmin;
+    tmax = t1 < tmax ? t1 : tmax;
+    if (tmax < tmin) return false;
+    t0 = (lo.y - o.y) * inv.y; t1 = (hi.y - o.y) * inv.y;
+    if (inv.y < 0) { float s = t0; t0 = t1; t1 = s; }
+    tmin = t0 > tmin ? t0 : tmin;
+    tmax = t1 < tmax ? t1 : tmax;
+    if (tmax < tmin) return false;
+    t0 = (lo.z - o.z) * inv.z; t1 = (hi.z - o.z) * inv.z;
+    if (inv.z < 0) { float s = t0; t0 = t1; t1 = s; }
+    tmin = t0 > tmin ? t0 : tmin;
+    tmax = t1 < tmax ? t1 : tmax;
+    if (tmax < tmin) return false;
+    return true;
+}
+
+// Möller-Trumbore as src/Triangle.cpp:44-66 computes it.
+__device__ __forceinline__ bool tri_hit(const SceneView& s, int slot, F3 o, F3 d, float tmin, float tmax,
+                                        float& t_out, float& u_out, float& v_out) {
+    float4 a = __ldg(&s.tri_v0[slot]);
+    float4 b = __ldg(&s.tri_e1[slot]);
+    float4 c = __ldg(&s.tri_e2[slot]);
+    F3 v0 = xyz(a), e1 = xyz(b), e2 = xyz(c);
+    F3 pvec = cross(d, e2);
+    float det = dot(e1, pvec);
+    if (fabsf(det) < 0.0000001f) return false;
+    float inv_det = 1.0f / det;
+    F3 tvec = o - v0;
+    float u = dot(tvec, pvec) * inv_det;
+    if (u < 0.0f || u > 1.0f) return false;
+    F3 qvec = cross(tvec, e1);
+    float v = dot(d, qvec) * inv_det;
+    if (v < 0.0f || u + v > 1.0f) return false;
+    float t = dot(e2, qvec) * inv_det;
+    if (t > tmin && t < tmax) {
+        t_out = t; u_out = u; v_out = v;
+        return true;
+    }
+    return false;
+}
+
+// Mesh::hit on one mesh with the running record of the current world leaf.
+// Returns false (and sets *overflow) if the stack would exceed kStackSize.
+__device__ __forceinline__ bool mesh_traverse(const SceneView& s, int mesh, F3 o, F3 d, F3 inv, float tmin,
+                                              HitRec& rec, bool& any, int* overflow) {
+    int stack[kStackSize];
+    int sp = 0;
+    stack[sp++] = __ldg(&s.mesh_root[mesh]);
+    while (sp) {
+        int id = stack[--sp];
+        float4 lo = __ldg(&s.node_lo[id]);
+        float4 hi = __ldg(&s.node_hi[id]);
+        if (!box_hit(lo, hi, o, inv, tmin, rec.t)) continue;
+        uint32_t w0 = __float_as_uint(lo.w), w1 = __float_as_uint(hi.w);
+        if (w0 & 0x80000000u) {
+            int cnt = (int)(w0 & 0x7fffffffu);
+            for (int k = 0; k < cnt; ++k) {
+                int slot = (int)w1 + k;
+                float t, u, v;
+                if (tri_hit(s, slot, o, d, tmin, rec.t, t, u, v)) {
+                    rec.t = t; rec.u = u; rec.v = v; rec.slot = slot;
+                    any = true;
+                }
+            }
+        } else {
+            if (sp + 2 > kStackSize) { *overflow = 1; return false; }
+            stack[sp++] = (int)w1;   // right first ...
+            stack[sp++] = (int)w0;   // ... so the left child is popped first
+        }
+    }
+    return true;
+}
+
+// Scene::hit.  `out` is the reported record (t = inf when nothing was hit).
+__device__ __forceinline__ bool scene_hit(const SceneView& s, F3 o, F3 d, float tmin, HitRec& out, int* overflow) {
+    F3 inv = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+    out.t = INFINITY; out.u = 0.0f; out.v = 0.0f; out.slot = -1;
+    bool hit = false;
+    if (s.num_world_nodes == 1) {
+        // single world leaf: the common case (one leaf holding every mesh)
+        float4 lo = __ldg(&s.wnode_lo[0]);
+        float4 hi = __ldg(&s.wnode_hi[0]);
+        if (!box_hit(lo, hi, o, inv, tmin, out.t)) return false;
+        uint32_t w0 = __float_as_uint(lo.w), w1 = __float_as_uint(hi.w);
+        int cnt = (int)(w0 & 0x7fffffffu);
+        HitRec leaf = {INFINITY, 0.0f, 0.0f, -1};
+        bool any = false;
+        for (int k = 0; k < cnt; ++k) {
+            int mesh = __ldg(&s.world_mesh[w1 + k]);
+            bool mesh_any = false;
+            if (!mesh_traverse(s, mesh, o, d, inv, tmin, leaf, mesh_any, overflow)) return false;
+            any |= mesh_any;
+        }
+        if (any) out = leaf;
+        return any;
+    }
+    int stack[kStackSize];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        int id = stack[--sp];
+        float4 lo = __ldg(&s.wnode_lo[id]);
+        float4 hi = __ldg(&s.wnode_hi[id]);
+        if (!box_hit(lo, hi, o, inv, tmin, out.t)) continue;
+        uint32_t w0 = __float_as_uint(lo.w), w1 = __float_as_uint(hi.w);
+        if (w0 & 0x80000000u) {
+            int cnt = (int)(w0 & 0x7fffffffu);
+            HitRec leaf = {INFINITY, 0.0f, 0.0f, -1};   // fresh Isect temp_rec
+            bool any = false;
+            for (int k = 0; k < cnt; ++k) {
+                int mesh = __ldg(&s.world_mesh[w1 + k]);
+                bool mesh_any = false;
+                if (!mesh_traverse(s, mesh, o, d, inv, tmin, leaf, mesh_any, overflow)) return false;
+                any |= mesh_any;
+            }
+            if (any) { out = leaf; hit = true; }   // unconditional overwrite (world-leaf quirk)
+        } else {
+            if (sp + 2 > kStackSize) { *overflow = 1; return false; }
+            stack[sp++] = (int)w1;
+            stack[sp++] = (int)w0;
+        }
+    }
+    return hit;
+}
+
+// Attributes Triangle::hit fills in (src/Triangle.cpp:68-80), for the reported triangle.
+struct Isect {
+    F3 ng, ns, pos, dir;
+    float t, u, v;
+    bool front;
+    int material;
+    int tri;     // global triangle id
+    int mesh;
+};
+
+__device__ __forceinline__ void fill_isect(const SceneView& s, const HitRec& h, F3 o, F3 d, Isect& is) {
+    float4 a = __ldg(&s.tri_v0[h.slot]);
+    float4 b = __ldg(&s.tri_e1[h.slot]);
+    float4 c = __ldg(&s.tri_e2[h.slot]);
+    F3 e1 = xyz(b), e2 = xyz(c);
+    is.t = h.t; is.u = h.u; is.v = h.v;
+    is.ng = normalize(cross(e1, e2));
+    F3 n0 = xyz(__ldg(&s.tri_n0[h.slot]));
+    F3 n1 = xyz(__ldg(&s.tri_n1[h.slot]));
+    F3 n2 = xyz(__ldg(&s.tri_n2[h.slot]));
+    float w = 1 - h.u - h.v;
+    is.ns = n0 * w + n1 * h.u + n2 * h.v;
+    is.front = dot(is.ns, d) < 0;
+    is.pos = o + d * h.t;
+    is.dir = d;
+    is.tri = (int)__float_as_uint(a.w);
+    is.material = (int)__float_as_uint(b.w);
+    is.mesh = (int)__float_as_uint(c.w);
+}
+
+}  // namespace rc

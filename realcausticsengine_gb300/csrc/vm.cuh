@@ -1,0 +1,78 @@
+// Vertex-merging iteration on the device: shared declarations of the kernels in
+// vm_kernels.cu and gather.cu and the buffers they exchange.
+//
+// One progressive iteration (src/Vertex_Merging.cpp:196-366):
+//   light pass   - light sub-paths, photons stored at non-delta vertices reached by a
+//                  glossy event (Path_Vertex records)
+//   KD build     - photon KD-tree over the stored photons (kdtree.cu)
+//   camera pass  - one camera sub-path per pixel; every non-delta vertex becomes a
+//                  merge query
+//   gather       - photons within the merge radius of each query, MIS-weighted BSDF
+//                  contribution, accumulated into the FP64 per-pixel running sum
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "rc_device_types.h"
+#include "trace.cuh"
+#include "kdtree.cuh"
+
+namespace rc {
+
+// Photon records (Path_Vertex, src/Path_Vertices.h:10-20), structure of arrays:
+//   pos  = position.xyz | dVM          dir = direction_world.xyz | throughput.r
+//   tp   = throughput.g, throughput.b  path = light path index
+struct PhotonBuf {
+    float4* pos;
+    float4* dir;
+    float2* tp;
+    uint32_t* path;
+    long long capacity;
+    unsigned long long* count;   // device counter (may exceed capacity: overflow)
+};
+
+// Merge queries written by the camera pass (one per non-delta camera vertex):
+//   q0 = position.xyz | camera dVM      q1 = shading normal.xyz | material
+//   q2 = geometric normal.xyz | pixel   q3 = throughput * VM_normalization | 0
+//   q4 = incoming ray direction.xyz | 0
+struct QueryBuf {
+    float4* q0; float4* q1; float4* q2; float4* q3; float4* q4;
+    long long capacity;
+    unsigned long long* count;
+};
+
+struct LightsView {
+    const DevLight* lights;
+    const float* cdf;      // n + 1 entries
+    int count;
+    float integral;
+};
+
+struct VMParams {
+    SceneView scene;
+    LightsView lights;
+    const DevMaterial* materials;
+    int num_materials;
+    DevCamera camera;
+    uint64_t seed;
+    uint32_t iteration;
+    long long num_light_paths;
+    int max_path_length;
+    float radius_sqr;
+    float vm_norm;
+    int* error;             // device flags: [0] stack overflow, [1] bad material
+};
+
+// error flag slots
+enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_COUNT = 8 };
+
+void launch_light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s);
+void launch_camera_pass(const VMParams& p, QueryBuf qb, cudaStream_t s);
+void launch_trace_rays(const SceneView& s, int n, const float* o, const float* d, float tmin, float* out_full,
+                       unsigned* out_words, int* err, cudaStream_t st);
+void launch_gather(const VMParams& p, const KdTree& tree, PhotonBuf ph, QueryBuf qb, long long num_queries,
+                   double* accum, cudaStream_t s);
+// Radius query hook: counts (and, if idx != nullptr, ids at offsets) per query.
+void launch_kd_query(const KdTree& tree, int q, const float* qpos, float r2, int* counts,
+                     const long long* offsets, int* idx, cudaStream_t s);
+
+}  // namespace rc

@@ -1,0 +1,238 @@
+// Light pass, camera pass and the closest-hit parity kernel.
+#include "vm.cuh"
+#include "bsdf.cuh"
+#include "rng.cuh"
+
+namespace rc {
+
+namespace {
+
+// find_interval (src/utils.h:142-157)
+__device__ __forceinline__ int find_interval(const float* cdf, int size, float u) {
+    int first = 0, len = size;
+    while (len > 0) {
+        int half = len >> 1, middle = first + half;
+        if (cdf[middle] < u) { first = middle + 1; len -= half + 1; }
+        else len = half;
+    }
+    int v = first - 1;
+    return v < 0 ? 0 : (v > size - 2 ? size - 2 : v);
+}
+
+// Lights_list::sample_lights (src/Light_list.cpp:10-30) with Area_Light::sample_light
+// (src/Lights.cpp:41-55) and Sun_Light::sample_light (src/Lights.cpp:122-136).
+// The point light, a stub in the reference, emits uniformly over the sphere.
+__device__ __forceinline__ void sample_light(const LightsView& L, float u0, float u1, float u2, float u3, float u4,
+                                             F3& o, F3& d, F3& tp) {
+    int idx = find_interval(L.cdf, L.count + 1, u0);
+    const DevLight& l = L.lights[idx];
+    float pick = l.power / (L.count * L.integral);
+    if (l.type == LIGHT_AREA) {
+        o = ld3(l.bl) + ld3(l.hz) * u1 + ld3(l.vt) * u2;
+        F3 local = cos_hemisphere(u3, u4);
+        d = ld3(l.fx) * local.x + ld3(l.fy) * local.y + ld3(l.fz) * local.z;
+        tp = f3(l.cr, l.cg, l.cb) * kPI;
+    } else if (l.type == LIGHT_SUN) {
+        o = ld3(l.bl) + ld3(l.hz) * u1 + ld3(l.vt) * u2;
+        d = ld3(l.fz);
+        tp = f3(l.cr, l.cg, l.cb);
+    } else {
+        o = ld3(l.pos);
+        float z = 1.0f - 2.0f * u3;
+        float r = sqrtf(ref_max(0.0f, 1.0f - z * z));
+        float s, c;
+        sincosf(kPI2 * u4, &s, &c);
+        d = f3(r * c, r * s, z);
+        tp = f3(l.cr, l.cg, l.cb) * (4.0f * kPI);
+    }
+    tp = div_each(tp, pick);
+}
+
+// Warp-aggregated append: one atomic per converged group of lanes.
+__device__ __forceinline__ unsigned long long warp_append(unsigned long long* counter) {
+    unsigned m = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    unsigned lower = m & ((1u << lane) - 1u);
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(lower);
+}
+
+__global__ void __launch_bounds__(256) k_light_pass(const VMParams P, PhotonBuf ph) {
+    long long pidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (pidx >= P.num_light_paths) return;
+    PathRng rng;
+    rng.init(P.seed, (uint64_t)pidx, P.iteration, STREAM_LIGHT);
+    U4 b0 = rng.block(0), b1 = rng.block(1);
+    F3 o, d, tp;
+    sample_light(P.lights, u01(b0.a), u01(b0.b), u01(b0.c), u01(b0.d), u01(b1.a), o, d, tp);
+    int diffuse = 0, last = EV_DIFFUSE;
+    float dVM = 0.0f;
+    for (int len = 0;; ++len) {
+        F3 ro = o + d * kRayEps;
+        HitRec h;
+        if (!scene_hit(P.scene, ro, d, kRayEps, h, P.error + ERR_STACK)) break;
+        Isect is;
+        fill_isect(P.scene, h, ro, d, is);
+        if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); break; }
+        Bsdf b;
+        b.init(P.materials[is.material], is.ns, is.dir, false);
+        if (!b.valid()) break;
+        dVM /= fabsf(b.cos_theta_in());
+        bool stored = false;
+        if (!b.is_delta() && (last & EV_GLOSSY)) {
+            unsigned long long slot = warp_append(ph.count);
+            if (slot < (unsigned long long)ph.capacity) {
+                ph.pos[slot] = make_float4(is.pos.x, is.pos.y, is.pos.z, dVM);
+                ph.dir[slot] = make_float4(-is.dir.x, -is.dir.y, -is.dir.z, tp.x);
+                ph.tp[slot] = make_float2(tp.y, tp.z);
+                ph.path[slot] = (uint32_t)pidx;
+            }
+            stored = true;
+        }
+        if (len > P.max_path_length || diffuse > kMaxDiffuse) break;
+        U4 bb = rng.block(2 + len);
+        BsdfSample s = b.sample(u01(bb.a), u01(bb.b), u01(bb.c), is.ng);
+        if (is_zero(s.f)) break;
+        F3 f = s.f;
+        if (len > kRRDepth) {
+            if (u01(bb.d) > s.cont) break;
+            f = div_each(f, s.cont);
+        }
+        o = is.pos;
+        d = s.wi;
+        if (s.event & EV_DIFFUSE) diffuse++;
+        tp = tp * f;
+        last = s.event;
+        if (!stored) dVM *= (s.cos_out / s.fwd) * s.rev;
+        else dVM = (s.cos_out / s.fwd) * (1.0f + s.rev * dVM);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_camera_pass(const VMParams P, QueryBuf qb) {
+    long long pix = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int W = P.camera.width, H = P.camera.height;
+    if (pix >= (long long)W * H) return;
+    PathRng rng;
+    rng.init(P.seed, (uint64_t)pix, P.iteration, STREAM_CAMERA);
+    U4 b1 = rng.block(1);
+    // Generate_camera_sample (src/Vertex_Merging.cpp:27-46)
+    const float x = (float)(int)(pix % W);
+    const float y = (float)(int)(pix / W);
+    const float sx = x + u01(b1.b), sy = y + u01(b1.c);
+    // Image_Buffer::add_color (src/Image_Buffer.h:24-37): Y = ResY - (int)y, so camera
+    // row 0 falls outside the buffer and is dropped; its path contributes nothing.
+    if (sx < 0 || sx >= (float)W || sy < 0 || sy >= (float)H) return;
+    const int X = (int)sx, Y = H - (int)sy;
+    const long long target = (long long)X + (long long)Y * W;
+    if (target > (long long)W * H - 1) return;
+    // Camera::get_ray (src/Camera.h:29-34)
+    F3 dir = ld3(P.camera.bottom_left) + ld3(P.camera.horizontal) * (sx / (float)W) +
+             ld3(P.camera.vertical) * (sy / (float)H);
+    dir = dir - ld3(P.camera.origin);
+    F3 o = ld3(P.camera.origin);
+    F3 d = normalize(dir);
+    F3 tp = f3(1.0f);
+    float dVM = 0.0f;
+    for (int len = 0;; ++len) {
+        F3 ro = o + d * kRayEps;
+        HitRec h;
+        if (!scene_hit(P.scene, ro, d, kRayEps, h, P.error + ERR_STACK)) break;
+        Isect is;
+        fill_isect(P.scene, h, ro, d, is);
+        if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); break; }
+        Bsdf b;
+        b.init(P.materials[is.material], is.ns, is.dir, true);
+        if (!b.valid()) break;
+        dVM /= fabsf(b.cos_theta_in());
+        if (!b.is_delta()) {
+            unsigned long long slot = warp_append(qb.count);
+            if (slot < (unsigned long long)qb.capacity) {
+                F3 w = tp * P.vm_norm;
+                qb.q0[slot] = make_float4(is.pos.x, is.pos.y, is.pos.z, dVM);
+                qb.q1[slot] = make_float4(is.ns.x, is.ns.y, is.ns.z, __int_as_float(is.material));
+                qb.q2[slot] = make_float4(is.ng.x, is.ng.y, is.ng.z, __int_as_float((int)target));
+                qb.q3[slot] = make_float4(w.x, w.y, w.z, 0.0f);
+                qb.q4[slot] = make_float4(is.dir.x, is.dir.y, is.dir.z, 0.0f);
+            }
+        }
+        if (len > P.max_path_length) break;
+        U4 bb = rng.block(2 + len);
+        BsdfSample s = b.sample(u01(bb.a), u01(bb.b), u01(bb.c), is.ng);
+        if (is_zero(s.f)) break;
+        F3 f = s.f;
+        if (len > kRRDepth) {
+            if (u01(bb.d) > s.cont) break;
+            f = div_each(f, s.cont);
+        }
+        o = is.pos;
+        d = s.wi;
+        tp = tp * f;
+        if (s.event & EV_SPECULAR) dVM *= (s.cos_out / s.fwd) * s.rev;
+        else dVM = (s.cos_out / s.fwd) * (1.0f + s.rev * dVM);
+    }
+}
+
+__global__ void k_trace_rays(const SceneView S, int n, const float* __restrict__ o, const float* __restrict__ d,
+                             float tmin, float* out_full, unsigned* out_words, int* err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    F3 ro = f3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
+    F3 rd = f3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+    HitRec h;
+    bool hit = scene_hit(S, ro, rd, tmin, h, err);
+    Isect is;
+    if (hit) fill_isect(S, h, ro, rd, is);
+    if (out_words) {
+        unsigned* w = out_words + 8 * i;
+        w[0] = hit ? 1u : 0u;
+        w[1] = __float_as_uint(h.t);
+        w[2] = __float_as_uint(h.u);
+        w[3] = __float_as_uint(h.v);
+        w[4] = hit ? (unsigned)is.tri : 0xffffffffu;
+        w[5] = hit ? (unsigned)is.material : 0xffffffffu;
+        w[6] = hit ? (unsigned)is.mesh : 0xffffffffu;
+        w[7] = 0u;
+    }
+    if (out_full) {
+        float* f = out_full + 16 * i;
+        f[0] = hit ? 1.0f : 0.0f;
+        f[1] = h.t; f[2] = h.u; f[3] = h.v;
+        if (hit) {
+            f[4] = is.ng.x; f[5] = is.ng.y; f[6] = is.ng.z;
+            f[7] = is.ns.x; f[8] = is.ns.y; f[9] = is.ns.z;
+            f[10] = is.pos.x; f[11] = is.pos.y; f[12] = is.pos.z;
+            f[13] = is.front ? 1.0f : 0.0f;
+            f[14] = (float)is.material;
+            f[15] = __int_as_float(is.tri);
+        } else {
+            for (int k = 4; k < 16; ++k) f[k] = 0.0f;
+            f[14] = -1.0f;
+            f[15] = __int_as_float(-1);
+        }
+    }
+}
+
+}  // namespace
+
+void launch_light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s) {
+    long long n = p.num_light_paths;
+    if (n <= 0) return;
+    k_light_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, ph);
+}
+
+void launch_camera_pass(const VMParams& p, QueryBuf qb, cudaStream_t s) {
+    long long n = (long long)p.camera.width * p.camera.height;
+    if (n <= 0) return;
+    k_camera_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, qb);
+}
+
+void launch_trace_rays(const SceneView& sv, int n, const float* o, const float* d, float tmin, float* out_full,
+                       unsigned* out_words, int* err, cudaStream_t st) {
+    if (n <= 0) return;
+    k_trace_rays<<<(n + 127) / 128, 128, 0, st>>>(sv, n, o, d, tmin, out_full, out_words, err);
+}
+
+}  // namespace rc
