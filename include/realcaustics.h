@@ -112,6 +112,18 @@ int rc_set_config(const rc_config* cfg);
  * src/main.cpp:150-168).  Called implicitly by rc_render/main. */
 int rc_prepare(void);
 
+/* Host half of rc_prepare (no GPU needed): BVH build, lights, materials, radius.
+ * info (optional, 9 floats): scene bbox min/max, scene radius, scaled base radius,
+ * number of world BVH nodes - the values the reference computes at src/main.cpp:150-168. */
+int rc_prepare_host(float* info);
+
+/* The host-built BVH of one mesh / of the world in the reference's flattened layout
+ * (CacheBVHNode_mesh / CacheBVHNode_world, src/BVH/BVH_mesh.h:51-71): 8 words per node
+ * (min xyz, max xyz as float bits, the two union words) and the 1-based index list.
+ * Returns the node count (copies at most cap nodes / index_cap indices). */
+int rc_host_mesh_bvh(int mesh, unsigned* nodes, int cap, int* index, int index_cap, float* cost);
+int rc_host_world_bvh(unsigned* nodes, int cap, int* index, int index_cap);
+
 /* Render `iterations` more progressive iterations into the FP64 running mean. */
 int rc_render(int iterations);
 
@@ -144,6 +156,12 @@ int rc_trace_rays(int n, const float* origins, const float* directions, float tm
 /* Same closest hit, with the full hit record as floats (16 per ray, same layout as the
  * oracle): [hit, t, u, v, Ng xyz, Ns xyz, position xyz, front_face, material, tri]. */
 int rc_trace_rays_full(int n, const float* origins, const float* directions, float tmin, float* out);
+
+/* One light pass (iteration `iteration`, current config) on the GPU; copies the stored
+ * photons (Path_Vertex records, src/Path_Vertices.h:10-20), in storage order, as 12
+ * floats each: [position xyz, direction_world xyz, throughput rgb, dVM, light path index
+ * (u32 bits), 0].  *count receives the number stored (may exceed cap). */
+int rc_light_photons(int iteration, float* out, long long cap, long long* count);
 
 /* Build the photon KD-tree on the GPU over n photon positions (3 floats each) and
  * answer q radius queries (squared radius r2): counts[j] = number of photons with

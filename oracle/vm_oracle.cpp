@@ -151,7 +151,7 @@ struct Scene {
     std::vector<Mesh> meshes;
     int W = 0, H = 0;
     V3<float> cam_o, cam_bl, cam_h, cam_v;
-    const unsigned char* py_lights = nullptr;
+    std::vector<unsigned char> py_lights;   // copied at init (the reference borrows them)
     unsigned num_lights = 0;
     std::vector<Material> mats;
     Bvh world;
@@ -979,7 +979,7 @@ int prepare(Scene& s, std::string& err) {
     s.bounds = s.world.bounds;
     s.scene_radius = (s.bounds.mn - (s.bounds.mn + s.bounds.mx) * 0.5f).length();
     // lights (src/Scene.cpp:70-108, src/Lights.cpp:18-119)
-    const unsigned char* pl = s.py_lights;
+    const unsigned char* pl = s.py_lights.data();
     s.lights.clear();
     for (unsigned i = 0; i < s.num_lights; ++i) {
         const unsigned char* r = pl + 64 * (size_t)i;
@@ -1441,7 +1441,8 @@ void oracle_init(int samples, float base_radius, float radius_reduction, long lo
     s.cam_bl = V3<float>(c2.x, c2.y, c2.z);
     s.cam_h = V3<float>(c1.x, c1.y, c1.z) - s.cam_bl;
     s.cam_v = V3<float>(c3.x, c3.y, c3.z) - s.cam_bl;
-    s.py_lights = lights; s.num_lights = number_of_lights;
+    s.py_lights.assign(lights, lights + 64 * (size_t)number_of_lights);
+    s.num_lights = number_of_lights;
     s.mats.clear();
     for (unsigned i = 0; i < number_of_materials; ++i) {
         const unsigned char* r = materials + 28 * (size_t)i;

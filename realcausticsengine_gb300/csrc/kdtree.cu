@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level
 // One warp per node: find the bin holding rank krem, narrow the prefix, clear the
 // histogram for the next pass.  After the last pass, write the node's split.
 __global__ void k_select(long long count, long long first, int level, long long n, NodeSel* sel, uint32_t* hist,
-                         int pass, uint2* nodes) {
+                         int pass, uint2* nodes, int* err) {
     long long t = blockIdx.x * (long long)(blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
     if (t >= count) return;
@@ -233,6 +233,10 @@ __global__ void k_select(long long count, long long first, int level, long long 
     bool mine = (uint32_t)krem >= excl && (uint32_t)krem < incl;
     unsigned bal = __ballot_sync(0xffffffffu, mine);
     int owner = __ffs(bal) - 1;
+    if (owner < 0) {
+        if (lane == 0) atomicOr(err, 1);   // histogram does not hold rank krem
+        return;
+    }
     if (lane == owner) {
         uint32_t cum = excl;
         int bin = 0;
@@ -283,7 +287,7 @@ __device__ __forceinline__ void block_scan6(int (&v)[6], int (&excl)[6], int (&t
 }
 
 __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int level, long long n, long long first,
-                                                        NodeSel* sel, uint2* nodes) {
+                                                        NodeSel* sel, uint2* nodes, int* err) {
     __shared__ ChunkNodes cn;
     __shared__ int ax[2], krem[2], eq[2];
     __shared__ uint32_t med[2];
@@ -349,6 +353,7 @@ __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int 
                     nodes[e].x = idv | odd_mask(ax[w]);
                 } else d = s + k + odd + (r - kl - odd);
             } else d = s + k + odd + (eq[w] - kl - odd) + r;
+            if (d < s || d >= s + c) { atomicOr(err, 2); continue; }   // inconsistent counts
         }
         B.x[dst][d] = xv; B.y[dst][d] = yv; B.z[dst][d] = zv; B.id[dst][d] = idv;
     }
@@ -384,8 +389,8 @@ struct SmemLayout {
     static constexpr size_t tid = tz + 4 * kSmemSeg;
     static constexpr size_t v = tid + 4 * kSmemSeg;               // 2*kSmemSeg uint64 keys
     static constexpr size_t box = v + 8 * 2 * kSmemSeg;           // kSmemSeg/2 * 6 ints
-    static constexpr size_t segs = box + 4 * 6 * (kSmemSeg / 2);  // kSmemSeg/2 starts
-    static constexpr size_t axes = segs + 4 * (kSmemSeg / 2);     // kSmemSeg/2 axes
+    static constexpr size_t segs = box + 4 * 6 * (kSmemSeg / 2);  // sub-node starts: up to kSmemSeg (leaf level)
+    static constexpr size_t axes = segs + 4 * kSmemSeg;           // kSmemSeg/2 axes (levels with >= 2 photons)
     static constexpr size_t total = axes + 4 * (kSmemSeg / 2);
 };
 
@@ -571,7 +576,7 @@ size_t kd_scratch_bytes(long long n) {
 }
 
 int kd_build(const float4* pos4, long long n, KdTree& tree, void* scratch, size_t scratch_bytes,
-             cudaStream_t stream, int* launches) {
+             cudaStream_t stream, int* launches, int* err) {
     int nl = 0;
     tree.n = n;
     if (n <= 0) { tree.levels = 0; tree.num_nodes = 0; if (launches) *launches = 0; return 0; }
@@ -609,10 +614,11 @@ int kd_build(const float4* pos4, long long n, KdTree& tree, void* scratch, size_
         nl += 3;
         for (int pass = 0; pass < 4; ++pass) {
             k_hist<<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, sel, hist, pass);
-            k_select<<<(unsigned)((count + 7) / 8), 256, 0, stream>>>(count, first, l, n, sel, hist, pass, tree.nodes);
+            k_select<<<(unsigned)((count + 7) / 8), 256, 0, stream>>>(count, first, l, n, sel, hist, pass, tree.nodes,
+                                                                       err);
             nl += 2;
         }
-        k_partition<<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, sel, tree.nodes);
+        k_partition<<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, sel, tree.nodes, err);
         nl++;
         cur ^= 1;
     }

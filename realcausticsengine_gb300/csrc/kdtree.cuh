@@ -54,7 +54,9 @@ size_t kd_scratch_bytes(long long n);
 // All buffers are device memory owned by the caller: tree arrays sized for n (nodes:
 // kd_node_array_len(n)), scratch of kd_scratch_bytes(n).  Runs on `stream`.
 long long kd_node_array_len(long long n);
+// err: device int that receives a non-zero flag if the selection or partition finds
+// inconsistent counts (the affected photons are not written).
 int kd_build(const float4* pos4, long long n, KdTree& tree, void* scratch, size_t scratch_bytes,
-             cudaStream_t stream, int* launches);
+             cudaStream_t stream, int* launches, int* err);
 
 }  // namespace rc

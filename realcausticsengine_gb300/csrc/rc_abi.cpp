@@ -191,10 +191,13 @@ int upload_scene(HostScene& sc) {
     return RC_OK;
 }
 
-int prepare() {
+bool g_host_ready = false;
+
+// Host half of the pre-render steps of main() (src/main.cpp:150-168).
+int prepare_host() {
     if (!g_scene) { g_err = "no scene: init() was not called"; return RC_E_NO_SCENE; }
     HostScene& sc = *g_scene;
-    if (sc.prepared) return RC_OK;
+    if (g_host_ready) return RC_OK;
     if (sc.meshes.empty()) { g_err = "scene has no meshes"; return RC_E_INVALID; }
     // Scene::update_bvh (src/Scene.cpp:110-152)
     for (HostMesh& m : sc.meshes) build_mesh_bvh(m);
@@ -205,6 +208,15 @@ int prepare() {
     convert_materials(sc);
     // base_radius *= SceneRadius (src/main.cpp:166-168)
     sc.base_radius *= sc.scene_radius;
+    g_host_ready = true;
+    return RC_OK;
+}
+
+int prepare() {
+    int r = prepare_host();
+    if (r) return r;
+    HostScene& sc = *g_scene;
+    if (sc.prepared) return RC_OK;
     r = upload_scene(sc);
     if (r) return r;
     sc.prepared = true;
@@ -216,6 +228,7 @@ int check_errors() {
     RC_CUDA(cudaMemcpy(h, g_dev.errors.p, sizeof(h), cudaMemcpyDeviceToHost));
     if (h[ERR_STACK]) { g_err = "BVH traversal stack overflow (depth > 64)"; return RC_E_CAPACITY; }
     if (h[ERR_MATERIAL]) { g_err = "triangle material index out of range"; return RC_E_INVALID; }
+    if (h[ERR_KD]) { g_err = "KD-tree build found inconsistent counts"; return RC_E_INVALID; }
     return RC_OK;
 }
 
@@ -300,7 +313,7 @@ int render_iteration(HostScene& sc) {
     tree.nodes = d.kd_nodes.p; tree.x = d.kd_x.p; tree.y = d.kd_y.p; tree.z = d.kd_z.p; tree.id = d.kd_id.p;
     int kd_launches = 0;
     RC_CUDA(cudaEventRecord(d.ev[2], s));
-    if (kd_build(d.ph_pos.p, n, tree, d.kd_scratch.p, d.kd_scratch.n, s, &kd_launches)) {
+    if (kd_build(d.ph_pos.p, n, tree, d.kd_scratch.p, d.kd_scratch.n, s, &kd_launches, d.errors.p + ERR_KD)) {
         g_err = "KD scratch too small"; return RC_E_CAPACITY;
     }
     RC_CUDA(cudaGetLastError());
@@ -425,6 +438,19 @@ int read_image(float* rgb, int w, int h) {
 void release_all() {
     g_dev.release();
     g_scene.reset();
+    g_host_ready = false;
+}
+
+int dump_bvh(const std::vector<BvhNode>& nodes, const std::vector<int>& index, unsigned* out, int cap, int* idx, int idx_cap) {
+    int n = (int)nodes.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        float f[6] = {nodes[i].box.mn.x, nodes[i].box.mn.y, nodes[i].box.mn.z, nodes[i].box.mx.x, nodes[i].box.mx.y, nodes[i].box.mx.z};
+        std::memcpy(out + 8 * i, f, 24);
+        out[8 * i + 6] = nodes[i].w0;
+        out[8 * i + 7] = nodes[i].w1;
+    }
+    for (int i = 0; i < (int)index.size() && i < idx_cap; ++i) idx[i] = index[i];
+    return n;
 }
 
 }  // namespace
@@ -515,6 +541,34 @@ int rc_set_config(const rc_config* c) {
 
 int rc_prepare(void) { return prepare(); }
 
+int rc_prepare_host(float* info) {
+    int r = prepare_host();
+    if (r) return r;
+    const HostScene& sc = *g_scene;
+    if (info) {
+        info[0] = sc.bounds.mn.x; info[1] = sc.bounds.mn.y; info[2] = sc.bounds.mn.z;
+        info[3] = sc.bounds.mx.x; info[4] = sc.bounds.mx.y; info[5] = sc.bounds.mx.z;
+        info[6] = sc.scene_radius; info[7] = sc.base_radius; info[8] = (float)sc.world.nodes.size();
+    }
+    return RC_OK;
+}
+
+int rc_host_mesh_bvh(int mesh, unsigned* nodes, int cap, int* index, int index_cap, float* cost) {
+    int r = prepare_host();
+    if (r) return r;
+    if (mesh < 0 || mesh >= (int)g_scene->meshes.size() || !nodes || !index) { g_err = "bad mesh index"; return RC_E_INVALID; }
+    const MeshBvh& b = g_scene->meshes[mesh].bvh;
+    if (cost) *cost = b.cost;
+    return dump_bvh(b.nodes, b.index, nodes, cap, index, index_cap);
+}
+
+int rc_host_world_bvh(unsigned* nodes, int cap, int* index, int index_cap) {
+    int r = prepare_host();
+    if (r) return r;
+    if (!nodes || !index) { g_err = "null output"; return RC_E_INVALID; }
+    return dump_bvh(g_scene->world.nodes, g_scene->world.index, nodes, cap, index, index_cap);
+}
+
 int rc_render(int iterations) {
     if (iterations < 0) { g_err = "iterations < 0"; return RC_E_INVALID; }
     int r = prepare();
@@ -534,6 +588,53 @@ const char* rc_last_error(void) { return g_err.c_str(); }
 int rc_get_stats(double* out, int n) {
     if (!out || n < 0) return RC_E_INVALID;
     for (int i = 0; i < n && i < 16; ++i) out[i] = g_dev.stats[i];
+    return RC_OK;
+}
+
+int rc_light_photons(int iteration, float* out, long long cap, long long* count) {
+    int r = prepare();
+    if (r) return r;
+    if (iteration < 0 || (cap > 0 && !out)) { g_err = "bad photon output"; return RC_E_INVALID; }
+    HostScene& sc = *g_scene;
+    DeviceState& d = g_dev;
+    cudaStream_t s = d.stream;
+    VMParams p = make_params(sc, iteration);
+    long long pcap = std::max<long long>(p.num_light_paths * 2, 1024);
+    unsigned long long nph = 0;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        RC_CUDA(d.ph_pos.reserve(pcap)); RC_CUDA(d.ph_dir.reserve(pcap));
+        RC_CUDA(d.ph_tp.reserve(pcap)); RC_CUDA(d.ph_path.reserve(pcap));
+        RC_CUDA(d.counters.reserve(4));
+        RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
+        PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, (long long)d.ph_pos.n, d.counters.p};
+        launch_light_pass(p, ph, s);
+        RC_CUDA(cudaGetLastError());
+        RC_CUDA(cudaMemcpyAsync(&nph, d.counters.p, sizeof(nph), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(cudaStreamSynchronize(s));
+        if ((long long)nph <= (long long)d.ph_pos.n) break;
+        pcap = (long long)nph + 1024;
+    }
+    r = check_errors();
+    if (r) return r;
+    if (count) *count = (long long)nph;
+    long long n = std::min<long long>((long long)nph, cap);
+    if (n > 0) {
+        std::vector<float4> pos(n), dir(n);
+        std::vector<float2> tp(n);
+        std::vector<uint32_t> path(n);
+        RC_CUDA(cudaMemcpy(pos.data(), d.ph_pos.p, 16 * n, cudaMemcpyDeviceToHost));
+        RC_CUDA(cudaMemcpy(dir.data(), d.ph_dir.p, 16 * n, cudaMemcpyDeviceToHost));
+        RC_CUDA(cudaMemcpy(tp.data(), d.ph_tp.p, 8 * n, cudaMemcpyDeviceToHost));
+        RC_CUDA(cudaMemcpy(path.data(), d.ph_path.p, 4 * n, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < n; ++i) {
+            float* w = out + 12 * i;
+            w[0] = pos[i].x; w[1] = pos[i].y; w[2] = pos[i].z;
+            w[3] = dir[i].x; w[4] = dir[i].y; w[5] = dir[i].z;
+            w[6] = dir[i].w; w[7] = tp[i].x; w[8] = tp[i].y; w[9] = pos[i].w;
+            std::memcpy(&w[10], &path[i], 4);
+            w[11] = 0.0f;
+        }
+    }
     return RC_OK;
 }
 
@@ -577,6 +678,9 @@ int rc_trace_rays_full(int n, const float* origins, const float* directions, flo
 static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, DevBuf<uint2>& nodes, DevBuf<float>& x,
                          DevBuf<float>& y, DevBuf<float>& z, DevBuf<uint32_t>& id, DevBuf<unsigned char>& scratch,
                          KdTree& tree, cudaStream_t s) {
+    DevBuf<int> err;
+    RC_CUDA(err.reserve(1));
+    RC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
     std::vector<float4> p4((size_t)n);
     for (int i = 0; i < n; ++i) p4[i] = make_float4(positions[3 * i], positions[3 * i + 1], positions[3 * i + 2], 0.0f);
     RC_CUDA(pos.reserve(std::max(n, 1)));
@@ -587,8 +691,13 @@ static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, Dev
     RC_CUDA(z.reserve(std::max(n, 1))); RC_CUDA(id.reserve(std::max(n, 1)));
     RC_CUDA(scratch.reserve(kd_scratch_bytes(n)));
     tree.nodes = nodes.p; tree.x = x.p; tree.y = y.p; tree.z = z.p; tree.id = id.p;
-    if (kd_build(pos.p, n, tree, scratch.p, scratch.n, s, nullptr)) { g_err = "KD scratch"; return RC_E_CAPACITY; }
+    if (kd_build(pos.p, n, tree, scratch.p, scratch.n, s, nullptr, err.p)) { g_err = "KD scratch"; return RC_E_CAPACITY; }
     RC_CUDA(cudaGetLastError());
+    int h = 0;
+    RC_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RC_CUDA(cudaStreamSynchronize(s));
+    err.release();
+    if (h) { g_err = "KD-tree build found inconsistent counts"; return RC_E_INVALID; }
     return RC_OK;
 }
 

@@ -63,7 +63,7 @@ struct VMParams {
 };
 
 // error flag slots
-enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_COUNT = 8 };
+enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_KD = 4, ERR_COUNT = 8 };
 
 void launch_light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s);
 void launch_camera_pass(const VMParams& p, QueryBuf qb, cudaStream_t s);

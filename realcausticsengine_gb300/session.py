@@ -1,0 +1,118 @@
+"""Host-side session over the C ABI, shaped like the Blender add-on's use of the
+reference DLL: init(...) with the scene's Blender data, then render, then read the
+image.  All work runs in librealcaustics.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._native import check, lib
+from .scene import InitArgs, Scene
+
+STAT_NAMES = ["light_paths", "photons", "queries", "merged", "light_ms", "kd_ms", "camera_ms", "gather_ms",
+              "accum_ms", "device_ms", "iterations", "scene_radius", "radius", "launches"]
+
+
+class Renderer:
+    """One scene loaded into the library (the library holds one scene at a time,
+    like the reference's global `scene`)."""
+
+    def __init__(self, scene: Scene, max_path_length: int = 6, photons_per_iter: int = 0, seed: int = 0,
+                 sampler: int = abi.SAMPLER_UNIFORM, verbose: bool = False):
+        self.scene = scene
+        self.L = lib()
+        cfg = abi.RcConfig()
+        check(self.L.rc_default_config(C.byref(cfg)), "rc_default_config")
+        cfg.max_path_length = max_path_length
+        cfg.photons_per_iter = photons_per_iter
+        cfg.seed = seed
+        cfg.sampler = sampler
+        cfg.write_exr = 0
+        cfg.verbose = int(verbose)
+        check(self.L.rc_set_config(C.byref(cfg)), "rc_set_config")
+        self.args = InitArgs(scene)
+        self.args.call(self.L.init)
+        err = self.L.rc_last_error().decode()
+        if err:
+            raise RuntimeError(f"init failed: {err}")
+
+    def prepare(self):
+        check(self.L.rc_prepare(), "rc_prepare")
+
+    def prepare_host(self) -> np.ndarray:
+        info = (C.c_float * 9)()
+        check(self.L.rc_prepare_host(info), "rc_prepare_host")
+        return np.array(info, np.float32)
+
+    def render(self, iterations: int):
+        check(self.L.rc_render(int(iterations)), "rc_render")
+
+    def image(self) -> np.ndarray:
+        W, H = self.scene.camera.width, self.scene.camera.height
+        out = np.zeros((H, W, 3), np.float32)
+        check(self.L.rc_read_image(out.ctypes.data, W, H), "rc_read_image")
+        return out
+
+    def stats(self) -> dict:
+        a = np.zeros(16, np.float64)
+        check(self.L.rc_get_stats(a.ctypes.data, 16), "rc_get_stats")
+        return dict(zip(STAT_NAMES, a.tolist()))
+
+    def trace(self, origins: np.ndarray, dirs: np.ndarray, tmin: float = 0.001) -> np.ndarray:
+        o = np.ascontiguousarray(origins, np.float32)
+        d = np.ascontiguousarray(dirs, np.float32)
+        n = len(o)
+        out = np.zeros((n, 16), np.float32)
+        check(self.L.rc_trace_rays_full(n, o.ctypes.data, d.ctypes.data, C.c_float(tmin), out.ctypes.data),
+              "rc_trace_rays_full")
+        return out
+
+    def light_photons(self, iteration: int) -> np.ndarray:
+        n = C.c_longlong()
+        check(self.L.rc_light_photons(int(iteration), None, 0, C.byref(n)), "rc_light_photons")
+        out = np.zeros((max(n.value, 1), 12), np.float32)
+        check(self.L.rc_light_photons(int(iteration), out.ctypes.data, n.value, C.byref(n)), "rc_light_photons")
+        return out[: n.value]
+
+    def host_mesh_bvh(self, mesh: int, cap: int = 1 << 22):
+        nodes = np.zeros((cap, 8), np.uint32)
+        idx = np.zeros(cap + 1, np.int32)
+        cost = C.c_float()
+        n = self.L.rc_host_mesh_bvh(mesh, nodes.ctypes.data, cap, idx.ctypes.data, cap + 1, C.byref(cost))
+        if n < 0:
+            check(n, "rc_host_mesh_bvh")
+        return nodes[:n], cost.value
+
+    def release(self):
+        self.L.rc_release()
+
+
+def kd_query(positions: np.ndarray, queries: np.ndarray, r2: float, with_indices: bool = True):
+    """GPU KD-tree radius query on caller-chosen photons: (counts, [index arrays])."""
+    L = lib()
+    p = np.ascontiguousarray(positions, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    counts = np.zeros(len(q), np.int32)
+    total = C.c_longlong()
+    check(L.rc_kd_query(len(p), p.ctypes.data, len(q), q.ctypes.data, C.c_float(r2), counts.ctypes.data, None, 0,
+                        C.byref(total)), "rc_kd_query")
+    if not with_indices:
+        return counts, None
+    idx = np.zeros(max(total.value, 1), np.int32)
+    check(L.rc_kd_query(len(p), p.ctypes.data, len(q), q.ctypes.data, C.c_float(r2), counts.ctypes.data,
+                        idx.ctypes.data, len(idx), C.byref(total)), "rc_kd_query")
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    return counts, [idx[offs[j]:offs[j + 1]] for j in range(len(q))]
+
+
+def kd_build_nodes(positions: np.ndarray) -> np.ndarray:
+    L = lib()
+    p = np.ascontiguousarray(positions, np.float32)
+    nn = C.c_longlong()
+    check(L.rc_kd_build_nodes(len(p), p.ctypes.data, None, 0, C.byref(nn)), "rc_kd_build_nodes")
+    out = np.zeros((max(nn.value, 1), 2), np.uint32)
+    check(L.rc_kd_build_nodes(len(p), p.ctypes.data, out.ctypes.data, nn.value, C.byref(nn)), "rc_kd_build_nodes")
+    return out[:nn.value]

@@ -1,0 +1,290 @@
+"""GPU parity: the sm_103a kernels through the C ABI against the reference's golden
+outputs and the CPU oracle (which the other tests pin to the reference).
+
+Bit-exact: closest hits (t, u, v, Ng, Ns, position, front face, material, triangle
+id) and KD radius sets (photon index sets).  Tolerance-based: photon records of a
+light pass (same counter-based samples; the kernels' sinf/cosf/acosf differ from the
+C library's by a few ulps, so a few paths drift) and rendered images (relative RMSE
+thresholds written at each test).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from realcausticsengine_gb300 import scenes
+from realcausticsengine_gb300.scene import InitArgs
+from realcausticsengine_gb300.session import Renderer, kd_build_nodes, kd_query
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_scene(orc, sc):
+    args = InitArgs(sc)
+    args.call(orc.oracle_init)
+    assert orc.oracle_prepare(None) == 0
+    return args
+
+
+def _oracle_trace(orc, o, d, tmin=0.001):
+    out = np.zeros((len(o), 16), np.float32)
+    orc.oracle_trace(len(o), o.ctypes.data, d.ctypes.data, C.c_float(tmin), out.ctypes.data, 32)
+    return out
+
+
+def _random_rays(rng, n, lo=-4.0, hi=4.0, zlo=0.2, zhi=5.0, aim=None):
+    o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    o[:, 2] = rng.uniform(zlo, zhi, n)
+    d = rng.normal(size=(n, 3))
+    if aim is not None:
+        t = rng.uniform(aim[0], aim[1], (n // 2, 3))
+        d[: n // 2] = t - o[: n // 2]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return o, d.astype(np.float32)
+
+
+def test_closest_hits_golden(golden):
+    sc = scenes.test_scene(48, 36, subdiv=2, samples=2)
+    r = Renderer(sc)
+    got = r.trace(golden["ray_o"], golden["ray_d"])
+    want = golden["ray_hits"]
+    r.release()
+    assert (got[:, :15].view(np.uint32) == want[:, :15].view(np.uint32)).all()
+
+
+@pytest.mark.parametrize("name", ["test_scene", "sun_scene", "glass_sphere", "water"])
+def test_closest_hits_vs_oracle(orc, name):
+    rng = np.random.default_rng(11)
+    if name == "test_scene":
+        sc, aim = scenes.test_scene(32, 24, subdiv=3), (-2.5, 2.5)
+    elif name == "sun_scene":
+        sc, aim = scenes.sun_scene(), (-2.5, 2.5)
+    elif name == "glass_sphere":
+        sc, aim = scenes.glass_sphere_point(32, 32, subdiv=5), (-1.0, 1.0)
+    else:
+        sc, aim = scenes.water_pool(32, 18, grid=96), (-4.0, 4.0)
+    n = 60000
+    o, d = _random_rays(rng, n, aim=aim)
+    if name == "water":
+        o[:, 2] = rng.uniform(-1.4, 3.0, n)
+    r = Renderer(sc)
+    got = r.trace(o, d)
+    r.release()
+    _oracle_scene(orc, sc)
+    want = _oracle_trace(orc, o, d)
+    assert want[:, 0].sum() > n * 0.3
+    mism = (got.view(np.uint32) != want.view(np.uint32)).any(1)
+    assert not mism.any(), f"{int(mism.sum())} of {n} rays differ"
+
+
+@pytest.mark.parametrize("k", range(5))
+def test_kd_sets_golden(golden, k):
+    pos, q, r2 = golden[f"kd{k}_pos"], golden[f"kd{k}_q"], float(golden[f"kd{k}_r2"][0])
+    counts, sets = kd_query(pos, q, r2)
+    assert (counts == golden[f"kd{k}_counts"]).all()
+    wi = golden[f"kd{k}_idx"]
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    for j in range(len(q)):
+        assert sorted(sets[j].tolist()) == sorted(wi[offs[j]:offs[j + 1]].tolist())
+
+
+def _oracle_kd(orc, pos, q, r2):
+    cnt = np.zeros(len(q), np.int32)
+    cap = int(len(q) * 4096)
+    idx = np.zeros(cap, np.int32)
+    tot = orc.oracle_kd_query(len(pos), pos.ctypes.data, len(q), q.ctypes.data, C.c_float(r2), cnt.ctypes.data,
+                              idx.ctypes.data, cap)
+    assert tot <= cap
+    offs = np.concatenate([[0], np.cumsum(cnt)])
+    return cnt, [np.sort(idx[offs[j]:offs[j + 1]]) for j in range(len(q))]
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 3, 4, 2047, 2048, 2049, 4097, 65537, 1000003])
+def test_kd_sets_vs_oracle(orc, n):
+    rng = np.random.default_rng(n + 5)
+    pos = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    if n > 100:
+        pos[: n // 8] = np.round(pos[: n // 8] * 16) / 16          # tied coordinates
+        pos[n // 8: n // 6] = pos[0]                                # duplicated photons
+        pos[n // 6: n // 5, 2] = 0.25                               # a flat sheet
+    q = rng.uniform(-1.05, 1.05, (3000, 3)).astype(np.float32)
+    q[:100] = pos[:100] if n >= 100 else q[:100]                    # queries on photons
+    r = 0.04 if n < 100000 else 0.012
+    r2 = float(np.float32(r * r))
+    counts, sets = kd_query(pos, q, r2)
+    ocnt, osets = _oracle_kd(orc, pos, q, r2)
+    assert (counts == ocnt).all()
+    for j in range(len(q)):
+        assert (np.sort(sets[j]) == osets[j]).all()
+
+
+def test_kd_nodes_reference_format():
+    rng = np.random.default_rng(3)
+    for n in [1, 2, 5, 1000, 4099, 70001]:
+        pos = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+        nodes = kd_build_nodes(pos)
+        L = int(np.floor(np.log2(n)))
+        assert len(nodes) >= 2 ** (L + 1)
+        seen = np.zeros(n, np.int64)
+
+        # walk the implicit heap (root 1, children 2e / 2e+1, every node on level l
+        # holds n >> l photons); check flags, split planes and that every photon
+        # appears exactly once
+        def walk(e, level, lo, hi):
+            c = n >> level
+            word, split_bits = int(nodes[e, 0]), int(nodes[e, 1])
+            if c < 2:
+                assert word & 0x80000000 == 0
+                seen[word] += 1
+                p = pos[word]
+                assert (p >= lo).all() and (p <= hi).all()
+                return
+            assert word & 0x80000000
+            ax = {0: 0, 0x20000000: 1, 0x60000000: 2}[word & 0x60000000]
+            split = np.frombuffer(np.uint32(split_bits).tobytes(), np.float32)[0]
+            if c & 1:
+                assert word & 0x10000000
+                i = word & 0x0FFFFFFF
+                seen[i] += 1
+                assert pos[i, ax] == split
+            lo2, hi2 = lo.copy(), hi.copy()
+            hi2[ax] = min(hi2[ax], split)
+            lo2[ax] = max(lo2[ax], split)   # even nodes: split = median + 1.175494e-38f
+            walk(2 * e, level + 1, lo, hi2)
+            walk(2 * e + 1, level + 1, lo2, hi)
+
+        import sys
+        sys.setrecursionlimit(10000)
+        walk(1, 0, np.full(3, -np.inf, np.float32), np.full(3, np.inf, np.float32))
+        assert (seen == 1).all()
+
+
+def test_light_pass_vs_oracle(orc):
+    sc = scenes.test_scene(32, 24, subdiv=2)
+    paths, seed = 40000, 5
+    r = Renderer(sc, max_path_length=6, photons_per_iter=paths, seed=seed)
+    gpu = r.light_photons(3)
+    r.release()
+    _oracle_scene(orc, sc)
+    cap = paths * 8
+    out = np.zeros((cap, 12), np.float32)
+    n = orc.oracle_light_photons(3, seed, paths, 6, out.ctypes.data, cap, 8)
+    cpu = out[:n]
+    assert abs(len(gpu) - n) <= 0.01 * n
+    gp = gpu[:, 10].view(np.uint32)
+    cp = cpu[:, 10].view(np.uint32)
+    order = np.lexsort((gpu[:, 2], gpu[:, 1], gpu[:, 0], gp))
+    gpu, gp = gpu[order], gp[order]
+    # per light path, the stored photons (in path order on the oracle side)
+    g_by = {}
+    for i, p in enumerate(gp):
+        g_by.setdefault(int(p), []).append(i)
+    c_by = {}
+    for i, p in enumerate(cp):
+        c_by.setdefault(int(p), []).append(i)
+    same = 0
+    for p, ci in c_by.items():
+        gi = g_by.get(p, [])
+        if len(gi) == len(ci):
+            a = cpu[ci][:, :10]
+            b = gpu[gi][:, :10]
+            b = b[np.lexsort((b[:, 2], b[:, 1], b[:, 0]))]
+            a = a[np.lexsort((a[:, 2], a[:, 1], a[:, 0]))]
+            if np.allclose(a, b, rtol=1e-3, atol=1e-4):
+                same += 1
+    frac = same / max(len(c_by), 1)
+    assert frac > 0.98, f"only {frac:.4f} of light paths agree"
+
+
+def _rel_rmse(a, b):
+    return float(np.sqrt(np.mean((a - b) ** 2)) / max(np.sqrt(np.mean(b ** 2)), 1e-30))
+
+
+def test_render_vs_oracle_same_samples(orc):
+    """Same seed and iterations: GPU FP32 against oracle FP32 and FP64.  Both use the
+    same primary samples, so differences come from rounding only (plus paths that
+    drift after a transcendental differs by an ulp): relative RMSE < 3%."""
+    sc = scenes.test_scene(48, 36, subdiv=2)
+    paths, seed, iters = 30000, 9, 3
+    r = Renderer(sc, max_path_length=6, photons_per_iter=paths, seed=seed)
+    r.render(iters)
+    img = r.image().reshape(-1)
+    st = r.stats()
+    r.release()
+    assert st["photons"] > 0 and st["queries"] > 0
+    for prec in (32, 64):
+        _oracle_scene(orc, sc)
+        acc = np.zeros(img.size, np.float64)
+        assert orc.oracle_render_plain(0, iters, prec, seed, paths, 6, 8, acc.ctypes.data, None) == 0
+        ref = acc / iters
+        rel = _rel_rmse(img, ref)
+        print(f"FP{prec}: rel RMSE {rel:.3e}, mean ratio {img.mean() / ref.mean():.5f}")
+        assert rel < 0.03
+
+
+def test_main_writes_exr_like_reference(tmp_path, monkeypatch):
+    """init() + main(): renders `samples` iterations and writes the EXR the add-on reads."""
+    from realcausticsengine_gb300 import _native, abi
+    lib = _native.lib()
+    monkeypatch.chdir(tmp_path)
+    sc = scenes.test_scene(40, 30, subdiv=2, samples=2)
+    cfg = abi.RcConfig()
+    lib.rc_default_config(C.byref(cfg))
+    cfg.photons_per_iter = 20000
+    lib.rc_set_config(C.byref(cfg))
+    args = InitArgs(sc)
+    args.call(lib.init)
+    assert lib.main() == 0, lib.rc_last_error()
+    exr = tmp_path / "D:\\caustics.exr"
+    assert exr.exists()
+    data = exr.read_bytes()
+    assert data[:4] == bytes([0x76, 0x2F, 0x31, 0x01])
+    # same render through the additive API
+    r = Renderer(sc, photons_per_iter=20000)
+    r.render(2)
+    img = r.image()
+    r.release()
+    W, H = 40, 30
+    p, attrs = 8, {}
+    while data[p] != 0:
+        e = data.index(b"\0", p); name = data[p:e].decode(); p = e + 1
+        e = data.index(b"\0", p); typ = data[p:e].decode(); p = e + 1
+        size = int.from_bytes(data[p:p + 4], "little"); p += 4
+        attrs[name] = (typ, data[p:p + size]); p += size
+    p += 1
+    assert attrs["compression"][1] == b"\x00" and attrs["channels"][0] == "chlist"
+    offs = np.frombuffer(data[p: p + 8 * H], np.uint64)
+    rows = []
+    for y in range(H):
+        o = int(offs[y])
+        assert np.frombuffer(data[o:o + 4], np.int32)[0] == y
+        px = np.frombuffer(data[o + 8: o + 8 + 12 * W], np.float32).reshape(3, W)
+        rows.append(np.stack([px[2], px[1], px[0]], -1))   # channels stored B, G, R
+    exr_img = np.stack(rows)
+    assert np.allclose(exr_img, img, rtol=1e-5, atol=1e-7)
+    assert img[0].sum() == 0.0            # the reference's add_color never writes row 0
+    assert img.sum() > 0
+
+
+def test_point_and_sun_lights_render():
+    for sc in (scenes.glass_sphere_point(32, 32, subdiv=3, samples=1), scenes.sun_scene(32, 24)):
+        r = Renderer(sc, max_path_length=8, photons_per_iter=50000, seed=1)
+        r.render(2)
+        img = r.image()
+        st = r.stats()
+        r.release()
+        assert np.isfinite(img).all() and img.sum() > 0, sc.name
+        assert st["photons"] > 0
+
+
+def test_no_photons_is_not_an_error():
+    """A scene with no glossy surface stores no photons (the reference crashes there)."""
+    sc = scenes.test_scene(24, 16, subdiv=1)
+    for m in sc.materials:
+        m.kind, m.roughness, m.specular = "P", 1.0, 0.0
+    r = Renderer(sc, photons_per_iter=5000)
+    r.render(1)
+    st = r.stats()
+    img = r.image()
+    r.release()
+    assert st["photons"] == 0 and (img == 0).all()
