@@ -1,0 +1,292 @@
+"""Benchmark: photons/s of progressive vertex-merging iterations on the water-pool
+workload (512x512-vertex water heightfield, GGX dielectric roughness 0.02 IOR 1.33,
+diffuse floor 1.5 below, 2x2 area light, 1920x1080, 16M photons per iteration, max
+path depth 8), one JSON line on stdout.
+
+A step is one progressive iteration: light pass (16M light paths, photon store), GPU
+KD-tree build over the stored photons, camera pass (one path per pixel, merge
+queries), radius gather with FP64 accumulation.
+
+  value   photons/s with the scene already resident in HBM (device-timed with CUDA
+          events recorded by the library on its stream around the K steps)
+  e2e     photons/s through the public C ABI with host buffers: init() from the
+          Blender-layout host arrays, BVH build, upload, and per step one iteration
+          plus the image read back to host memory
+  roofline  the gather kernel (HBM-bound): algorithmic bytes per launch / its mean
+          event-timed duration, against MEASURED_PEAKS.json hbm_gbs
+  cpu_baseline  the reference's own estimator on the host cores (oracle port of the
+          reference, bit-identical to it on the reference-renderable variant)
+
+--impl reference times that CPU implementation alone.  --gpus N > 1 runs N
+independent replicas (the path is not sharded; torchrun launches one rank per GPU).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = "water_pool"
+PHOTONS_PER_ITER = 16 << 20
+MAX_PATH = 8
+METRIC = "photons/s"
+# bytes per unit of the gather (algorithmic): photon record read once, query record
+# read once, FP64 RGB pixel read+write once per query
+PHOTON_BYTES, QUERY_BYTES, PIXEL_BYTES = 40, 80, 48
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = Path(tempfile.mkdtemp()) / "clocks.csv"
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        if self.path.exists():
+            for line in self.path.read_text().splitlines():
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 7:
+                    try:
+                        rows.append((float(parts[0]), float(parts[1]), float(parts[2]), parts[3:7]))
+                    except ValueError:
+                        pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(seconds: float = 12.0, cores: int | None = None):
+    """The reference's own estimator (oracle port, reference mode: its RNG stream, its
+    hybrid Metropolis light sampler, its KD-tree) on the water scene's nearest
+    reference-renderable variant (smooth glass instead of the rough dielectric, depth
+    6, photons per iteration = pixels), one process per core, each rendering one
+    iteration of a reduced-resolution frame; photons/s summed over processes."""
+    cores = cores or os.cpu_count() or 1
+    W, H = 960, 540
+    code = f"""
+import sys, time, numpy as np, ctypes as C
+sys.path.insert(0, {str(ROOT)!r})
+import oracle
+from realcausticsengine_gb300 import scenes
+from realcausticsengine_gb300.scene import InitArgs
+sc = scenes.water_pool({W}, {H}, grid=512, samples=1)
+sc.materials[0].kind = 'G'
+o = oracle.oracle()
+a = InitArgs(sc); a.call(o.oracle_init); o.oracle_prepare(None)
+img = np.zeros(3*{W}*{H}, np.float32)
+t = time.perf_counter(); o.oracle_render_reference(img.ctypes.data, 1); dt = time.perf_counter() - t
+print(dt)
+"""
+    import oracle
+    oracle.build()
+    procs = [subprocess.Popen([sys.executable, "-c", code], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL)
+             for _ in range(cores)]
+    times = []
+    for p in procs:
+        out, _ = p.communicate()
+        try:
+            times.append(float(out.decode().strip().splitlines()[-1]))
+        except (ValueError, IndexError):
+            pass
+    if not times:
+        return None
+    photons_each = W * H
+    value = sum(photons_each / t for t in times)
+    return {"value": value, "unit": METRIC, "cores": len(times), "kind": "port",
+            "sample": f"water_pool variant (smooth glass, depth 6) {W}x{H}, {photons_each} light paths + "
+                      f"{photons_each} camera paths per process, 1 iteration, {len(times)} processes; "
+                      f"mean {np.mean(times):.2f} s per process"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(cores=args.cpu_cores)
+    t0 = time.perf_counter()
+    last = None
+    for _ in range(args.steps):
+        last = cpu_baseline(cores=args.cpu_cores)
+        vals.append(last["value"])
+    dt = time.perf_counter() - t0
+    v = float(np.mean(vals))
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * dt / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD + " (reference-renderable variant)", "parallelism": "processes"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": last["cores"], "kind": last["kind"],
+                             "sample": last["sample"]},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    from realcausticsengine_gb300 import _native, scenes
+    from realcausticsengine_gb300.scene import InitArgs
+    from realcausticsengine_gb300.session import Renderer
+    from realcausticsengine_gb300 import abi
+
+    rank, world, local = dist_env()
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+    lib = _native.lib()
+    sc = scenes.water_pool(args.width, args.height, grid=args.grid, samples=args.steps)
+    paths = args.photons
+
+    # ---- device-resident throughput
+    r = Renderer(sc, max_path_length=MAX_PATH, photons_per_iter=paths, seed=rank)
+    r.prepare()
+    r.render(args.warmup)
+    dev = np.zeros(4, np.float64)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        _native.check(lib.rc_render_timed(args.steps, dev.ctypes.data), "rc_render_timed")
+        wall = time.perf_counter() - t0
+    st = r.stats()
+    device_ms = dev[0]
+    gather_ms_mean, gather_bytes, nq, nph = dev[1], dev[2], st["queries"], st["photons"]
+    value_rank = paths * args.steps / (device_ms / 1000.0)
+    r.release()
+
+    # ---- end to end through the C ABI with host buffers
+    cfg = abi.RcConfig()
+    lib.rc_default_config(C.byref(cfg))
+    cfg.max_path_length = MAX_PATH
+    cfg.photons_per_iter = paths
+    cfg.seed = rank
+    cfg.write_exr = 0
+    lib.rc_set_config(C.byref(cfg))
+    img = np.zeros((args.height, args.width, 3), np.float32)
+    t0 = time.perf_counter()
+    ia = InitArgs(sc)
+    ia.call(lib.init)
+    _native.check(lib.rc_prepare(), "rc_prepare")
+    for _ in range(args.steps):
+        _native.check(lib.rc_render(1), "rc_render")
+        _native.check(lib.rc_read_image(img.ctypes.data, args.width, args.height), "rc_read_image")
+    e2e_s = time.perf_counter() - t0
+    lib.rc_release()
+    h2d = sum(m.verts.nbytes + m.normals.nbytes + m.tris.nbytes for m in sc.meshes)
+    d2h = args.width * args.height * 3 * 8
+    e2e_rank = paths * args.steps / e2e_s
+
+    vals = [value_rank]
+    e2es = [e2e_rank]
+    dms = [device_ms]
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        t = torch.tensor([device_ms, e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        device_ms, e2e_s = t.tolist()
+        vals = [paths * args.steps * world / (device_ms / 1000.0)]
+        e2es = [paths * args.steps * world / e2e_s]
+        dms = [device_ms]
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    achieved = gather_bytes / (gather_ms_mean / 1000.0) / 1e9 if gather_ms_mean > 0 else 0.0
+    traffic = None
+    tp = ROOT / "profiles" / "gather_traffic.json"
+    if tp.exists():
+        traffic = json.loads(tp.read_text()).get("bytes_per_launch")
+    line = {
+        "metric": METRIC, "value": float(vals[0]) if world == 1 else float(vals[0]), "unit": METRIC,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dms[0] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{WORKLOAD} {args.width}x{args.height}, {args.grid}x{args.grid}-vertex heightfield "
+                               f"({sc.num_tris()} tris), {paths} photons/iter, max depth {MAX_PATH}",
+                   "photons_per_iter": paths, "stored_photons_per_iter": nph, "merge_queries_per_iter": nq,
+                   "l2": "inputs larger than L2 (photon map and query buffers > 129 MB)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": float(e2es[0]), "unit": METRIC, "h2d_bytes_per_step": int(h2d // max(args.steps, 1)),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"kernel": "k_gather", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": gather_bytes},
+        "gpu_launches": int(dev[3]),
+        "clocks": clk.summary(),
+        "phase_ms_per_step": {k: st[k] for k in ("light_ms", "kd_ms", "camera_ms", "gather_ms")},
+        "wall_s": wall,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(cores=args.cpu_cores)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--grid", type=int, default=512)
+    ap.add_argument("--photons", type=int, default=PHOTONS_PER_ITER)
+    ap.add_argument("--cpu-cores", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -127,6 +127,12 @@ int rc_host_world_bvh(unsigned* nodes, int cap, int* index, int index_cap);
 /* Render `iterations` more progressive iterations into the FP64 running mean. */
 int rc_render(int iterations);
 
+/* rc_render timed on the device: CUDA events on the library's stream around all
+ * `iterations`.  out[0] = elapsed ms, out[1] = mean gather-kernel ms per iteration,
+ * out[2] = gather algorithmic bytes per iteration (40 B per photon + 80 B per merge
+ * query + 48 B FP64 pixel read/write per query), out[3] = kernel launches. */
+int rc_render_timed(int iterations, double* out);
+
 /* Copy the current image (mean over rendered iterations) as FP32 RGB, rows in the
  * reference's buffer order (the order SaveEXR receives, src/main.cpp:192-206). */
 int rc_read_image(float* rgb, int width, int height);

@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
     L.rc_kd_query.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
                               C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_kd_build_nodes.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
+    L.rc_render_timed.argtypes = [C.c_int, C.c_void_p]
     L.rc_light_photons.argtypes = [C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     _lib = L
     return L
@@ -60,4 +61,4 @@ def check(rc: int, what: str = "") -> None:
 EXPORTS = ["init", "main", "rc_default_config", "rc_set_config", "rc_prepare", "rc_prepare_host",
            "rc_host_mesh_bvh", "rc_host_world_bvh", "rc_render", "rc_read_image", "rc_release",
            "rc_last_error", "rc_get_stats", "rc_trace_rays", "rc_trace_rays_full", "rc_kd_query",
-           "rc_kd_build_nodes", "rc_light_photons"]
+           "rc_kd_build_nodes", "rc_light_photons", "rc_render_timed"]

@@ -73,6 +73,10 @@ struct DeviceState {
     DevBuf<double> accum;
     int iterations_done = 0;
     double stats[16] = {};
+    // accumulated over a timed render call
+    double acc_gather_ms = 0, acc_gather_bytes = 0, acc_launches = 0;
+    int acc_iters = 0;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
 
     void release() {
         DevBuf<float4>* f4[] = {&node_lo, &node_hi, &wnode_lo, &wnode_hi, &tri_v0, &tri_e1, &tri_e2, &tri_n0,
@@ -83,6 +87,8 @@ struct DeviceState {
         kd_nodes.release(); kd_x.release(); kd_y.release(); kd_z.release(); kd_id.release(); kd_scratch.release();
         accum.release();
         for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
+        if (t0) { cudaEventDestroy(t0); t0 = nullptr; }
+        if (t1) { cudaEventDestroy(t1); t1 = nullptr; }
         if (stream) { cudaStreamDestroy(stream); stream = nullptr; }
         ready = false;
         iterations_done = 0;
@@ -127,6 +133,8 @@ int upload_scene(HostScene& sc) {
     if (!d.stream) {
         RC_CUDA(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
         for (auto& e : d.ev) RC_CUDA(cudaEventCreate(&e));
+        RC_CUDA(cudaEventCreate(&d.t0));
+        RC_CUDA(cudaEventCreate(&d.t1));
     }
     std::vector<float4> nlo, nhi, v0, e1, e2, n0, n1, n2;
     std::vector<int> mesh_root;
@@ -364,6 +372,12 @@ int render_iteration(HostScene& sc) {
     st[11] = sc.scene_radius;
     st[12] = std::sqrt(p.radius_sqr);
     st[13] = kd_launches + 3;
+    d.acc_gather_ms += st[7];
+    // gather algorithmic bytes: each photon record read once (40 B), each query record
+    // read once (80 B), each query's FP64 RGB pixel read and written once (48 B)
+    d.acc_gather_bytes += 40.0 * (double)nph + 80.0 * (double)nq + 48.0 * (double)nq;
+    d.acc_launches += st[13];
+    d.acc_iters += 1;
     if (cfg().verbose)
         std::printf("{\"iteration\": %d, \"light_paths\": %lld, \"photons\": %llu, \"queries\": %llu, "
                     "\"light_ms\": %.3f, \"kd_ms\": %.3f, \"camera_ms\": %.3f, \"gather_ms\": %.3f}\n",
@@ -574,6 +588,29 @@ int rc_render(int iterations) {
     int r = prepare();
     for (int i = 0; i < iterations && !r; ++i) r = render_iteration(*g_scene);
     return r;
+}
+
+int rc_render_timed(int iterations, double* out) {
+    if (iterations < 0 || !out) { g_err = "bad arguments"; return RC_E_INVALID; }
+    int r = prepare();
+    if (r) return r;
+    DeviceState& d = g_dev;
+    d.acc_gather_ms = d.acc_gather_bytes = d.acc_launches = 0;
+    d.acc_iters = 0;
+    RC_CUDA(cudaStreamSynchronize(d.stream));
+    RC_CUDA(cudaEventRecord(d.t0, d.stream));
+    for (int i = 0; i < iterations && !r; ++i) r = render_iteration(*g_scene);
+    if (r) return r;
+    RC_CUDA(cudaEventRecord(d.t1, d.stream));
+    RC_CUDA(cudaEventSynchronize(d.t1));
+    float ms = 0.0f;
+    RC_CUDA(cudaEventElapsedTime(&ms, d.t0, d.t1));
+    int n = std::max(d.acc_iters, 1);
+    out[0] = ms;
+    out[1] = d.acc_gather_ms / n;
+    out[2] = d.acc_gather_bytes / n;
+    out[3] = d.acc_launches;
+    return RC_OK;
 }
 
 int rc_read_image(float* rgb, int width, int height) { return read_image(rgb, width, height); }
