@@ -182,6 +182,23 @@ int rc_kd_query(int n, const float* positions, int q, const float* queries, floa
  * *num_nodes and copies up to cap nodes as (index word, split bits) pairs. */
 int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes, long long cap, long long* num_nodes);
 
+/* KD-tree build that allocates no GPU memory, for callers that cannot allocate at
+ * the point they need a photon tree (a host application that hands this library only
+ * pre-allocated device buffers, or forbids foreign allocations in its context).  No
+ * counterpart in the reference.  Same tree as rc_kd_build_nodes.  All pointers are
+ * device memory owned by the caller: positions4 = n float4 (xyz used), nodes =
+ * node_cap entries of 2 words (node_cap >= the node-array length of rc_kd_build_nodes
+ * for n), x/y/z/ids = n entries each (photons in tree order).  Working memory is one
+ * fixed array inside the library (held by every device that loads it), so n is
+ * limited to 524288 photons (RC_E_CAPACITY beyond).  The first call on a device looks
+ * up that array's address and should come before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race.  Runs on `stream` (a cudaStream_t, NULL
+ * = legacy default stream) and synchronises it before returning; on error the message
+ * is in rc_kd_noalloc_last_error(). */
+int rc_kd_build_noalloc(const float* positions4, long long n, unsigned* nodes, long long node_cap,
+                        float* x, float* y, float* z, unsigned* ids, void* stream);
+const char* rc_kd_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,6 +31,7 @@ SOURCES = [
     ("vm_kernels.cu", "nvcc"),
     ("gather.cu", "nvcc"),
     ("kdtree.cu", "nvcc"),
+    ("kd_noalloc.cu", "nvcc"),
 ]
 
 
