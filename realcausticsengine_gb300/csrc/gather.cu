@@ -1,14 +1,22 @@
 // Radius gather at the camera vertices (Path_Vertices::get_contrib,
 // src/Path_Vertices.h:46-68, over KD_Tree::find_closest_in_radius,
-// src/KD_Tree.cpp:217-280).
+// src/KD_Tree.cpp:217-280), one merge query per warp.
 //
-// Descent: the reference's near-side-first recursion with the far side (and an odd
-// node's median photon) visited only when (q[axis] - split)^2 < r^2.  Once a node
-// holds at most kBucket photons its whole contiguous range is tested.  Every photon
-// that reaches the test is accepted by the reference's own predicate
-// ((dx*dx + dy*dy) + dz*dz) < r^2 in FP32 without contraction, so the set of photons
-// found is exactly the reference's: pruning never drops a photon inside the radius
-// (rounding is monotonic, so |q - p|^2 >= (q[axis] - split)^2 holds in floats too).
+// Queries are first ordered by the KD cell they fall in (launch_query_order), so the
+// queries a warp processes one after another touch the same nodes and photons (L1/L2
+// reuse).  For each query the warp runs the reference's descent uniformly (near side
+// first; far side and an odd node's median photon only when (q[axis] - split)^2 < r^2)
+// and, at a node of at most 32 photons, tests the whole contiguous tree-order range at
+// once, one photon per lane, with the reference's acceptance predicate
+// ((dx*dx + dy*dy) + dz*dz) < r^2 in FP32 without contraction.  Accepted photons are
+// compacted in shared memory and their MIS-weighted BSDF contributions are evaluated
+// lane-parallel, then summed across the warp.
+//
+// The set of photons a query accepts is exactly the reference's: the descent is the
+// reference's own, a bucket is tested exhaustively, and pruning never drops a photon
+// inside the radius (rounding is monotonic, so |q - p|^2 >= (q[axis] - split)^2 holds in
+// floats too).  Accumulation order differs from the reference's recursion, so
+// contributions agree to FP32 rounding.
 #include "vm.cuh"
 #include "bsdf.cuh"
 
@@ -16,7 +24,10 @@ namespace rc {
 
 namespace {
 
-constexpr int kBucket = 8;
+constexpr int kWarpsPerBlock = 8;
+constexpr int kStack = 64;
+constexpr int kQueriesPerWarp = 16;
+constexpr int kBucket = 64;   // photons tested per bucket (kBucket / 32 per lane)
 
 struct KdNav {
     const uint2* __restrict__ nodes;
@@ -24,111 +35,433 @@ struct KdNav {
     const float* __restrict__ y;
     const float* __restrict__ z;
     const uint32_t* __restrict__ id;
+    const float4* __restrict__ box_lo;   // per node down to the bucket level (nullptr: none)
+    const float4* __restrict__ box_hi;
+    int box_levels;                      // boxes exist for levels [0, box_levels)
     long long n;
 };
+
+// Squared distance from q to a box, formed like the acceptance test so that it never
+// exceeds the squared distance to any photon inside the box (rounding is monotonic).
+__device__ __forceinline__ bool box_outside(F3 q, float4 lo, float4 hi, float r2) {
+    float dx = q.x < lo.x ? lo.x - q.x : (q.x > hi.x ? q.x - hi.x : 0.0f);
+    float dy = q.y < lo.y ? lo.y - q.y : (q.y > hi.y ? q.y - hi.y : 0.0f);
+    float dz = q.z < lo.z ? lo.z - q.z : (q.z > hi.z ? q.z - hi.z : 0.0f);
+    return !(dx * dx + dy * dy + dz * dz < r2);
+}
 
 __device__ __forceinline__ bool in_radius(F3 q, float px, float py, float pz, float r2) {
     float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
     return dx * dx + dy * dy + dz * dz < r2;
 }
 
-// Visit every photon within the radius: fn(tree position).
-template <class Fn>
-__device__ __forceinline__ void kd_visit(const KdNav& t, F3 q, float r2, Fn&& fn) {
+// Warp-uniform traversal; fn(tree position) runs on each lane for each photon its
+// query accepts.  `stack` is this warp's shared-memory stack (kStack (e, start) pairs).
+struct VisitCounts { unsigned nodes, buckets, tests; };
+
+// One query per warp.  The traversal is the reference's descent for that single query
+// (uniform across the warp): near side first, far side and an odd node's median photon
+// only when (q[axis] - split)^2 < r^2.  The stack lives in registers spread over the
+// lanes (entry k in lane k % 32 of register pair k / 32); push and pop are uniform.
+// A node of at most kBucket photons is a bucket, tested kBucket/32 photons per lane.
+// Accepted tree positions are appended to the warp's pending list in shared memory;
+// `flush(count, list)` runs on all lanes whenever the list holds 32 or more entries
+// and once at the end, so the per-photon work is spread over the lanes.
+template <class Flush>
+__device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend,
+                                              VisitCounts& vc, Flush&& flush) {
+    const int lane = threadIdx.x & 31;
     if (t.n <= 0) return;
-    struct Item { long long e, start; int level; };
-    Item stack[64];
-    int sp = 0;
-    stack[sp++] = {1, 0, 0};
+    uint32_t se0 = 0, ss0 = 0, se1 = 0, ss1 = 0;   // stack entries lane and lane+32
+    if (lane == 0) { se0 = start_node.x; ss0 = start_node.y; }
+    {
+        const int l0 = 31 - __clz(start_node.x);
+        if (l0 < t.box_levels && box_outside(q, __ldg(&t.box_lo[start_node.x]), __ldg(&t.box_hi[start_node.x]), r2))
+            return;
+    }
+    int sp = 1;
+    int np = 0;   // pending entries (uniform)
     while (sp) {
-        Item it = stack[--sp];
-        long long c = t.n >> it.level;
+        --sp;
+        uint32_t e, st;
+        if (sp < 32) { e = __shfl_sync(0xffffffffu, se0, sp); st = __shfl_sync(0xffffffffu, ss0, sp); }
+        else { e = __shfl_sync(0xffffffffu, se1, sp - 32); st = __shfl_sync(0xffffffffu, ss1, sp - 32); }
+        const long long start = st;
+        const int level = 31 - __clz(e);
+        const long long c = t.n >> level;
         if (c <= kBucket) {
-            for (long long p = it.start; p < it.start + c; ++p)
-                if (in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2)) fn(p);
+            if (level < t.box_levels && box_outside(q, __ldg(&t.box_lo[e]), __ldg(&t.box_hi[e]), r2)) continue;
+            vc.buckets++;
+            vc.tests += (unsigned)c;
+#pragma unroll
+            for (int k = 0; k < kBucket / 32; ++k) {
+                const int i = k * 32 + lane;
+                bool acc = false;
+                if (i < c) acc = in_radius(q, __ldg(&t.x[start + i]), __ldg(&t.y[start + i]), __ldg(&t.z[start + i]), r2);
+                const unsigned m = __ballot_sync(0xffffffffu, acc);
+                if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = (uint32_t)(start + i);
+                np += __popc(m);
+                __syncwarp();
+                if (np >= 32) { flush(np, pend); np = 0; __syncwarp(); }
+            }
             continue;
         }
-        uint2 nd = __ldg(&t.nodes[it.e]);
+        vc.nodes++;
+        const uint2 nd = __ldg(&t.nodes[e]);
+        const uint32_t ax = nd.x & 0x60000000u;
+        const float split = __uint_as_float(nd.y);
+        const float qa = ax == 0 ? q.x : (ax == 0x20000000u ? q.y : q.z);
+        const float d = qa - split;
+        const long long half = c >> 1, odd = c & 1;
+        const bool left_near = d < 0;
+        const bool within = d * d < r2;
+        if (odd && within) {
+            const long long p = start + half;
+            const bool a = in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2);
+            if (a && lane == 0) pend[np] = (uint32_t)p;
+            np += a ? 1 : 0;
+            __syncwarp();
+            if (np >= 32) { flush(np, pend); np = 0; __syncwarp(); }
+        }
+        const uint32_t le = 2u * e, ls = (uint32_t)start;
+        const uint32_t re = 2u * e + 1u, rs = (uint32_t)(start + half + odd);
+        // far side first (when within), then the near side, which is popped next
+        if (within && sp < kStack) {
+            const uint32_t fe = left_near ? re : le, fs = left_near ? rs : ls;
+            if ((sp & 31) == lane) { if (sp < 32) { se0 = fe; ss0 = fs; } else { se1 = fe; ss1 = fs; } }
+            ++sp;
+        }
+        if (sp < kStack) {
+            const uint32_t ne = left_near ? le : re, ns = left_near ? ls : rs;
+            if ((sp & 31) == lane) { if (sp < 32) { se0 = ne; ss0 = ns; } else { se1 = ne; ss1 = ns; } }
+            ++sp;
+        }
+    }
+    if (np > 0) flush(np, pend);
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 3) k_gather(const VMParams P, const KdNav t, TreePhotons tp,
+                                                                 QueryBuf qb, const uint32_t* __restrict__ order,
+                                                                 const uint2* __restrict__ start_nodes,
+                                                                 long long nq, double* __restrict__ accum,
+                                                                 unsigned long long* __restrict__ counters) {
+    __shared__ uint32_t pend[kWarpsPerBlock][64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long w = blockIdx.x * (long long)kWarpsPerBlock + warp;
+    const long long first = w * kQueriesPerWarp;
+    if (first >= nq) return;
+    const long long last = first + kQueriesPerWarp < nq ? first + kQueriesPerWarp : nq;
+    VisitCounts vc{0u, 0u, 0u};
+    unsigned accepted = 0;
+    for (long long slot = first; slot < last; ++slot) {
+        const long long qi = __ldg(&order[slot]);
+        const uint2 sn = __ldg(&start_nodes[qi]);
+        const float4 a = qb.q0[qi], b = qb.q1[qi], c = qb.q2[qi], ww = qb.q3[qi], e = qb.q4[qi];
+        const F3 q = xyz(a), ng = xyz(c);
+        const float cam_dVM = a.w;
+        Bsdf bs;
+        bs.init(P.materials[__float_as_int(b.w)], xyz(b), xyz(e), true);
+        F3 color = f3(0.0f);
+        kd_query_warp(t, q, P.radius_sqr, sn, pend[warp], vc, [&](int n, const uint32_t* list) {
+            for (int j = lane; j < n; j += 32) {
+                const uint32_t p = list[j];
+                const float4 p0 = __ldg(&tp.t0[p]);
+                const float4 p1 = __ldg(&tp.t1[p]);
+                const float2 p2 = __ldg(&tp.t2[p]);
+                const F3 wi = xyz(p1);
+                float fwd, rev;
+                bs.pdf(wi, fwd, rev);
+                const float weight = 1.0f / (1.0f + cam_dVM * rev + p0.w * fwd);
+                const F3 ev = bs.evaluate(wi, ng);
+                color = color + ev * f3(p1.w, p2.x, p2.y) * weight;
+            }
+            accepted += (unsigned)n;
+        });
+        // warp sum of the per-lane partial colours
+        for (int o = 16; o > 0; o >>= 1) {
+            color.x += __shfl_xor_sync(0xffffffffu, color.x, o);
+            color.y += __shfl_xor_sync(0xffffffffu, color.y, o);
+            color.z += __shfl_xor_sync(0xffffffffu, color.z, o);
+        }
+        if (lane == 0) {
+            const F3 r = xyz(ww) * color;
+            if (r.x != 0.0f || r.y != 0.0f || r.z != 0.0f) {
+                const long long pixel = __float_as_int(c.w);
+                atomicAdd(&accum[3 * pixel + 0], (double)r.x);
+                atomicAdd(&accum[3 * pixel + 1], (double)r.y);
+                atomicAdd(&accum[3 * pixel + 2], (double)r.z);
+            }
+        }
+    }
+    if (counters && lane == 0) {
+        atomicAdd(&counters[0], (unsigned long long)accepted);
+        atomicAdd(&counters[1], (unsigned long long)vc.tests);
+        atomicAdd(&counters[2], (unsigned long long)vc.buckets);
+        atomicAdd(&counters[3], (unsigned long long)vc.nodes);
+    }
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_kd_query(const KdNav t, int q, const float* __restrict__ qpos,
+                                                                   const uint32_t* __restrict__ order,
+                                                                   const uint2* __restrict__ start_nodes, float r2,
+                                                                   int* counts, const long long* offsets, int* idx) {
+    __shared__ uint32_t pend[kWarpsPerBlock][64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long w = blockIdx.x * (long long)kWarpsPerBlock + warp;
+    const long long first = w * kQueriesPerWarp;
+    if (first >= q) return;
+    const long long last = first + kQueriesPerWarp < q ? first + kQueriesPerWarp : q;
+    VisitCounts vc{0u, 0u, 0u};
+    for (long long slot = first; slot < last; ++slot) {
+        const long long j = order[slot];
+        const F3 p = f3(qpos[3 * j], qpos[3 * j + 1], qpos[3 * j + 2]);
+        const long long off = offsets ? offsets[j] : 0;
+        int n = 0;
+        kd_query_warp(t, p, r2, start_nodes[j], pend[warp], vc, [&](int cnt, const uint32_t* list) {
+            if (idx)
+                for (int k = lane; k < cnt; k += 32) idx[off + n + k] = (int)__ldg(&t.id[list[k]]);
+            n += cnt;
+        });
+        if (lane == 0) counts[j] = n;
+    }
+}
+
+// Query ordering: each query descends the tree's near sides to `level` (cells of
+// n >> level photons); a counting sort by cell puts neighbouring queries in the same
+// warp, which keeps the union of a warp's tree paths close to one query's path.
+// The same descent also finds where the reference's traversal for this query first
+// branches: the shallowest node on the near path with (q[axis] - split)^2 < r^2.  Above
+// it the traversal only follows near sides and tests no median photon, so starting
+// there visits exactly the same photons.  start_nodes[i] = (node, first position).
+__global__ void k_query_cells(const KdNav t, const float* __restrict__ qpos, int stride, long long nq, int level,
+                              float r2, uint32_t* __restrict__ keys, uint32_t* __restrict__ counts,
+                              uint2* __restrict__ start_nodes) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    F3 q = f3(qpos[stride * i], qpos[stride * i + 1], qpos[stride * i + 2]);
+    uint32_t e = 1;
+    long long st = 0, c = t.n;
+    uint2 start = make_uint2(0u, 0u);
+    bool found = false;
+    int l = 0;
+    for (; l < level || !found; ++l) {
+        if (c <= kBucket) {                       // reached a bucket without branching
+            if (!found) { start = make_uint2(e, (uint32_t)st); found = true; }
+            break;
+        }
+        uint2 nd = __ldg(&t.nodes[e]);
         uint32_t ax = nd.x & 0x60000000u;
         float split = __uint_as_float(nd.y);
         float qa = ax == 0 ? q.x : (ax == 0x20000000u ? q.y : q.z);
-        float dist = qa - split;
+        float d = qa - split;
+        if (!found && d * d < r2) { start = make_uint2(e, (uint32_t)st); found = true; }
         long long half = c >> 1, odd = c & 1;
-        Item left = {2 * it.e, it.start, it.level + 1};
-        Item right = {2 * it.e + 1, it.start + half + odd, it.level + 1};
-        bool go_left_first = dist < 0;
-        if (dist * dist < r2) {
-            if (odd) {
-                long long p = it.start + half;
-                if (in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2)) fn(p);
-            }
-            if (sp < 63) stack[sp++] = go_left_first ? right : left;
+        if (d < 0) { e = 2 * e; }
+        else { e = 2 * e + 1; st += half + odd; }
+        c = half;
+        if (l + 1 >= level && found) { ++l; break; }
+    }
+    // cell key at `level` (continue the near descent if the start was found early)
+    uint32_t ek = e;
+    int lk = l;
+    long long ck = c;
+    while (lk < level) {
+        if (ck <= 1) break;
+        uint2 nd = __ldg(&t.nodes[ek]);
+        uint32_t ax = nd.x & 0x60000000u;
+        float split = __uint_as_float(nd.y);
+        float qa = ax == 0 ? q.x : (ax == 0x20000000u ? q.y : q.z);
+        ek = 2 * ek + ((qa - split) < 0 ? 0u : 1u);
+        ck >>= 1;
+        ++lk;
+    }
+    while (lk < level) { ek = 2 * ek; ++lk; }
+    if (lk > level) ek >>= (lk - level);
+    uint32_t key = ek - (1u << level);
+    keys[i] = key;
+    start_nodes[i] = start;
+    atomicAdd(&counts[key], 1u);
+}
+
+// Exclusive scan of m counters in one CTA of 1024 threads (m up to a few million).
+__global__ void __launch_bounds__(1024) k_scan_counts(uint32_t* counts, long long m) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (long long base = 0; base < m; base += 1024 * 8) {
+        uint32_t v[8];
+        uint32_t sum = 0;
+        long long i0 = base + (long long)threadIdx.x * 8;
+        for (int k = 0; k < 8; ++k) { v[k] = (i0 + k < m) ? counts[i0 + k] : 0u; sum += v[k]; }
+        uint32_t incl = sum;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
         }
-        if (sp < 64) stack[sp++] = go_left_first ? left : right;
+        if (lane == 31) warp_sums[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t w = warp_sums[lane], wi = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            warp_sums[lane] = wi - w;
+        }
+        __syncthreads();
+        uint32_t run = carry + warp_sums[wid] + incl - sum;
+        for (int k = 0; k < 8; ++k) {
+            if (i0 + k < m) counts[i0 + k] = run;
+            run += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = run;
+        __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(256) k_gather(const VMParams P, const KdNav t, PhotonBuf ph, QueryBuf qb,
-                                                long long nq, double* __restrict__ accum) {
-    long long qi = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (qi >= nq) return;
-    float4 a = qb.q0[qi], b = qb.q1[qi], c = qb.q2[qi], w = qb.q3[qi], e = qb.q4[qi];
-    F3 q = xyz(a);
-    float cam_dVM = a.w;
-    int mat = __float_as_int(b.w);
-    int pixel = __float_as_int(c.w);
-    F3 ng = xyz(c);
-    Bsdf bs;
-    bs.init(P.materials[mat], xyz(b), xyz(e), true);
-    F3 color = f3(0.0f);
-    kd_visit(t, q, P.radius_sqr, [&](long long p) {
-        uint32_t i = __ldg(&t.id[p]);
-        float4 pp = __ldg(&ph.pos[i]);
-        float4 pd = __ldg(&ph.dir[i]);
-        float2 pt = __ldg(&ph.tp[i]);
-        F3 wi = xyz(pd);
-        float fwd, rev;
-        bs.pdf(wi, fwd, rev);
-        float weight = 1.0f / (1.0f + cam_dVM * rev + pp.w * fwd);
-        F3 ev = bs.evaluate(wi, ng);
-        color = color + ev * f3(pd.w, pt.x, pt.y) * weight;
-    });
-    F3 r = xyz(w) * color;
-    if (r.x != 0.0f || r.y != 0.0f || r.z != 0.0f) {
-        atomicAdd(&accum[3 * (long long)pixel + 0], (double)r.x);
-        atomicAdd(&accum[3 * (long long)pixel + 1], (double)r.y);
-        atomicAdd(&accum[3 * (long long)pixel + 2], (double)r.z);
+__global__ void k_scatter_queries(const uint32_t* __restrict__ keys, long long nq, uint32_t* __restrict__ cursor,
+                                  uint32_t* __restrict__ order) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    uint32_t pos = atomicAdd(&cursor[keys[i]], 1u);
+    order[pos] = (uint32_t)i;
+}
+
+// Node bounding boxes, bottom-up: a warp per node on the lowest boxed level reduces
+// its contiguous photon range; each upper node unites its children and its median.
+__global__ void k_leaf_boxes(const KdNav t, int level, float4* lo, float4* hi) {
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long first = 1LL << level;
+    if (w >= first) return;
+    const long long e = first + w;
+    const long long c = t.n >> level;
+    const long long s = kd_node_start(e, level, t.n);
+    float mnx = INFINITY, mny = INFINITY, mnz = INFINITY, mxx = -INFINITY, mxy = -INFINITY, mxz = -INFINITY;
+    for (long long i = lane; i < c; i += 32) {
+        float x = t.x[s + i], y = t.y[s + i], z = t.z[s + i];
+        mnx = fminf(mnx, x); mny = fminf(mny, y); mnz = fminf(mnz, z);
+        mxx = fmaxf(mxx, x); mxy = fmaxf(mxy, y); mxz = fmaxf(mxz, z);
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o)); mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mnz = fminf(mnz, __shfl_xor_sync(0xffffffffu, mnz, o)); mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o)); mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
+    }
+    if (lane == 0) { lo[e] = make_float4(mnx, mny, mnz, 0.0f); hi[e] = make_float4(mxx, mxy, mxz, 0.0f); }
 }
 
-__global__ void k_kd_query(const KdNav t, int q, const float* __restrict__ qpos, float r2, int* counts,
-                           const long long* offsets, int* idx) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= q) return;
-    F3 p = f3(qpos[3 * j], qpos[3 * j + 1], qpos[3 * j + 2]);
-    int n = 0;
-    long long off = offsets ? offsets[j] : 0;
-    kd_visit(t, p, r2, [&](long long pos) {
-        if (idx) idx[off + n] = (int)__ldg(&t.id[pos]);
-        ++n;
-    });
-    counts[j] = n;
+__global__ void k_parent_boxes(const KdNav t, int level, float4* lo, float4* hi) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long first = 1LL << level;
+    if (i >= first) return;
+    const long long e = first + i;
+    float4 a = lo[2 * e], b = lo[2 * e + 1], c = hi[2 * e], d = hi[2 * e + 1];
+    float4 l = make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
+    float4 h = make_float4(fmaxf(c.x, d.x), fmaxf(c.y, d.y), fmaxf(c.z, d.z), 0.0f);
+    const long long cnt = t.n >> level;
+    if (cnt & 1) {
+        const long long p = kd_node_start(e, level, t.n) + (cnt >> 1);
+        l.x = fminf(l.x, t.x[p]); l.y = fminf(l.y, t.y[p]); l.z = fminf(l.z, t.z[p]);
+        h.x = fmaxf(h.x, t.x[p]); h.y = fmaxf(h.y, t.y[p]); h.z = fmaxf(h.z, t.z[p]);
+    }
+    lo[e] = l;
+    hi[e] = h;
 }
 
-KdNav nav_of(const KdTree& tr) { return KdNav{tr.nodes, tr.x, tr.y, tr.z, tr.id, tr.n}; }
+// Photon records gathered into tree order, so the gather reads them contiguously.
+__global__ void k_tree_records(PhotonBuf ph, const uint32_t* __restrict__ id, long long n, TreePhotons tp) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    uint32_t i = id[p];
+    tp.t0[p] = ph.pos[i];
+    tp.t1[p] = ph.dir[i];
+    tp.t2[p] = ph.tp[i];
+}
+
+KdNav nav_of(const KdTree& tr) {
+    return KdNav{tr.nodes, tr.x, tr.y, tr.z, tr.id, tr.box_lo, tr.box_hi, tr.box_lo ? tr.box_levels : 0, tr.n};
+}
 
 }  // namespace
 
-void launch_gather(const VMParams& p, const KdTree& tree, PhotonBuf ph, QueryBuf qb, long long nq, double* accum,
-                   cudaStream_t s) {
-    if (nq <= 0) return;
-    k_gather<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(p, nav_of(tree), ph, qb, nq, accum);
+int kd_box_levels(long long n) {
+    // boxes for every level whose nodes hold more than half a bucket: the bucket level
+    // (nodes of at most kBucket photons) and everything above it
+    if (n <= 0) return 0;
+    int l = 0;
+    while ((n >> l) > kBucket) ++l;
+    return l + 1;
 }
 
-void launch_kd_query(const KdTree& tree, int q, const float* qpos, float r2, int* counts, const long long* offsets,
-                     int* idx, cudaStream_t s) {
+void launch_kd_boxes(const KdTree& tree, cudaStream_t s, int* launches) {
+    if (tree.n <= 0 || !tree.box_lo) return;
+    KdNav t = nav_of(tree);
+    const int lb = tree.box_levels - 1;
+    const long long nodes = 1LL << lb;
+    k_leaf_boxes<<<(unsigned)((nodes * 32 + 255) / 256), 256, 0, s>>>(t, lb, tree.box_lo, tree.box_hi);
+    int nl = 1;
+    for (int l = lb - 1; l >= 0; --l) {
+        const long long cnt = 1LL << l;
+        k_parent_boxes<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(t, l, tree.box_lo, tree.box_hi);
+        ++nl;
+    }
+    if (launches) *launches += nl;
+}
+
+int query_order_level(long long nq, const KdTree& tree) {
+    if (tree.n < 64 || nq <= 0) return 0;
+    int lq = 0;
+    while ((nq >> (lq + 1)) >= 16) ++lq;
+    int lmax = tree.levels - 5;      // cells keep at least 32 photons
+    if (lq > lmax) lq = lmax;
+    if (lq > 24) lq = 24;
+    return lq < 0 ? 0 : lq;
+}
+
+size_t query_order_scratch_bytes(long long nq, const KdTree& tree) {
+    int lq = query_order_level(nq, tree);
+    return 4 * (size_t)(nq > 0 ? nq : 1) + 4 * ((size_t)1 << lq) + 256;
+}
+
+void launch_query_order(const KdTree& tree, const float* qpos, int stride, long long nq, float r2, void* scratch,
+                        uint32_t* order, uint2* start_nodes, int* launches, cudaStream_t s) {
+    if (nq <= 0) return;
+    int lq = query_order_level(nq, tree);
+    uint32_t* keys = (uint32_t*)scratch;
+    uint32_t* counts = keys + ((nq + 63) & ~63LL);
+    long long m = 1LL << lq;
+    cudaMemsetAsync(counts, 0, 4 * (size_t)m, s);
+    unsigned g = (unsigned)((nq + 255) / 256);
+    k_query_cells<<<g, 256, 0, s>>>(nav_of(tree), qpos, stride, nq, lq, r2, keys, counts, start_nodes);
+    k_scan_counts<<<1, 1024, 0, s>>>(counts, m);
+    k_scatter_queries<<<g, 256, 0, s>>>(keys, nq, counts, order);
+    if (launches) *launches += 3;
+}
+
+void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaStream_t s) {
+    if (tree.n <= 0) return;
+    k_tree_records<<<(unsigned)((tree.n + 255) / 256), 256, 0, s>>>(ph, tree.id, tree.n, tp);
+}
+
+void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
+                   const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters, cudaStream_t s) {
+    if (nq <= 0) return;
+    long long warps = (nq + kQueriesPerWarp - 1) / kQueriesPerWarp;
+    k_gather<<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
+        p, nav_of(tree), tp, qb, order, start_nodes, nq, accum, counters);
+}
+
+void launch_kd_query(const KdTree& tree, int q, const float* qpos, const uint32_t* order, const uint2* start_nodes,
+                     float r2, int* counts, const long long* offsets, int* idx, cudaStream_t s) {
     if (q <= 0) return;
-    k_kd_query<<<(q + 127) / 128, 128, 0, s>>>(nav_of(tree), q, qpos, r2, counts, offsets, idx);
+    long long warps = (q + kQueriesPerWarp - 1) / kQueriesPerWarp;
+    k_kd_query<<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
+        nav_of(tree), q, qpos, order, start_nodes, r2, counts, offsets, idx);
 }
 
 }  // namespace rc

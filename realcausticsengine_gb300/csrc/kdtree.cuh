@@ -32,6 +32,10 @@ struct KdTree {
     // photons in tree order (SoA) and their photon-buffer index
     float* x = nullptr; float* y = nullptr; float* z = nullptr;
     uint32_t* id = nullptr;
+    // optional node bounding boxes for levels [0, box_levels) (launch_kd_boxes)
+    float4* box_lo = nullptr;
+    float4* box_hi = nullptr;
+    int box_levels = 0;
 };
 
 // Start of node e's photon range (root e = 1, level = floor(log2 e)).

@@ -70,9 +70,15 @@ struct DeviceState {
     DevBuf<float> kd_x, kd_y, kd_z;
     DevBuf<uint32_t> kd_id;
     DevBuf<unsigned char> kd_scratch;
+    DevBuf<float4> tp0, tp1, box_lo, box_hi;
+    DevBuf<float2> tp2;
+    DevBuf<uint32_t> qorder;
+    DevBuf<uint2> qstart;
+    DevBuf<unsigned char> qscratch;
     DevBuf<double> accum;
     int iterations_done = 0;
     double stats[16] = {};
+    double last_nodes = 0;
     // accumulated over a timed render call
     double acc_gather_ms = 0, acc_gather_bytes = 0, acc_launches = 0;
     int acc_iters = 0;
@@ -85,6 +91,8 @@ struct DeviceState {
         world_mesh.release(); mesh_root.release(); lights.release(); cdf.release(); materials.release();
         ph_tp.release(); ph_path.release(); counters.release(); errors.release();
         kd_nodes.release(); kd_x.release(); kd_y.release(); kd_z.release(); kd_id.release(); kd_scratch.release();
+        tp0.release(); tp1.release(); tp2.release(); qorder.release(); qstart.release(); qscratch.release();
+        box_lo.release(); box_hi.release();
         accum.release();
         for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
         if (t0) { cudaEventDestroy(t0); t0 = nullptr; }
@@ -183,7 +191,7 @@ int upload_scene(HostScene& sc) {
         (r = upload(d.lights, sc.lights, s)) || (r = upload(d.cdf, sc.light_cdf, s)) ||
         (r = upload(d.materials, sc.materials, s)))
         return r;
-    RC_CUDA(d.counters.reserve(4));
+    RC_CUDA(d.counters.reserve(8));
     RC_CUDA(d.errors.reserve(ERR_COUNT));
     RC_CUDA(cudaMemsetAsync(d.errors.p, 0, sizeof(int) * ERR_COUNT, s));
     RC_CUDA(cudaStreamSynchronize(s));
@@ -325,6 +333,22 @@ int render_iteration(HostScene& sc) {
         g_err = "KD scratch too small"; return RC_E_CAPACITY;
     }
     RC_CUDA(cudaGetLastError());
+    RC_CUDA(d.tp0.reserve(std::max<long long>(n, 1))); RC_CUDA(d.tp1.reserve(std::max<long long>(n, 1)));
+    RC_CUDA(d.tp2.reserve(std::max<long long>(n, 1)));
+    TreePhotons tph{d.tp0.p, d.tp1.p, d.tp2.p};
+    tree.box_levels = kd_box_levels(n);
+    if (tree.box_levels > 0) {
+        RC_CUDA(d.box_lo.reserve((size_t)1 << tree.box_levels));
+        RC_CUDA(d.box_hi.reserve((size_t)1 << tree.box_levels));
+        tree.box_lo = d.box_lo.p; tree.box_hi = d.box_hi.p;
+        launch_kd_boxes(tree, s, &kd_launches);
+        RC_CUDA(cudaGetLastError());
+    }
+    {
+        PhotonBuf phb{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, (long long)d.ph_pos.n, d.counters.p};
+        launch_tree_records(phb, tree, tph, s);
+        RC_CUDA(cudaGetLastError());
+    }
     RC_CUDA(cudaEventRecord(d.ev[3], s));
     // camera pass -> merge queries
     long long qcap = (long long)d.q0.n;
@@ -349,19 +373,30 @@ int render_iteration(HostScene& sc) {
     }
     r = check_errors();
     if (r) return r;
-    PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, (long long)d.ph_pos.n, d.counters.p};
     QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, (long long)d.q0.n, d.counters.p + 1};
+    RC_CUDA(d.qorder.reserve(std::max<unsigned long long>(nq, 1)));
+    RC_CUDA(d.qstart.reserve(std::max<unsigned long long>(nq, 1)));
+    RC_CUDA(d.qscratch.reserve(query_order_scratch_bytes((long long)nq, tree)));
     RC_CUDA(cudaEventRecord(d.ev[6], s));
-    launch_gather(p, tree, ph, qb, (long long)nq, d.accum.p, s);
+    int qlaunch = 0;
+    launch_query_order(tree, reinterpret_cast<const float*>(d.q0.p), 4, (long long)nq, p.radius_sqr, d.qscratch.p,
+                       d.qorder.p, d.qstart.p, &qlaunch, s);
+    RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
+    launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.accum.p, d.counters.p + 2, s);
     RC_CUDA(cudaGetLastError());
     RC_CUDA(cudaEventRecord(d.ev[7], s));
+    unsigned long long gc[4] = {0, 0, 0, 0};
+    RC_CUDA(cudaMemcpyAsync(gc, d.counters.p + 2, sizeof(gc), cudaMemcpyDeviceToHost, s));
     RC_CUDA(cudaStreamSynchronize(s));
     d.iterations_done++;
     double* st = d.stats;
     st[0] = (double)p.num_light_paths;
     st[1] = (double)nph;
     st[2] = (double)nq;
-    st[3] = 0.0;
+    st[3] = (double)gc[0];   // accepted photon-query pairs
+    st[14] = (double)gc[1];  // photon tests
+    st[15] = (double)gc[2];  // buckets visited (per warp)
+    d.last_nodes = (double)gc[3];
     st[4] = t_light;
     st[5] = ms_between(d.ev[2], d.ev[3]);
     st[6] = t_cam;
@@ -371,7 +406,7 @@ int render_iteration(HostScene& sc) {
     st[10] = d.iterations_done;
     st[11] = sc.scene_radius;
     st[12] = std::sqrt(p.radius_sqr);
-    st[13] = kd_launches + 3;
+    st[13] = kd_launches + 4 + qlaunch;
     d.acc_gather_ms += st[7];
     // gather algorithmic bytes: each photon record read once (40 B), each query record
     // read once (80 B), each query's FP64 RGB pixel read and written once (48 B)
@@ -380,8 +415,9 @@ int render_iteration(HostScene& sc) {
     d.acc_iters += 1;
     if (cfg().verbose)
         std::printf("{\"iteration\": %d, \"light_paths\": %lld, \"photons\": %llu, \"queries\": %llu, "
+                    "\"merged\": %llu, \"tests\": %llu, \"buckets\": %llu, \"nodes\": %llu, "
                     "\"light_ms\": %.3f, \"kd_ms\": %.3f, \"camera_ms\": %.3f, \"gather_ms\": %.3f}\n",
-                    it, p.num_light_paths, nph, nq, st[4], st[5], st[6], st[7]);
+                    it, p.num_light_paths, nph, nq, gc[0], gc[1], gc[2], gc[3], st[4], st[5], st[6], st[7]);
     return RC_OK;
 }
 
@@ -641,7 +677,7 @@ int rc_light_photons(int iteration, float* out, long long cap, long long* count)
     for (int attempt = 0; attempt < 3; ++attempt) {
         RC_CUDA(d.ph_pos.reserve(pcap)); RC_CUDA(d.ph_dir.reserve(pcap));
         RC_CUDA(d.ph_tp.reserve(pcap)); RC_CUDA(d.ph_path.reserve(pcap));
-        RC_CUDA(d.counters.reserve(4));
+        RC_CUDA(d.counters.reserve(8));
         RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, (long long)d.ph_pos.n, d.counters.p};
         launch_light_pass(p, ph, s);
@@ -714,7 +750,7 @@ int rc_trace_rays_full(int n, const float* origins, const float* directions, flo
 
 static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, DevBuf<uint2>& nodes, DevBuf<float>& x,
                          DevBuf<float>& y, DevBuf<float>& z, DevBuf<uint32_t>& id, DevBuf<unsigned char>& scratch,
-                         KdTree& tree, cudaStream_t s) {
+                         DevBuf<float4>& boxes, KdTree& tree, cudaStream_t s) {
     DevBuf<int> err;
     RC_CUDA(err.reserve(1));
     RC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
@@ -730,6 +766,14 @@ static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, Dev
     tree.nodes = nodes.p; tree.x = x.p; tree.y = y.p; tree.z = z.p; tree.id = id.p;
     if (kd_build(pos.p, n, tree, scratch.p, scratch.n, s, nullptr, err.p)) { g_err = "KD scratch"; return RC_E_CAPACITY; }
     RC_CUDA(cudaGetLastError());
+    tree.box_levels = kd_box_levels(n);
+    if (tree.box_levels > 0) {
+        RC_CUDA(boxes.reserve((size_t)2 << tree.box_levels));
+        tree.box_lo = boxes.p;
+        tree.box_hi = boxes.p + ((size_t)1 << tree.box_levels);
+        launch_kd_boxes(tree, s, nullptr);
+        RC_CUDA(cudaGetLastError());
+    }
     int h = 0;
     RC_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     RC_CUDA(cudaStreamSynchronize(s));
@@ -744,14 +788,20 @@ int rc_kd_query(int n, const float* positions, int q, const float* queries, floa
     cudaStream_t s = nullptr;
     RC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     DevBuf<float4> pos; DevBuf<uint2> nodes; DevBuf<float> x, y, z, qp; DevBuf<uint32_t> id;
-    DevBuf<unsigned char> scratch; DevBuf<int> cnt, out; DevBuf<long long> off;
+    DevBuf<unsigned char> scratch, osc; DevBuf<int> cnt, out; DevBuf<long long> off; DevBuf<uint32_t> ord;
+    DevBuf<uint2> qst;
     KdTree tree;
-    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, tree, s);
+    DevBuf<float4> boxes;
+    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, boxes, tree, s);
     if (!r && q > 0) {
         do {
             RC_CUDA(qp.reserve(3 * (size_t)q)); RC_CUDA(cnt.reserve(q)); RC_CUDA(off.reserve(q));
             RC_CUDA(cudaMemcpyAsync(qp.p, queries, 12 * (size_t)q, cudaMemcpyHostToDevice, s));
-            launch_kd_query(tree, q, qp.p, r2, cnt.p, nullptr, nullptr, s);
+            RC_CUDA(ord.reserve(q));
+            RC_CUDA(qst.reserve(q));
+            RC_CUDA(osc.reserve(query_order_scratch_bytes(q, tree)));
+            launch_query_order(tree, qp.p, 3, q, r2, osc.p, ord.p, qst.p, nullptr, s);
+            launch_kd_query(tree, q, qp.p, ord.p, qst.p, r2, cnt.p, nullptr, nullptr, s);
             RC_CUDA(cudaGetLastError());
             RC_CUDA(cudaMemcpyAsync(counts, cnt.p, 4 * (size_t)q, cudaMemcpyDeviceToHost, s));
             RC_CUDA(cudaStreamSynchronize(s));
@@ -762,7 +812,7 @@ int rc_kd_query(int n, const float* positions, int q, const float* queries, floa
             if (idx && t > 0 && t <= cap) {
                 RC_CUDA(out.reserve(t));
                 RC_CUDA(cudaMemcpyAsync(off.p, offs.data(), 8 * (size_t)q, cudaMemcpyHostToDevice, s));
-                launch_kd_query(tree, q, qp.p, r2, cnt.p, off.p, out.p, s);
+                launch_kd_query(tree, q, qp.p, ord.p, qst.p, r2, cnt.p, off.p, out.p, s);
                 RC_CUDA(cudaGetLastError());
                 RC_CUDA(cudaMemcpyAsync(idx, out.p, 4 * (size_t)t, cudaMemcpyDeviceToHost, s));
                 RC_CUDA(cudaStreamSynchronize(s));
@@ -772,7 +822,7 @@ int rc_kd_query(int n, const float* positions, int q, const float* queries, floa
         *total = 0;
     }
     pos.release(); nodes.release(); x.release(); y.release(); z.release(); id.release(); scratch.release();
-    cnt.release(); out.release(); off.release(); qp.release();
+    cnt.release(); out.release(); off.release(); qp.release(); ord.release(); osc.release(); boxes.release(); qst.release();
     cudaStreamDestroy(s);
     return r;
 }
@@ -783,7 +833,8 @@ int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes_out, long l
     RC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     DevBuf<float4> pos; DevBuf<uint2> nodes; DevBuf<float> x, y, z; DevBuf<uint32_t> id; DevBuf<unsigned char> scratch;
     KdTree tree;
-    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, tree, s);
+    DevBuf<float4> boxes;
+    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, boxes, tree, s);
     if (!r) {
         long long nn = kd_node_array_len(n);
         if (num_nodes) *num_nodes = nn;
@@ -795,6 +846,7 @@ int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes_out, long l
         }
     }
     pos.release(); nodes.release(); x.release(); y.release(); z.release(); id.release(); scratch.release();
+    boxes.release();
     cudaStreamDestroy(s);
     return r;
 }

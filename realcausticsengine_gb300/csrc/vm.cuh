@@ -40,6 +40,14 @@ struct QueryBuf {
     unsigned long long* count;
 };
 
+// Photon records in KD-tree order (filled after the build by launch_tree_records):
+//   t0 = position.xyz | dVM   t1 = direction_world.xyz | throughput.r   t2 = throughput.gb
+struct TreePhotons {
+    float4* t0;
+    float4* t1;
+    float2* t2;
+};
+
 struct LightsView {
     const DevLight* lights;
     const float* cdf;      // n + 1 entries
@@ -69,10 +77,24 @@ void launch_light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s);
 void launch_camera_pass(const VMParams& p, QueryBuf qb, cudaStream_t s);
 void launch_trace_rays(const SceneView& s, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st);
-void launch_gather(const VMParams& p, const KdTree& tree, PhotonBuf ph, QueryBuf qb, long long num_queries,
-                   double* accum, cudaStream_t s);
+void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaStream_t s);
+// Node bounding boxes used by the gather to prune exactly: levels [0, kd_box_levels(n)),
+// arrays of 2^kd_box_levels(n) float4 each.
+int kd_box_levels(long long n);
+void launch_kd_boxes(const KdTree& tree, cudaStream_t s, int* launches);
+// Spatial order of queries (positions at qpos + stride*i): order[] receives query
+// indices grouped by KD cell.  scratch: query_order_scratch_bytes(nq, tree).
+size_t query_order_scratch_bytes(long long nq, const KdTree& tree);
+void launch_query_order(const KdTree& tree, const float* qpos, int stride, long long nq, float r2, void* scratch,
+                        uint32_t* order, uint2* start_nodes, int* launches, cudaStream_t s);
+// start_nodes[i]: the node where query i's traversal first branches (from launch_query_order).
+// counters (optional, 4 u64 accumulated): accepted photon-query pairs, photon tests
+// (lanes x staged photons), buckets visited, inner nodes visited
+void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
+                   const uint2* start_nodes, long long num_queries, double* accum, unsigned long long* counters,
+                   cudaStream_t s);
 // Radius query hook: counts (and, if idx != nullptr, ids at offsets) per query.
-void launch_kd_query(const KdTree& tree, int q, const float* qpos, float r2, int* counts,
-                     const long long* offsets, int* idx, cudaStream_t s);
+void launch_kd_query(const KdTree& tree, int q, const float* qpos, const uint32_t* order, const uint2* start_nodes,
+                     float r2, int* counts, const long long* offsets, int* idx, cudaStream_t s);
 
 }  // namespace rc

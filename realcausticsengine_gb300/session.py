@@ -13,7 +13,8 @@ from ._native import check, lib
 from .scene import InitArgs, Scene
 
 STAT_NAMES = ["light_paths", "photons", "queries", "merged", "light_ms", "kd_ms", "camera_ms", "gather_ms",
-              "accum_ms", "device_ms", "iterations", "scene_radius", "radius", "launches"]
+              "accum_ms", "device_ms", "iterations", "scene_radius", "radius", "launches", "photon_tests",
+              "buckets_visited"]
 
 
 class Renderer:
