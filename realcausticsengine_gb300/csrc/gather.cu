@@ -81,25 +81,28 @@ __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, ui
     }
     int sp = 1;
     int np = 0;   // pending entries (uniform)
+    const uint32_t n32 = (uint32_t)t.n;   // photon counts stay below 2^28 (28-bit index field)
     while (sp) {
         --sp;
-        uint32_t e, st;
-        if (sp < 32) { e = __shfl_sync(0xffffffffu, se0, sp); st = __shfl_sync(0xffffffffu, ss0, sp); }
-        else { e = __shfl_sync(0xffffffffu, se1, sp - 32); st = __shfl_sync(0xffffffffu, ss1, sp - 32); }
-        const long long start = st;
+        uint32_t e, start;
+        if (sp < 32) { e = __shfl_sync(0xffffffffu, se0, sp); start = __shfl_sync(0xffffffffu, ss0, sp); }
+        else { e = __shfl_sync(0xffffffffu, se1, sp - 32); start = __shfl_sync(0xffffffffu, ss1, sp - 32); }
         const int level = 31 - __clz(e);
-        const long long c = t.n >> level;
-        if (c <= kBucket) {
+        const uint32_t c = n32 >> level;
+        if (c <= (uint32_t)kBucket) {
             if (level < t.box_levels && box_outside(q, __ldg(&t.box_lo[e]), __ldg(&t.box_hi[e]), r2)) continue;
             vc.buckets++;
-            vc.tests += (unsigned)c;
+            vc.tests += c;
 #pragma unroll
             for (int k = 0; k < kBucket / 32; ++k) {
-                const int i = k * 32 + lane;
+                const uint32_t i = (uint32_t)(k * 32 + lane);
                 bool acc = false;
-                if (i < c) acc = in_radius(q, __ldg(&t.x[start + i]), __ldg(&t.y[start + i]), __ldg(&t.z[start + i]), r2);
+                if (i < c) {
+                    const uint32_t p = start + i;
+                    acc = in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2);
+                }
                 const unsigned m = __ballot_sync(0xffffffffu, acc);
-                if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = (uint32_t)(start + i);
+                if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = start + i;
                 np += __popc(m);
                 __syncwarp();
                 if (np >= 32) { flush(np, pend); np = 0; __syncwarp(); }
@@ -112,19 +115,19 @@ __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, ui
         const float split = __uint_as_float(nd.y);
         const float qa = ax == 0 ? q.x : (ax == 0x20000000u ? q.y : q.z);
         const float d = qa - split;
-        const long long half = c >> 1, odd = c & 1;
+        const uint32_t half = c >> 1, odd = c & 1u;
         const bool left_near = d < 0;
         const bool within = d * d < r2;
         if (odd && within) {
-            const long long p = start + half;
+            const uint32_t p = start + half;
             const bool a = in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2);
-            if (a && lane == 0) pend[np] = (uint32_t)p;
+            if (a && lane == 0) pend[np] = p;
             np += a ? 1 : 0;
             __syncwarp();
             if (np >= 32) { flush(np, pend); np = 0; __syncwarp(); }
         }
-        const uint32_t le = 2u * e, ls = (uint32_t)start;
-        const uint32_t re = 2u * e + 1u, rs = (uint32_t)(start + half + odd);
+        const uint32_t le = 2u * e, ls = start;
+        const uint32_t re = 2u * e + 1u, rs = start + half + odd;
         // far side first (when within), then the near side, which is popped next
         if (within && sp < kStack) {
             const uint32_t fe = left_near ? re : le, fs = left_near ? rs : ls;

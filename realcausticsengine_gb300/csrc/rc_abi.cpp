@@ -305,7 +305,7 @@ int render_iteration(HostScene& sc) {
         RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
         PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, cap, d.counters.p};
         RC_CUDA(cudaEventRecord(d.ev[0], s));
-        launch_light_pass(p, ph, s);
+        launch_light_pass(p, ph, d.counters.p + 6, s);
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaEventRecord(d.ev[1], s));
         RC_CUDA(cudaMemcpyAsync(&nph, d.counters.p, sizeof(nph), cudaMemcpyDeviceToHost, s));
@@ -680,7 +680,7 @@ int rc_light_photons(int iteration, float* out, long long cap, long long* count)
         RC_CUDA(d.counters.reserve(8));
         RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, (long long)d.ph_pos.n, d.counters.p};
-        launch_light_pass(p, ph, s);
+        launch_light_pass(p, ph, d.counters.p + 6, s);
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaMemcpyAsync(&nph, d.counters.p, sizeof(nph), cudaMemcpyDeviceToHost, s));
         RC_CUDA(cudaStreamSynchronize(s));

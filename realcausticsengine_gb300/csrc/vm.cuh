@@ -73,7 +73,8 @@ struct VMParams {
 // error flag slots
 enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_KD = 4, ERR_COUNT = 8 };
 
-void launch_light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s);
+// next_path: device counter for the persistent kernel (nullptr: one thread per path)
+void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s);
 void launch_camera_pass(const VMParams& p, QueryBuf qb, cudaStream_t s);
 void launch_trace_rays(const SceneView& s, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st);

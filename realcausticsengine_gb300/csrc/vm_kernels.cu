@@ -60,6 +60,101 @@ __device__ __forceinline__ unsigned long long warp_append(unsigned long long* co
     return base + __popc(lower);
 }
 
+// Persistent light pass with path regeneration: each loop iteration advances every
+// live path by one bounce; lanes whose path ended fetch the next unstarted light path
+// (one atomic per warp), so a warp's lanes stay busy until the pool is empty instead of
+// waiting for the warp's longest path.  Photons, their order within a path and every
+// random number are the same as one-thread-per-path execution (counter-based samples).
+struct LightPath {
+    F3 o, d, tp;
+    float dVM;
+    int diffuse, last, len;
+    long long idx;
+    PathRng rng;
+};
+
+__device__ __forceinline__ void light_path_start(const VMParams& P, long long pidx, LightPath& s) {
+    s.idx = pidx;
+    s.rng.init(P.seed, (uint64_t)pidx, P.iteration, STREAM_LIGHT);
+    U4 b0 = s.rng.block(0), b1 = s.rng.block(1);
+    sample_light(P.lights, u01(b0.a), u01(b0.b), u01(b0.c), u01(b0.d), u01(b1.a), s.o, s.d, s.tp);
+    s.diffuse = 0;
+    s.last = EV_DIFFUSE;
+    s.dVM = 0.0f;
+    s.len = 0;
+}
+
+// One bounce of Vertex_Merging::trace_light_path (src/Vertex_Merging.cpp:140-194);
+// returns false when the path ends.
+__device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& ph, LightPath& s) {
+    F3 ro = s.o + s.d * kRayEps;
+    HitRec h;
+    if (!scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK)) return false;
+    Isect is;
+    fill_isect(P.scene, h, ro, s.d, is);
+    if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); return false; }
+    Bsdf b;
+    b.init(P.materials[is.material], is.ns, is.dir, false);
+    if (!b.valid()) return false;
+    s.dVM /= fabsf(b.cos_theta_in());
+    bool stored = false;
+    if (!b.is_delta() && (s.last & EV_GLOSSY)) {
+        unsigned long long slot = warp_append(ph.count);
+        if (slot < (unsigned long long)ph.capacity) {
+            ph.pos[slot] = make_float4(is.pos.x, is.pos.y, is.pos.z, s.dVM);
+            ph.dir[slot] = make_float4(-is.dir.x, -is.dir.y, -is.dir.z, s.tp.x);
+            ph.tp[slot] = make_float2(s.tp.y, s.tp.z);
+            ph.path[slot] = (uint32_t)s.idx;
+        }
+        stored = true;
+    }
+    if (s.len > P.max_path_length || s.diffuse > kMaxDiffuse) return false;
+    U4 bb = s.rng.block(2 + s.len);
+    BsdfSample smp = b.sample(u01(bb.a), u01(bb.b), u01(bb.c), is.ng);
+    if (is_zero(smp.f)) return false;
+    F3 f = smp.f;
+    if (s.len > kRRDepth) {
+        if (u01(bb.d) > smp.cont) return false;
+        f = div_each(f, smp.cont);
+    }
+    s.o = is.pos;
+    s.d = smp.wi;
+    if (smp.event & EV_DIFFUSE) s.diffuse++;
+    s.tp = s.tp * f;
+    s.last = smp.event;
+    if (!stored) s.dVM *= (smp.cos_out / smp.fwd) * smp.rev;
+    else s.dVM = (smp.cos_out / smp.fwd) * (1.0f + smp.rev * s.dVM);
+    s.len++;
+    return true;
+}
+
+__global__ void __launch_bounds__(256) k_light_pass_persistent(const VMParams P, PhotonBuf ph,
+                                                                unsigned long long* __restrict__ next_path) {
+    const int lane = threadIdx.x & 31;
+    LightPath s;
+    bool alive = false;
+    bool pool_left = true;
+    while (true) {
+        // refill lanes without a path
+        const unsigned need = __ballot_sync(0xffffffffu, !alive);
+        if (need && pool_left) {
+            unsigned long long base = 0;
+            if (lane == __ffs(need) - 1) base = atomicAdd(next_path, (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
+            if (!alive) {
+                const unsigned long long mine = base + __popc(need & ((1u << lane) - 1u));
+                if (mine < (unsigned long long)P.num_light_paths) {
+                    light_path_start(P, (long long)mine, s);
+                    alive = true;
+                }
+            }
+            if (base + __popc(need) >= (unsigned long long)P.num_light_paths) pool_left = false;
+        }
+        if (!__any_sync(0xffffffffu, alive)) break;
+        if (alive) alive = light_path_bounce(P, ph, s);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_light_pass(const VMParams P, PhotonBuf ph) {
     long long pidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (pidx >= P.num_light_paths) return;
@@ -217,10 +312,25 @@ __global__ void k_trace_rays(const SceneView S, int n, const float* __restrict__
 
 }  // namespace
 
-void launch_light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s) {
+void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s) {
     long long n = p.num_light_paths;
     if (n <= 0) return;
-    k_light_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, ph);
+    if (!next_path) {
+        k_light_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, ph);
+        return;
+    }
+    static int blocks = 0;
+    if (!blocks) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_light_pass_persistent, 256, 0);
+        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    long long need = (n + 255) / 256;
+    unsigned grid = (unsigned)(need < blocks ? need : blocks);
+    cudaMemsetAsync(next_path, 0, sizeof(unsigned long long), s);
+    k_light_pass_persistent<<<grid, 256, 0, s>>>(p, ph, next_path);
 }
 
 void launch_camera_pass(const VMParams& p, QueryBuf qb, cudaStream_t s) {
