@@ -32,6 +32,7 @@ SOURCES = [
     ("gather.cu", "nvcc"),
     ("kdtree.cu", "nvcc"),
     ("kd_noalloc.cu", "nvcc"),
+    ("vm_mlt.cu", "nvcc"),
 ]
 
 

@@ -79,6 +79,7 @@ struct DeviceState {
     int iterations_done = 0;
     double stats[16] = {};
     double last_nodes = 0;
+    float stats_mlt_visible = 0.0f;
     // accumulated over a timed render call
     double acc_gather_ms = 0, acc_gather_bytes = 0, acc_launches = 0;
     int acc_iters = 0;
@@ -298,17 +299,22 @@ int render_iteration(HostScene& sc) {
     long long cap = (long long)d.ph_pos.n;
     if (cap < p.num_light_paths * 2) cap = p.num_light_paths * 2;
     unsigned long long nph = 0;
+    unsigned long long mlt[2] = {0, 0};
     float t_light = 0.0f;
+    const int sampler = cfg().sampler;
     for (int attempt = 0; attempt < 3; ++attempt) {
         RC_CUDA(d.ph_pos.reserve(cap)); RC_CUDA(d.ph_dir.reserve(cap));
         RC_CUDA(d.ph_tp.reserve(cap)); RC_CUDA(d.ph_path.reserve(cap));
         RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
         PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, cap, d.counters.p};
         RC_CUDA(cudaEventRecord(d.ev[0], s));
-        launch_light_pass(p, ph, d.counters.p + 6, s);
+        if (sampler == RC_SAMPLER_UNIFORM) launch_light_pass(p, ph, d.counters.p + 6, s);
+        else launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaEventRecord(d.ev[1], s));
         RC_CUDA(cudaMemcpyAsync(&nph, d.counters.p, sizeof(nph), cudaMemcpyDeviceToHost, s));
+        if (sampler != RC_SAMPLER_UNIFORM)
+            RC_CUDA(cudaMemcpyAsync(mlt, d.counters.p + 2, sizeof(mlt), cudaMemcpyDeviceToHost, s));
         RC_CUDA(cudaStreamSynchronize(s));
         t_light = ms_between(d.ev[0], d.ev[1]);
         if ((long long)nph <= cap) break;
@@ -317,6 +323,12 @@ int render_iteration(HostScene& sc) {
     }
     int r = check_errors();
     if (r) return r;
+    if (sampler != RC_SAMPLER_UNIFORM) {
+        // visibility normalisation of the Metropolis samplers (src/Vertex_Merging.cpp:277-282)
+        const float vis = mlt[1] ? (float)mlt[0] / (float)mlt[1] : 0.0f;
+        p.vm_norm *= vis;
+        d.stats_mlt_visible = vis;
+    }
     // KD tree over the stored photons
     long long n = (long long)nph;
     long long nn = kd_node_array_len(n);
@@ -582,7 +594,16 @@ int rc_set_config(const rc_config* c) {
     if (!c) { g_err = "null config"; return RC_E_INVALID; }
     if (c->max_path_length < 0 || c->max_path_length > 30) { g_err = "max_path_length out of range [0, 30]"; return RC_E_INVALID; }
     if (c->photons_per_iter < 0) { g_err = "photons_per_iter < 0"; return RC_E_INVALID; }
-    if (c->sampler != RC_SAMPLER_UNIFORM) { g_err = "sampler not available in this build"; return RC_E_UNSUPPORTED; }
+    if (c->sampler != RC_SAMPLER_UNIFORM && c->sampler != RC_SAMPLER_HYBRID && c->sampler != RC_SAMPLER_PSSMLT) {
+        g_err = "unknown sampler"; return RC_E_INVALID;
+    }
+    if (c->sampler != RC_SAMPLER_UNIFORM) {
+        if (c->mlt_chains <= 0) { g_err = "mlt_chains must be positive"; return RC_E_INVALID; }
+        if (c->max_path_length > kMltMaxPathLength) { g_err = "Metropolis samplers support max_path_length <= 12"; return RC_E_UNSUPPORTED; }
+        if (c->sampler == RC_SAMPLER_PSSMLT && !(c->large_step_prob > 0.0f && c->large_step_prob <= 1.0f)) {
+            g_err = "large_step_prob must be in (0, 1]"; return RC_E_INVALID;
+        }
+    }
     g_cfg = *c;
     g_cfg.exr_path[sizeof(g_cfg.exr_path) - 1] = 0;
     g_cfg_set = true;

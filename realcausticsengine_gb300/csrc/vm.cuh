@@ -73,6 +73,12 @@ struct VMParams {
 // error flag slots
 enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_KD = 4, ERR_COUNT = 8 };
 
+// Metropolis light pass (RC_SAMPLER_HYBRID / RC_SAMPLER_PSSMLT), `chains` chains in one
+// launch; stats[0] = visible large steps, stats[1] = large steps (HYBRID: light paths).
+// The photons must be scaled by stats[0] / stats[1] (applied through VM_normalization).
+constexpr int kMltMaxPathLength = 12;
+void launch_mlt_pass(const VMParams& p, PhotonBuf ph, int sampler, int chains, float p_large,
+                     unsigned long long* stats, cudaStream_t s);
 // next_path: device counter for the persistent kernel (nullptr: one thread per path)
 void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s);
 void launch_camera_pass(const VMParams& p, QueryBuf qb, cudaStream_t s);
