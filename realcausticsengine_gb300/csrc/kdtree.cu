@@ -20,11 +20,11 @@ namespace rc {
 
 namespace {
 
-constexpr int kSmemSeg = 2048;      // largest node finished in shared memory
-constexpr int kChunk = 2048;        // positions per CTA in the global passes
-constexpr int kThreads = 256;
+constexpr int kSmemSeg = 1024;      // largest node finished in shared memory (~66 KB: 3 CTAs per SM)
+constexpr int kChunk = 1024;        // positions per CTA in the global passes (<= kSmemSeg)
+constexpr int kThreads = 128;
 constexpr int kItems = kChunk / kThreads;
-constexpr int kSmemThreads = 512;
+constexpr int kSmemThreads = 256;
 constexpr float kSplitBias = 1.175494e-38f;   // src/KD_Tree.cpp:150
 
 __device__ __forceinline__ uint32_t f2key(float f) {

@@ -373,7 +373,7 @@ int render_iteration(HostScene& sc) {
         RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s));
         QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qcap, d.counters.p + 1};
         RC_CUDA(cudaEventRecord(d.ev[4], s));
-        launch_camera_pass(p, qb, s);
+        launch_camera_pass(p, qb, d.counters.p + 7, s);
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaEventRecord(d.ev[5], s));
         RC_CUDA(cudaMemcpyAsync(&nq, d.counters.p + 1, sizeof(nq), cudaMemcpyDeviceToHost, s));

@@ -270,6 +270,105 @@ __global__ void __launch_bounds__(256) k_camera_pass(const VMParams P, QueryBuf 
     }
 }
 
+// Persistent camera pass with path regeneration (same scheme as the light pass).
+struct CameraPath {
+    F3 o, d, tp;
+    float dVM;
+    int len;
+    int target;
+    PathRng rng;
+};
+
+// Generate_camera_sample + Image_Buffer::add_color's row mapping; false when the
+// sample falls outside the image buffer (camera row 0, src/Image_Buffer.h:28-31).
+__device__ __forceinline__ bool camera_path_start(const VMParams& P, long long pix, CameraPath& s) {
+    const int W = P.camera.width, H = P.camera.height;
+    s.rng.init(P.seed, (uint64_t)pix, P.iteration, STREAM_CAMERA);
+    U4 b1 = s.rng.block(1);
+    const float x = (float)(int)(pix % W);
+    const float y = (float)(int)(pix / W);
+    const float sx = x + u01(b1.b), sy = y + u01(b1.c);
+    if (sx < 0 || sx >= (float)W || sy < 0 || sy >= (float)H) return false;
+    const int X = (int)sx, Y = H - (int)sy;
+    const long long target = (long long)X + (long long)Y * W;
+    if (target > (long long)W * H - 1) return false;
+    F3 dir = ld3(P.camera.bottom_left) + ld3(P.camera.horizontal) * (sx / (float)W) +
+             ld3(P.camera.vertical) * (sy / (float)H);
+    dir = dir - ld3(P.camera.origin);
+    s.o = ld3(P.camera.origin);
+    s.d = normalize(dir);
+    s.tp = f3(1.0f);
+    s.dVM = 0.0f;
+    s.len = 0;
+    s.target = (int)target;
+    return true;
+}
+
+__device__ __forceinline__ bool camera_path_bounce(const VMParams& P, QueryBuf& qb, CameraPath& s) {
+    F3 ro = s.o + s.d * kRayEps;
+    HitRec h;
+    if (!scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK)) return false;
+    Isect is;
+    fill_isect(P.scene, h, ro, s.d, is);
+    if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); return false; }
+    Bsdf b;
+    b.init(P.materials[is.material], is.ns, is.dir, true);
+    if (!b.valid()) return false;
+    s.dVM /= fabsf(b.cos_theta_in());
+    if (!b.is_delta()) {
+        unsigned long long slot = warp_append(qb.count);
+        if (slot < (unsigned long long)qb.capacity) {
+            F3 w = s.tp * P.vm_norm;
+            qb.q0[slot] = make_float4(is.pos.x, is.pos.y, is.pos.z, s.dVM);
+            qb.q1[slot] = make_float4(is.ns.x, is.ns.y, is.ns.z, __int_as_float(is.material));
+            qb.q2[slot] = make_float4(is.ng.x, is.ng.y, is.ng.z, __int_as_float(s.target));
+            qb.q3[slot] = make_float4(w.x, w.y, w.z, 0.0f);
+            qb.q4[slot] = make_float4(is.dir.x, is.dir.y, is.dir.z, 0.0f);
+        }
+    }
+    if (s.len > P.max_path_length) return false;
+    U4 bb = s.rng.block(2 + s.len);
+    BsdfSample smp = b.sample(u01(bb.a), u01(bb.b), u01(bb.c), is.ng);
+    if (is_zero(smp.f)) return false;
+    F3 f = smp.f;
+    if (s.len > kRRDepth) {
+        if (u01(bb.d) > smp.cont) return false;
+        f = div_each(f, smp.cont);
+    }
+    s.o = is.pos;
+    s.d = smp.wi;
+    s.tp = s.tp * f;
+    if (smp.event & EV_SPECULAR) s.dVM *= (smp.cos_out / smp.fwd) * smp.rev;
+    else s.dVM = (smp.cos_out / smp.fwd) * (1.0f + smp.rev * s.dVM);
+    s.len++;
+    return true;
+}
+
+__global__ void __launch_bounds__(256) k_camera_pass_persistent(const VMParams P, QueryBuf qb,
+                                                                 unsigned long long* __restrict__ next_pixel) {
+    const int lane = threadIdx.x & 31;
+    const long long npix = (long long)P.camera.width * P.camera.height;
+    CameraPath s;
+    bool alive = false;
+    bool pool_left = true;
+    while (true) {
+        unsigned need = __ballot_sync(0xffffffffu, !alive);
+        while (need && pool_left) {
+            unsigned long long base = 0;
+            if (lane == __ffs(need) - 1) base = atomicAdd(next_pixel, (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
+            if (!alive) {
+                const unsigned long long mine = base + __popc(need & ((1u << lane) - 1u));
+                if (mine < (unsigned long long)npix) alive = camera_path_start(P, (long long)mine, s);
+            }
+            if (base + __popc(need) >= (unsigned long long)npix) pool_left = false;
+            need = __ballot_sync(0xffffffffu, !alive);   // samples outside the buffer: draw again
+        }
+        if (!__any_sync(0xffffffffu, alive)) break;
+        if (alive) alive = camera_path_bounce(P, qb, s);
+    }
+}
+
 __global__ void k_trace_rays(const SceneView S, int n, const float* __restrict__ o, const float* __restrict__ d,
                              float tmin, float* out_full, unsigned* out_words, int* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -333,10 +432,25 @@ void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next
     k_light_pass_persistent<<<grid, 256, 0, s>>>(p, ph, next_path);
 }
 
-void launch_camera_pass(const VMParams& p, QueryBuf qb, cudaStream_t s) {
+void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s) {
     long long n = (long long)p.camera.width * p.camera.height;
     if (n <= 0) return;
-    k_camera_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, qb);
+    if (!next_pixel) {
+        k_camera_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, qb);
+        return;
+    }
+    static int blocks = 0;
+    if (!blocks) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_camera_pass_persistent, 256, 0);
+        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    long long need = (n + 255) / 256;
+    unsigned grid = (unsigned)(need < blocks ? need : blocks);
+    cudaMemsetAsync(next_pixel, 0, sizeof(unsigned long long), s);
+    k_camera_pass_persistent<<<grid, 256, 0, s>>>(p, qb, next_pixel);
 }
 
 void launch_trace_rays(const SceneView& sv, int n, const float* o, const float* d, float tmin, float* out_full,
