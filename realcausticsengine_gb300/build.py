@@ -33,6 +33,7 @@ SOURCES = [
     ("kdtree.cu", "nvcc"),
     ("kd_noalloc.cu", "nvcc"),
     ("vm_mlt.cu", "nvcc"),
+    ("tc_selftest.cu", "nvcc"),
 ]
 
 
