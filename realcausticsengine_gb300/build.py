@@ -34,6 +34,7 @@ SOURCES = [
     ("kd_noalloc.cu", "nvcc"),
     ("vm_mlt.cu", "nvcc"),
     ("tc_selftest.cu", "nvcc"),
+    ("mlp.cu", "nvcc"),
 ]
 
 
