@@ -103,6 +103,21 @@ typedef struct rc_config {
     int write_exr;              /* main(): 1 = write EXR (reference behaviour)           */
     char exr_path[256];         /* main(): output file, default "D:\\caustics.exr"       */
     int verbose;                /* 1 = print per-iteration JSON lines to stdout          */
+    /* learned emission proposal (UNIFORM sampler, area and point lights): an MLP maps
+     * the emission position to a 16-lobe von Mises-Fisher mixture over directions, used
+     * in a defensive mixture with the light's own density (fraction 0.2).  It is trained
+     * online on the light paths whose photons the camera merged, during the first
+     * `train_iterations` iterations (`train_steps` Adam steps of 16384 samples each,
+     * learning rate `learning_rate`), and guides emission from the iteration after the
+     * first training round.  No counterpart in the reference. */
+    int learned_proposal;
+    int train_iterations;       /* default 8                                             */
+    int train_steps;            /* default 64                                            */
+    float learning_rate;        /* default 1e-3                                          */
+    /* seed of the camera-path samples (pixel jitter, camera BSDF choices); 0 = `seed`.
+     * Two renders with the same camera_seed and different seeds share their merge
+     * queries and differ only in their photons. */
+    unsigned long long camera_seed;
 } rc_config;
 
 int rc_default_config(rc_config* cfg);
@@ -147,8 +162,17 @@ const char* rc_last_error(void);
  * out[0] light paths, [1] stored photons, [2] merge queries, [3] photons merged,
  * [4] light-pass ms, [5] KD-build ms, [6] camera-pass ms, [7] gather ms,
  * [8] accumulate ms, [9] total device ms, [10] iterations rendered so far,
- * [11] scene radius, [12] current merge radius, [13] gather kernel launches. */
+ * [11] scene radius, [12] current merge radius, [13] kernel launches,
+ * [14] photon-query distance tests in the gather, [15] 64-photon buckets visited.
+ * With the learned proposal, [8] is the proposal inference + training time. */
 int rc_get_stats(double* out, int n);
+
+/* Learned-proposal state of the last rendered iteration (no counterpart in the
+ * reference): for the first n light paths, prop4 = [direction xyz, p_light / q] (zeros
+ * before the network has been trained once) and contrib = the sum over the path's
+ * merges of the squared luminance each adds to its pixel (recorded during training
+ * iterations only).  Either output may be NULL. */
+int rc_proposal_state(long long n, float* prop4, float* contrib);
 
 /* ---- parity hooks (device kernels on caller-chosen inputs) ---- */
 

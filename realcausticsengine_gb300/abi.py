@@ -44,7 +44,9 @@ class PythonMaterial(C.Structure):
 class RcConfig(C.Structure):
     _fields_ = [("max_path_length", C.c_int), ("photons_per_iter", C.c_longlong), ("sampler", C.c_int),
                 ("mlt_chains", C.c_int), ("large_step_prob", C.c_float), ("seed", C.c_ulonglong),
-                ("write_exr", C.c_int), ("exr_path", C.c_char * 256), ("verbose", C.c_int)]
+                ("write_exr", C.c_int), ("exr_path", C.c_char * 256), ("verbose", C.c_int),
+                ("learned_proposal", C.c_int), ("train_iterations", C.c_int), ("train_steps", C.c_int),
+                ("learning_rate", C.c_float), ("camera_seed", C.c_ulonglong)]
 
 
 SAMPLER_UNIFORM, SAMPLER_HYBRID, SAMPLER_PSSMLT = 0, 1, 2

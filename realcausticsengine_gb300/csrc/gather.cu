@@ -177,7 +177,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 3) k_gather(const VMParam
                 bs.pdf(wi, fwd, rev);
                 const float weight = 1.0f / (1.0f + cam_dVM * rev + p0.w * fwd);
                 const F3 ev = bs.evaluate(wi, ng);
-                color = color + ev * f3(p1.w, p2.x, p2.y) * weight;
+                const F3 cpair = ev * f3(p1.w, p2.x, p2.y) * weight;
+                color = color + cpair;
+                if (P.path_contrib) {
+                    // learned-proposal training signal: the squared luminance this merge adds
+                    // to its pixel, summed per light path
+                    const F3 img = xyz(ww) * cpair;
+                    const float lum = (fabsf(img.x) + fabsf(img.y) + fabsf(img.z)) * (1.0f / 3.0f);
+                    if (lum > 0.0f)
+                        atomicAdd(&P.path_contrib[__ldg(&P.photon_path[__ldg(&t.id[p])])], lum * lum);
+                }
             }
             accepted += (unsigned)n;
         });

@@ -1,5 +1,6 @@
 // MLP emission proposal: tcgen05 forward / backward kernels, loss, Adam.
 #include "mlp.cuh"
+#include "lights.cuh"
 #include "tc_gemm.cuh"
 #include "rng.cuh"
 
@@ -65,10 +66,8 @@ struct SmemFwd {
     static constexpr int w1 = w0 + 64 * 80 * 2;                   // 64 x 64
     static constexpr int w2 = w1 + 64 * 64 * 2;
     static constexpr int w3 = w2 + 64 * 64 * 2;                   // 80 x 64
-    static constexpr int x = w3 + 80 * 64 * 2;                    // 128 x 80
-    static constexpr int h0 = x + 128 * 80 * 2;                   // 128 x 64
-    static constexpr int h1 = h0 + 128 * 64 * 2;
-    static constexpr int bias = h1 + 128 * 64 * 2;                // 272 floats
+    static constexpr int act = w3 + 80 * 64 * 2;                  // 128 x 80 activations, in place
+    static constexpr int bias = act + 128 * 80 * 2;               // 272 floats
     static constexpr int total = bias + 272 * 4;
 };
 
@@ -102,15 +101,17 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpParams P, IO io, l
         bias[i] = P.b[l][i - off];
     }
     if (tid == 0) tc::mbar_init(&mbar, 1);
-    if (warp == 0) tc::tmem_alloc(&tmem_base, 256);
+    if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tm = tmem_base;
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-    unsigned char* Xs = sm + SmemFwd::x;
-    unsigned char* H[2] = {sm + SmemFwd::h0, sm + SmemFwd::h1};
+    // one activation tile: each layer's product is complete (waited on) before its
+    // epilogue overwrites the tile with the next layer's input, and every thread's TMEM
+    // reads are done (barrier) before the next product reuses TMEM columns 0..79
+    unsigned char* Act = sm + SmemFwd::act;
     uint32_t phase = 0;
     bool failed = false;
     for (long long tile = blockIdx.x; tile * 128 < n && !failed; tile += gridDim.x) {
@@ -119,18 +120,16 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpParams P, IO io, l
         {
             float x[kMlpIn];
             io.input(row, valid, x);
-            store_row_bf16(Xs, tid, x, kMlpIn);
+            store_row_bf16(Act, tid, x, kMlpIn);
         }
-        const unsigned char* a_in = Xs;
         for (int l = 0; l < 4 && !failed; ++l) {
             const int K = mlp_in_dim(l), N = mlp_out_dim(l);
-            const uint32_t dcol = (l == 3) ? 128u : ((l & 1) ? 64u : 0u);
             tc::fence_proxy_async();
             tc::fence_before_sync();
             __syncthreads();
             if (tid == 0) {
                 tc::fence_after_sync();
-                tc::gemm_issue(tm + dcol, a_in, Ws[l], K, N, false, &mbar);
+                tc::gemm_issue(tm, Act, Ws[l], K, N, false, &mbar);
             }
             bool ok = tc::mbar_wait(&mbar, phase, kWait);
             phase ^= 1u;
@@ -141,13 +140,12 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpParams P, IO io, l
             }
             tc::fence_after_sync();
             float v[kMlpOut];
-            for (int c = 0; c < N; c += 16) tc::tmem_ld16(tm + lane_base + dcol + (uint32_t)c, v + c);
+            for (int c = 0; c < N; c += 16) tc::tmem_ld16(tm + lane_base + (uint32_t)c, v + c);
             const float* bl = bias + 64 * l;
             if (l < 3) {
                 for (int c = 0; c < N; ++c) v[c] = fmaxf(v[c] + bl[c], 0.0f);
                 io.save_hidden(l, row, valid, v);
-                store_row_bf16(H[l & 1], tid, v, N);
-                a_in = H[l & 1];
+                store_row_bf16(Act, tid, v, N);
             } else {
                 for (int c = 0; c < N; ++c) v[c] += bl[c];
                 io.output(row, valid, v);
@@ -156,7 +154,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpParams P, IO io, l
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tm, 256);
+    if (warp == 0) tc::tmem_dealloc(tm, 128);
 }
 
 struct BatchIO {
@@ -181,161 +179,397 @@ struct BatchIO {
     }
 };
 
-// ----------------------------------------------------------------------------- generic GEMM
-// D[m][n] = sum_k A(m, k) B(n, k); A(m, k) = A[m*sam + k*sak], B(n, k) = B[n*sbn + k*sbk].
-// One CTA: 128 rows of D, a K range [k0, k1) staged 128 at a time.
-// mode 0: out[m*N + n] = D; 1: atomicAdd(out[m*N + n], D); 2: outb[m*N + n] = bf16(D if mask[m*N+n] > 0 else 0)
-struct GemmArgs {
-    const __nv_bfloat16* A; long long sam, sak;
-    const __nv_bfloat16* B; long long sbn, sbk;
-    long long M, K;
-    int N;
-    int mode;
-    float* out;
-    __nv_bfloat16* outb;
-    const __nv_bfloat16* mask;
-    long long kchunk;
-};
-
-__global__ void __launch_bounds__(128) k_tc_gemm(const GemmArgs g, int* err) {
-    extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ __align__(8) uint64_t mbar;
-    __shared__ uint32_t tmem_base;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    unsigned char* As = sm;                 // 128 x 128
-    unsigned char* Bs = sm + 128 * 128 * 2; // N x 128
-    const long long m0 = (long long)blockIdx.x * 128;
-    const long long k0 = (long long)blockIdx.y * g.kchunk;
-    const long long k1 = k0 + g.kchunk < g.K ? k0 + g.kchunk : g.K;
-    if (tid == 0) tc::mbar_init(&mbar, 1);
-    if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t tm = tmem_base;
-    uint32_t phase = 0;
-    bool failed = false, any = false;
-    for (long long ks = k0; ks < k1; ks += 128) {
-        const int kk = (int)((k1 - ks) < 128 ? (k1 - ks) : 128);
-        const int KS = (kk + 15) & ~15;
-        for (int i = tid; i < 128 * KS; i += 128) {
-            const int r = i / KS, c = i % KS;
-            const long long m = m0 + r, k = ks + c;
-            __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
-            if (m < g.M && c < kk) v = g.A[m * g.sam + k * g.sak];
-            *reinterpret_cast<__nv_bfloat16*>(As + tc::kmajor_offset(r, c, KS)) = v;
-        }
-        for (int i = tid; i < g.N * KS; i += 128) {
-            const int r = i / KS, c = i % KS;
-            const long long k = ks + c;
-            __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
-            if (c < kk) v = g.B[(long long)r * g.sbn + k * g.sbk];
-            *reinterpret_cast<__nv_bfloat16*>(Bs + tc::kmajor_offset(r, c, KS)) = v;
-        }
-        tc::fence_proxy_async();
-        tc::fence_before_sync();
-        __syncthreads();
-        if (tid == 0) {
-            tc::fence_after_sync();
-            tc::gemm_issue(tm, As, Bs, KS, g.N, any, &mbar);
-        }
-        bool ok = tc::mbar_wait(&mbar, phase, kWait);
-        phase ^= 1u;
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicOr(err, 2);
-            failed = true;
-            break;
-        }
-        tc::fence_after_sync();
-        any = true;
-    }
-    if (!failed && any) {
-        const long long m = m0 + tid;
-        float v[128];
-        for (int c = 0; c < g.N; c += 16) tc::tmem_ld16(tm + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v + c);
-        if (m < g.M) {
-            for (int c = 0; c < g.N; ++c) {
-                const long long o = m * g.N + c;
-                if (g.mode == 0) g.out[o] = v[c];
-                else if (g.mode == 1) atomicAdd(&g.out[o], v[c]);
-                else g.outb[o] = __float2bfloat16_rn(__bfloat162float(g.mask[o]) > 0.0f ? v[c] : 0.0f);
-            }
-        }
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tm, 128);
+// ----------------------------------------------------------------------------- proposal
+__device__ __forceinline__ F3 sample_vmf(F3 mu, float kappa, float u1, float u2) {
+    u1 = fmaxf(u1, 1e-7f);
+    const float w = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * kappa)) / kappa;
+    const float st = sqrtf(fmaxf(0.0f, 1.0f - w * w));
+    Frame f;
+    f.set_from_z(mu);
+    float sp, cp;
+    sincosf(kPI2 * u2, &sp, &cp);
+    return f.x * (st * cp) + f.y * (st * sp) + mu * w;
 }
 
-// ----------------------------------------------------------------------------- loss, biases, Adam
-// L = -w log q(dir) with q = a p_light + (1 - a) sum_k pi_k vMF_k (w = dir.w, the
-// light's own density p_light at dir = pos.w).  Gradient w.r.t. the 80 outputs, / n.
-__global__ void k_loss_grad(const float* __restrict__ out, const float4* __restrict__ dir,
-                            const float4* __restrict__ pos, int n, __nv_bfloat16* __restrict__ dy,
-                            float* __restrict__ loss) {
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= n) return;
-    const float* o = out + (long long)row * kMlpOut;
+struct ProposalIO {
+    ProposalCtx c;
+    float4* prop;
+    __device__ void input(long long row, bool valid, float* x) const {
+        if (!valid) { for (int i = 0; i < kMlpIn; ++i) x[i] = 0.0f; return; }
+        PathRng g;
+        g.init(c.seed, (uint64_t)row, c.iteration, STREAM_LIGHT);
+        const U4 b0 = g.block(0);
+        const LightSample ls = light_position(c.lights, u01(b0.a), u01(b0.b), u01(b0.c));
+        encode((ls.o.x - c.bmin[0]) * c.binv[0], (ls.o.y - c.bmin[1]) * c.binv[1], (ls.o.z - c.bmin[2]) * c.binv[2], x);
+    }
+    __device__ void save_hidden(int, long long, bool, const float*) const {}
+    __device__ void output(long long row, bool valid, const float* o) const {
+        if (!valid) return;
+        PathRng g;
+        g.init(c.seed, (uint64_t)row, c.iteration, STREAM_LIGHT);
+        const U4 b0 = g.block(0), b1 = g.block(1);
+        const LightSample ls = light_position(c.lights, u01(b0.a), u01(b0.b), u01(b0.c));
+        const DevLight& l = c.lights.lights[ls.idx];
+        if (l.type == LIGHT_SUN) { prop[row] = make_float4(l.fz[0], l.fz[1], l.fz[2], 1.0f); return; }
+        // mixture over the 80 outputs with static indexing only (keeps them in registers)
+        float mxl = -INFINITY;
+#pragma unroll
+        for (int k = 0; k < kMlpLobes; ++k) mxl = fmaxf(mxl, o[5 * k]);
+        float e[kMlpLobes], sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kMlpLobes; ++k) { e[k] = expf(o[5 * k] - mxl); sum += e[k]; }
+        const float xi = u01(b1.b), u3 = u01(b0.d), u4 = u01(b1.a);
+        F3 w;
+        if (xi < kMlpDefensive) {
+            w = light_direction(l, u3, u4);
+        } else {
+            const float t = (xi - kMlpDefensive) / (1.0f - kMlpDefensive) * sum;
+            float cum = 0.0f, kap = 1.0f;
+            F3 mu = f3(0.0f, 0.0f, 1.0f);
+            bool chosen = false;
+#pragma unroll
+            for (int k = 0; k < kMlpLobes; ++k) {
+                cum += e[k];
+                if (!chosen && (t < cum || k == kMlpLobes - 1)) {
+                    chosen = true;
+                    const float x = o[5 * k + 1], y = o[5 * k + 2], z = o[5 * k + 3];
+                    const float len = fmaxf(sqrtf(x * x + y * y + z * z), 1e-6f);
+                    mu = f3(x / len, y / len, z / len);
+                    kap = fminf(kKappaMin + softplus(o[5 * k + 4]), kKappaMax);
+                }
+            }
+            w = sample_vmf(mu, kap, u3, u4);
+        }
+        const float pl = light_direction_pdf(l, w);
+        float S = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kMlpLobes; ++k) {
+            const float x = o[5 * k + 1], y = o[5 * k + 2], z = o[5 * k + 3];
+            const float len = fmaxf(sqrtf(x * x + y * y + z * z), 1e-6f);
+            const float kap = fminf(kKappaMin + softplus(o[5 * k + 4]), kKappaMax);
+            S += e[k] * vmf_pdf(kap, (x * w.x + y * w.y + z * w.z) / len);
+        }
+        const float q = kMlpDefensive * pl + (1.0f - kMlpDefensive) * (S / sum);
+        prop[row] = make_float4(w.x, w.y, w.z, (pl > 0.0f && q > 0.0f) ? pl / q : 0.0f);
+    }
+};
+
+__global__ void k_collect(const ProposalCtx c, long long n, const float* __restrict__ contrib,
+                          const float4* __restrict__ prop, int cap, float4* pos4, float4* dir4, unsigned* count,
+                          float* wsum) {
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float f = contrib[p];
+    if (!(f > 0.0f)) return;
+    PathRng g;
+    g.init(c.seed, (uint64_t)p, c.iteration, STREAM_LIGHT);
+    const U4 b0 = g.block(0), b1 = g.block(1);
+    const LightSample ls = light_position(c.lights, u01(b0.a), u01(b0.b), u01(b0.c));
+    const DevLight& l = c.lights.lights[ls.idx];
+    if (l.type == LIGHT_SUN) return;
+    F3 w;
+    float q_old, pl;
+    if (prop) {
+        const float4 pr = prop[p];
+        w = f3(pr.x, pr.y, pr.z);
+        pl = light_direction_pdf(l, w);
+        q_old = pr.w > 0.0f ? pl / pr.w : 0.0f;
+    } else {
+        w = light_direction(l, u01(b0.d), u01(b1.a));
+        pl = light_direction_pdf(l, w);
+        q_old = pl;
+    }
+    if (!(q_old > 0.0f)) return;
+    const unsigned slot = atomicAdd(count, 1u);
+    if (slot >= (unsigned)cap) return;
+    // Per-pixel image variance, summed over pixels, is (1/N) sum_j int F_j(w)^2 / q(w) dw
+    // minus a constant (F_j: the path's contribution to pixel j as a function of its
+    // emission direction), minimised by q proportional to sqrt(sum_j F_j^2).  The path's
+    // throughput already holds p_light / q_old, so the gather's sum of squared per-merge
+    // contributions is sum_j (F_j / q_old)^2 and its square root is the importance weight
+    // of this direction sample for that target.
+    const float wt = sqrtf(f);
+    pos4[slot] = make_float4((ls.o.x - c.bmin[0]) * c.binv[0], (ls.o.y - c.bmin[1]) * c.binv[1],
+                             (ls.o.z - c.bmin[2]) * c.binv[2], pl);
+    dir4[slot] = make_float4(w.x, w.y, w.z, wt);
+    atomicAdd(wsum, wt);
+}
+
+__global__ void k_norm_weights(float4* dir4, int n, const float* wsum) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float mean = *wsum / (float)n;
+    if (mean > 0.0f) dir4[i].w /= mean;
+}
+
+// ----------------------------------------------------------------------------- loss gradient
+// Per row: L = -w log q(dir) with q = a p_light + (1 - a) sum_k pi_k vMF_k (w = dir.w,
+// the light's own density at dir = pl).  g = dL/d(outputs) * inv_n; returns L * inv_n.
+__device__ float loss_grad_row(const float* o, float4 d, float pl, float inv_n, float* g) {
     Lobes L;
     lobes_from(o, L);
-    const float4 d = dir[row];
     const float w = d.w;
     float s[kMlpLobes], ca[kMlpLobes];
     float S = 0.0f;
+#pragma unroll
     for (int k = 0; k < kMlpLobes; ++k) {
         ca[k] = L.mx[k] * d.x + L.my[k] * d.y + L.mz[k] * d.z;
         s[k] = L.pi[k] * vmf_pdf(L.kappa[k], ca[k]);
         S += s[k];
     }
-    const float pl = pos[row].w;   // the light's own emission density at dir
     const float q = fmaxf(kMlpDefensive * pl + (1.0f - kMlpDefensive) * S, 1e-20f);
-    atomicAdd(loss, -w * logf(q) / n);
-    const float c = -(1.0f - kMlpDefensive) * w / (q * n);
+    const float c = -(1.0f - kMlpDefensive) * w * inv_n / q;
+#pragma unroll
     for (int k = 0; k < kMlpLobes; ++k) {
-        float g[5];
-        g[0] = c * (s[k] - L.pi[k] * S);
+        g[5 * k] = c * (s[k] - L.pi[k] * S);
         const float kap = L.kappa[k];
         const float gm = c * s[k] * kap / L.rlen[k];
-        g[1] = gm * (d.x - ca[k] * L.mx[k]);
-        g[2] = gm * (d.y - ca[k] * L.my[k]);
-        g[3] = gm * (d.z - ca[k] * L.mz[k]);
+        g[5 * k + 1] = gm * (d.x - ca[k] * L.mx[k]);
+        g[5 * k + 2] = gm * (d.y - ca[k] * L.my[k]);
+        g[5 * k + 3] = gm * (d.z - ca[k] * L.mz[k]);
         const float e2 = expf(-2.0f * kap);
         const float dlog = 1.0f / kap - 2.0f * e2 / (1.0f - e2) + (ca[k] - 1.0f);
-        const float raw = o[5 * k + 4];
-        const float dk = (kap >= kKappaMax) ? 0.0f : sigmoid(raw);
-        g[4] = c * s[k] * dlog * dk;
-        for (int j = 0; j < 5; ++j) dy[(long long)row * kMlpOut + 5 * k + j] = __float2bfloat16_rn(g[j]);
+        const float dk = (kap >= kKappaMax) ? 0.0f : sigmoid(o[5 * k + 4]);
+        g[5 * k + 4] = c * s[k] * dlog * dk;
+    }
+    return -w * logf(q) * inv_n;
+}
+
+// ----------------------------------------------------------------------------- fused training step
+// One CTA of 128 threads takes 128-row tiles of the batch (thread = row) and runs, per
+// tile, the forward pass, the loss gradient and the backward pass on the tensor cores:
+//   dW_l += dY_l^T . In_l        (M = 128 (out rows, zero-padded), N = in,  K = 128 rows)
+//   db_l += dY_l^T . 1           (N = 16 columns of ones)
+//   dX_l  = dY_l . W_l           (M = 128 rows, N = in, K = out), dY_{l-1} = dX_l * relu'(In_l)
+// The weight and bias gradients accumulate in TMEM across the CTA's tiles and are
+// written once per CTA as a partial sum; k_reduce_adam adds the partials.
+// Operands with the batch rows as the reduction dimension (In_l^T, dY_l^T) are written
+// transposed by the epilogues: element (feature i, row r) at kmajor_offset(i, r, 128).
+struct SmemTrain {
+    static constexpr int wf0 = 0;                       // forward weights (out x in), K-major over in
+    static constexpr int wf1 = wf0 + 64 * 80 * 2;
+    static constexpr int wf2 = wf1 + 64 * 64 * 2;
+    static constexpr int wf3 = wf2 + 64 * 64 * 2;
+    static constexpr int wt1 = wf3 + 80 * 64 * 2;       // W_l^T (in x out), K-major over out
+    static constexpr int wt2 = wt1 + 64 * 64 * 2;
+    static constexpr int wt3 = wt2 + 64 * 64 * 2;
+    static constexpr int act = wt3 + 64 * 80 * 2;       // 128 x 80 activations (forward A operand)
+    static constexpr int xt = act + 128 * 80 * 2;       // X^T 80 x 128
+    static constexpr int ht0 = xt + 80 * 128 * 2;       // H_l^T 64 x 128
+    static constexpr int ht1 = ht0 + 64 * 128 * 2;
+    static constexpr int ht2 = ht1 + 64 * 128 * 2;
+    static constexpr int dy = ht2 + 64 * 128 * 2;       // 128 x out output gradients
+    static constexpr int dyt = dy + 128 * 80 * 2;       // dY^T 128 x 128, rows >= out zero
+    static constexpr int ones = dyt + 128 * 128 * 2;    // 16 x 128 ones
+    static constexpr int bias = ones + 16 * 128 * 2;    // 272 floats
+    static constexpr int total = bias + 272 * 4;
+};
+static_assert(SmemTrain::total <= 227 * 1024, "training step shared memory");
+
+// TMEM columns: dW_l accumulators (N = in_l) at 0, 80, 144, 208; db_l (N = 16) at
+// 272 + 16 l; per-tile products (N <= 80) at 336.
+__device__ __forceinline__ uint32_t col_w(int l) { return l == 0 ? 0u : 16u + 64u * (uint32_t)l; }
+__device__ __forceinline__ uint32_t col_b(int l) { return 272u + 16u * (uint32_t)l; }
+constexpr uint32_t kColT = 336;
+
+__device__ __forceinline__ void store_col_bf16(unsigned char* base, int r, const float* v, int cnt) {
+    for (int i = 0; i < cnt; ++i)
+        *reinterpret_cast<__nv_bfloat16*>(base + tc::kmajor_offset(i, r, 128)) = __float2bfloat16_rn(v[i]);
+}
+
+// MMAs of one K extent without the completion commit (several products share one).
+__device__ __forceinline__ void gemm_issue_nc(uint32_t d_tmem, const void* a_smem, const void* b_smem, int K, int N,
+                                              bool accumulate) {
+    const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+    const uint32_t a0 = tc::smem_u32(a_smem), b0 = tc::smem_u32(b_smem);
+    const uint32_t sbo = (uint32_t)(K >> 3) * 128u;
+    for (int k = 0; k < K; k += 16) {
+        const uint64_t ad = tc::smem_desc(a0 + (uint32_t)(k >> 3) * 128u, 128u, sbo);
+        const uint64_t bd = tc::smem_desc(b0 + (uint32_t)(k >> 3) * 128u, 128u, sbo);
+        tc::mma_bf16(d_tmem, ad, bd, idesc, accumulate || k > 0);
     }
 }
 
-__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dy, int n, int cols, float* __restrict__ gb) {
-    const int c = blockIdx.x;
-    float acc = 0.0f;
-    for (int r = threadIdx.x; r < n; r += blockDim.x) acc += __bfloat162float(dy[(long long)r * cols + c]);
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    __shared__ float ws[32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+__device__ __forceinline__ bool cta_sync_wait(uint64_t* mbar, uint32_t& phase, int* err, int code) {
+    const bool ok = tc::mbar_wait(mbar, phase, kWait);
+    phase ^= 1u;
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicOr(err, code);
+        return false;
+    }
+    tc::fence_after_sync();
+    return true;
+}
+
+__device__ __forceinline__ void publish_smem() {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float t = 0.0f;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += ws[i];
-        gb[c] = t;
-    }
 }
 
-__global__ void k_adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* wb, int n, float lr, float b1t,
-                       float b2t) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__global__ void __launch_bounds__(128, 1) k_mlp_train(const MlpParams P, const float4* __restrict__ pos,
+                                                       const float4* __restrict__ dir, int n, float inv_n,
+                                                       float* __restrict__ part, int part_stride,
+                                                       float* __restrict__ loss, int* err) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    unsigned char* Wf[4] = {sm + SmemTrain::wf0, sm + SmemTrain::wf1, sm + SmemTrain::wf2, sm + SmemTrain::wf3};
+    unsigned char* Wt[4] = {nullptr, sm + SmemTrain::wt1, sm + SmemTrain::wt2, sm + SmemTrain::wt3};
+    unsigned char* InT[4] = {sm + SmemTrain::xt, sm + SmemTrain::ht0, sm + SmemTrain::ht1, sm + SmemTrain::ht2};
+    unsigned char* Act = sm + SmemTrain::act;
+    unsigned char* Dy = sm + SmemTrain::dy;
+    unsigned char* DyT = sm + SmemTrain::dyt;
+    unsigned char* Ones = sm + SmemTrain::ones;
+    for (int l = 0; l < 4; ++l) {
+        const int in = mlp_in_dim(l), out = mlp_out_dim(l);
+        for (int i = tid; i < in * out; i += 128) {
+            const int o = i / in, c = i % in;
+            const __nv_bfloat16 v = P.w[l][i];
+            *reinterpret_cast<__nv_bfloat16*>(Wf[l] + tc::kmajor_offset(o, c, in)) = v;
+            if (l > 0) *reinterpret_cast<__nv_bfloat16*>(Wt[l] + tc::kmajor_offset(c, o, out)) = v;
+        }
+    }
+    for (int i = tid; i < 128 * 128 * 2 / 16; i += 128) reinterpret_cast<uint4*>(DyT)[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < 16 * 128 * 2 / 16; i += 128)
+        reinterpret_cast<uint4*>(Ones)[i] = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
+    float* bias = reinterpret_cast<float*>(sm + SmemTrain::bias);
+    for (int i = tid; i < 272; i += 128) {
+        const int l = i < 64 ? 0 : (i < 128 ? 1 : (i < 192 ? 2 : 3));
+        bias[i] = P.b[l][i - 64 * l];
+    }
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
+    publish_smem();
+    tc::fence_after_sync();
+    const uint32_t tm = tmem_base;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    uint32_t phase = 0;
+    bool failed = false, first = true;
+    float loss_acc = 0.0f;
+    for (long long tile = blockIdx.x; tile * 128 < n && !failed; tile += gridDim.x) {
+        const long long row = tile * 128 + tid;
+        const bool valid = row < n;
+        const float4 pd = valid ? pos[row] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float4 dd = valid ? dir[row] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float v[kMlpOut];
+        {
+            float x[kMlpIn];
+            if (valid) encode(pd.x, pd.y, pd.z, x);
+            else for (int i = 0; i < kMlpIn; ++i) x[i] = 0.0f;
+            store_row_bf16(Act, tid, x, kMlpIn);
+            store_col_bf16(InT[0], tid, x, kMlpIn);
+        }
+        for (int l = 0; l < 4 && !failed; ++l) {
+            const int K = mlp_in_dim(l), N = mlp_out_dim(l);
+            publish_smem();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                tc::gemm_issue(tm + kColT, Act, Wf[l], K, N, false, &mbar);
+            }
+            if (!cta_sync_wait(&mbar, phase, err, 4)) { failed = true; break; }
+            for (int c = 0; c < N; c += 16) tc::tmem_ld16(tm + lane_base + kColT + (uint32_t)c, v + c);
+            const float* bl = bias + 64 * l;
+            if (l < 3) {
+                for (int c = 0; c < N; ++c) v[c] = fmaxf(v[c] + bl[c], 0.0f);
+                store_row_bf16(Act, tid, v, N);
+                store_col_bf16(InT[l + 1], tid, v, N);
+            } else {
+                for (int c = 0; c < N; ++c) v[c] += bl[c];
+            }
+        }
+        if (failed) break;
+        {
+            float g[kMlpOut];
+            if (valid) loss_acc += loss_grad_row(v, dd, pd.w, inv_n, g);
+            else for (int i = 0; i < kMlpOut; ++i) g[i] = 0.0f;
+            store_row_bf16(Dy, tid, g, kMlpOut);
+            store_col_bf16(DyT, tid, g, kMlpOut);
+        }
+        for (int l = 3; l >= 0 && !failed; --l) {
+            const int in = mlp_in_dim(l), out = mlp_out_dim(l);
+            publish_smem();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                gemm_issue_nc(tm + col_w(l), DyT, InT[l], 128, in, !first);
+                gemm_issue_nc(tm + col_b(l), DyT, Ones, 128, 16, !first);
+                if (l > 0) gemm_issue_nc(tm + kColT, Dy, Wt[l], out, in, false);
+                tc::mma_commit(&mbar);
+            }
+            if (!cta_sync_wait(&mbar, phase, err, 8)) { failed = true; break; }
+            if (l == 3) {
+                // rows 64..79 of dY^T held the output layer's extra gradients
+                uint4* z = reinterpret_cast<uint4*>(DyT + tc::kmajor_offset(64, 0, 128));
+                for (int i = tid; i < 16 * 128 * 2 / 16; i += 128) z[i] = make_uint4(0, 0, 0, 0);
+            }
+            if (l > 0) {
+                float g[kMlpHid];
+                for (int c = 0; c < in; c += 16) tc::tmem_ld16(tm + lane_base + kColT + (uint32_t)c, g + c);
+                for (int i = 0; i < in; ++i) {
+                    const float h = __bfloat162float(
+                        *reinterpret_cast<const __nv_bfloat16*>(InT[l] + tc::kmajor_offset(i, tid, 128)));
+                    if (!(h > 0.0f)) g[i] = 0.0f;
+                }
+                store_row_bf16(Dy, tid, g, in);
+                store_col_bf16(DyT, tid, g, in);
+            }
+        }
+        first = false;
+    }
+    for (int o = 16; o > 0; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
+    if ((tid & 31) == 0 && loss_acc != 0.0f) atomicAdd(loss, loss_acc);
+    if (!failed && !first) {
+        // this CTA's gradient sums, packed like the parameters (per layer: W out x in, b)
+        float* mine = part + (size_t)blockIdx.x * part_stride;
+        int off = 0;
+        for (int l = 0; l < 4; ++l) {
+            const int in = mlp_in_dim(l), out = mlp_out_dim(l);
+            float t[16];
+            for (int c = 0; c < in; c += 16) {
+                tc::tmem_ld16(tm + lane_base + col_w(l) + (uint32_t)c, t);
+                if (tid < out)
+                    for (int j = 0; j < 16; ++j) mine[off + tid * in + c + j] = t[j];
+            }
+            tc::tmem_ld16(tm + lane_base + col_b(l), t);
+            if (tid < out) mine[off + out * in + tid] = t[0];
+            off += out * in + out;
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tm, 512);
+}
+
+// Sum of the per-CTA partial gradients into gw/gb, then (apply) one Adam step.
+__global__ void k_reduce_adam(const MlpParams P, const float* __restrict__ part, int nparts, int total, int apply,
+                              float lr, float b1t, float b2t) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= total) return;
+    float g = 0.0f;
+    for (int b = 0; b < nparts; ++b) g += part[(size_t)b * total + j];
+    int l = 0, idx = j;
+    for (; l < 3; ++l) {
+        const int sz = mlp_in_dim(l) * mlp_out_dim(l) + mlp_out_dim(l);
+        if (idx < sz) break;
+        idx -= sz;
+    }
+    const int nw = mlp_in_dim(l) * mlp_out_dim(l);
+    const bool is_w = idx < nw;
+    const int i = is_w ? idx : idx - nw;
+    float* w = is_w ? P.wm[l] : P.b[l];
+    float* m = is_w ? P.mw[l] : P.mb[l];
+    float* v = is_w ? P.vw[l] : P.vb[l];
+    (is_w ? P.gw[l] : P.gb[l])[i] = g;
+    if (!apply) return;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    float gi = g[i];
-    float mi = b1 * m[i] + (1.0f - b1) * gi;
-    float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
-    m[i] = mi; v[i] = vi;
-    float mh = mi / (1.0f - b1t), vh = vi / (1.0f - b2t);
-    float wi = w[i] - lr * mh / (sqrtf(vh) + eps);
+    const float mi = b1 * m[i] + (1.0f - b1) * g;
+    const float vi = b2 * v[i] + (1.0f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / (1.0f - b1t)) / (sqrtf(vi / (1.0f - b2t)) + eps);
     w[i] = wi;
-    if (wb) wb[i] = __float2bfloat16_rn(wi);
+    if (is_w) P.w[l][i] = __float2bfloat16_rn(wi);
 }
 
 __global__ void k_to_bf16(const float* w, __nv_bfloat16* wb, int n) {
@@ -343,29 +577,19 @@ __global__ void k_to_bf16(const float* w, __nv_bfloat16* wb, int n) {
     if (i < n) wb[i] = __float2bfloat16_rn(w[i]);
 }
 
-int forward_blocks() {
-    static int blocks = 0;
-    if (!blocks) {
-        int dev = 0, sms = 0;
+int sm_count() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        blocks = 2 * sms;
     }
-    return blocks;
+    return sms;
 }
 
-int launch_gemm(const GemmArgs& g, cudaStream_t s, int* err) {
-    const unsigned gx = (unsigned)((g.M + 127) / 128);
-    const unsigned gy = (unsigned)((g.K + g.kchunk - 1) / g.kchunk);
-    const size_t smem = 128 * 128 * 2 + 128 * 128 * 2;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = true;
-    }
-    k_tc_gemm<<<dim3(gx, gy), 128, smem, s>>>(g, err);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
-}
+// Persistent forward grid: 3 CTAs per SM (58 KB of shared memory and 128 TMEM columns
+// each), so one CTA's tensor-core products overlap the others' epilogues.
+int forward_blocks() { return 3 * sm_count(); }
 
 }  // namespace
 
@@ -419,46 +643,102 @@ int mlp_forward_batch(const MlpParams& p, MlpBatch& b, cudaStream_t s, int* err)
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int mlp_backward_batch(const MlpParams& p, MlpBatch& b, cudaStream_t s, int* err) {
-    const int n = b.n;
+int mlp_proposal(const MlpParams& p, const ProposalCtx& c, long long n, float4* prop, cudaStream_t s, int* err) {
     if (n <= 0) return 0;
-    for (int l = 0; l < kMlpLayers; ++l) {
-        cudaMemsetAsync(p.gw[l], 0, 4 * (size_t)mlp_in_dim(l) * mlp_out_dim(l), s);
-        cudaMemsetAsync(p.gb[l], 0, 4 * (size_t)mlp_out_dim(l), s);
+    ProposalIO io{c, prop};
+    const size_t smem = SmemFwd::total;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_mlp_forward<ProposalIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
     }
-    cudaMemsetAsync(b.loss, 0, sizeof(float), s);
-    k_loss_grad<<<(n + 127) / 128, 128, 0, s>>>(b.out, b.dir, b.pos, n, b.dy[3], b.loss);
-    // activation gradients: dy[l] = (dy[l+1] . W[l+1]) * relu'(h[l])
-    for (int l = 2; l >= 0; --l) {
-        GemmArgs g{};
-        const int out_next = mlp_out_dim(l + 1), in_next = mlp_in_dim(l + 1);
-        g.A = b.dy[l + 1]; g.sam = out_next; g.sak = 1;
-        g.B = p.w[l + 1]; g.sbn = 1; g.sbk = in_next;
-        g.M = n; g.K = out_next; g.N = in_next; g.mode = 2;
-        g.outb = b.dy[l]; g.mask = b.h[l]; g.kchunk = 128;
-        if (launch_gemm(g, s, err)) return -1;
-    }
-    // weight gradients: gw[l] (out x in) = sum_rows dy[l]^T . in[l]
-    for (int l = 0; l < kMlpLayers; ++l) {
-        GemmArgs g{};
-        const int out = mlp_out_dim(l), in = mlp_in_dim(l);
-        g.A = b.dy[l]; g.sam = 1; g.sak = out;
-        g.B = l == 0 ? b.x : b.h[l - 1]; g.sbn = 1; g.sbk = in;
-        g.M = out; g.K = n; g.N = in; g.mode = 1; g.out = p.gw[l]; g.kchunk = 1024;
-        if (launch_gemm(g, s, err)) return -1;
-        k_bias_grad<<<out, 256, 0, s>>>(b.dy[l], n, out, p.gb[l]);
-    }
+    const long long tiles = (n + 127) / 128;
+    const int grid = (int)(tiles < forward_blocks() ? tiles : forward_blocks());
+    k_mlp_forward<ProposalIO><<<grid, 128, smem, s>>>(p, io, n, err);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-void mlp_adam(MlpParams& p, float lr, cudaStream_t s) {
-    p.adam_step++;
-    const float b1t = std::pow(0.9f, (float)p.adam_step), b2t = std::pow(0.999f, (float)p.adam_step);
-    for (int l = 0; l < kMlpLayers; ++l) {
-        const int nw = mlp_in_dim(l) * mlp_out_dim(l), nb = mlp_out_dim(l);
-        k_adam<<<(nw + 255) / 256, 256, 0, s>>>(p.wm[l], p.mw[l], p.vw[l], p.gw[l], p.w[l], nw, lr, b1t, b2t);
-        k_adam<<<(nb + 255) / 256, 256, 0, s>>>(p.b[l], p.mb[l], p.vb[l], p.gb[l], nullptr, nb, lr, b1t, b2t);
+void mlp_collect(const ProposalCtx& c, long long n, const float* contrib, const float4* prop, int cap, float4* pos4,
+                 float4* dir4, unsigned* count, float* wsum, cudaStream_t s) {
+    if (n <= 0) return;
+    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+    cudaMemsetAsync(wsum, 0, sizeof(float), s);
+    k_collect<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c, n, contrib, prop, cap, pos4, dir4, count, wsum);
+}
+
+void mlp_normalize_weights(float4* dir4, int n, const float* wsum, cudaStream_t s) {
+    if (n <= 0) return;
+    k_norm_weights<<<(n + 255) / 256, 256, 0, s>>>(dir4, n, wsum);
+}
+
+int mlp_train_step(MlpParams& p, MlpBatch& b, const float4* pos4, const float4* dir4, int n, float lr, bool apply,
+                   cudaStream_t s, int* err) {
+    if (n <= 0) return 0;
+    const size_t smem = SmemTrain::total;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
     }
+    const int total = (int)mlp_param_floats();
+    const int tiles = (n + 127) / 128;
+    const int grid = std::min(std::min(tiles, sm_count()), b.part_rows);
+    cudaMemsetAsync(b.loss, 0, sizeof(float), s);
+    k_mlp_train<<<grid, 128, smem, s>>>(p, pos4, dir4, n, 1.0f / (float)n, b.part, total, b.loss, err);
+    if (apply) p.adam_step++;
+    const float b1t = std::pow(0.9f, (float)std::max(p.adam_step, 1));
+    const float b2t = std::pow(0.999f, (float)std::max(p.adam_step, 1));
+    k_reduce_adam<<<(total + 255) / 256, 256, 0, s>>>(p, b.part, grid, total, apply ? 1 : 0, lr, b1t, b2t);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int mlp_train(MlpParams& p, MlpBatch& b, const float4* pos4, const float4* dir4, int total, int steps, float lr,
+              cudaStream_t s, int* err) {
+    if (total <= 0 || steps <= 0) return 0;
+    const int bn = b.n < total ? b.n : total;
+    for (int i = 0; i < steps; ++i) {
+        const int span = total - bn;
+        const int off = span > 0 ? (int)(((long long)i * 7919 * bn) % (span + 1)) : 0;
+        if (mlp_train_step(p, b, pos4 + off, dir4 + off, bn, lr, true, s, err)) return -1;
+    }
+    return 0;
+}
+
+void* MlpStore::alloc_bytes(size_t bytes) {
+    void* ptr = nullptr;
+    if (cudaMalloc(&ptr, bytes) != cudaSuccess) return nullptr;
+    cudaMemset(ptr, 0, bytes);
+    allocs.push_back(ptr);
+    return ptr;
+}
+
+bool MlpStore::setup(int n) {
+    release();
+    for (int l = 0; l < kMlpLayers; ++l) {
+        const size_t nw = (size_t)mlp_in_dim(l) * mlp_out_dim(l), nb = mlp_out_dim(l);
+        p.w[l] = alloc<__nv_bfloat16>(nw); p.b[l] = alloc<float>(nb); p.wm[l] = alloc<float>(nw);
+        p.gw[l] = alloc<float>(nw); p.gb[l] = alloc<float>(nb); p.mw[l] = alloc<float>(nw);
+        p.vw[l] = alloc<float>(nw); p.mb[l] = alloc<float>(nb); p.vb[l] = alloc<float>(nb);
+    }
+    b.n = n;
+    b.pos = alloc<float4>(n); b.dir = alloc<float4>(n); b.x = alloc<__nv_bfloat16>((size_t)n * kMlpIn);
+    for (int i = 0; i < 3; ++i) b.h[i] = alloc<__nv_bfloat16>((size_t)n * kMlpHid);
+    b.out = alloc<float>((size_t)n * kMlpOut);
+    b.loss = alloc<float>(1);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    b.part_rows = std::max(sms, 1);
+    b.part = alloc<float>((size_t)b.part_rows * mlp_param_floats());
+    for (void* a : allocs) if (!a) return false;
+    return true;
+}
+
+void MlpStore::release() {
+    for (void* a : allocs) if (a) cudaFree(a);
+    allocs.clear();
+    p = MlpParams{};
+    b = MlpBatch{};
 }
 
 }  // namespace rc
@@ -467,33 +747,7 @@ void mlp_adam(MlpParams& p, float lr, cudaStream_t s) {
 namespace rc {
 namespace {
 
-struct HostMlp {
-    MlpParams p{};
-    MlpBatch b{};
-    std::vector<void*> allocs;
-    template <class T> T* alloc(size_t n) {
-        void* ptr = nullptr;
-        if (cudaMalloc(&ptr, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
-        cudaMemset(ptr, 0, std::max<size_t>(n, 1) * sizeof(T));
-        allocs.push_back(ptr);
-        return static_cast<T*>(ptr);
-    }
-    bool setup(int n) {
-        for (int l = 0; l < kMlpLayers; ++l) {
-            const size_t nw = (size_t)mlp_in_dim(l) * mlp_out_dim(l), nb = mlp_out_dim(l);
-            p.w[l] = alloc<__nv_bfloat16>(nw); p.b[l] = alloc<float>(nb); p.wm[l] = alloc<float>(nw);
-            p.gw[l] = alloc<float>(nw); p.gb[l] = alloc<float>(nb); p.mw[l] = alloc<float>(nw);
-            p.vw[l] = alloc<float>(nw); p.mb[l] = alloc<float>(nb); p.vb[l] = alloc<float>(nb);
-        }
-        b.n = n;
-        b.pos = alloc<float4>(n); b.dir = alloc<float4>(n); b.x = alloc<__nv_bfloat16>((size_t)n * kMlpIn);
-        for (int i = 0; i < 3; ++i) b.h[i] = alloc<__nv_bfloat16>((size_t)n * kMlpHid);
-        b.out = alloc<float>((size_t)n * kMlpOut);
-        for (int l = 0; l < kMlpLayers; ++l) b.dy[l] = alloc<__nv_bfloat16>((size_t)n * mlp_out_dim(l));
-        b.loss = alloc<float>(1);
-        for (void* a : allocs) if (!a) return false;
-        return true;
-    }
+struct HostMlp : MlpStore {
     void set_weights(const float* packed) {
         size_t o = 0;
         for (int l = 0; l < kMlpLayers; ++l) {
@@ -511,7 +765,6 @@ struct HostMlp {
             cudaMemcpy(packed + o, src_b[l], 4 * nb, cudaMemcpyDeviceToHost); o += nb;
         }
     }
-    ~HostMlp() { for (void* a : allocs) cudaFree(a); }
 };
 
 }  // namespace
@@ -539,8 +792,9 @@ extern "C" int rc_mlp_forward_test(int n, const float* params, const float* pos4
     return 0;
 }
 
-// Loss and gradients: pos4 (xyz, w = light density at dir), dir4 (xyz, w = sample
-// weight); grads packed like params; *loss = mean weighted negative log-likelihood.
+// Loss and gradients (the fused training step without the Adam update): pos4 (xyz,
+// w = light density at dir), dir4 (xyz, w = sample weight); grads packed like params;
+// *loss = mean weighted negative log-likelihood.
 extern "C" int rc_mlp_grad_test(int n, const float* params, const float* pos4, const float* dir4, float* grads,
                                 float* loss) {
     using namespace rc;
@@ -551,7 +805,7 @@ extern "C" int rc_mlp_grad_test(int n, const float* params, const float* pos4, c
     cudaMemcpy(m.b.pos, pos4, 16 * (size_t)n, cudaMemcpyHostToDevice);
     cudaMemcpy(m.b.dir, dir4, 16 * (size_t)n, cudaMemcpyHostToDevice);
     int* err = m.alloc<int>(1);
-    if (mlp_forward_batch(m.p, m.b, 0, err) || mlp_backward_batch(m.p, m.b, 0, err)) return -3;
+    if (mlp_train_step(m.p, m.b, m.b.pos, m.b.dir, n, 0.0f, false, 0, err)) return -3;
     if (cudaDeviceSynchronize() != cudaSuccess) return -3;
     int h = 0;
     cudaMemcpy(&h, err, 4, cudaMemcpyDeviceToHost);
@@ -573,9 +827,8 @@ extern "C" int rc_mlp_train_test(int n, const float* params, const float* pos4, 
     cudaMemcpy(m.b.dir, dir4, 16 * (size_t)n, cudaMemcpyHostToDevice);
     int* err = m.alloc<int>(1);
     for (int i = 0; i < steps; ++i) {
-        if (mlp_forward_batch(m.p, m.b, 0, err) || mlp_backward_batch(m.p, m.b, 0, err)) return -3;
+        if (mlp_train_step(m.p, m.b, m.b.pos, m.b.dir, n, lr, true, 0, err)) return -3;
         cudaMemcpy(&losses[i], m.b.loss, 4, cudaMemcpyDeviceToHost);
-        mlp_adam(m.p, lr, 0);
     }
     if (cudaDeviceSynchronize() != cudaSuccess) return -3;
     int h = 0;

@@ -11,8 +11,13 @@
 // with the defensive fraction a = 0.2 of the light's own emission density.
 #pragma once
 #include <cuda_bf16.h>
-#include <cstdint>
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "vm.cuh"
 
 namespace rc {
 
@@ -43,26 +48,62 @@ struct MlpBatch {
     __nv_bfloat16* x;               // n x 80 encoded inputs
     __nv_bfloat16* h[3];            // n x 64 post-ReLU activations
     float* out;                     // n x 80 network outputs
-    __nv_bfloat16* dy[kMlpLayers];  // n x out_dim(l) gradients w.r.t. pre-activations
-    float* loss;                    // accumulated weighted loss (1 float)
+    float* loss;                    // weighted loss of the last step (1 float)
+    float* part;                    // per-CTA partial gradients (part_rows x parameters)
+    int part_rows;
     int n;
 };
 
-// Proposal context for the light pass.
-struct ProposalView {
-    const float4* prop;             // per light path: direction xyz | p_light / q
-    int enabled;
+// Owns the device buffers of one network (weights, gradients, Adam moments) and one
+// training batch of `n` rows.
+struct MlpStore {
+    MlpParams p{};
+    MlpBatch b{};
+    std::vector<void*> allocs;
+    void* alloc_bytes(size_t bytes);
+    template <class T>
+    T* alloc(size_t n) { return static_cast<T*>(alloc_bytes(std::max<size_t>(n, 1) * sizeof(T))); }
+    bool setup(int n);
+    void release();
+    MlpStore() = default;
+    MlpStore(const MlpStore&) = delete;
+    MlpStore& operator=(const MlpStore&) = delete;
+    ~MlpStore() { release(); }
+};
+
+// Emission proposal for the light pass: per light path index, the emission position
+// from the path's own primary samples, the MLP's mixture, a direction sample and the
+// throughput factor p_light / q.
+struct ProposalCtx {
+    LightsView lights;
+    float bmin[3], binv[3];   // scene box: normalised position = (p - bmin) * binv
+    uint64_t seed;
+    uint32_t iteration;
 };
 
 size_t mlp_param_floats();
+int mlp_proposal(const MlpParams& p, const ProposalCtx& c, long long n, float4* prop, cudaStream_t s, int* err);
+// Training samples from the light paths that contributed to the image (contrib > 0,
+// contrib = the gather's per-path sum of squared per-merge luminance):
+// pos4 = (normalised emission position, p_light(dir)), dir4 = (dir, sqrt(contrib)),
+// *wsum = the sum of the weights.  *count (device) receives the number of contributing
+// paths (may exceed cap; rows beyond cap are dropped).
+void mlp_collect(const ProposalCtx& c, long long n, const float* contrib, const float4* prop, int cap,
+                 float4* pos4, float4* dir4, unsigned* count, float* wsum, cudaStream_t s);
+void mlp_normalize_weights(float4* dir4, int n, const float* wsum, cudaStream_t s);
+// `steps` Adam steps on minibatches of b.n rows taken from (pos4, dir4)[0, total).
+int mlp_train(MlpParams& p, MlpBatch& b, const float4* pos4, const float4* dir4, int total, int steps, float lr,
+              cudaStream_t s, int* err);
 // Initialise weights (seeded), zero Adam state.
 int mlp_init(MlpParams& p, uint64_t seed, cudaStream_t s);
 // Forward on `n` normalised positions -> outputs (n x 80 FP32); saves activations when
 // the batch buffers are given.
 int mlp_forward_batch(const MlpParams& p, MlpBatch& b, cudaStream_t s, int* err);
-// Loss and its gradient w.r.t. the outputs, backward through the layers, weight and
-// bias gradients (zeroed first).  Tensor-core GEMMs for all matrix products.
-int mlp_backward_batch(const MlpParams& p, MlpBatch& b, cudaStream_t s, int* err);
-void mlp_adam(MlpParams& p, float lr, cudaStream_t s);
+// One training step on rows (pos4, dir4)[0, n): forward, loss gradient and backward
+// fused in one tensor-core kernel (weight gradients accumulated in TMEM per CTA), then
+// the partial sums reduced into gw/gb and, when `apply`, one Adam step (learning rate lr).
+// *b.loss receives the step's loss.
+int mlp_train_step(MlpParams& p, MlpBatch& b, const float4* pos4, const float4* dir4, int n, float lr, bool apply,
+                   cudaStream_t s, int* err);
 
 }  // namespace rc

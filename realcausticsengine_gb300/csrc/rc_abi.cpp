@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "host_scene.h"
+#include "mlp.cuh"
 #include "realcaustics.h"
 #include "vm.cuh"
 
@@ -76,6 +77,14 @@ struct DeviceState {
     DevBuf<uint2> qstart;
     DevBuf<unsigned char> qscratch;
     DevBuf<double> accum;
+    // learned emission proposal
+    std::unique_ptr<MlpStore> mlp;
+    DevBuf<float4> prop, train_pos, train_dir;
+    DevBuf<float> contrib, train_wsum;
+    DevBuf<unsigned> train_count;
+    cudaEvent_t evm[2] = {};
+    int mlp_rounds = 0;          // training rounds done (the proposal is used after the first)
+    double mlp_last_rows = 0;    // training samples collected in the last round
     int iterations_done = 0;
     double stats[16] = {};
     double last_nodes = 0;
@@ -95,6 +104,12 @@ struct DeviceState {
         tp0.release(); tp1.release(); tp2.release(); qorder.release(); qstart.release(); qscratch.release();
         box_lo.release(); box_hi.release();
         accum.release();
+        mlp.reset();
+        prop.release(); train_pos.release(); train_dir.release(); contrib.release(); train_wsum.release();
+        train_count.release();
+        mlp_rounds = 0;
+        mlp_last_rows = 0;
+        for (auto& e : evm) if (e) { cudaEventDestroy(e); e = nullptr; }
         for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
         if (t0) { cudaEventDestroy(t0); t0 = nullptr; }
         if (t1) { cudaEventDestroy(t1); t1 = nullptr; }
@@ -117,6 +132,10 @@ void default_config(rc_config* c) {
     c->write_exr = 1;
     std::snprintf(c->exr_path, sizeof(c->exr_path), "%s", "D:\\caustics.exr");
     c->verbose = 0;
+    c->learned_proposal = 0;
+    c->train_iterations = 8;
+    c->train_steps = 64;
+    c->learning_rate = 1e-3f;
 }
 
 const rc_config& cfg() {
@@ -142,6 +161,7 @@ int upload_scene(HostScene& sc) {
     if (!d.stream) {
         RC_CUDA(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
         for (auto& e : d.ev) RC_CUDA(cudaEventCreate(&e));
+        for (auto& e : d.evm) RC_CUDA(cudaEventCreate(&e));
         RC_CUDA(cudaEventCreate(&d.t0));
         RC_CUDA(cudaEventCreate(&d.t1));
     }
@@ -246,6 +266,7 @@ int check_errors() {
     if (h[ERR_STACK]) { g_err = "BVH traversal stack overflow (depth > 64)"; return RC_E_CAPACITY; }
     if (h[ERR_MATERIAL]) { g_err = "triangle material index out of range"; return RC_E_INVALID; }
     if (h[ERR_KD]) { g_err = "KD-tree build found inconsistent counts"; return RC_E_INVALID; }
+    if (h[ERR_MLP]) { g_err = "tensor-core pipeline wait timed out in the MLP"; return RC_E_CUDA; }
     return RC_OK;
 }
 
@@ -261,6 +282,7 @@ VMParams make_params(const HostScene& sc, int iteration) {
     const V3* src[4] = {&c.origin, &c.bottom_left, &c.horizontal, &c.vertical};
     for (int k = 0; k < 4; ++k) { dst[k][0] = src[k]->x; dst[k][1] = src[k]->y; dst[k][2] = src[k]->z; }
     p.seed = cfg().seed;
+    p.camera_seed = cfg().camera_seed ? cfg().camera_seed : cfg().seed;
     p.iteration = (uint32_t)iteration;
     long long npix = (long long)c.width * c.height;
     p.num_light_paths = cfg().photons_per_iter > 0 ? cfg().photons_per_iter : npix;
@@ -284,11 +306,85 @@ float ms_between(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
+ProposalCtx proposal_ctx(const HostScene& sc, const VMParams& p) {
+    ProposalCtx c{};
+    c.lights = p.lights;
+    const float mn[3] = {sc.bounds.mn.x, sc.bounds.mn.y, sc.bounds.mn.z};
+    const float mx[3] = {sc.bounds.mx.x, sc.bounds.mx.y, sc.bounds.mx.z};
+    for (int k = 0; k < 3; ++k) {
+        const float ext = mx[k] - mn[k];
+        c.bmin[k] = mn[k];
+        c.binv[k] = ext > 0.0f ? 1.0f / ext : 0.0f;
+    }
+    c.seed = p.seed;
+    c.iteration = p.iteration;
+    return c;
+}
+
+constexpr int kTrainBatchRows = 16384;
+constexpr int kTrainCapacity = 1 << 20;
+
+// Before the light pass: make sure the network exists and, once it has been trained,
+// write every light path's proposed emission direction and weight.
+int proposal_before(const HostScene& sc, VMParams& p, bool train) {
+    DeviceState& d = g_dev;
+    cudaStream_t s = d.stream;
+    const long long n = p.num_light_paths;
+    if (!d.mlp) {
+        d.mlp = std::make_unique<MlpStore>();
+        if (!d.mlp->setup(kTrainBatchRows)) { g_err = "MLP allocation failed"; return RC_E_CUDA; }
+        if (mlp_init(d.mlp->p, cfg().seed ^ 0x9E3779B97F4A7C15ull, s)) { g_err = "MLP init failed"; return RC_E_CUDA; }
+        RC_CUDA(d.train_pos.reserve(kTrainCapacity)); RC_CUDA(d.train_dir.reserve(kTrainCapacity));
+        RC_CUDA(d.train_count.reserve(1)); RC_CUDA(d.train_wsum.reserve(1));
+    }
+    if (d.mlp_rounds > 0) {
+        RC_CUDA(d.prop.reserve(std::max<long long>(n, 1)));
+        if (mlp_proposal(d.mlp->p, proposal_ctx(sc, p), n, d.prop.p, s, d.errors.p + ERR_MLP)) {
+            g_err = "proposal launch failed"; return RC_E_CUDA;
+        }
+        p.proposal = d.prop.p;
+    }
+    if (train) {
+        RC_CUDA(d.contrib.reserve(std::max<long long>(n, 1)));
+        RC_CUDA(cudaMemsetAsync(d.contrib.p, 0, sizeof(float) * std::max<long long>(n, 1), s));
+        p.path_contrib = d.contrib.p;
+        p.photon_path = d.ph_path.p;
+    }
+    return RC_OK;
+}
+
+// After the gather: collect (position, direction, weight) of the paths that reached the
+// image and take Adam steps on them.
+int proposal_train(const HostScene& sc, const VMParams& p) {
+    DeviceState& d = g_dev;
+    cudaStream_t s = d.stream;
+    unsigned rows = 0;
+    mlp_collect(proposal_ctx(sc, p), p.num_light_paths, d.contrib.p, p.proposal, kTrainCapacity, d.train_pos.p,
+                d.train_dir.p, d.train_count.p, d.train_wsum.p, s);
+    RC_CUDA(cudaGetLastError());
+    RC_CUDA(cudaMemcpyAsync(&rows, d.train_count.p, sizeof(rows), cudaMemcpyDeviceToHost, s));
+    RC_CUDA(cudaStreamSynchronize(s));
+    const int total = (int)std::min<unsigned>(rows, (unsigned)kTrainCapacity);
+    d.mlp_last_rows = total;
+    if (total < 256) return RC_OK;   // too few merged paths to learn from this round
+    mlp_normalize_weights(d.train_dir.p, total, d.train_wsum.p, s);
+    if (mlp_train(d.mlp->p, d.mlp->b, d.train_pos.p, d.train_dir.p, total, cfg().train_steps, cfg().learning_rate, s,
+                  d.errors.p + ERR_MLP)) {
+        g_err = "MLP training launch failed"; return RC_E_CUDA;
+    }
+    RC_CUDA(cudaGetLastError());
+    d.mlp_rounds++;
+    return RC_OK;
+}
+
 int render_iteration(HostScene& sc) {
     DeviceState& d = g_dev;
     cudaStream_t s = d.stream;
     const int it = d.iterations_done;
     VMParams p = make_params(sc, it);
+    const bool learned = cfg().learned_proposal && cfg().sampler == RC_SAMPLER_UNIFORM;
+    const bool train = learned && it < cfg().train_iterations;
+    float t_mlp = 0.0f;
     const long long npix = (long long)sc.camera.width * sc.camera.height;
     if (d.accum.n < (size_t)(3 * npix)) {
         RC_CUDA(d.accum.reserve(3 * npix));
@@ -307,6 +403,12 @@ int render_iteration(HostScene& sc) {
         RC_CUDA(d.ph_tp.reserve(cap)); RC_CUDA(d.ph_path.reserve(cap));
         RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
         PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, cap, d.counters.p};
+        if (learned) {
+            RC_CUDA(cudaEventRecord(d.evm[0], s));
+            int r = proposal_before(sc, p, train);
+            if (r) return r;
+            RC_CUDA(cudaEventRecord(d.evm[1], s));
+        }
         RC_CUDA(cudaEventRecord(d.ev[0], s));
         if (sampler == RC_SAMPLER_UNIFORM) launch_light_pass(p, ph, d.counters.p + 6, s);
         else launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
@@ -317,6 +419,7 @@ int render_iteration(HostScene& sc) {
             RC_CUDA(cudaMemcpyAsync(mlt, d.counters.p + 2, sizeof(mlt), cudaMemcpyDeviceToHost, s));
         RC_CUDA(cudaStreamSynchronize(s));
         t_light = ms_between(d.ev[0], d.ev[1]);
+        if (learned) t_mlp = ms_between(d.evm[0], d.evm[1]);
         if ((long long)nph <= cap) break;
         cap = (long long)nph + nph / 8 + 1024;
         if (attempt == 2) { g_err = "photon buffer overflow"; return RC_E_CAPACITY; }
@@ -400,6 +503,16 @@ int render_iteration(HostScene& sc) {
     unsigned long long gc[4] = {0, 0, 0, 0};
     RC_CUDA(cudaMemcpyAsync(gc, d.counters.p + 2, sizeof(gc), cudaMemcpyDeviceToHost, s));
     RC_CUDA(cudaStreamSynchronize(s));
+    if (train) {
+        RC_CUDA(cudaEventRecord(d.evm[0], s));
+        r = proposal_train(sc, p);
+        if (r) return r;
+        RC_CUDA(cudaEventRecord(d.evm[1], s));
+        RC_CUDA(cudaEventSynchronize(d.evm[1]));
+        t_mlp += ms_between(d.evm[0], d.evm[1]);
+        r = check_errors();
+        if (r) return r;
+    }
     d.iterations_done++;
     double* st = d.stats;
     st[0] = (double)p.num_light_paths;
@@ -413,8 +526,8 @@ int render_iteration(HostScene& sc) {
     st[5] = ms_between(d.ev[2], d.ev[3]);
     st[6] = t_cam;
     st[7] = ms_between(d.ev[6], d.ev[7]);
-    st[8] = 0.0;
-    st[9] = st[4] + st[5] + st[6] + st[7];
+    st[8] = t_mlp;           // proposal inference + training
+    st[9] = st[4] + st[5] + st[6] + st[7] + st[8];
     st[10] = d.iterations_done;
     st[11] = sc.scene_radius;
     st[12] = std::sqrt(p.radius_sqr);
@@ -597,6 +710,12 @@ int rc_set_config(const rc_config* c) {
     if (c->sampler != RC_SAMPLER_UNIFORM && c->sampler != RC_SAMPLER_HYBRID && c->sampler != RC_SAMPLER_PSSMLT) {
         g_err = "unknown sampler"; return RC_E_INVALID;
     }
+    if (c->learned_proposal) {
+        if (c->sampler != RC_SAMPLER_UNIFORM) { g_err = "learned_proposal requires the uniform sampler"; return RC_E_UNSUPPORTED; }
+        if (c->train_iterations < 0 || c->train_steps < 0 || !(c->learning_rate > 0.0f && c->learning_rate < 1.0f)) {
+            g_err = "learned proposal: train_iterations/train_steps >= 0, learning_rate in (0, 1)"; return RC_E_INVALID;
+        }
+    }
     if (c->sampler != RC_SAMPLER_UNIFORM) {
         if (c->mlt_chains <= 0) { g_err = "mlt_chains must be positive"; return RC_E_INVALID; }
         if (c->max_path_length > kMltMaxPathLength) { g_err = "Metropolis samplers support max_path_length <= 12"; return RC_E_UNSUPPORTED; }
@@ -682,6 +801,22 @@ const char* rc_last_error(void) { return g_err.c_str(); }
 int rc_get_stats(double* out, int n) {
     if (!out || n < 0) return RC_E_INVALID;
     for (int i = 0; i < n && i < 16; ++i) out[i] = g_dev.stats[i];
+    return RC_OK;
+}
+
+int rc_proposal_state(long long n, float* prop4, float* contrib) {
+    if (n < 0) { g_err = "n < 0"; return RC_E_INVALID; }
+    DeviceState& d = g_dev;
+    if (prop4) {
+        std::memset(prop4, 0, sizeof(float) * 4 * (size_t)n);
+        const long long m = std::min<long long>(n, (long long)d.prop.n);
+        if (d.mlp_rounds > 0 && m > 0) RC_CUDA(cudaMemcpy(prop4, d.prop.p, sizeof(float4) * m, cudaMemcpyDeviceToHost));
+    }
+    if (contrib) {
+        std::memset(contrib, 0, sizeof(float) * (size_t)n);
+        const long long m = std::min<long long>(n, (long long)d.contrib.n);
+        if (m > 0) RC_CUDA(cudaMemcpy(contrib, d.contrib.p, sizeof(float) * m, cudaMemcpyDeviceToHost));
+    }
     return RC_OK;
 }
 

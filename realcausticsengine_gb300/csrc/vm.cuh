@@ -61,17 +61,22 @@ struct VMParams {
     const DevMaterial* materials;
     int num_materials;
     DevCamera camera;
-    uint64_t seed;
+    uint64_t seed;            // light-path samples
+    uint64_t camera_seed;     // camera-path samples
     uint32_t iteration;
     long long num_light_paths;
     int max_path_length;
     float radius_sqr;
     float vm_norm;
     int* error;             // device flags: [0] stack overflow, [1] bad material
+    const float4* proposal; // learned emission proposal per light path (nullptr: none)
+    float* path_contrib;    // gather: per light path, sum over its merges of the squared
+                            // luminance each adds to its pixel (proposal training)
+    const uint32_t* photon_path;   // photon buffer index -> light path (with path_contrib)
 };
 
 // error flag slots
-enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_KD = 4, ERR_COUNT = 8 };
+enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_KD = 4, ERR_MLP = 5, ERR_COUNT = 8 };
 
 // Metropolis light pass (RC_SAMPLER_HYBRID / RC_SAMPLER_PSSMLT), `chains` chains in one
 // launch; stats[0] = visible large steps, stats[1] = large steps (HYBRID: light paths).

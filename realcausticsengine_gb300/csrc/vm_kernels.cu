@@ -1,52 +1,12 @@
 // Light pass, camera pass and the closest-hit parity kernel.
 #include "vm.cuh"
 #include "bsdf.cuh"
+#include "lights.cuh"
 #include "rng.cuh"
 
 namespace rc {
 
 namespace {
-
-// find_interval (src/utils.h:142-157)
-__device__ __forceinline__ int find_interval(const float* cdf, int size, float u) {
-    int first = 0, len = size;
-    while (len > 0) {
-        int half = len >> 1, middle = first + half;
-        if (cdf[middle] < u) { first = middle + 1; len -= half + 1; }
-        else len = half;
-    }
-    int v = first - 1;
-    return v < 0 ? 0 : (v > size - 2 ? size - 2 : v);
-}
-
-// Lights_list::sample_lights (src/Light_list.cpp:10-30) with Area_Light::sample_light
-// (src/Lights.cpp:41-55) and Sun_Light::sample_light (src/Lights.cpp:122-136).
-// The point light, a stub in the reference, emits uniformly over the sphere.
-__device__ __forceinline__ void sample_light(const LightsView& L, float u0, float u1, float u2, float u3, float u4,
-                                             F3& o, F3& d, F3& tp) {
-    int idx = find_interval(L.cdf, L.count + 1, u0);
-    const DevLight& l = L.lights[idx];
-    float pick = l.power / (L.count * L.integral);
-    if (l.type == LIGHT_AREA) {
-        o = ld3(l.bl) + ld3(l.hz) * u1 + ld3(l.vt) * u2;
-        F3 local = cos_hemisphere(u3, u4);
-        d = ld3(l.fx) * local.x + ld3(l.fy) * local.y + ld3(l.fz) * local.z;
-        tp = f3(l.cr, l.cg, l.cb) * kPI;
-    } else if (l.type == LIGHT_SUN) {
-        o = ld3(l.bl) + ld3(l.hz) * u1 + ld3(l.vt) * u2;
-        d = ld3(l.fz);
-        tp = f3(l.cr, l.cg, l.cb);
-    } else {
-        o = ld3(l.pos);
-        float z = 1.0f - 2.0f * u3;
-        float r = sqrtf(ref_max(0.0f, 1.0f - z * z));
-        float s, c;
-        sincosf(kPI2 * u4, &s, &c);
-        d = f3(r * c, r * s, z);
-        tp = f3(l.cr, l.cg, l.cb) * (4.0f * kPI);
-    }
-    tp = div_each(tp, pick);
-}
 
 // Warp-aggregated append: one atomic per converged group of lanes.
 __device__ __forceinline__ unsigned long long warp_append(unsigned long long* counter) {
@@ -73,15 +33,28 @@ struct LightPath {
     PathRng rng;
 };
 
-__device__ __forceinline__ void light_path_start(const VMParams& P, long long pidx, LightPath& s) {
+// Emission: the light's own direction sampling, or the learned proposal's direction
+// with throughput factor p_light / q (0 when the direction leaves no emission).
+__device__ __forceinline__ bool light_path_start(const VMParams& P, long long pidx, LightPath& s) {
     s.idx = pidx;
     s.rng.init(P.seed, (uint64_t)pidx, P.iteration, STREAM_LIGHT);
     U4 b0 = s.rng.block(0), b1 = s.rng.block(1);
-    sample_light(P.lights, u01(b0.a), u01(b0.b), u01(b0.c), u01(b0.d), u01(b1.a), s.o, s.d, s.tp);
+    const LightSample ls = light_position(P.lights, u01(b0.a), u01(b0.b), u01(b0.c));
+    s.o = ls.o;
+    if (P.proposal) {
+        const float4 pr = __ldg(&P.proposal[pidx]);
+        if (!(pr.w > 0.0f)) return false;
+        s.d = f3(pr.x, pr.y, pr.z);
+        s.tp = ls.tp * pr.w;
+    } else {
+        s.d = light_direction(P.lights.lights[ls.idx], u01(b0.d), u01(b1.a));
+        s.tp = ls.tp;
+    }
     s.diffuse = 0;
     s.last = EV_DIFFUSE;
     s.dVM = 0.0f;
     s.len = 0;
+    return true;
 }
 
 // One bounce of Vertex_Merging::trace_light_path (src/Vertex_Merging.cpp:140-194);
@@ -143,10 +116,7 @@ __global__ void __launch_bounds__(256) k_light_pass_persistent(const VMParams P,
             base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
             if (!alive) {
                 const unsigned long long mine = base + __popc(need & ((1u << lane) - 1u));
-                if (mine < (unsigned long long)P.num_light_paths) {
-                    light_path_start(P, (long long)mine, s);
-                    alive = true;
-                }
+                if (mine < (unsigned long long)P.num_light_paths) alive = light_path_start(P, (long long)mine, s);
             }
             if (base + __popc(need) >= (unsigned long long)P.num_light_paths) pool_left = false;
         }
@@ -211,7 +181,7 @@ __global__ void __launch_bounds__(256) k_camera_pass(const VMParams P, QueryBuf 
     const int W = P.camera.width, H = P.camera.height;
     if (pix >= (long long)W * H) return;
     PathRng rng;
-    rng.init(P.seed, (uint64_t)pix, P.iteration, STREAM_CAMERA);
+    rng.init(P.camera_seed, (uint64_t)pix, P.iteration, STREAM_CAMERA);
     U4 b1 = rng.block(1);
     // Generate_camera_sample (src/Vertex_Merging.cpp:27-46)
     const float x = (float)(int)(pix % W);
@@ -283,7 +253,7 @@ struct CameraPath {
 // sample falls outside the image buffer (camera row 0, src/Image_Buffer.h:28-31).
 __device__ __forceinline__ bool camera_path_start(const VMParams& P, long long pix, CameraPath& s) {
     const int W = P.camera.width, H = P.camera.height;
-    s.rng.init(P.seed, (uint64_t)pix, P.iteration, STREAM_CAMERA);
+    s.rng.init(P.camera_seed, (uint64_t)pix, P.iteration, STREAM_CAMERA);
     U4 b1 = s.rng.block(1);
     const float x = (float)(int)(pix % W);
     const float y = (float)(int)(pix / W);
