@@ -15,21 +15,27 @@ namespace {
 constexpr uint32_t kWait = 1u << 22;
 constexpr float kKappaMin = 0.1f, kKappaMax = 2000.0f;
 
+// sin/cos(2^k pi c) for k = 0..11: sincospi at k = 0, then the double-angle identities
+// sin 2a = 2 sin a cos a, cos 2a = 1 - 2 sin^2 a (rounding error doubles per step:
+// below 3e-4 at k = 11, under the BF16 rounding of the network input).
 __device__ __forceinline__ void encode(float px, float py, float pz, float* x) {
     const float c[3] = {px, py, pz};
-    int o = 0;
+#pragma unroll
     for (int i = 0; i < 3; ++i) {
-        x[o++] = c[i];
-        float f = 1.0f;
+        float sn, cs;
+        sincospif(c[i], &sn, &cs);
+        x[25 * i] = c[i];
+#pragma unroll
         for (int k = 0; k < kMlpFreqs; ++k) {
-            float s, co;
-            sincospif(f * c[i], &s, &co);
-            x[o++] = s;
-            x[o++] = co;
-            f *= 2.0f;
+            x[25 * i + 1 + 2 * k] = sn;
+            x[25 * i + 2 + 2 * k] = cs;
+            const float s2 = 2.0f * sn * cs;
+            cs = 1.0f - 2.0f * sn * sn;
+            sn = s2;
         }
     }
-    for (; o < kMlpIn; ++o) x[o] = 0.0f;
+#pragma unroll
+    for (int o = 3 * (1 + 2 * kMlpFreqs); o < kMlpIn; ++o) x[o] = 0.0f;
 }
 
 __device__ __forceinline__ float softplus(float v) { return v > 20.0f ? v : log1pf(expf(v)); }
@@ -71,12 +77,54 @@ struct SmemFwd {
     static constexpr int total = bias + 272 * 4;
 };
 
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    const __nv_bfloat162 t = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&t);
+}
+
 __device__ __forceinline__ void store_row_bf16(unsigned char* base, int row, const float* v, int K) {
+#pragma unroll
     for (int k = 0; k < K; k += 8) {
-        __align__(16) __nv_bfloat16 t[8];
-        for (int j = 0; j < 8; ++j) t[j] = __float2bfloat16_rn(v[k + j]);
-        *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, k, K)) = *reinterpret_cast<const uint4*>(t);
+        const uint4 t = make_uint4(pack_bf16x2(v[k], v[k + 1]), pack_bf16x2(v[k + 2], v[k + 3]),
+                                   pack_bf16x2(v[k + 4], v[k + 5]), pack_bf16x2(v[k + 6], v[k + 7]));
+        *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, k, K)) = t;
     }
+}
+
+// One layer of the fused forward: product on the tensor cores, bias (+ ReLU for the
+// hidden layers) in the epilogue; hidden activations go back to the activation tile,
+// the output layer's 80 values stay in v.  False if the product did not complete.
+template <int L>
+__device__ __forceinline__ bool fwd_layer(uint32_t tm, uint32_t lane_base, unsigned char* Act,
+                                          const unsigned char* W, const float* bias, float* v, uint64_t* mbar,
+                                          uint32_t& phase, int* err) {
+    constexpr int K = mlp_in_dim(L), N = mlp_out_dim(L);
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+        tc::gemm_issue(tm, Act, W, K, N, false, mbar);
+    }
+    const bool ok = tc::mbar_wait(mbar, phase, kWait);
+    phase ^= 1u;
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicOr(err, 1);
+        return false;
+    }
+    tc::fence_after_sync();
+#pragma unroll
+    for (int c = 0; c < N; c += 16) tc::tmem_ld16(tm + lane_base + (uint32_t)c, v + c);
+    const float* bl = bias + 64 * L;
+    if (L < 3) {
+#pragma unroll
+        for (int c = 0; c < N; ++c) v[c] = fmaxf(v[c] + bl[c], 0.0f);
+        store_row_bf16(Act, threadIdx.x, v, N);
+    } else {
+#pragma unroll
+        for (int c = 0; c < N; ++c) v[c] += bl[c];
+    }
+    return true;
 }
 
 template <class IO>
@@ -117,40 +165,18 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpParams P, IO io, l
     for (long long tile = blockIdx.x; tile * 128 < n && !failed; tile += gridDim.x) {
         const long long row = tile * 128 + tid;
         const bool valid = row < n;
+        typename IO::State st;
         {
             float x[kMlpIn];
-            io.input(row, valid, x);
+            io.input(row, valid, x, st);
             store_row_bf16(Act, tid, x, kMlpIn);
         }
-        for (int l = 0; l < 4 && !failed; ++l) {
-            const int K = mlp_in_dim(l), N = mlp_out_dim(l);
-            tc::fence_proxy_async();
-            tc::fence_before_sync();
-            __syncthreads();
-            if (tid == 0) {
-                tc::fence_after_sync();
-                tc::gemm_issue(tm, Act, Ws[l], K, N, false, &mbar);
-            }
-            bool ok = tc::mbar_wait(&mbar, phase, kWait);
-            phase ^= 1u;
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) atomicOr(err, 1);
-                failed = true;
-                break;
-            }
-            tc::fence_after_sync();
-            float v[kMlpOut];
-            for (int c = 0; c < N; c += 16) tc::tmem_ld16(tm + lane_base + (uint32_t)c, v + c);
-            const float* bl = bias + 64 * l;
-            if (l < 3) {
-                for (int c = 0; c < N; ++c) v[c] = fmaxf(v[c] + bl[c], 0.0f);
-                io.save_hidden(l, row, valid, v);
-                store_row_bf16(Act, tid, v, N);
-            } else {
-                for (int c = 0; c < N; ++c) v[c] += bl[c];
-                io.output(row, valid, v);
-            }
-        }
+        float v[kMlpOut];
+        failed = !fwd_layer<0>(tm, lane_base, Act, Ws[0], bias, v, &mbar, phase, err) ||
+                 !fwd_layer<1>(tm, lane_base, Act, Ws[1], bias, v, &mbar, phase, err) ||
+                 !fwd_layer<2>(tm, lane_base, Act, Ws[2], bias, v, &mbar, phase, err) ||
+                 !fwd_layer<3>(tm, lane_base, Act, Ws[3], bias, v, &mbar, phase, err);
+        if (!failed) io.output(row, valid, v, st);
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -158,23 +184,21 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const MlpParams P, IO io, l
 }
 
 struct BatchIO {
+    struct State {};
     const float4* pos;
-    __nv_bfloat16* x;
-    __nv_bfloat16* h0; __nv_bfloat16* h1; __nv_bfloat16* h2;
     float* out;
-    __device__ void input(long long row, bool valid, float* x_out) const {
-        if (!valid) { for (int i = 0; i < kMlpIn; ++i) x_out[i] = 0.0f; return; }
+    __device__ __forceinline__ void input(long long row, bool valid, float* x_out, State&) const {
+        if (!valid) {
+#pragma unroll
+            for (int i = 0; i < kMlpIn; ++i) x_out[i] = 0.0f;
+            return;
+        }
         float4 p = pos[row];
         encode(p.x, p.y, p.z, x_out);
-        if (x) for (int i = 0; i < kMlpIn; ++i) x[row * kMlpIn + i] = __float2bfloat16_rn(x_out[i]);
     }
-    __device__ void save_hidden(int l, long long row, bool valid, const float* h) const {
-        __nv_bfloat16* dst = l == 0 ? h0 : (l == 1 ? h1 : h2);
-        if (!valid || !dst) return;
-        for (int i = 0; i < kMlpHid; ++i) dst[row * kMlpHid + i] = __float2bfloat16_rn(h[i]);
-    }
-    __device__ void output(long long row, bool valid, const float* o) const {
+    __device__ __forceinline__ void output(long long row, bool valid, const float* o, const State&) const {
         if (!valid) return;
+#pragma unroll
         for (int i = 0; i < kMlpOut; ++i) out[row * kMlpOut + i] = o[i];
     }
 };
@@ -191,25 +215,42 @@ __device__ __forceinline__ F3 sample_vmf(F3 mu, float kappa, float u1, float u2)
     return f.x * (st * cp) + f.y * (st * sp) + mu * w;
 }
 
+// Fast-intrinsic vMF density for the proposal weights (relative error ~1e-6 against
+// the sampler's own density: a bias of that order in p_light / q).
+__device__ __forceinline__ float vmf_pdf_fast(float kappa, float cosang) {
+    return kappa * __expf(kappa * (cosang - 1.0f)) / (kPI2 * (1.0f - __expf(-2.0f * kappa)));
+}
+__device__ __forceinline__ float kappa_of(float raw) {
+    const float sp = raw > 20.0f ? raw : __logf(1.0f + __expf(raw));
+    return fminf(kKappaMin + sp, kKappaMax);
+}
+
 struct ProposalIO {
+    struct State {
+        int light;
+        float u3, u4, xi;
+    };
     ProposalCtx c;
     float4* prop;
-    __device__ void input(long long row, bool valid, float* x) const {
-        if (!valid) { for (int i = 0; i < kMlpIn; ++i) x[i] = 0.0f; return; }
-        PathRng g;
-        g.init(c.seed, (uint64_t)row, c.iteration, STREAM_LIGHT);
-        const U4 b0 = g.block(0);
-        const LightSample ls = light_position(c.lights, u01(b0.a), u01(b0.b), u01(b0.c));
-        encode((ls.o.x - c.bmin[0]) * c.binv[0], (ls.o.y - c.bmin[1]) * c.binv[1], (ls.o.z - c.bmin[2]) * c.binv[2], x);
-    }
-    __device__ void save_hidden(int, long long, bool, const float*) const {}
-    __device__ void output(long long row, bool valid, const float* o) const {
-        if (!valid) return;
+    __device__ __forceinline__ void input(long long row, bool valid, float* x, State& st) const {
+        if (!valid) {
+#pragma unroll
+            for (int i = 0; i < kMlpIn; ++i) x[i] = 0.0f;
+            return;
+        }
         PathRng g;
         g.init(c.seed, (uint64_t)row, c.iteration, STREAM_LIGHT);
         const U4 b0 = g.block(0), b1 = g.block(1);
         const LightSample ls = light_position(c.lights, u01(b0.a), u01(b0.b), u01(b0.c));
-        const DevLight& l = c.lights.lights[ls.idx];
+        st.light = ls.idx;
+        st.u3 = u01(b0.d);
+        st.u4 = u01(b1.a);
+        st.xi = u01(b1.b);
+        encode((ls.o.x - c.bmin[0]) * c.binv[0], (ls.o.y - c.bmin[1]) * c.binv[1], (ls.o.z - c.bmin[2]) * c.binv[2], x);
+    }
+    __device__ __forceinline__ void output(long long row, bool valid, const float* o, const State& st) const {
+        if (!valid) return;
+        const DevLight& l = c.lights.lights[st.light];
         if (l.type == LIGHT_SUN) { prop[row] = make_float4(l.fz[0], l.fz[1], l.fz[2], 1.0f); return; }
         // mixture over the 80 outputs with static indexing only (keeps them in registers)
         float mxl = -INFINITY;
@@ -217,13 +258,12 @@ struct ProposalIO {
         for (int k = 0; k < kMlpLobes; ++k) mxl = fmaxf(mxl, o[5 * k]);
         float e[kMlpLobes], sum = 0.0f;
 #pragma unroll
-        for (int k = 0; k < kMlpLobes; ++k) { e[k] = expf(o[5 * k] - mxl); sum += e[k]; }
-        const float xi = u01(b1.b), u3 = u01(b0.d), u4 = u01(b1.a);
+        for (int k = 0; k < kMlpLobes; ++k) { e[k] = __expf(o[5 * k] - mxl); sum += e[k]; }
         F3 w;
-        if (xi < kMlpDefensive) {
-            w = light_direction(l, u3, u4);
+        if (st.xi < kMlpDefensive) {
+            w = light_direction(l, st.u3, st.u4);
         } else {
-            const float t = (xi - kMlpDefensive) / (1.0f - kMlpDefensive) * sum;
+            const float t = (st.xi - kMlpDefensive) / (1.0f - kMlpDefensive) * sum;
             float cum = 0.0f, kap = 1.0f;
             F3 mu = f3(0.0f, 0.0f, 1.0f);
             bool chosen = false;
@@ -235,19 +275,18 @@ struct ProposalIO {
                     const float x = o[5 * k + 1], y = o[5 * k + 2], z = o[5 * k + 3];
                     const float len = fmaxf(sqrtf(x * x + y * y + z * z), 1e-6f);
                     mu = f3(x / len, y / len, z / len);
-                    kap = fminf(kKappaMin + softplus(o[5 * k + 4]), kKappaMax);
+                    kap = kappa_of(o[5 * k + 4]);
                 }
             }
-            w = sample_vmf(mu, kap, u3, u4);
+            w = sample_vmf(mu, kap, st.u3, st.u4);
         }
         const float pl = light_direction_pdf(l, w);
         float S = 0.0f;
 #pragma unroll
         for (int k = 0; k < kMlpLobes; ++k) {
             const float x = o[5 * k + 1], y = o[5 * k + 2], z = o[5 * k + 3];
-            const float len = fmaxf(sqrtf(x * x + y * y + z * z), 1e-6f);
-            const float kap = fminf(kKappaMin + softplus(o[5 * k + 4]), kKappaMax);
-            S += e[k] * vmf_pdf(kap, (x * w.x + y * w.y + z * w.z) / len);
+            const float rl = rsqrtf(fmaxf(x * x + y * y + z * z, 1e-12f));
+            S += e[k] * vmf_pdf_fast(kappa_of(o[5 * k + 4]), (x * w.x + y * w.y + z * w.z) * rl);
         }
         const float q = kMlpDefensive * pl + (1.0f - kMlpDefensive) * (S / sum);
         prop[row] = make_float4(w.x, w.y, w.z, (pl > 0.0f && q > 0.0f) ? pl / q : 0.0f);
@@ -373,6 +412,7 @@ __device__ __forceinline__ uint32_t col_b(int l) { return 272u + 16u * (uint32_t
 constexpr uint32_t kColT = 336;
 
 __device__ __forceinline__ void store_col_bf16(unsigned char* base, int r, const float* v, int cnt) {
+#pragma unroll
     for (int i = 0; i < cnt; ++i)
         *reinterpret_cast<__nv_bfloat16*>(base + tc::kmajor_offset(i, r, 128)) = __float2bfloat16_rn(v[i]);
 }
@@ -469,13 +509,16 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(const MlpParams P, const f
                 tc::gemm_issue(tm + kColT, Act, Wf[l], K, N, false, &mbar);
             }
             if (!cta_sync_wait(&mbar, phase, err, 4)) { failed = true; break; }
+#pragma unroll
             for (int c = 0; c < N; c += 16) tc::tmem_ld16(tm + lane_base + kColT + (uint32_t)c, v + c);
             const float* bl = bias + 64 * l;
             if (l < 3) {
+#pragma unroll
                 for (int c = 0; c < N; ++c) v[c] = fmaxf(v[c] + bl[c], 0.0f);
                 store_row_bf16(Act, tid, v, N);
                 store_col_bf16(InT[l + 1], tid, v, N);
             } else {
+#pragma unroll
                 for (int c = 0; c < N; ++c) v[c] += bl[c];
             }
         }
@@ -505,7 +548,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(const MlpParams P, const f
             }
             if (l > 0) {
                 float g[kMlpHid];
+#pragma unroll
                 for (int c = 0; c < in; c += 16) tc::tmem_ld16(tm + lane_base + kColT + (uint32_t)c, g + c);
+#pragma unroll
                 for (int i = 0; i < in; ++i) {
                     const float h = __bfloat162float(
                         *reinterpret_cast<const __nv_bfloat16*>(InT[l] + tc::kmajor_offset(i, tid, 128)));
@@ -526,6 +571,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(const MlpParams P, const f
         for (int l = 0; l < 4; ++l) {
             const int in = mlp_in_dim(l), out = mlp_out_dim(l);
             float t[16];
+#pragma unroll
             for (int c = 0; c < in; c += 16) {
                 tc::tmem_ld16(tm + lane_base + col_w(l) + (uint32_t)c, t);
                 if (tid < out)
@@ -630,7 +676,7 @@ int mlp_init(MlpParams& p, uint64_t seed, cudaStream_t s) {
 
 int mlp_forward_batch(const MlpParams& p, MlpBatch& b, cudaStream_t s, int* err) {
     if (b.n <= 0) return 0;
-    BatchIO io{b.pos, b.x, b.h[0], b.h[1], b.h[2], b.out};
+    BatchIO io{b.pos, b.out};
     const size_t smem = SmemFwd::total;
     static bool attr = false;
     if (!attr) {
@@ -721,8 +767,7 @@ bool MlpStore::setup(int n) {
         p.vw[l] = alloc<float>(nw); p.mb[l] = alloc<float>(nb); p.vb[l] = alloc<float>(nb);
     }
     b.n = n;
-    b.pos = alloc<float4>(n); b.dir = alloc<float4>(n); b.x = alloc<__nv_bfloat16>((size_t)n * kMlpIn);
-    for (int i = 0; i < 3; ++i) b.h[i] = alloc<__nv_bfloat16>((size_t)n * kMlpHid);
+    b.pos = alloc<float4>(n); b.dir = alloc<float4>(n);
     b.out = alloc<float>((size_t)n * kMlpOut);
     b.loss = alloc<float>(1);
     int dev = 0, sms = 0;

@@ -45,9 +45,7 @@ struct MlpParams {
 struct MlpBatch {
     float4* pos;                    // normalised position (xyz)
     float4* dir;                    // sampled direction (xyz) | weight f / q_old
-    __nv_bfloat16* x;               // n x 80 encoded inputs
-    __nv_bfloat16* h[3];            // n x 64 post-ReLU activations
-    float* out;                     // n x 80 network outputs
+    float* out;                     // n x 80 network outputs (forward test)
     float* loss;                    // weighted loss of the last step (1 float)
     float* part;                    // per-CTA partial gradients (part_rows x parameters)
     int part_rows;
@@ -96,8 +94,7 @@ int mlp_train(MlpParams& p, MlpBatch& b, const float4* pos4, const float4* dir4,
               cudaStream_t s, int* err);
 // Initialise weights (seeded), zero Adam state.
 int mlp_init(MlpParams& p, uint64_t seed, cudaStream_t s);
-// Forward on `n` normalised positions -> outputs (n x 80 FP32); saves activations when
-// the batch buffers are given.
+// Forward on b.n normalised positions (b.pos) -> b.out (n x 80 FP32).
 int mlp_forward_batch(const MlpParams& p, MlpBatch& b, cudaStream_t s, int* err);
 // One training step on rows (pos4, dir4)[0, n): forward, loss gradient and backward
 // fused in one tensor-core kernel (weight gradients accumulated in TMEM per CTA), then
