@@ -16,6 +16,8 @@ queries), radius gather with FP64 accumulation.
           event-timed duration, against MEASURED_PEAKS.json hbm_gbs
   cpu_baseline  the reference's own estimator on the host cores (oracle port of the
           reference, bit-identical to it on the reference-renderable variant)
+  learned_vs_plain  per-pixel RMSE against a reference image versus device time for
+          learned-guided and plain vertex merging (same workload, 16 iterations each)
 
 --impl reference times that CPU implementation alone.  --gpus N > 1 runs N
 independent replicas (the path is not sharded; torchrun launches one rank per GPU).
@@ -264,9 +266,65 @@ def run_ours(args):
         "phase_ms_per_step": {k: st[k] for k in ("light_ms", "kd_ms", "camera_ms", "gather_ms")},
         "wall_s": wall,
     }
+    if not args.no_learned:
+        line["learned_vs_plain"] = learned_equal_time(args)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cores=args.cpu_cores)
     print(json.dumps(line), flush=True)
+
+
+def learned_equal_time(args, iters: int = 16, ref_iters: int = 48):
+    """Learned-guided vs plain vertex merging on the same workload, per-pixel RMSE of the
+    FP64-accumulated image against a reference image, as a function of device time.
+
+    Reference: plain, `ref_iters` iterations, independent light and camera seeds.  Plain
+    and learned share their seeds (camera paths identical between them, not with the
+    reference); learned trains on iterations 0..7 (64 Adam steps each, lr 1e-3) and
+    guides from iteration 1.  Reports both curves' end points, the learned RMSE at the
+    plain run's total device time, and the device-time ratio to reach the plain run's
+    final RMSE (None when the learned run does not reach it in `iters` iterations)."""
+    from realcausticsengine_gb300 import scenes
+    from realcausticsengine_gb300.session import Renderer
+
+    sc = scenes.water_pool(args.width, args.height, grid=args.grid, samples=ref_iters)
+
+    def run(n, seed, camera_seed, learned, ref=None):
+        r = Renderer(sc, max_path_length=MAX_PATH, photons_per_iter=args.photons, seed=seed, camera_seed=camera_seed,
+                     learned_proposal=learned, train_iterations=8, train_steps=64, learning_rate=1e-3)
+        r.prepare()
+        t, curve = 0.0, []
+        for _ in range(n):
+            r.render(1)
+            t += r.stats()["device_ms"]
+            if ref is not None:
+                img = r.image().astype(np.float64)
+                curve.append((t, float(np.sqrt(((img - ref) ** 2).mean()))))
+        img = r.image().astype(np.float64)
+        r.release()
+        return img, curve
+
+    ref, _ = run(ref_iters, 1001, 1002, False)
+    _, plain = run(iters, 7, 8, False, ref)
+    _, learned = run(iters, 7, 8, True, ref)
+    t_plain, e_plain = plain[-1]
+
+    def at_time(curve, t):
+        prev = None
+        for tc_, e in curve:
+            if tc_ > t:
+                return prev
+            prev = e
+        return prev
+
+    reach = next((tc_ for tc_, e in learned if e <= e_plain), None)
+    return {"workload": "same as the line's config; reference image: plain, "
+                        f"{ref_iters} iterations, independent seeds, FP64 accumulation",
+            "iterations": iters, "plain_rmse": e_plain, "plain_device_ms": t_plain,
+            "learned_rmse": learned[-1][1], "learned_device_ms": learned[-1][0],
+            "learned_rmse_at_plain_time": at_time(learned, t_plain),
+            "time_ratio_to_plain_rmse": (reach / t_plain) if reach is not None else None,
+            "curve_plain": [(round(a, 2), round(b, 6)) for a, b in plain],
+            "curve_learned": [(round(a, 2), round(b, 6)) for a, b in learned]}
 
 
 def main():
@@ -281,6 +339,7 @@ def main():
     ap.add_argument("--photons", type=int, default=PHOTONS_PER_ITER)
     ap.add_argument("--cpu-cores", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

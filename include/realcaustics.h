@@ -167,6 +167,13 @@ const char* rc_last_error(void);
  * With the learned proposal, [8] is the proposal inference + training time. */
 int rc_get_stats(double* out, int n);
 
+/* Debug view of the reference's debug_test modes (src/Debug_scene.cpp, dispatched by
+ * src/main.cpp:172-180): mode 2 shading normals, 3 front/back facing, 4 Fresnel
+ * reflectance with the IOR of Debug_stuff::specular.  One unjittered primary ray per
+ * pixel; replaces the image (rc_read_image returns it).  main() runs the same view when
+ * init() got debug_test 2-4. */
+int rc_render_debug(int mode);
+
 /* Learned-proposal state of the last rendered iteration (no counterpart in the
  * reference): for the first n light paths, prop4 = [direction xyz, p_light / q] (zeros
  * before the network has been trained once) and contrib = the sum over the path's

@@ -73,6 +73,7 @@ def oracle() -> C.CDLL:
         lib.oracle_world_bvh.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         lib.oracle_scene_info.argtypes = [C.c_void_p]
         lib.oracle_last_error.restype = C.c_char_p
+        lib.oracle_debug_view.argtypes = [C.c_int, C.c_float, C.c_void_p]
         _oracle = lib
     return _oracle
 
@@ -99,5 +100,6 @@ def reference() -> C.CDLL | None:
         lib.ref_mesh_bvh.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_float)]
         lib.ref_world_bvh.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         lib.ref_layout.argtypes = [C.c_void_p]
+        lib.ref_debug.argtypes = [C.c_int, C.c_void_p]
         _ref = lib
     return _ref

@@ -302,6 +302,25 @@ int ref_render(float* rgb)
     return 0;
 }
 
+// Debug view `mode` (2 normals, 3 facing, 4 materials) by the reference's own
+// Vertex_Merging::run_debug_* (src/Debug_scene.cpp) after ref_prepare; copies the
+// image buffer and releases the scene.
+int ref_debug(int mode, float* rgb)
+{
+    if (!scene) return -1;
+    if (mode == 2) scene->integrator.run_debug_normals();
+    else if (mode == 3) scene->integrator.run_debug_facing();
+    else if (mode == 4) scene->integrator.run_debug_materials();
+    else return -2;
+    const std::vector<vec3>& c = scene->integrator.image_buffer.color;
+    for (size_t i = 0; i < c.size(); ++i) {
+        rgb[3 * i] = c[i].x; rgb[3 * i + 1] = c[i].y; rgb[3 * i + 2] = c[i].z;
+    }
+    delete scene;
+    scene = nullptr;
+    return 0;
+}
+
 int ref_release()
 {
     delete scene;

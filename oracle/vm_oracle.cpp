@@ -1596,6 +1596,50 @@ int oracle_render_reference(float* rgb, int jitter_order) {
     return 0;
 }
 
+// Debug views of the reference (src/Debug_scene.cpp:21-65 normals, :67-117 facing,
+// :156-214 materials): one unjittered primary ray per pixel corner (x, y), closest hit
+// with tmin 1e-4 from the camera origin, colour added through Image_Buffer::add_color
+// (row 0 dropped); no averaging (src/main.cpp:170-200).  mode 2: shading normal;
+// 3: (0,0,1) front / (1,0,0) back, times |dot(dir, Ns)|; 4: Fresnel reflectance with
+// IOR `ior` (Debug_stuff::specular) of the view direction in the Ns frame.
+int oracle_debug_view(int mode, float ior, float* rgb) {
+    if (!g) return -1;
+    int r = prepare(*g, g_err);
+    if (r) return r;
+    if (mode < 2 || mode > 4) { g_err = "debug mode must be 2, 3 or 4"; return -2; }
+    const Scene& s = *g;
+    const int W = s.W, H = s.H;
+    std::vector<float> img(3 * (size_t)W * H, 0.0f);
+    for (int p = 0; p < W * H; ++p) {
+        const float x = p % W, y = p / W;
+        V3<float> dir = s.cam_bl + (x / (float)W) * s.cam_h + (y / (float)H) * s.cam_v;
+        dir = dir - s.cam_o;
+        const V3<float> o = s.cam_o, d = normalize(dir);
+        Hit<float> h;
+        if (!scene_hit<float>(s, o, d, 0.0001f, h)) continue;
+        Isect<float> is; fill<float>(s, h, o, d, is);
+        V3<float> c;
+        if (mode == 2) {
+            c = is.ns;
+        } else if (mode == 3) {
+            const V3<float> base = is.front ? V3<float>(0, 0, 1) : V3<float>(1, 0, 0);
+            c = base * std::abs(dot(d, is.ns));
+        } else {
+            Frame<float> fr;
+            fr.set_from_z(is.ns);
+            const V3<float> dl = fr.to_local(-is.dir);
+            float eta = ior;
+            if (dl.z > 0) eta = 1.0f / ior;
+            c = V3<float>(fresnel_eta<float>((float)std::fabs((double)dl.z), eta));
+        }
+        int X = (int)x, Y = H - (int)y;
+        if ((size_t)(X + Y * W) > (size_t)W * H - 1) continue;
+        img[3 * (X + Y * W)] += c.x; img[3 * (X + Y * W) + 1] += c.y; img[3 * (X + Y * W) + 2] += c.z;
+    }
+    std::memcpy(rgb, img.data(), img.size() * sizeof(float));
+    return 0;
+}
+
 // Plain-mode render: iterations [it0, it0 + iters) accumulated (sum, not mean) into
 // acc (3*W*H doubles).  precision 32 or 64.  stats[0] += light paths, stats[1] += photons.
 int oracle_render_plain(int it0, int iters, int precision, unsigned long long seed, long long paths,

@@ -61,6 +61,7 @@ struct HostScene {
     float base_radius = 0.0f;
     float radius_alpha = 0.0f;
     int debug_test = 1;
+    float debug_ior = 1.0f;       // Debug_stuff::specular (the materials debug view's IOR)
     std::vector<HostMesh> meshes;
     HostCamera camera;
     const rc_python_light* py_lights = nullptr;  // borrowed until main() returns

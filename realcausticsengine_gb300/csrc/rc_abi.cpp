@@ -546,6 +546,24 @@ int render_iteration(HostScene& sc) {
     return RC_OK;
 }
 
+// Debug view `mode` (2-4) into the image accumulation, counted as one iteration.
+int render_debug(HostScene& sc, int mode) {
+    if (mode < 2 || mode > 4) { g_err = "debug view must be 2 (normals), 3 (facing) or 4 (materials)"; return RC_E_INVALID; }
+    DeviceState& d = g_dev;
+    cudaStream_t s = d.stream;
+    VMParams p = make_params(sc, 0);
+    const long long npix = (long long)sc.camera.width * sc.camera.height;
+    RC_CUDA(d.accum.reserve(std::max<long long>(3 * npix, 1)));
+    RC_CUDA(cudaMemsetAsync(d.accum.p, 0, sizeof(double) * std::max<long long>(3 * npix, 1), s));
+    launch_debug_view(p, mode, sc.debug_ior, d.accum.p, s);
+    RC_CUDA(cudaGetLastError());
+    RC_CUDA(cudaStreamSynchronize(s));
+    int r = check_errors();
+    if (r) return r;
+    d.iterations_done = 1;
+    return RC_OK;
+}
+
 // Minimal single-part scanline OpenEXR writer: FP32 RGB, no compression.
 int write_exr(const char* path, const float* rgb, int w, int h) {
     FILE* f = std::fopen(path, "wb");
@@ -641,7 +659,6 @@ void init(int samples, float base_radius, float radius_reduction, long long* mes
           rc_vec3 camera_corner0, rc_vec3 camera_corner1, rc_vec3 camera_corner2, rc_vec3 camera_corner3,
           rc_python_light* lights, unsigned int number_of_lights, rc_python_material* materials,
           unsigned int number_of_materials, int** materials_indices, int debug_test, rc_debug_stuff debug_stuff) {
-    (void)debug_stuff;
     release_all();
     g_err.clear();
     auto sc = std::make_unique<HostScene>();
@@ -649,6 +666,7 @@ void init(int samples, float base_radius, float radius_reduction, long long* mes
     sc->base_radius = base_radius;
     sc->radius_alpha = radius_reduction;
     sc->debug_test = debug_test;
+    sc->debug_ior = debug_stuff.specular;   // src/main.cpp:116 (read by run_debug_materials)
     if (number_of_meshes && (!meshes_pointers || !mesh_matrices || !meshes_number_of_verts ||
                              !meshes_number_of_tris || !materials_indices)) {
         g_err = "init: null mesh arrays";
@@ -682,8 +700,18 @@ int main(void) {
     if (!g_scene) { g_err = "main: no scene (init was not called or failed: " + g_err + ")"; return RC_E_NO_SCENE; }
     int r = prepare();
     if (!r) {
-        int iters = g_scene->samples;
-        for (int i = 0; i < iters && !r; ++i) r = render_iteration(*g_scene);
+        // src/main.cpp:170-186: 1 = vertex merging, 2-4 = debug views (one pass, no
+        // averaging), 5 = BVH dump to OBJ files (not provided here)
+        const int mode = g_scene->debug_test;
+        if (mode == 1) {
+            int iters = g_scene->samples;
+            for (int i = 0; i < iters && !r; ++i) r = render_iteration(*g_scene);
+        } else if (mode >= 2 && mode <= 4) {
+            r = render_debug(*g_scene, mode);
+        } else {
+            g_err = "debug_test must be 1 (render) or 2-4 (debug views); 5 (BVH OBJ dump) is not provided";
+            r = RC_E_UNSUPPORTED;
+        }
     }
     if (!r && cfg().write_exr) {
         int w = g_scene->camera.width, h = g_scene->camera.height;
@@ -764,6 +792,12 @@ int rc_render(int iterations) {
     int r = prepare();
     for (int i = 0; i < iterations && !r; ++i) r = render_iteration(*g_scene);
     return r;
+}
+
+int rc_render_debug(int mode) {
+    int r = prepare();
+    if (r) return r;
+    return render_debug(*g_scene, mode);
 }
 
 int rc_render_timed(int iterations, double* out) {

@@ -87,6 +87,9 @@ void launch_mlt_pass(const VMParams& p, PhotonBuf ph, int sampler, int chains, f
 // next_path: device counter for the persistent kernel (nullptr: one thread per path)
 void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s);
 void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s);
+// Debug view `mode` (2 normals, 3 facing, 4 materials with IOR `ior`) added into the
+// FP64 image accumulation.
+void launch_debug_view(const VMParams& p, int mode, float ior, double* accum, cudaStream_t s);
 void launch_trace_rays(const SceneView& s, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st);
 void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaStream_t s);

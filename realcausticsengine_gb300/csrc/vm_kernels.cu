@@ -423,6 +423,52 @@ void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next
     k_camera_pass_persistent<<<grid, 256, 0, s>>>(p, qb, next_pixel);
 }
 
+// Debug views (src/Debug_scene.cpp:21-214, dispatched by src/main.cpp:172-180): one
+// unjittered primary ray per pixel corner, closest hit with tmin 1e-4 from the camera
+// origin, the colour added to the pixel Image_Buffer::add_color picks (row 0 dropped).
+__global__ void __launch_bounds__(256) k_debug_view(const VMParams P, int mode, float ior, double* accum) {
+    const long long pix = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int W = P.camera.width, H = P.camera.height;
+    if (pix >= (long long)W * H) return;
+    const float x = (float)(int)(pix % W);
+    const float y = (float)(int)(pix / W);
+    F3 dir = ld3(P.camera.bottom_left) + ld3(P.camera.horizontal) * (x / (float)W) +
+             ld3(P.camera.vertical) * (y / (float)H);
+    dir = dir - ld3(P.camera.origin);
+    const F3 o = ld3(P.camera.origin);
+    const F3 d = normalize(dir);
+    HitRec h;
+    if (!scene_hit(P.scene, o, d, 0.0001f, h, P.error + ERR_STACK)) return;
+    Isect is;
+    fill_isect(P.scene, h, o, d, is);
+    F3 c;
+    if (mode == 2) {
+        c = is.ns;                                            // run_debug_normals
+    } else if (mode == 3) {                                   // run_debug_facing
+        const F3 base = is.front ? f3(0.0f, 0.0f, 1.0f) : f3(1.0f, 0.0f, 0.0f);
+        c = base * fabsf(dot(d, is.ns));
+    } else {                                                  // run_debug_materials
+        Frame fr;
+        fr.set_from_z(is.ns);
+        const F3 dl = fr.to_local(-is.dir);
+        float eta = ior;
+        if (dl.z > 0.0f) eta = 1.0f / ior;
+        c = f3(fresnel_eta(fabsf(dl.z), eta));
+    }
+    const int X = (int)x, Y = H - (int)y;
+    const long long target = (long long)X + (long long)Y * W;
+    if (target > (long long)W * H - 1) return;
+    accum[3 * target] += (double)c.x;
+    accum[3 * target + 1] += (double)c.y;
+    accum[3 * target + 2] += (double)c.z;
+}
+
+void launch_debug_view(const VMParams& p, int mode, float ior, double* accum, cudaStream_t s) {
+    const long long n = (long long)p.camera.width * p.camera.height;
+    if (n <= 0) return;
+    k_debug_view<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, mode, ior, accum);
+}
+
 void launch_trace_rays(const SceneView& sv, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st) {
     if (n <= 0) return;

@@ -99,7 +99,7 @@ def look_at_camera(width, height, eye, target, up, fov_deg) -> Camera:
 class InitArgs:
     """The argument list of init(), with every buffer kept alive by this object."""
 
-    def __init__(self, scene: Scene, debug_test: int = 1):
+    def __init__(self, scene: Scene, debug_test: int = 1, debug_ior: float = 0.0):
         self.scene = scene
         n = len(scene.meshes)
         self._keep = []
@@ -157,7 +157,7 @@ class InitArgs:
             ptrs, n, mats, nverts, ntris, int(cam.width), int(cam.height),
             abi.vec3(cam.position), abi.vec3(cam.corners[0]), abi.vec3(cam.corners[1]),
             abi.vec3(cam.corners[2]), abi.vec3(cam.corners[3]),
-            lights, nl, mats_py, nm, midx, int(debug_test), abi.DebugStuff(),
+            lights, nl, mats_py, nm, midx, int(debug_test), abi.DebugStuff(specular=float(debug_ior)),
         )
 
     def call(self, init_fn):

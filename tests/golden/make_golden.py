@@ -3,8 +3,9 @@
 Runs the reference compiled from its own sources (oracle/build_ref.sh ->
 oracle/_ref/libref_oracle.so) on seeded synthetic inputs and stores its outputs:
   scene prep info, every mesh BVH and the world BVH, closest hits of random rays,
-  KD-tree radius sets, BSDF sample/evaluate/pdf probes, light samples, and a full
-  reference render (its own estimator and RNG stream).
+  KD-tree radius sets, BSDF sample/evaluate/pdf probes, light samples, the debug
+  views (debug_test 2-4), and a full reference render (its own estimator and RNG
+  stream).
 Run in a fresh process (the reference keeps process-global RNG state):
     python tests/golden/make_golden.py
 """
@@ -122,6 +123,14 @@ def main():
                                idx.ctypes.data, len(idx))
         g[f"kd{k}_pos"], g[f"kd{k}_q"], g[f"kd{k}_r2"] = pos, qp, np.array([r * r], np.float32)
         g[f"kd{k}_counts"], g[f"kd{k}_idx"] = cnt, idx[:tot]
+    # --- debug views (debug_test 2-4, Debug_stuff::specular = 1.5)
+    for mode in (2, 3, 4):
+        args = InitArgs(sc, debug_test=mode, debug_ior=1.5)
+        args.call(ref.init)
+        ref.ref_prepare(None)
+        img = np.zeros(3 * 48 * 36, np.float32)
+        assert ref.ref_debug(mode, img.ctypes.data) == 0
+        g[f"debug{mode}_image"] = img
     # --- full render by the reference integrator (fresh RNG state matters: do it last
     # in a process whose earlier calls consumed the stream? no - re-init resets nothing,
     # so the render runs in a child process)

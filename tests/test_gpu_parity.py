@@ -327,3 +327,36 @@ def test_pssmlt_is_consistent_with_plain_vm():
     plain = _render_mean(sc, 0, 1, 120, paths=20000, seed=11)
     pss = _render_mean(sc, 2, 256, 120, paths=20000, seed=11)
     assert abs(pss / plain - 1.0) < 0.05, (pss, plain)
+
+
+@pytest.mark.parametrize("mode", [2, 3, 4])
+def test_debug_views_match_reference(golden, mode):
+    """debug_test 2-4 on the GPU (one primary ray per pixel corner, closest hit, colour by
+    view) against the reference's own debug images: bit-exact."""
+    from realcausticsengine_gb300 import _native
+    sc = scenes.test_scene(48, 36, subdiv=2, samples=2)
+    L = _native.lib()
+    args = InitArgs(sc, debug_test=mode, debug_ior=1.5)
+    args.call(L.init)
+    _native.check(L.rc_render_debug(mode), "rc_render_debug")
+    img = np.zeros((36, 48, 3), np.float32)
+    _native.check(L.rc_read_image(img.ctypes.data, 48, 36), "rc_read_image")
+    L.rc_release()
+    want = golden[f"debug{mode}_image"].reshape(36, 48, 3)
+    assert (img.view(np.uint32) == want.view(np.uint32)).all(), np.argwhere(img != want)[:5]
+
+
+def test_main_runs_debug_view(tmp_path):
+    """init(debug_test=2) + main() writes the normals view (one pass, no averaging)."""
+    from realcausticsengine_gb300 import _native, abi
+    sc = scenes.test_scene(32, 24, subdiv=1, samples=3)
+    L = _native.lib()
+    cfg = abi.RcConfig()
+    L.rc_default_config(C.byref(cfg))
+    cfg.exr_path = str(tmp_path / "dbg.exr").encode()
+    assert L.rc_set_config(C.byref(cfg)) == 0
+    InitArgs(sc, debug_test=2).call(L.init)
+    assert L.main() == 0, L.rc_last_error()
+    assert (tmp_path / "dbg.exr").stat().st_size > 32 * 24 * 12
+    InitArgs(sc, debug_test=5).call(L.init)
+    assert L.main() != 0 and b"debug_test" in L.rc_last_error()

@@ -124,3 +124,15 @@ def test_reference_mode_render(golden, orc):
     want = golden["render_image"]
     assert want.sum() > 0
     assert (img.view(np.uint32) == want.view(np.uint32)).all()
+
+
+@pytest.mark.parametrize("mode", [2, 3, 4])
+def test_debug_views(golden, orc, mode):
+    """debug_test 2 (normals), 3 (facing), 4 (materials, IOR 1.5): bit-exact."""
+    sc = _golden_scene()
+    InitArgs(sc, debug_test=mode, debug_ior=1.5).call(orc.oracle_init)
+    img = np.zeros(3 * 48 * 36, np.float32)
+    assert orc.oracle_debug_view(mode, 1.5, img.ctypes.data) == 0
+    want = golden[f"debug{mode}_image"]
+    assert np.abs(want).sum() > 0
+    assert (img.view(np.uint32) == want.view(np.uint32)).all()
