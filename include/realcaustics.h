@@ -167,6 +167,18 @@ const char* rc_last_error(void);
  * With the learned proposal, [8] is the proposal inference + training time. */
 int rc_get_stats(double* out, int n);
 
+/* Checkpoint / resume of a progressive render (no counterpart in the reference, whose
+ * BVH/KD file caches are commented out: src/KD_Tree.cpp:192-214, src/Scene.cpp:137-150).
+ * rc_save_state writes the FP64 image sum, the iteration count, the sampling settings
+ * (seeds, photons per iteration, depth, sampler) and the learned proposal's network and
+ * Adam moments.  rc_load_state, after init() of the same scene, restores them; further
+ * rc_render calls continue with the next iteration's counter-based samples, so the
+ * result equals an uninterrupted render up to FP64 summation order.  A state saved for
+ * another scene (fingerprint of geometry, camera, lights, materials, radius) is
+ * RC_E_INVALID. */
+int rc_save_state(const char* path);
+int rc_load_state(const char* path);
+
 /* Debug view of the reference's debug_test modes (src/Debug_scene.cpp, dispatched by
  * src/main.cpp:172-180): mode 2 shading normals, 3 front/back facing, 4 Fresnel
  * reflectance with the IOR of Debug_stuff::specular.  One unjittered primary ray per

@@ -53,6 +53,8 @@ def lib() -> C.CDLL:
     L.rc_light_photons.argtypes = [C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_proposal_state.argtypes = [C.c_longlong, C.c_void_p, C.c_void_p]
     L.rc_render_debug.argtypes = [C.c_int]
+    L.rc_save_state.argtypes = [C.c_char_p]
+    L.rc_load_state.argtypes = [C.c_char_p]
     _lib = L
     return L
 
@@ -67,4 +69,5 @@ EXPORTS = ["init", "main", "rc_default_config", "rc_set_config", "rc_prepare", "
            "rc_host_mesh_bvh", "rc_host_world_bvh", "rc_render", "rc_read_image", "rc_release",
            "rc_last_error", "rc_get_stats", "rc_trace_rays", "rc_trace_rays_full", "rc_kd_query",
            "rc_kd_build_nodes", "rc_light_photons", "rc_render_timed", "rc_kd_build_noalloc",
-           "rc_kd_noalloc_last_error", "rc_proposal_state", "rc_render_debug"]
+           "rc_kd_noalloc_last_error", "rc_proposal_state", "rc_render_debug",
+           "rc_save_state", "rc_load_state"]

@@ -645,6 +645,38 @@ size_t mlp_param_floats() {
     return t;
 }
 
+size_t mlp_state_floats() { return 3 * mlp_param_floats(); }
+
+int mlp_export(const MlpParams& p, float* out) {
+    size_t o = 0;
+    for (int l = 0; l < kMlpLayers; ++l) {
+        const size_t nw = (size_t)mlp_in_dim(l) * mlp_out_dim(l), nb = mlp_out_dim(l);
+        const float* src[6] = {p.wm[l], p.b[l], p.mw[l], p.vw[l], p.mb[l], p.vb[l]};
+        const size_t cnt[6] = {nw, nb, nw, nw, nb, nb};
+        for (int k = 0; k < 6; ++k) {
+            if (cudaMemcpy(out + o, src[k], 4 * cnt[k], cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+            o += cnt[k];
+        }
+    }
+    return 0;
+}
+
+int mlp_import(MlpParams& p, const float* in, int adam_step, cudaStream_t s) {
+    size_t o = 0;
+    for (int l = 0; l < kMlpLayers; ++l) {
+        const size_t nw = (size_t)mlp_in_dim(l) * mlp_out_dim(l), nb = mlp_out_dim(l);
+        float* dst[6] = {p.wm[l], p.b[l], p.mw[l], p.vw[l], p.mb[l], p.vb[l]};
+        const size_t cnt[6] = {nw, nb, nw, nw, nb, nb};
+        for (int k = 0; k < 6; ++k) {
+            if (cudaMemcpyAsync(dst[k], in + o, 4 * cnt[k], cudaMemcpyHostToDevice, s) != cudaSuccess) return -1;
+            o += cnt[k];
+        }
+        k_to_bf16<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(p.wm[l], p.w[l], (int)nw);
+    }
+    p.adam_step = adam_step;
+    return cudaStreamSynchronize(s) == cudaSuccess ? 0 : -1;
+}
+
 int mlp_init(MlpParams& p, uint64_t seed, cudaStream_t s) {
     // Xavier-uniform weights from a seeded host generator (Philox over the index);
     // biases zero; the output layer's concentrations start broad.

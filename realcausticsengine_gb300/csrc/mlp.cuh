@@ -92,6 +92,11 @@ void mlp_normalize_weights(float4* dir4, int n, const float* wsum, cudaStream_t 
 // `steps` Adam steps on minibatches of b.n rows taken from (pos4, dir4)[0, total).
 int mlp_train(MlpParams& p, MlpBatch& b, const float4* pos4, const float4* dir4, int total, int steps, float lr,
               cudaStream_t s, int* err);
+// Training state as host floats (per layer: FP32 master weights, biases, the four Adam
+// moments) for checkpoints; mlp_import restores it and refreshes the BF16 weights.
+size_t mlp_state_floats();
+int mlp_export(const MlpParams& p, float* out);
+int mlp_import(MlpParams& p, const float* in, int adam_step, cudaStream_t s);
 // Initialise weights (seeded), zero Adam state.
 int mlp_init(MlpParams& p, uint64_t seed, cudaStream_t s);
 // Forward on b.n normalised positions (b.pos) -> b.out (n x 80 FP32).

@@ -564,6 +564,130 @@ int render_debug(HostScene& sc, int mode) {
     return RC_OK;
 }
 
+// ---------------------------------------------------------------- progressive state
+// Checkpoint of a progressive render: the FP64 image sum, the iteration index (the
+// counter RNG continues from it, so a resumed render draws the same samples as an
+// uninterrupted one), the sampling configuration, and the learned proposal's network
+// and Adam state.  The scene itself is not stored; a fingerprint of the prepared scene
+// (triangles, vertices, camera, lights, materials, radius) must match on load.
+constexpr char kStateMagic[8] = {'R', 'C', 'S', 'T', 'A', 'T', 'E', '1'};
+
+uint64_t fnv1a(uint64_t h, const void* data, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(data);
+    for (size_t i = 0; i < n; ++i) { h ^= c[i]; h *= 1099511628211ull; }
+    return h;
+}
+
+uint64_t scene_fingerprint(const HostScene& sc) {
+    uint64_t h = 14695981039346656037ull;
+    for (const HostMesh& m : sc.meshes) {
+        h = fnv1a(h, m.wpos.data(), m.wpos.size() * sizeof(V3));
+        h = fnv1a(h, m.tri.data(), m.tri.size() * sizeof(uint32_t));
+        h = fnv1a(h, m.mat.data(), m.mat.size() * sizeof(uint32_t));
+    }
+    h = fnv1a(h, &sc.camera, sizeof(sc.camera));
+    h = fnv1a(h, sc.lights.data(), sc.lights.size() * sizeof(DevLight));
+    h = fnv1a(h, sc.materials.data(), sc.materials.size() * sizeof(DevMaterial));
+    h = fnv1a(h, &sc.base_radius, sizeof(float));
+    h = fnv1a(h, &sc.radius_alpha, sizeof(float));
+    return h;
+}
+
+struct StateHeader {
+    char magic[8];
+    int32_t width, height, iterations_done, max_path_length;
+    uint64_t seed, camera_seed, fingerprint;
+    int64_t photons_per_iter;
+    int32_t sampler, learned, mlp_rounds, adam_step;
+    uint64_t accum_doubles, mlp_floats;
+};
+
+int save_state(const char* path) {
+    if (!g_scene || !g_scene->prepared) { g_err = "save_state: no prepared scene"; return RC_E_NO_SCENE; }
+    if (!path) { g_err = "save_state: null path"; return RC_E_INVALID; }
+    const HostScene& sc = *g_scene;
+    DeviceState& d = g_dev;
+    const size_t npix = (size_t)sc.camera.width * sc.camera.height;
+    StateHeader h{};
+    std::memcpy(h.magic, kStateMagic, 8);
+    h.width = sc.camera.width; h.height = sc.camera.height;
+    h.iterations_done = d.iterations_done;
+    h.max_path_length = cfg().max_path_length;
+    h.seed = cfg().seed;
+    h.camera_seed = cfg().camera_seed ? cfg().camera_seed : cfg().seed;
+    h.fingerprint = scene_fingerprint(sc);
+    h.photons_per_iter = cfg().photons_per_iter;
+    h.sampler = cfg().sampler;
+    h.learned = cfg().learned_proposal;
+    h.mlp_rounds = d.mlp_rounds;
+    h.adam_step = d.mlp ? d.mlp->p.adam_step : 0;
+    h.accum_doubles = 3 * npix;
+    h.mlp_floats = d.mlp ? mlp_state_floats() : 0;
+    std::vector<double> acc(3 * npix, 0.0);
+    if (d.accum.p && d.accum.n >= 3 * npix)
+        RC_CUDA(cudaMemcpy(acc.data(), d.accum.p, acc.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<float> ml(h.mlp_floats);
+    if (h.mlp_floats && mlp_export(d.mlp->p, ml.data())) { g_err = "save_state: MLP read-back failed"; return RC_E_CUDA; }
+    FILE* f = std::fopen(path, "wb");
+    if (!f) { g_err = std::string("cannot open ") + path; return RC_E_IO; }
+    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+              std::fwrite(acc.data(), sizeof(double), acc.size(), f) == acc.size() &&
+              std::fwrite(ml.data(), sizeof(float), ml.size(), f) == ml.size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) { g_err = std::string("write failed: ") + path; return RC_E_IO; }
+    return RC_OK;
+}
+
+int load_state(const char* path) {
+    int r = prepare();
+    if (r) return r;
+    if (!path) { g_err = "load_state: null path"; return RC_E_INVALID; }
+    const HostScene& sc = *g_scene;
+    DeviceState& d = g_dev;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) { g_err = std::string("cannot open ") + path; return RC_E_IO; }
+    StateHeader h{};
+    const size_t npix = (size_t)sc.camera.width * sc.camera.height;
+    bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kStateMagic, 8) == 0;
+    if (ok && (h.width != sc.camera.width || h.height != sc.camera.height || h.fingerprint != scene_fingerprint(sc) ||
+               h.accum_doubles != 3 * npix || (h.mlp_floats && h.mlp_floats != mlp_state_floats()) ||
+               h.iterations_done < 0)) {
+        std::fclose(f);
+        g_err = "load_state: the state was saved for another scene";
+        return RC_E_INVALID;
+    }
+    std::vector<double> acc(ok ? h.accum_doubles : 0);
+    std::vector<float> ml(ok ? h.mlp_floats : 0);
+    ok = ok && std::fread(acc.data(), sizeof(double), acc.size(), f) == acc.size() &&
+         std::fread(ml.data(), sizeof(float), ml.size(), f) == ml.size();
+    std::fclose(f);
+    if (!ok) { g_err = std::string("load_state: unreadable or truncated state file ") + path; return RC_E_IO; }
+    // sampling configuration continues as saved
+    rc_config c = cfg();
+    c.seed = h.seed;
+    c.camera_seed = h.camera_seed;
+    c.photons_per_iter = h.photons_per_iter;
+    c.max_path_length = h.max_path_length;
+    c.sampler = h.sampler;
+    c.learned_proposal = h.learned;
+    g_cfg = c;
+    RC_CUDA(d.accum.reserve(std::max<size_t>(acc.size(), 1)));
+    RC_CUDA(cudaMemcpy(d.accum.p, acc.data(), acc.size() * sizeof(double), cudaMemcpyHostToDevice));
+    d.iterations_done = h.iterations_done;
+    d.mlp_rounds = 0;
+    if (h.mlp_floats) {
+        if (!d.mlp) {
+            d.mlp = std::make_unique<MlpStore>();
+            if (!d.mlp->setup(kTrainBatchRows)) { g_err = "MLP allocation failed"; return RC_E_CUDA; }
+            RC_CUDA(d.train_pos.reserve(kTrainCapacity)); RC_CUDA(d.train_dir.reserve(kTrainCapacity));
+            RC_CUDA(d.train_count.reserve(1)); RC_CUDA(d.train_wsum.reserve(1));
+        }
+        if (mlp_import(d.mlp->p, ml.data(), h.adam_step, d.stream)) { g_err = "MLP upload failed"; return RC_E_CUDA; }
+        d.mlp_rounds = h.mlp_rounds;
+    }
+    return RC_OK;
+}
+
 // Minimal single-part scanline OpenEXR writer: FP32 RGB, no compression.
 int write_exr(const char* path, const float* rgb, int w, int h) {
     FILE* f = std::fopen(path, "wb");
@@ -793,6 +917,9 @@ int rc_render(int iterations) {
     for (int i = 0; i < iterations && !r; ++i) r = render_iteration(*g_scene);
     return r;
 }
+
+int rc_save_state(const char* path) { return save_state(path); }
+int rc_load_state(const char* path) { return load_state(path); }
 
 int rc_render_debug(int mode) {
     int r = prepare();

@@ -24,6 +24,7 @@
 #include "realcaustics.h"
 #include "vm.cuh"
 #include "bsdf.cuh"
+#include "lights.cuh"
 #include "rng.cuh"
 
 namespace rc {
@@ -34,43 +35,6 @@ constexpr int kMltMaxLen = 12;                        // longest path the sample
 constexpr int kMltDims = 5 + 3 * (kMltMaxLen + 1);    // (max_path_length + 2) * 3 + 2
 constexpr int kPhotonBuf = kMltMaxLen + 2;
 
-// find_interval (src/utils.h:142-157)
-__device__ __forceinline__ int find_interval_m(const float* cdf, int size, float u) {
-    int first = 0, len = size;
-    while (len > 0) {
-        int half = len >> 1, middle = first + half;
-        if (cdf[middle] < u) { first = middle + 1; len -= half + 1; }
-        else len = half;
-    }
-    int v = first - 1;
-    return v < 0 ? 0 : (v > size - 2 ? size - 2 : v);
-}
-
-__device__ __forceinline__ void sample_light_m(const LightsView& L, const float* u, F3& o, F3& d, F3& tp) {
-    int idx = find_interval_m(L.cdf, L.count + 1, u[0]);
-    const DevLight& l = L.lights[idx];
-    float pick = l.power / (L.count * L.integral);
-    if (l.type == LIGHT_AREA) {
-        o = ld3(l.bl) + ld3(l.hz) * u[1] + ld3(l.vt) * u[2];
-        F3 local = cos_hemisphere(u[3], u[4]);
-        d = ld3(l.fx) * local.x + ld3(l.fy) * local.y + ld3(l.fz) * local.z;
-        tp = f3(l.cr, l.cg, l.cb) * kPI;
-    } else if (l.type == LIGHT_SUN) {
-        o = ld3(l.bl) + ld3(l.hz) * u[1] + ld3(l.vt) * u[2];
-        d = ld3(l.fz);
-        tp = f3(l.cr, l.cg, l.cb);
-    } else {
-        o = ld3(l.pos);
-        float z = 1.0f - 2.0f * u[3];
-        float r = sqrtf(ref_max(0.0f, 1.0f - z * z));
-        float s, c;
-        sincosf(kPI2 * u[4], &s, &c);
-        d = f3(r * c, r * s, z);
-        tp = f3(l.cr, l.cg, l.cb) * (4.0f * kPI);
-    }
-    tp = div_each(tp, pick);
-}
-
 struct PhotonRec { float4 pos, dir; float2 tp; };
 
 // Trace one light path driven by the primary samples u[0..kMltDims); photons go to
@@ -78,7 +42,7 @@ struct PhotonRec { float4 pos, dir; float2 tp; };
 // takes them from its global stream).  Returns the number of photons.
 __device__ int trace_light_samples(const VMParams& P, const float* u, const PathRng& rr, int maxlen, PhotonRec* out) {
     F3 o, d, tp;
-    sample_light_m(P.lights, u, o, d, tp);
+    sample_light(P.lights, u[0], u[1], u[2], u[3], u[4], o, d, tp);
     int diffuse = 0, last = EV_DIFFUSE, n = 0;
     float dVM = 0.0f;
     for (int len = 0;; ++len) {
