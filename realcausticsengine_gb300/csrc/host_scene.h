@@ -64,7 +64,7 @@ struct HostScene {
     float debug_ior = 1.0f;       // Debug_stuff::specular (the materials debug view's IOR)
     std::vector<HostMesh> meshes;
     HostCamera camera;
-    const rc_python_light* py_lights = nullptr;  // borrowed until main() returns
+    std::vector<rc_python_light> py_lights;      // copied at init, converted at prepare
     unsigned num_lights = 0;
     std::vector<rc_python_material> py_materials;
     // after prepare()

@@ -813,7 +813,11 @@ void init(int samples, float base_radius, float radius_reduction, long long* mes
     c.bottom_left = {camera_corner2.x, camera_corner2.y, camera_corner2.z};
     c.horizontal = {camera_corner1.x - camera_corner2.x, camera_corner1.y - camera_corner2.y, camera_corner1.z - camera_corner2.z};
     c.vertical = {camera_corner3.x - camera_corner2.x, camera_corner3.y - camera_corner2.y, camera_corner3.z - camera_corner2.z};
-    sc->py_lights = lights;
+    // The reference keeps the caller's light array and converts it in main()
+    // (src/main.cpp:134,163); the records are copied here so that the caller may free
+    // them after init (converted at prepare time all the same).
+    if (number_of_lights && !lights) { g_err = "init: null lights"; return; }
+    sc->py_lights.assign(lights, lights + number_of_lights);
     sc->num_lights = number_of_lights;
     if (number_of_materials && !materials) { g_err = "init: null materials"; return; }
     sc->py_materials.assign(materials, materials + number_of_materials);
