@@ -6,8 +6,8 @@
 // queries a warp processes one after another touch the same nodes and photons (L1/L2
 // reuse).  For each query the warp runs the reference's descent uniformly (near side
 // first; far side and an odd node's median photon only when (q[axis] - split)^2 < r^2)
-// and, at a node of at most 32 photons, tests the whole contiguous tree-order range at
-// once, one photon per lane, with the reference's acceptance predicate
+// and, at a node of at most kBucket photons, tests the whole contiguous tree-order range
+// at once, one photon per lane, with the reference's acceptance predicate
 // ((dx*dx + dy*dy) + dz*dz) < r^2 in FP32 without contraction.  Accepted photons are
 // compacted in shared memory and their MIS-weighted BSDF contributions are evaluated
 // lane-parallel, then summed across the warp.
@@ -27,7 +27,7 @@ namespace {
 constexpr int kWarpsPerBlock = 8;
 constexpr int kStack = 64;
 constexpr int kQueriesPerWarp = 16;
-constexpr int kBucket = 64;   // photons tested per bucket (kBucket / 32 per lane)
+constexpr int kBucket = 32;   // photons tested per bucket (kBucket / 32 per lane)
 
 struct KdNav {
     const uint2* __restrict__ nodes;
@@ -144,12 +144,121 @@ __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, ui
     __syncwarp();
 }
 
+// Lane-parallel variant of the same query, used when node boxes exist down to the bucket
+// level Lb (every node at level Lb holds n >> Lb <= kBucket photons).  A subtree root at
+// level L < Lb is expanded k = min(5, Lb - L) levels at once: lane j box-tests the j-th
+// descendant at level L + k and survivors are pushed as new roots, while lanes test the
+// median photons of the 2^k - 1 inner nodes in between (odd counts only).  Roots at
+// level >= Lb are scanned like buckets.  The accepted set is the reference's: every
+// photon of the start node's range lies in a bucket or is an inner node's median; a
+// culled box holds no photon within the radius (box distance <= photon distance under
+// monotonic rounding), a median outside its node's split slab fails the predicate
+// (its distance >= |q[axis] - split|), and every photon that is tested is tested with
+// the reference's predicate.  DFS over roots keeps at most 31 pending roots per
+// expansion level: with n < 2^28 (Lb <= 27) at most 6 x 31 + 1 = 187 < kRootStack.
+constexpr int kRootStack = 256;
+
+template <class Flush>
+__device__ __forceinline__ void kd_query_expand(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend,
+                                                uint2* stk, VisitCounts& vc, Flush&& flush) {
+    const int lane = threadIdx.x & 31;
+    if (t.n <= 0) return;
+    const uint32_t n32 = (uint32_t)t.n;
+    const int Lb = t.box_levels - 1;
+    {
+        const int l0 = 31 - __clz(start_node.x);
+        if (l0 <= Lb && box_outside(q, __ldg(&t.box_lo[start_node.x]), __ldg(&t.box_hi[start_node.x]), r2)) return;
+    }
+    int np = 0;
+    auto append = [&](bool acc, uint32_t p) {
+        const unsigned m = __ballot_sync(0xffffffffu, acc);
+        if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = p;
+        np += __popc(m);
+        __syncwarp();
+        if (np >= 32) { flush(np, pend); np = 0; __syncwarp(); }
+    };
+    if (lane == 0) stk[0] = start_node;
+    __syncwarp();
+    int sp = 1;
+    while (sp) {
+        --sp;
+        const uint2 rt = stk[sp];
+        __syncwarp();
+        const uint32_t e = rt.x, start = rt.y;
+        const int L = 31 - __clz(e);
+        if (L >= Lb) {
+            const uint32_t c = n32 >> L;
+            vc.buckets++;
+            vc.tests += c;
+#pragma unroll
+            for (int k = 0; k < kBucket / 32; ++k) {
+                const uint32_t i = (uint32_t)(k * 32 + lane);
+                bool acc = false;
+                if (i < c) acc = in_radius(q, __ldg(&t.x[start + i]), __ldg(&t.y[start + i]), __ldg(&t.z[start + i]), r2);
+                append(acc, start + i);
+            }
+            continue;
+        }
+        const int k = (Lb - L) < 5 ? (Lb - L) : 5;
+        const uint32_t m = 1u << k;
+        vc.nodes += m - 1;
+        {
+            // median photons of the inner nodes at levels L .. L+k-1 (1-based BFS index)
+            bool acc = false;
+            uint32_t p = 0;
+            if ((uint32_t)lane < m - 1) {
+                const uint32_t i1 = (uint32_t)lane + 1u;
+                const int li = 31 - __clz(i1);
+                const uint32_t pi = i1 - (1u << li);
+                const uint32_t c = n32 >> (L + li);
+                if (c & 1u) {
+                    uint32_t st = start;
+                    for (int b = 0; b < li; ++b) {
+                        const uint32_t cl = n32 >> (L + b);
+                        if ((pi >> (li - 1 - b)) & 1u) st += (cl >> 1) + (cl & 1u);
+                    }
+                    p = st + (c >> 1);
+                    acc = in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2);
+                }
+            }
+            append(acc, p);
+        }
+        {
+            // the 2^k descendants at level L + k: box test, survivors become roots
+            bool keep = false;
+            uint32_t st = start;
+            const uint32_t ce = (e << k) + (uint32_t)lane;
+            if ((uint32_t)lane < m) {
+                for (int b = 0; b < k; ++b) {
+                    const uint32_t cl = n32 >> (L + b);
+                    if (((uint32_t)lane >> (k - 1 - b)) & 1u) st += (cl >> 1) + (cl & 1u);
+                }
+                keep = !box_outside(q, __ldg(&t.box_lo[ce]), __ldg(&t.box_hi[ce]), r2);
+            }
+            const unsigned bm = __ballot_sync(0xffffffffu, keep);
+            if (keep) stk[sp + __popc(bm & ((1u << lane) - 1u))] = make_uint2(ce, st);
+            sp += __popc(bm);
+            __syncwarp();
+        }
+    }
+    if (np > 0) flush(np, pend);
+    __syncwarp();
+}
+
+template <class Flush>
+__device__ __forceinline__ void kd_query(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend, uint2* stk,
+                                         VisitCounts& vc, Flush&& flush) {
+    if (t.box_levels > 0) kd_query_expand(t, q, r2, start_node, pend, stk, vc, flush);
+    else kd_query_warp(t, q, r2, start_node, pend, vc, flush);
+}
+
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, 3) k_gather(const VMParams P, const KdNav t, TreePhotons tp,
                                                                  QueryBuf qb, const uint32_t* __restrict__ order,
                                                                  const uint2* __restrict__ start_nodes,
                                                                  long long nq, double* __restrict__ accum,
                                                                  unsigned long long* __restrict__ counters) {
     __shared__ uint32_t pend[kWarpsPerBlock][64];
+    __shared__ uint2 stk[kWarpsPerBlock][kRootStack];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long w = blockIdx.x * (long long)kWarpsPerBlock + warp;
     const long long first = w * kQueriesPerWarp;
@@ -166,7 +275,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 3) k_gather(const VMParam
         Bsdf bs;
         bs.init(P.materials[__float_as_int(b.w)], xyz(b), xyz(e), true);
         F3 color = f3(0.0f);
-        kd_query_warp(t, q, P.radius_sqr, sn, pend[warp], vc, [&](int n, const uint32_t* list) {
+        kd_query(t, q, P.radius_sqr, sn, pend[warp], stk[warp], vc, [&](int n, const uint32_t* list) {
             for (int j = lane; j < n; j += 32) {
                 const uint32_t p = list[j];
                 const float4 p0 = __ldg(&tp.t0[p]);
@@ -219,6 +328,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_kd_query(const KdNav t,
                                                                    const uint2* __restrict__ start_nodes, float r2,
                                                                    int* counts, const long long* offsets, int* idx) {
     __shared__ uint32_t pend[kWarpsPerBlock][64];
+    __shared__ uint2 stk[kWarpsPerBlock][kRootStack];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long w = blockIdx.x * (long long)kWarpsPerBlock + warp;
     const long long first = w * kQueriesPerWarp;
@@ -230,7 +340,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_kd_query(const KdNav t,
         const F3 p = f3(qpos[3 * j], qpos[3 * j + 1], qpos[3 * j + 2]);
         const long long off = offsets ? offsets[j] : 0;
         int n = 0;
-        kd_query_warp(t, p, r2, start_nodes[j], pend[warp], vc, [&](int cnt, const uint32_t* list) {
+        kd_query(t, p, r2, start_nodes[j], pend[warp], stk[warp], vc, [&](int cnt, const uint32_t* list) {
             if (idx)
                 for (int k = lane; k < cnt; k += 32) idx[off + n + k] = (int)__ldg(&t.id[list[k]]);
             n += cnt;
