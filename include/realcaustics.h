@@ -118,6 +118,10 @@ typedef struct rc_config {
      * Two renders with the same camera_seed and different seeds share their merge
      * queries and differ only in their photons. */
     unsigned long long camera_seed;
+    /* 1 (default): the first iteration of each query-count class times the gather's
+     * launch shapes (resident blocks per SM x queries per warp) on a scratch image and
+     * keeps the fastest; 0: the fixed default shape. */
+    int autotune;
 } rc_config;
 
 int rc_default_config(rc_config* cfg);

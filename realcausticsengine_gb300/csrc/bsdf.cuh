@@ -375,6 +375,69 @@ struct Bsdf {
         }
     }
 
+    // evaluate() and pdf() for one incoming direction with their common subexpressions
+    // computed once, for the gather's merges.  wo_ng = dot(fr.to_world(wo), Ng) (the
+    // second factor of side()) and fwo = fresnel_reflectance(|wo.z|, s) (plastic kinds)
+    // are the query's constants.  Every output is formed by the same operations, in the
+    // same order, as evaluate() and pdf() form it.
+    __device__ __forceinline__ void eval_pdf(F3 wi, F3 ng, float wo_ng, float fwo, F3& f, float& fwd,
+                                             float& rev) const {
+        f = f3(0.0f);
+        fwd = 0.0f; rev = 0.0f;
+        const float sd = dot(wi, ng) * wo_ng;
+        switch (kind) {
+        case BSDF_K_LAMBERT: {
+            if (sd > 0.0f) f = R * kInvPI * abs_dot(wi, fr.z);
+            fwd = fabsf(fr.to_local(wi).z) * kInvPI;
+            rev = fabsf(wo.z) * kInvPI;
+            return;
+        }
+        case BSDF_K_GGX_REFLECTION: {
+            const F3 wl = fr.to_local(wi);
+            const F3 h = normalize(wo + wl);
+            const float chn = fabsf(h.z);
+            const float d = ggx_D(chn, a2);
+            fwd = rev = d * chn * 0.25f / abs_dot(h, wo);
+            if (sd <= 0.0f || wl.z * wo.z <= 0.0f) return;
+            const float g2 = ggx_G2(fabsf(wo.z), fabsf(wl.z), a2);
+            f = div_recip(R * d * g2 * 0.25f, fabsf(wo.z));
+            return;
+        }
+        case BSDF_K_PLASTIC_GGX: {
+            const F3 wl = fr.to_local(wi);
+            const float fdp = fabsf(wl.z) * kInvPI, rdp = fabsf(wo.z) * kInvPI;
+            const F3 h = normalize(wo + wl);
+            const float chn = fabsf(h.z);
+            const float d = ggx_D(chn, a2);
+            const float sp = d * chn * 0.25f / abs_dot(h, wo);
+            if (fwo > 1.0f) { fwd = rev = sp; }
+            else { fwd = fdp * (1.0f - fwo) + sp * fwo; rev = rdp * (1.0f - fwo) + sp * fwo; }
+            if (sd <= 0.0f || wl.z * wo.z <= 0.0f) return;
+            const F3 diffuse = R * kInvPI;
+            const float g2 = ggx_G2(fabsf(wo.z), fabsf(wl.z), a2);
+            const float spec = fwo * d * g2 * 0.25f / fabsf(wo.z);
+            f = f3(diffuse.x + spec, diffuse.y + spec, diffuse.z + spec);
+            return;
+        }
+        case BSDF_K_PLASTIC_SMOOTH: {
+            const F3 wl = fr.to_local(wi);
+            if (!(fwo > 1.0f)) {
+                fwd = fabsf(wl.z) * kInvPI * (1.0f - fwo);
+                rev = fabsf(wo.z) * kInvPI * (1.0f - fwo);
+            }
+            if (sd <= 0.0f || wl.z * wo.z <= 0.0f) return;
+            f = R * kInvPI;
+            return;
+        }
+        case BSDF_K_GGX_DIELECTRIC:
+            f = evaluate(wi, ng);
+            pdf(wi, fwd, rev);
+            return;
+        default:
+            return;   // delta BSDFs
+        }
+    }
+
     // BxDF::pdf(wi, forward, reverse)
     __device__ void pdf(F3 wi, float& fwd, float& rev) const {
         switch (kind) {

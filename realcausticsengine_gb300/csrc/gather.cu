@@ -252,11 +252,16 @@ __device__ __forceinline__ void kd_query(const KdNav& t, F3 q, float r2, uint2 s
     else kd_query_warp(t, q, r2, start_node, pend, vc, flush);
 }
 
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, 3) k_gather(const VMParams P, const KdNav t, TreePhotons tp,
-                                                                 QueryBuf qb, const uint32_t* __restrict__ order,
-                                                                 const uint2* __restrict__ start_nodes,
-                                                                 long long nq, double* __restrict__ accum,
-                                                                 unsigned long long* __restrict__ counters) {
+// MinBlocks (resident blocks per SM the register allocation must allow) and QPW
+// (consecutive sorted queries per warp) are the autotuned shape parameters.
+template <int MinBlocks, int QPW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const VMParams P, const KdNav t,
+                                                                         TreePhotons tp, QueryBuf qb,
+                                                                         const uint32_t* __restrict__ order,
+                                                                         const uint2* __restrict__ start_nodes,
+                                                                         long long nq, double* __restrict__ accum,
+                                                                         unsigned long long* __restrict__ counters) {
+    constexpr int kQueriesPerWarp = QPW;
     __shared__ uint32_t pend[kWarpsPerBlock][64];
     __shared__ uint2 stk[kWarpsPerBlock][kRootStack];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -274,6 +279,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 3) k_gather(const VMParam
         const float cam_dVM = a.w;
         Bsdf bs;
         bs.init(P.materials[__float_as_int(b.w)], xyz(b), xyz(e), true);
+        // per-query constants of the merge evaluation
+        const float wo_ng = dot(bs.fr.to_world(bs.wo), ng);
+        const float fwo = (bs.kind == BSDF_K_PLASTIC_GGX || bs.kind == BSDF_K_PLASTIC_SMOOTH)
+                              ? fresnel_reflectance(fabsf(bs.wo.z), bs.s) : 0.0f;
         F3 color = f3(0.0f);
         kd_query(t, q, P.radius_sqr, sn, pend[warp], stk[warp], vc, [&](int n, const uint32_t* list) {
             for (int j = lane; j < n; j += 32) {
@@ -283,9 +292,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 3) k_gather(const VMParam
                 const float2 p2 = __ldg(&tp.t2[p]);
                 const F3 wi = xyz(p1);
                 float fwd, rev;
-                bs.pdf(wi, fwd, rev);
+                F3 ev;
+                bs.eval_pdf(wi, ng, wo_ng, fwo, ev, fwd, rev);
                 const float weight = 1.0f / (1.0f + cam_dVM * rev + p0.w * fwd);
-                const F3 ev = bs.evaluate(wi, ng);
                 const F3 cpair = ev * f3(p1.w, p2.x, p2.y) * weight;
                 color = color + cpair;
                 if (P.path_contrib) {
@@ -570,12 +579,37 @@ void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaS
     k_tree_records<<<(unsigned)((tree.n + 255) / 256), 256, 0, s>>>(ph, tree.id, tree.n, tp);
 }
 
+template <int MB, int QPW>
+void launch_gather_t(const VMParams& p, const KdNav& nav, TreePhotons tp, QueryBuf qb, const uint32_t* order,
+                     const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters,
+                     cudaStream_t s) {
+    const long long warps = (nq + QPW - 1) / QPW;
+    k_gather<MB, QPW><<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
+        p, nav, tp, qb, order, start_nodes, nq, accum, counters);
+}
+
+int gather_variants() { return 6; }
+
+const char* gather_variant_name(int v) {
+    static const char* names[6] = {"blocks/SM>=2, 8 queries/warp", "blocks/SM>=2, 16 queries/warp",
+                                   "blocks/SM>=3, 8 queries/warp", "blocks/SM>=3, 16 queries/warp",
+                                   "blocks/SM>=4, 8 queries/warp", "blocks/SM>=4, 16 queries/warp"};
+    return (v >= 0 && v < 6) ? names[v] : "?";
+}
+
 void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
-                   const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters, cudaStream_t s) {
+                   const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters, cudaStream_t s,
+                   int variant) {
     if (nq <= 0) return;
-    long long warps = (nq + kQueriesPerWarp - 1) / kQueriesPerWarp;
-    k_gather<<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
-        p, nav_of(tree), tp, qb, order, start_nodes, nq, accum, counters);
+    const KdNav nav = nav_of(tree);
+    switch (variant) {
+    case 0: launch_gather_t<2, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
+    case 1: launch_gather_t<2, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
+    case 2: launch_gather_t<3, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
+    case 4: launch_gather_t<4, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
+    case 5: launch_gather_t<4, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
+    default: launch_gather_t<3, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
+    }
 }
 
 void launch_kd_query(const KdTree& tree, int q, const float* qpos, const uint32_t* order, const uint2* start_nodes,

@@ -83,6 +83,12 @@ struct DeviceState {
     DevBuf<float> contrib, train_wsum;
     DevBuf<unsigned> train_count;
     cudaEvent_t evm[2] = {};
+    cudaEvent_t evg[2] = {};    // around the gather kernel alone
+    // gather autotuner: chosen launch variant per query-count class (log2), -1 = untuned;
+    // kept for the life of the process (a new scene reuses the choices)
+    int gather_variant[64] = {};
+    double gather_variant_ms[64][8];
+    DevBuf<double> tune_accum;
     int mlp_rounds = 0;          // training rounds done (the proposal is used after the first)
     double mlp_last_rows = 0;    // training samples collected in the last round
     int iterations_done = 0;
@@ -109,7 +115,9 @@ struct DeviceState {
         train_count.release();
         mlp_rounds = 0;
         mlp_last_rows = 0;
+        tune_accum.release();   // the chosen shapes stay: they are kept for the process
         for (auto& e : evm) if (e) { cudaEventDestroy(e); e = nullptr; }
+        for (auto& e : evg) if (e) { cudaEventDestroy(e); e = nullptr; }
         for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
         if (t0) { cudaEventDestroy(t0); t0 = nullptr; }
         if (t1) { cudaEventDestroy(t1); t1 = nullptr; }
@@ -136,6 +144,7 @@ void default_config(rc_config* c) {
     c->train_iterations = 8;
     c->train_steps = 64;
     c->learning_rate = 1e-3f;
+    c->autotune = 1;
 }
 
 const rc_config& cfg() {
@@ -162,6 +171,8 @@ int upload_scene(HostScene& sc) {
         RC_CUDA(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
         for (auto& e : d.ev) RC_CUDA(cudaEventCreate(&e));
         for (auto& e : d.evm) RC_CUDA(cudaEventCreate(&e));
+        for (auto& e : d.evg) RC_CUDA(cudaEventCreate(&e));
+        for (int& v : d.gather_variant) v = -1;
         RC_CUDA(cudaEventCreate(&d.t0));
         RC_CUDA(cudaEventCreate(&d.t1));
     }
@@ -496,8 +507,36 @@ int render_iteration(HostScene& sc) {
     int qlaunch = 0;
     launch_query_order(tree, reinterpret_cast<const float*>(d.q0.p), 4, (long long)nq, p.radius_sqr, d.qscratch.p,
                        d.qorder.p, d.qstart.p, &qlaunch, s);
+    int variant = 3;
+    if (cfg().autotune && nq > 0) {
+        const int cls = 63 - __builtin_clzll((unsigned long long)nq);
+        if (d.gather_variant[cls] < 0) {
+            // time every launch shape on this iteration's queries into a scratch image
+            // (warm-up launch first: the first launch of a shape loads its code)
+            RC_CUDA(d.tune_accum.reserve(std::max<long long>(3 * npix, 1)));
+            float best = 1e30f;
+            int best_v = 3;
+            for (int v = 0; v < gather_variants(); ++v) {
+                launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.tune_accum.p, nullptr, s, v);
+                RC_CUDA(cudaEventRecord(d.evm[0], s));
+                launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.tune_accum.p, nullptr, s, v);
+                RC_CUDA(cudaEventRecord(d.evm[1], s));
+                RC_CUDA(cudaEventSynchronize(d.evm[1]));
+                const float ms = ms_between(d.evm[0], d.evm[1]);
+                if (v < 8) d.gather_variant_ms[cls][v] = ms;
+                if (ms < best) { best = ms; best_v = v; }
+            }
+            d.gather_variant[cls] = best_v;
+            if (cfg().verbose)
+                std::printf("{\"autotune\": \"gather\", \"queries\": %llu, \"variant\": \"%s\", \"ms\": %.3f}\n",
+                            nq, gather_variant_name(best_v), best);
+        }
+        variant = d.gather_variant[cls];
+    }
     RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
-    launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.accum.p, d.counters.p + 2, s);
+    RC_CUDA(cudaEventRecord(d.evg[0], s));
+    launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.accum.p, d.counters.p + 2, s, variant);
+    RC_CUDA(cudaEventRecord(d.evg[1], s));
     RC_CUDA(cudaGetLastError());
     RC_CUDA(cudaEventRecord(d.ev[7], s));
     unsigned long long gc[4] = {0, 0, 0, 0};
@@ -532,7 +571,7 @@ int render_iteration(HostScene& sc) {
     st[11] = sc.scene_radius;
     st[12] = std::sqrt(p.radius_sqr);
     st[13] = kd_launches + 4 + qlaunch;
-    d.acc_gather_ms += st[7];
+    d.acc_gather_ms += ms_between(d.evg[0], d.evg[1]);   // the gather kernel alone
     // gather algorithmic bytes: each photon record read once (40 B), each query record
     // read once (80 B), each query's FP64 RGB pixel read and written once (48 B)
     d.acc_gather_bytes += 40.0 * (double)nph + 80.0 * (double)nq + 48.0 * (double)nq;

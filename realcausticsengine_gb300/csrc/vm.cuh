@@ -105,9 +105,13 @@ void launch_query_order(const KdTree& tree, const float* qpos, int stride, long 
 // start_nodes[i]: the node where query i's traversal first branches (from launch_query_order).
 // counters (optional, 4 u64 accumulated): accepted photon-query pairs, photon tests
 // (lanes x staged photons), buckets visited, inner nodes visited
+// `variant` picks the gather's launch shape (see gather_variant_name); 3 is the default
+// the autotuner starts from.
 void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
                    const uint2* start_nodes, long long num_queries, double* accum, unsigned long long* counters,
-                   cudaStream_t s);
+                   cudaStream_t s, int variant = 3);
+int gather_variants();
+const char* gather_variant_name(int v);
 // Radius query hook: counts (and, if idx != nullptr, ids at offsets) per query.
 void launch_kd_query(const KdTree& tree, int q, const float* qpos, const uint32_t* order, const uint2* start_nodes,
                      float r2, int* counts, const long long* offsets, int* idx, cudaStream_t s);
