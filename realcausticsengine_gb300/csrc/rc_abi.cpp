@@ -87,6 +87,8 @@ struct DeviceState {
     // gather autotuner: chosen launch variant per query-count class (log2), -1 = untuned;
     // kept for the life of the process (a new scene reuses the choices)
     int gather_variant[64] = {};
+    int light_variant[64] = {};
+    int camera_variant[64] = {};
     double gather_variant_ms[64][8];
     DevBuf<double> tune_accum;
     int mlp_rounds = 0;          // training rounds done (the proposal is used after the first)
@@ -172,7 +174,13 @@ int upload_scene(HostScene& sc) {
         for (auto& e : d.ev) RC_CUDA(cudaEventCreate(&e));
         for (auto& e : d.evm) RC_CUDA(cudaEventCreate(&e));
         for (auto& e : d.evg) RC_CUDA(cudaEventCreate(&e));
-        for (int& v : d.gather_variant) v = -1;
+        static bool tables_ready = false;   // autotuner choices live for the process
+        if (!tables_ready) {
+            for (int& v : d.gather_variant) v = -1;
+            for (int& v : d.light_variant) v = -1;
+            for (int& v : d.camera_variant) v = -1;
+            tables_ready = true;
+        }
         RC_CUDA(cudaEventCreate(&d.t0));
         RC_CUDA(cudaEventCreate(&d.t1));
     }
@@ -388,6 +396,30 @@ int proposal_train(const HostScene& sc, const VMParams& p) {
     return RC_OK;
 }
 
+// Autotuner: time each launch variant of a pass (warm-up launch, then one timed launch;
+// `run(v)` must reset whatever the pass appends to) and return the fastest.
+template <class Run>
+int autotune_variants(int nvariants, Run&& run, const char* what, long long size) {
+    DeviceState& d = g_dev;
+    float best = 1e30f;
+    int best_v = 0;
+    for (int v = 0; v < nvariants; ++v) {
+        run(v);
+        cudaEventRecord(d.evm[0], d.stream);
+        run(v);
+        cudaEventRecord(d.evm[1], d.stream);
+        cudaEventSynchronize(d.evm[1]);
+        const float ms = ms_between(d.evm[0], d.evm[1]);
+        if (ms < best) { best = ms; best_v = v; }
+    }
+    if (cfg().verbose)
+        std::printf("{\"autotune\": \"%s\", \"size\": %lld, \"variant\": %d, \"ms\": %.3f}\n", what, size, best_v,
+                    best);
+    return best_v;
+}
+
+int size_class(long long n) { return n > 0 ? 63 - __builtin_clzll((unsigned long long)n) : 0; }
+
 int render_iteration(HostScene& sc) {
     DeviceState& d = g_dev;
     cudaStream_t s = d.stream;
@@ -420,8 +452,19 @@ int render_iteration(HostScene& sc) {
             if (r) return r;
             RC_CUDA(cudaEventRecord(d.evm[1], s));
         }
+        int lvar = 0;
+        if (sampler == RC_SAMPLER_UNIFORM && cfg().autotune) {
+            int& slot = d.light_variant[size_class(p.num_light_paths)];
+            if (slot < 0)
+                slot = autotune_variants(pass_variants(), [&](int v) {
+                    cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s);
+                    launch_light_pass(p, ph, d.counters.p + 6, s, v);
+                }, "light pass", p.num_light_paths);
+            lvar = slot;
+            RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
+        }
         RC_CUDA(cudaEventRecord(d.ev[0], s));
-        if (sampler == RC_SAMPLER_UNIFORM) launch_light_pass(p, ph, d.counters.p + 6, s);
+        if (sampler == RC_SAMPLER_UNIFORM) launch_light_pass(p, ph, d.counters.p + 6, s, lvar);
         else launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaEventRecord(d.ev[1], s));
@@ -486,8 +529,19 @@ int render_iteration(HostScene& sc) {
         RC_CUDA(d.q3.reserve(qcap)); RC_CUDA(d.q4.reserve(qcap));
         RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s));
         QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qcap, d.counters.p + 1};
+        int cvar = 0;
+        if (cfg().autotune) {
+            int& slot = d.camera_variant[size_class(npix)];
+            if (slot < 0)
+                slot = autotune_variants(pass_variants(), [&](int v) {
+                    cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s);
+                    launch_camera_pass(p, qb, d.counters.p + 7, s, v);
+                }, "camera pass", npix);
+            cvar = slot;
+            RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s));
+        }
         RC_CUDA(cudaEventRecord(d.ev[4], s));
-        launch_camera_pass(p, qb, d.counters.p + 7, s);
+        launch_camera_pass(p, qb, d.counters.p + 7, s, cvar);
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaEventRecord(d.ev[5], s));
         RC_CUDA(cudaMemcpyAsync(&nq, d.counters.p + 1, sizeof(nq), cudaMemcpyDeviceToHost, s));

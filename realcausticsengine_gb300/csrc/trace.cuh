@@ -40,6 +40,22 @@ struct SceneView {
 
 constexpr int kStackSize = 64;   // BVH_STACK_SIZE in the reference
 
+// Traversal stacks.  LocalStack: a per-thread array (local memory).  SharedStack: the
+// thread's column of a [kStackSize][block size] shared-memory array (entry k of thread
+// t at k * stride + t: the lanes of a warp touch consecutive banks).
+struct LocalStack {
+    int s[kStackSize];
+    __device__ __forceinline__ int& operator[](int i) { return s[i]; }
+};
+// Tag: each mesh traversal declares its own LocalStack (the array's lifetime is the
+// traversal, which lets the compiler keep it tight).
+struct CallStack {};
+struct SharedStack {
+    int* base;     // &array[0][threadIdx.x]
+    int stride;    // threads per block
+    __device__ __forceinline__ int& operator[](int i) { return base[i * stride]; }
+};
+
 struct HitRec {
     float t, u, v;
     int slot;       // triangle slot (leaf order) of the reported hit, -1 if none
@@ -93,9 +109,13 @@ __device__ __forceinline__ bool tri_hit(const SceneView& s, int slot, F3 o, F3 d
 
 // Mesh::hit on one mesh with the running record of the current world leaf.
 // Returns false (and sets *overflow) if the stack would exceed kStackSize.
+template <class Stack>
 __device__ __forceinline__ bool mesh_traverse(const SceneView& s, int mesh, F3 o, F3 d, F3 inv, float tmin,
-                                              HitRec& rec, bool& any, int* overflow) {
-    int stack[kStackSize];
+                                              HitRec& rec, bool& any, int* overflow, Stack& stack);
+
+template <class Stack>
+__device__ __forceinline__ bool mesh_traverse_impl(const SceneView& s, int mesh, F3 o, F3 d, F3 inv, float tmin,
+                                                   HitRec& rec, bool& any, int* overflow, Stack& stack) {
     int sp = 0;
     stack[sp++] = __ldg(&s.mesh_root[mesh]);
     while (sp) {
@@ -123,8 +143,24 @@ __device__ __forceinline__ bool mesh_traverse(const SceneView& s, int mesh, F3 o
     return true;
 }
 
-// Scene::hit.  `out` is the reported record (t = inf when nothing was hit).
-__device__ __forceinline__ bool scene_hit(const SceneView& s, F3 o, F3 d, float tmin, HitRec& out, int* overflow) {
+template <class Stack>
+__device__ __forceinline__ bool mesh_traverse(const SceneView& s, int mesh, F3 o, F3 d, F3 inv, float tmin,
+                                              HitRec& rec, bool& any, int* overflow, Stack& stack) {
+    return mesh_traverse_impl(s, mesh, o, d, inv, tmin, rec, any, overflow, stack);
+}
+template <>
+__device__ __forceinline__ bool mesh_traverse<CallStack>(const SceneView& s, int mesh, F3 o, F3 d, F3 inv,
+                                                         float tmin, HitRec& rec, bool& any, int* overflow,
+                                                         CallStack&) {
+    LocalStack st;
+    return mesh_traverse_impl(s, mesh, o, d, inv, tmin, rec, any, overflow, st);
+}
+
+// Scene::hit.  `out` is the reported record (t = inf when nothing was hit).  `stack`
+// serves the mesh levels; the world level (several world leaves only) uses its own.
+template <class Stack>
+__device__ __forceinline__ bool scene_hit(const SceneView& s, F3 o, F3 d, float tmin, HitRec& out, int* overflow,
+                                          Stack& stack) {
     F3 inv = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
     out.t = INFINITY; out.u = 0.0f; out.v = 0.0f; out.slot = -1;
     bool hit = false;
@@ -140,17 +176,17 @@ __device__ __forceinline__ bool scene_hit(const SceneView& s, F3 o, F3 d, float 
         for (int k = 0; k < cnt; ++k) {
             int mesh = __ldg(&s.world_mesh[w1 + k]);
             bool mesh_any = false;
-            if (!mesh_traverse(s, mesh, o, d, inv, tmin, leaf, mesh_any, overflow)) return false;
+            if (!mesh_traverse(s, mesh, o, d, inv, tmin, leaf, mesh_any, overflow, stack)) return false;
             any |= mesh_any;
         }
         if (any) out = leaf;
         return any;
     }
-    int stack[kStackSize];
+    int wstack[kStackSize];
     int sp = 0;
-    stack[sp++] = 0;
+    wstack[sp++] = 0;
     while (sp) {
-        int id = stack[--sp];
+        int id = wstack[--sp];
         float4 lo = __ldg(&s.wnode_lo[id]);
         float4 hi = __ldg(&s.wnode_hi[id]);
         if (!box_hit(lo, hi, o, inv, tmin, out.t)) continue;
@@ -162,17 +198,23 @@ __device__ __forceinline__ bool scene_hit(const SceneView& s, F3 o, F3 d, float 
             for (int k = 0; k < cnt; ++k) {
                 int mesh = __ldg(&s.world_mesh[w1 + k]);
                 bool mesh_any = false;
-                if (!mesh_traverse(s, mesh, o, d, inv, tmin, leaf, mesh_any, overflow)) return false;
+                if (!mesh_traverse(s, mesh, o, d, inv, tmin, leaf, mesh_any, overflow, stack)) return false;
                 any |= mesh_any;
             }
             if (any) { out = leaf; hit = true; }   // unconditional overwrite (world-leaf quirk)
         } else {
             if (sp + 2 > kStackSize) { *overflow = 1; return false; }
-            stack[sp++] = (int)w1;
-            stack[sp++] = (int)w0;
+            wstack[sp++] = (int)w1;
+            wstack[sp++] = (int)w0;
         }
     }
     return hit;
+}
+
+// Scene::hit with per-traversal local-memory stacks.
+__device__ __forceinline__ bool scene_hit(const SceneView& s, F3 o, F3 d, float tmin, HitRec& out, int* overflow) {
+    CallStack st;
+    return scene_hit(s, o, d, tmin, out, overflow, st);
 }
 
 // Attributes Triangle::hit fills in (src/Triangle.cpp:68-80), for the reported triangle.

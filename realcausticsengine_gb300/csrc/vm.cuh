@@ -85,8 +85,8 @@ constexpr int kMltMaxPathLength = 12;
 void launch_mlt_pass(const VMParams& p, PhotonBuf ph, int sampler, int chains, float p_large,
                      unsigned long long* stats, cudaStream_t s);
 // next_path: device counter for the persistent kernel (nullptr: one thread per path)
-void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s);
-void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s);
+void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant = 0);
+void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s, int variant = 0);
 // Debug view `mode` (2 normals, 3 facing, 4 materials with IOR `ior`) added into the
 // FP64 image accumulation.
 void launch_debug_view(const VMParams& p, int mode, float ior, double* accum, cudaStream_t s);
@@ -111,6 +111,10 @@ void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryB
                    const uint2* start_nodes, long long num_queries, double* accum, unsigned long long* counters,
                    cudaStream_t s, int variant = 3);
 int gather_variants();
+// Launch shapes of the persistent light and camera passes (block size x traversal-stack
+// placement), chosen by the autotuner; 0 is the default.
+int pass_variants();
+const char* pass_variant_name(int v);
 const char* gather_variant_name(int v);
 // Radius query hook: counts (and, if idx != nullptr, ids at offsets) per query.
 void launch_kd_query(const KdTree& tree, int q, const float* qpos, const uint32_t* order, const uint2* start_nodes,

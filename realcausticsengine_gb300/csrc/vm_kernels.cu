@@ -59,10 +59,11 @@ __device__ __forceinline__ bool light_path_start(const VMParams& P, long long pi
 
 // One bounce of Vertex_Merging::trace_light_path (src/Vertex_Merging.cpp:140-194);
 // returns false when the path ends.
-__device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& ph, LightPath& s) {
+template <class Stack>
+__device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& ph, LightPath& s, Stack& stack) {
     F3 ro = s.o + s.d * kRayEps;
     HitRec h;
-    if (!scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK)) return false;
+    if (!scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK, stack)) return false;
     Isect is;
     fill_isect(P.scene, h, ro, s.d, is);
     if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); return false; }
@@ -101,8 +102,26 @@ __device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& 
     return true;
 }
 
-__global__ void __launch_bounds__(256) k_light_pass_persistent(const VMParams P, PhotonBuf ph,
-                                                                unsigned long long* __restrict__ next_path) {
+// Traversal-stack placement for the persistent passes: in shared memory (a
+// [kStackSize][block] int array, dynamic) or per-thread local memory.
+template <bool kSharedStack>
+struct PassStack;
+template <>
+struct PassStack<true> {
+    SharedStack st;
+    __device__ __forceinline__ PassStack(int* smem) : st{smem + threadIdx.x, (int)blockDim.x} {}
+};
+template <>
+struct PassStack<false> {
+    CallStack st;
+    __device__ __forceinline__ PassStack(int*) {}
+};
+
+template <int kBlock, bool kSharedStack>
+__global__ void __launch_bounds__(kBlock) k_light_pass_persistent(const VMParams P, PhotonBuf ph,
+                                                                   unsigned long long* __restrict__ next_path) {
+    extern __shared__ int pass_smem[];
+    PassStack<kSharedStack> stk(pass_smem);
     const int lane = threadIdx.x & 31;
     LightPath s;
     bool alive = false;
@@ -121,7 +140,7 @@ __global__ void __launch_bounds__(256) k_light_pass_persistent(const VMParams P,
             if (base + __popc(need) >= (unsigned long long)P.num_light_paths) pool_left = false;
         }
         if (!__any_sync(0xffffffffu, alive)) break;
-        if (alive) alive = light_path_bounce(P, ph, s);
+        if (alive) alive = light_path_bounce(P, ph, s, stk.st);
     }
 }
 
@@ -274,10 +293,11 @@ __device__ __forceinline__ bool camera_path_start(const VMParams& P, long long p
     return true;
 }
 
-__device__ __forceinline__ bool camera_path_bounce(const VMParams& P, QueryBuf& qb, CameraPath& s) {
+template <class Stack>
+__device__ __forceinline__ bool camera_path_bounce(const VMParams& P, QueryBuf& qb, CameraPath& s, Stack& stack) {
     F3 ro = s.o + s.d * kRayEps;
     HitRec h;
-    if (!scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK)) return false;
+    if (!scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK, stack)) return false;
     Isect is;
     fill_isect(P.scene, h, ro, s.d, is);
     if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); return false; }
@@ -314,8 +334,11 @@ __device__ __forceinline__ bool camera_path_bounce(const VMParams& P, QueryBuf& 
     return true;
 }
 
-__global__ void __launch_bounds__(256) k_camera_pass_persistent(const VMParams P, QueryBuf qb,
-                                                                 unsigned long long* __restrict__ next_pixel) {
+template <int kBlock, bool kSharedStack>
+__global__ void __launch_bounds__(kBlock) k_camera_pass_persistent(const VMParams P, QueryBuf qb,
+                                                                    unsigned long long* __restrict__ next_pixel) {
+    extern __shared__ int pass_smem[];
+    PassStack<kSharedStack> stk(pass_smem);
     const int lane = threadIdx.x & 31;
     const long long npix = (long long)P.camera.width * P.camera.height;
     CameraPath s;
@@ -335,7 +358,7 @@ __global__ void __launch_bounds__(256) k_camera_pass_persistent(const VMParams P
             need = __ballot_sync(0xffffffffu, !alive);   // samples outside the buffer: draw again
         }
         if (!__any_sync(0xffffffffu, alive)) break;
-        if (alive) alive = camera_path_bounce(P, qb, s);
+        if (alive) alive = camera_path_bounce(P, qb, s, stk.st);
     }
 }
 
@@ -379,48 +402,85 @@ __global__ void k_trace_rays(const SceneView S, int n, const float* __restrict__
     }
 }
 
+// Persistent grid for one shape: resident blocks per SM (occupancy with its dynamic
+// shared memory) x SMs, capped by the work.
+template <class K>
+unsigned persistent_grid(K kernel, int block, size_t smem, long long work_items) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+    const long long blocks = (long long)sms * (per_sm > 0 ? per_sm : 1);
+    const long long need = (work_items + block - 1) / block;
+    return (unsigned)(need < blocks ? need : blocks);
+}
+
+template <int B, bool SH>
+void launch_light_t(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s) {
+    const size_t smem = SH ? (size_t)kStackSize * B * sizeof(int) : 0;
+    static unsigned grid_cache = 0;
+    static long long grid_for = -1;
+    if (grid_for != p.num_light_paths) {
+        grid_cache = persistent_grid(k_light_pass_persistent<B, SH>, B, smem, p.num_light_paths);
+        grid_for = p.num_light_paths;
+    }
+    cudaMemsetAsync(next_path, 0, sizeof(unsigned long long), s);
+    k_light_pass_persistent<B, SH><<<grid_cache, B, smem, s>>>(p, ph, next_path);
+}
+
+template <int B, bool SH>
+void launch_camera_t(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s) {
+    const long long n = (long long)p.camera.width * p.camera.height;
+    const size_t smem = SH ? (size_t)kStackSize * B * sizeof(int) : 0;
+    static unsigned grid_cache = 0;
+    static long long grid_for = -1;
+    if (grid_for != n) {
+        grid_cache = persistent_grid(k_camera_pass_persistent<B, SH>, B, smem, n);
+        grid_for = n;
+    }
+    cudaMemsetAsync(next_pixel, 0, sizeof(unsigned long long), s);
+    k_camera_pass_persistent<B, SH><<<grid_cache, B, smem, s>>>(p, qb, next_pixel);
+}
+
 }  // namespace
 
-void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s) {
+int pass_variants() { return 4; }
+
+const char* pass_variant_name(int v) {
+    static const char* names[4] = {"256 threads, local-memory stack", "256 threads, shared-memory stack",
+                                   "128 threads, local-memory stack", "128 threads, shared-memory stack"};
+    return (v >= 0 && v < 4) ? names[v] : "?";
+}
+
+void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant) {
     long long n = p.num_light_paths;
     if (n <= 0) return;
     if (!next_path) {
         k_light_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, ph);
         return;
     }
-    static int blocks = 0;
-    if (!blocks) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_light_pass_persistent, 256, 0);
-        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    switch (variant) {
+    case 1: launch_light_t<256, true>(p, ph, next_path, s); break;
+    case 2: launch_light_t<128, false>(p, ph, next_path, s); break;
+    case 3: launch_light_t<128, true>(p, ph, next_path, s); break;
+    default: launch_light_t<256, false>(p, ph, next_path, s); break;
     }
-    long long need = (n + 255) / 256;
-    unsigned grid = (unsigned)(need < blocks ? need : blocks);
-    cudaMemsetAsync(next_path, 0, sizeof(unsigned long long), s);
-    k_light_pass_persistent<<<grid, 256, 0, s>>>(p, ph, next_path);
 }
 
-void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s) {
+void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s, int variant) {
     long long n = (long long)p.camera.width * p.camera.height;
     if (n <= 0) return;
     if (!next_pixel) {
         k_camera_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, qb);
         return;
     }
-    static int blocks = 0;
-    if (!blocks) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_camera_pass_persistent, 256, 0);
-        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    switch (variant) {
+    case 1: launch_camera_t<256, true>(p, qb, next_pixel, s); break;
+    case 2: launch_camera_t<128, false>(p, qb, next_pixel, s); break;
+    case 3: launch_camera_t<128, true>(p, qb, next_pixel, s); break;
+    default: launch_camera_t<256, false>(p, qb, next_pixel, s); break;
     }
-    long long need = (n + 255) / 256;
-    unsigned grid = (unsigned)(need < blocks ? need : blocks);
-    cudaMemsetAsync(next_pixel, 0, sizeof(unsigned long long), s);
-    k_camera_pass_persistent<<<grid, 256, 0, s>>>(p, qb, next_pixel);
 }
 
 // Debug views (src/Debug_scene.cpp:21-214, dispatched by src/main.cpp:172-180): one
