@@ -471,7 +471,7 @@ enum Kind { K_SPEC_REFL, K_FRESNEL_SPEC, K_GGX_REFL, K_PLASTIC, K_PLASTIC_SMOOTH
 template <class R> struct Bsdf {
     Kind kind; V3<R> Rc; R ior = 0, a2 = 0, s = 0, contp = 0; bool radiance;
     Frame<R> fr; V3<R> wo;
-    void init(const Material& m, const V3<R>& ns, const V3<R>& dir, bool rad) {   // src/materials.h:59-146
+    void init(const Material& m, const V3<R>& ns, const V3<R>& dir, bool rad, float ior_shift = 0.0f) {   // src/materials.h:59-146
         radiance = rad;
         Rc = cvt<R>(m.color);
         if (m.type == 'P') {
@@ -485,7 +485,7 @@ template <class R> struct Bsdf {
             if (m.roughness < 0.01f) kind = K_SPEC_REFL;
             else { kind = K_GGX_REFL; a2 = (R)(m.roughness * m.roughness); }
         } else if (m.type == 'R') {
-            ior = (R)m.ior;
+            ior = (R)(m.ior + ior_shift);
             if (m.roughness < 0.01f) kind = K_FRESNEL_SPEC;
             else { kind = K_GGX_DIEL; a2 = (R)(m.roughness * m.roughness); }
         } else {
@@ -1044,6 +1044,22 @@ int prepare(Scene& s, std::string& err) {
 // ---------------------------------------------------------------- plain-mode iteration (uniform light paths, Philox)
 template <class R> struct PlainCfg { uint64_t seed; long long paths; int maxlen; };
 
+// Dispersion (additive, no counterpart in the reference): material 'R' with specular > 0
+// has IOR ior - d, ior, ior + d for R, G, B.  A path keeps one channel c from its first
+// dispersive vertex on (uniform, from Philox block 48 + bounce), throughput 3 x channel c.
+inline float disp_of(const Material& m) { return (m.type == 'R' && m.specular > 0.0f) ? m.specular : 0.0f; }
+template <class R> float dispersion_shift(const Material& m, int& channel, V3<R>& tp, float u) {
+    const float dsp = disp_of(m);
+    if (!(dsp > 0.0f)) return 0.0f;
+    if (channel < 0) {
+        int c = (int)(u * 3.0f);
+        channel = c > 2 ? 2 : c;
+        tp = V3<R>(channel == 0 ? R(3.0f) * tp.x : R(0), channel == 1 ? R(3.0f) * tp.y : R(0),
+                   channel == 2 ? R(3.0f) * tp.z : R(0));
+    }
+    return (float)(channel - 1) * dsp;
+}
+
 template <class R> void trace_light(const Scene& s, const PlainCfg<R>& c, long long pidx, uint32_t it,
                                     std::vector<Photon<R>>& out) {
     PRng rng(c.seed, (uint64_t)pidx, it, 0u);
@@ -1051,14 +1067,17 @@ template <class R> void trace_light(const Scene& s, const PlainCfg<R>& c, long l
     R u[5] = {(R)u01(b0.a), (R)u01(b0.b), (R)u01(b0.c), (R)u01(b0.d), (R)u01(b1.a)};
     V3<R> o, d, tp;
     sample_light<R>(s, u, o, d, tp);
-    int diffuse = 0, last = EV_D;
+    int diffuse = 0, last = EV_D, channel = -1;
     R dVM = 0;
     for (int len = 0;; ++len) {
         V3<R> ro = o + d * R(0.001f);
         Hit<R> h;
         if (!scene_hit<R>(s, ro, d, R(0.001f), h)) break;
         Isect<R> is; fill<R>(s, h, ro, d, is);
-        Bsdf<R> b; b.init(s.mats[is.mat], is.ns, is.dir, false);
+        const Material& mt = s.mats[is.mat];
+        const float shift = disp_of(mt) > 0.0f
+            ? dispersion_shift<R>(mt, channel, tp, u01(rng.block(48 + len).a)) : 0.0f;
+        Bsdf<R> b; b.init(mt, is.ns, is.dir, false, shift);
         if (!b.valid()) break;
         dVM /= std::abs(std::abs(b.wo.z));
         bool stored = false;
@@ -1127,12 +1146,16 @@ template <class R> V3<R> camera_path(const Scene& s, const PhotonMap<R>& pm, con
     V3<R> o = cvt<R>(s.cam_o), d = normalize(dir), tp(1);
     R dVM = 0;
     V3<R> color(0);
+    int channel = -1;
     for (int len = 0;; ++len) {
         V3<R> ro = o + d * R(0.001f);
         Hit<R> h;
         if (!scene_hit<R>(s, ro, d, R(0.001f), h)) break;
         Isect<R> is; fill<R>(s, h, ro, d, is);
-        Bsdf<R> b; b.init(s.mats[is.mat], is.ns, is.dir, true);
+        const Material& mt = s.mats[is.mat];
+        const float shift = disp_of(mt) > 0.0f
+            ? dispersion_shift<R>(mt, channel, tp, u01(rng.block(48 + len).a)) : 0.0f;
+        Bsdf<R> b; b.init(mt, is.ns, is.dir, true, shift);
         if (!b.valid()) break;
         dVM /= std::abs(b.wo.z);
         if (!b.delta()) color += tp * vm_norm * contrib<R>(pm, is, b, r2, dVM);

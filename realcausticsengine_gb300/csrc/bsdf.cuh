@@ -86,6 +86,29 @@ __device__ __forceinline__ F3 ggx_half(float e1, float e2, float a2) {
     return {st * cp, st * sp, ct};
 }
 
+// Dispersion (per-channel IOR): a path that meets a dispersive material for the first
+// time keeps one colour channel c (uniform, from sample block kChannelBlock + bounce),
+// its throughput becomes 3 x that channel alone, and every dispersive interaction of the
+// path then uses IOR ior + (c - 1) * disp.  channel < 0: not chosen yet.
+constexpr uint32_t kChannelBlock = 48;
+
+__device__ __forceinline__ int pick_channel(float u) {
+    const int c = (int)(u * 3.0f);
+    return c > 2 ? 2 : c;
+}
+__device__ __forceinline__ F3 keep_channel(F3 tp, int c) {
+    return f3(c == 0 ? 3.0f * tp.x : 0.0f, c == 1 ? 3.0f * tp.y : 0.0f, c == 2 ? 3.0f * tp.z : 0.0f);
+}
+// IOR shift at a material for a path's channel (choosing it on first contact).
+__device__ __forceinline__ float dispersion_shift(const DevMaterial& m, int& channel, F3& tp, float u) {
+    if (!(m.disp > 0.0f)) return 0.0f;
+    if (channel < 0) {
+        channel = pick_channel(u);
+        tp = keep_channel(tp, channel);
+    }
+    return (float)(channel - 1) * m.disp;
+}
+
 struct BsdfSample {
     F3 f;           // throughput factor; zero = sampling failed
     F3 wi;          // sampled world direction
@@ -103,10 +126,11 @@ struct Bsdf {
     F3 wo;          // local direction towards the previous vertex
     bool radiance;  // TransportMode::Radiance (camera) vs Importance (light)
 
-    __device__ __forceinline__ void init(const DevMaterial& m, F3 ns, F3 ray_dir, bool radiance_mode) {
+    __device__ __forceinline__ void init(const DevMaterial& m, F3 ns, F3 ray_dir, bool radiance_mode,
+                                         float ior_shift = 0.0f) {
         kind = m.kind;
         R = f3(m.r, m.g, m.b);
-        ior = m.ior; a2 = m.a2; s = m.s; cont = m.cont;
+        ior = m.ior + ior_shift; a2 = m.a2; s = m.s; cont = m.cont;
         radiance = radiance_mode;
         fr.set_from_z(ns);
         wo = fr.to_local(-ray_dir);

@@ -278,7 +278,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const
         const F3 q = xyz(a), ng = xyz(c);
         const float cam_dVM = a.w;
         Bsdf bs;
-        bs.init(P.materials[__float_as_int(b.w)], xyz(b), xyz(e), true);
+        const DevMaterial& qm = P.materials[__float_as_int(b.w)];
+        const int channel = __float_as_int(e.w);   // the camera path's dispersion channel
+        bs.init(qm, xyz(b), xyz(e), true, (qm.disp > 0.0f && channel >= 0) ? (float)(channel - 1) * qm.disp : 0.0f);
         // per-query constants of the merge evaluation
         const float wo_ng = dot(bs.fr.to_world(bs.wo), ng);
         const float fwo = (bs.kind == BSDF_K_PLASTIC_GGX || bs.kind == BSDF_K_PLASTIC_SMOOTH)

@@ -507,9 +507,11 @@ void convert_materials(HostScene& scene) {
             if (pm.roughness < 0.01f) m.kind = BSDF_K_SPECULAR_REFLECTION;
             else { m.kind = BSDF_K_GGX_REFLECTION; m.a2 = pm.roughness * pm.roughness; }
         } else if (pm.type == 'R') {
-            // rough GGX dielectric (additive type): alpha = roughness
+            // rough GGX dielectric (additive type): alpha = roughness; `specular` > 0 is
+            // the per-channel IOR dispersion (R: ior - d, G: ior, B: ior + d)
             m.r = cr; m.g = cg; m.b = cb;
             m.ior = pm.ior;
+            m.disp = pm.specular > 0.0f ? pm.specular : 0.0f;
             if (pm.roughness < 0.01f) m.kind = BSDF_K_FRESNEL_SPECULAR;
             else { m.kind = BSDF_K_GGX_DIELECTRIC; m.a2 = pm.roughness * pm.roughness; }
         } else {

@@ -35,6 +35,7 @@ struct DevMaterial {
     float a2;             // GGX alpha^2 as the reference stores it (a2 member)
     float s;              // plastic specular reflectance (specular * 0.08)
     float cont;           // max(0.05, max colour)  (mContiniationProb)
+    float disp;           // per-channel IOR spread: R, G, B see ior - disp, ior, ior + disp
 };
 
 enum LightType : int { LIGHT_AREA = 0, LIGHT_SUN = 1, LIGHT_POINT = 2 };

@@ -29,6 +29,7 @@ struct LightPath {
     F3 o, d, tp;
     float dVM;
     int diffuse, last, len;
+    int channel;      // dispersion channel, -1 until a dispersive material is met
     long long idx;
     PathRng rng;
 };
@@ -54,6 +55,7 @@ __device__ __forceinline__ bool light_path_start(const VMParams& P, long long pi
     s.last = EV_DIFFUSE;
     s.dVM = 0.0f;
     s.len = 0;
+    s.channel = -1;
     return true;
 }
 
@@ -67,8 +69,11 @@ __device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& 
     Isect is;
     fill_isect(P.scene, h, ro, s.d, is);
     if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); return false; }
+    const DevMaterial& mat = P.materials[is.material];
+    const float shift = mat.disp > 0.0f
+        ? dispersion_shift(mat, s.channel, s.tp, u01(s.rng.block(kChannelBlock + s.len).a)) : 0.0f;
     Bsdf b;
-    b.init(P.materials[is.material], is.ns, is.dir, false);
+    b.init(mat, is.ns, is.dir, false, shift);
     if (!b.valid()) return false;
     s.dVM /= fabsf(b.cos_theta_in());
     bool stored = false;
@@ -144,126 +149,12 @@ __global__ void __launch_bounds__(kBlock) k_light_pass_persistent(const VMParams
     }
 }
 
-__global__ void __launch_bounds__(256) k_light_pass(const VMParams P, PhotonBuf ph) {
-    long long pidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (pidx >= P.num_light_paths) return;
-    PathRng rng;
-    rng.init(P.seed, (uint64_t)pidx, P.iteration, STREAM_LIGHT);
-    U4 b0 = rng.block(0), b1 = rng.block(1);
-    F3 o, d, tp;
-    sample_light(P.lights, u01(b0.a), u01(b0.b), u01(b0.c), u01(b0.d), u01(b1.a), o, d, tp);
-    int diffuse = 0, last = EV_DIFFUSE;
-    float dVM = 0.0f;
-    for (int len = 0;; ++len) {
-        F3 ro = o + d * kRayEps;
-        HitRec h;
-        if (!scene_hit(P.scene, ro, d, kRayEps, h, P.error + ERR_STACK)) break;
-        Isect is;
-        fill_isect(P.scene, h, ro, d, is);
-        if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); break; }
-        Bsdf b;
-        b.init(P.materials[is.material], is.ns, is.dir, false);
-        if (!b.valid()) break;
-        dVM /= fabsf(b.cos_theta_in());
-        bool stored = false;
-        if (!b.is_delta() && (last & EV_GLOSSY)) {
-            unsigned long long slot = warp_append(ph.count);
-            if (slot < (unsigned long long)ph.capacity) {
-                ph.pos[slot] = make_float4(is.pos.x, is.pos.y, is.pos.z, dVM);
-                ph.dir[slot] = make_float4(-is.dir.x, -is.dir.y, -is.dir.z, tp.x);
-                ph.tp[slot] = make_float2(tp.y, tp.z);
-                ph.path[slot] = (uint32_t)pidx;
-            }
-            stored = true;
-        }
-        if (len > P.max_path_length || diffuse > kMaxDiffuse) break;
-        U4 bb = rng.block(2 + len);
-        BsdfSample s = b.sample(u01(bb.a), u01(bb.b), u01(bb.c), is.ng);
-        if (is_zero(s.f)) break;
-        F3 f = s.f;
-        if (len > kRRDepth) {
-            if (u01(bb.d) > s.cont) break;
-            f = div_each(f, s.cont);
-        }
-        o = is.pos;
-        d = s.wi;
-        if (s.event & EV_DIFFUSE) diffuse++;
-        tp = tp * f;
-        last = s.event;
-        if (!stored) dVM *= (s.cos_out / s.fwd) * s.rev;
-        else dVM = (s.cos_out / s.fwd) * (1.0f + s.rev * dVM);
-    }
-}
-
-__global__ void __launch_bounds__(256) k_camera_pass(const VMParams P, QueryBuf qb) {
-    long long pix = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const int W = P.camera.width, H = P.camera.height;
-    if (pix >= (long long)W * H) return;
-    PathRng rng;
-    rng.init(P.camera_seed, (uint64_t)pix, P.iteration, STREAM_CAMERA);
-    U4 b1 = rng.block(1);
-    // Generate_camera_sample (src/Vertex_Merging.cpp:27-46)
-    const float x = (float)(int)(pix % W);
-    const float y = (float)(int)(pix / W);
-    const float sx = x + u01(b1.b), sy = y + u01(b1.c);
-    // Image_Buffer::add_color (src/Image_Buffer.h:24-37): Y = ResY - (int)y, so camera
-    // row 0 falls outside the buffer and is dropped; its path contributes nothing.
-    if (sx < 0 || sx >= (float)W || sy < 0 || sy >= (float)H) return;
-    const int X = (int)sx, Y = H - (int)sy;
-    const long long target = (long long)X + (long long)Y * W;
-    if (target > (long long)W * H - 1) return;
-    // Camera::get_ray (src/Camera.h:29-34)
-    F3 dir = ld3(P.camera.bottom_left) + ld3(P.camera.horizontal) * (sx / (float)W) +
-             ld3(P.camera.vertical) * (sy / (float)H);
-    dir = dir - ld3(P.camera.origin);
-    F3 o = ld3(P.camera.origin);
-    F3 d = normalize(dir);
-    F3 tp = f3(1.0f);
-    float dVM = 0.0f;
-    for (int len = 0;; ++len) {
-        F3 ro = o + d * kRayEps;
-        HitRec h;
-        if (!scene_hit(P.scene, ro, d, kRayEps, h, P.error + ERR_STACK)) break;
-        Isect is;
-        fill_isect(P.scene, h, ro, d, is);
-        if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); break; }
-        Bsdf b;
-        b.init(P.materials[is.material], is.ns, is.dir, true);
-        if (!b.valid()) break;
-        dVM /= fabsf(b.cos_theta_in());
-        if (!b.is_delta()) {
-            unsigned long long slot = warp_append(qb.count);
-            if (slot < (unsigned long long)qb.capacity) {
-                F3 w = tp * P.vm_norm;
-                qb.q0[slot] = make_float4(is.pos.x, is.pos.y, is.pos.z, dVM);
-                qb.q1[slot] = make_float4(is.ns.x, is.ns.y, is.ns.z, __int_as_float(is.material));
-                qb.q2[slot] = make_float4(is.ng.x, is.ng.y, is.ng.z, __int_as_float((int)target));
-                qb.q3[slot] = make_float4(w.x, w.y, w.z, 0.0f);
-                qb.q4[slot] = make_float4(is.dir.x, is.dir.y, is.dir.z, 0.0f);
-            }
-        }
-        if (len > P.max_path_length) break;
-        U4 bb = rng.block(2 + len);
-        BsdfSample s = b.sample(u01(bb.a), u01(bb.b), u01(bb.c), is.ng);
-        if (is_zero(s.f)) break;
-        F3 f = s.f;
-        if (len > kRRDepth) {
-            if (u01(bb.d) > s.cont) break;
-            f = div_each(f, s.cont);
-        }
-        o = is.pos;
-        d = s.wi;
-        tp = tp * f;
-        if (s.event & EV_SPECULAR) dVM *= (s.cos_out / s.fwd) * s.rev;
-        else dVM = (s.cos_out / s.fwd) * (1.0f + s.rev * dVM);
-    }
-}
-
 // Persistent camera pass with path regeneration (same scheme as the light pass).
 struct CameraPath {
     F3 o, d, tp;
     float dVM;
     int len;
+    int channel;      // dispersion channel, -1 until a dispersive material is met
     int target;
     PathRng rng;
 };
@@ -289,6 +180,7 @@ __device__ __forceinline__ bool camera_path_start(const VMParams& P, long long p
     s.tp = f3(1.0f);
     s.dVM = 0.0f;
     s.len = 0;
+    s.channel = -1;
     s.target = (int)target;
     return true;
 }
@@ -301,8 +193,11 @@ __device__ __forceinline__ bool camera_path_bounce(const VMParams& P, QueryBuf& 
     Isect is;
     fill_isect(P.scene, h, ro, s.d, is);
     if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); return false; }
+    const DevMaterial& mat = P.materials[is.material];
+    const float shift = mat.disp > 0.0f
+        ? dispersion_shift(mat, s.channel, s.tp, u01(s.rng.block(kChannelBlock + s.len).a)) : 0.0f;
     Bsdf b;
-    b.init(P.materials[is.material], is.ns, is.dir, true);
+    b.init(mat, is.ns, is.dir, true, shift);
     if (!b.valid()) return false;
     s.dVM /= fabsf(b.cos_theta_in());
     if (!b.is_delta()) {
@@ -313,7 +208,7 @@ __device__ __forceinline__ bool camera_path_bounce(const VMParams& P, QueryBuf& 
             qb.q1[slot] = make_float4(is.ns.x, is.ns.y, is.ns.z, __int_as_float(is.material));
             qb.q2[slot] = make_float4(is.ng.x, is.ng.y, is.ng.z, __int_as_float(s.target));
             qb.q3[slot] = make_float4(w.x, w.y, w.z, 0.0f);
-            qb.q4[slot] = make_float4(is.dir.x, is.dir.y, is.dir.z, 0.0f);
+            qb.q4[slot] = make_float4(is.dir.x, is.dir.y, is.dir.z, __int_as_float(s.channel));
         }
     }
     if (s.len > P.max_path_length) return false;
@@ -456,10 +351,7 @@ const char* pass_variant_name(int v) {
 void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant) {
     long long n = p.num_light_paths;
     if (n <= 0) return;
-    if (!next_path) {
-        k_light_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, ph);
-        return;
-    }
+    if (!next_path) return;
     switch (variant) {
     case 1: launch_light_t<256, true>(p, ph, next_path, s); break;
     case 2: launch_light_t<128, false>(p, ph, next_path, s); break;
@@ -471,10 +363,7 @@ void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next
 void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s, int variant) {
     long long n = (long long)p.camera.width * p.camera.height;
     if (n <= 0) return;
-    if (!next_pixel) {
-        k_camera_pass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, qb);
-        return;
-    }
+    if (!next_pixel) return;
     switch (variant) {
     case 1: launch_camera_t<256, true>(p, qb, next_pixel, s); break;
     case 2: launch_camera_t<128, false>(p, qb, next_pixel, s); break;

@@ -43,7 +43,7 @@ struct PhotonRec { float4 pos, dir; float2 tp; };
 __device__ int trace_light_samples(const VMParams& P, const float* u, const PathRng& rr, int maxlen, PhotonRec* out) {
     F3 o, d, tp;
     sample_light(P.lights, u[0], u[1], u[2], u[3], u[4], o, d, tp);
-    int diffuse = 0, last = EV_DIFFUSE, n = 0;
+    int diffuse = 0, last = EV_DIFFUSE, n = 0, channel = -1;
     float dVM = 0.0f;
     for (int len = 0;; ++len) {
         F3 ro = o + d * kRayEps;
@@ -52,8 +52,12 @@ __device__ int trace_light_samples(const VMParams& P, const float* u, const Path
         Isect is;
         fill_isect(P.scene, h, ro, d, is);
         if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); break; }
+        const DevMaterial& mat = P.materials[is.material];
+        // dispersion channel from the Russian-roulette stream (outside the primary samples)
+        const float shift = mat.disp > 0.0f
+            ? dispersion_shift(mat, channel, tp, u01(rr.block(kChannelBlock + len).a)) : 0.0f;
         Bsdf b;
-        b.init(P.materials[is.material], is.ns, is.dir, false);
+        b.init(mat, is.ns, is.dir, false, shift);
         if (!b.valid()) break;
         dVM /= fabsf(b.cos_theta_in());
         bool stored = false;

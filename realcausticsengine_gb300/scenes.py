@@ -154,11 +154,13 @@ def water_pool(width=1920, height=1080, grid=512, samples=64, roughness=0.02) ->
                  name="water_pool")
 
 
-def test_scene(width=64, height=48, subdiv=2, samples=2, rough_glass=False) -> Scene:
+def test_scene(width=64, height=48, subdiv=2, samples=2, rough_glass=False, dispersion=0.0) -> Scene:
     """Small scene for CPU parity: glass sphere, rough metal sphere, smooth and rough
     plastic boxes with rotations, a diffuse floor, an area light (reference-renderable
-    unless rough_glass)."""
-    mats = [Material("R" if rough_glass else "G", color=(1, 1, 1), ior=1.5, roughness=0.1 if rough_glass else 0.0),
+    unless rough_glass or dispersion; dispersion > 0 makes the sphere an 'R' dielectric
+    with that per-channel IOR spread)."""
+    glass = "R" if (rough_glass or dispersion > 0) else "G"
+    mats = [Material(glass, color=(1, 1, 1), ior=1.5, roughness=0.1 if rough_glass else 0.0, specular=dispersion),
             Material("P", color=(0.8, 0.8, 0.8), roughness=1.0, specular=0.0),
             Material("M", color=(0.9, 0.8, 0.6), roughness=0.3),
             Material("P", color=(0.3, 0.6, 0.9), roughness=0.05, specular=0.5),

@@ -222,6 +222,38 @@ def test_render_vs_oracle_same_samples(orc):
         assert rel < 0.03
 
 
+@pytest.mark.parametrize("rough", [False, True])
+def test_dispersion_vs_oracle_same_samples(orc, rough):
+    """Per-channel IOR dispersion (material 'R', spread 0.05) on a smooth or rough glass
+    sphere: GPU FP32 against the oracle's restatement with the same samples (channel
+    choice included): relative RMSE < 3%; and energy: the dispersive image's mean stays
+    within 5% of the same scene without dispersion (a 0.05 IOR spread moves the caustic,
+    not the energy, up to Fresnel changes)."""
+    sc = scenes.test_scene(48, 36, subdiv=2, rough_glass=rough, dispersion=0.05)
+    paths, seed, iters = 30000, 4, 3
+    r = Renderer(sc, max_path_length=6, photons_per_iter=paths, seed=seed)
+    r.render(iters)
+    img = r.image().reshape(-1)
+    r.release()
+    _oracle_scene(orc, sc)
+    acc = np.zeros(img.size, np.float64)
+    assert orc.oracle_render_plain(0, iters, 32, seed, paths, 6, 8, acc.ctypes.data, None) == 0
+    ref = acc / iters
+    rel = _rel_rmse(img, ref)
+    print(f"dispersion rough={rough}: rel RMSE {rel:.3e}")
+    assert rel < 0.03
+    plain = scenes.test_scene(48, 36, subdiv=2, rough_glass=rough)
+    r = Renderer(plain, max_path_length=6, photons_per_iter=200000, seed=seed)
+    r.render(6)
+    base = r.image().mean()
+    r.release()
+    r = Renderer(sc, max_path_length=6, photons_per_iter=200000, seed=seed)
+    r.render(6)
+    disp = r.image().mean()
+    r.release()
+    assert abs(disp / base - 1.0) < 0.05, (disp, base)
+
+
 def test_main_writes_exr_like_reference(tmp_path, monkeypatch):
     """init() + main(): renders `samples` iterations and writes the EXR the add-on reads."""
     from realcausticsengine_gb300 import _native, abi
