@@ -10,6 +10,10 @@ Workloads (sizes as specified; coordinates mapped from the y-up wording by
                        32 sines (wavelength log-uniform [0.2,3], amplitude ~ wl^1.5, max
                        0.05), GGX dielectric roughness 0.02 IOR 1.33, diffuse floor 1.5
                        below, 2x2 area light at height 6, 1920x1080, 16M photons/iter
+  gem_cluster          2,000 convex polyhedra of 60-200 facets (~260k triangles), IOR
+                       U(1.5,2.4), roughness U(0,0.05), per-channel IOR spread 0.02, 8 area
+                       lights of random size and colour, 3840x2160; 65,536 PSSMLT chains,
+                       large-step probability 0.3, 32M photons/iter
   small test scenes    the same ingredients at sizes the CPU oracle finishes in seconds
 """
 from __future__ import annotations
@@ -189,6 +193,97 @@ def sun_scene(width=48, height=32) -> Scene:
     s.lights = [Light("S", color=(1, 1, 0.9), rotation=(0.3, -0.2, 0.5), power=3.0)]
     s.name = "sun_scene"
     return s
+
+
+def _convex_gem(rng, n_points: int):
+    """A convex polyhedron: the hull of random points on an ellipsoid, flat-shaded
+    (vertices repeated per facet, normals = outward facet normals)."""
+    from scipy.spatial import ConvexHull
+    axes = np.array([1.0, rng.uniform(0.6, 1.0), rng.uniform(0.4, 0.8)])
+    p = rng.normal(size=(n_points, 3))
+    p /= np.linalg.norm(p, axis=1, keepdims=True)
+    p *= axes
+    hull = ConvexHull(p)
+    tris = hull.simplices.copy()
+    a, b, c = p[tris[:, 0]], p[tris[:, 1]], p[tris[:, 2]]
+    n = np.cross(b - a, c - a)
+    flip = (n * hull.equations[:, :3]).sum(1) < 0
+    tris[flip] = tris[flip][:, [0, 2, 1]]
+    n[flip] = -n[flip]
+    V = p[tris.reshape(-1)]
+    N = np.repeat(n, 3, axis=0)
+    F = np.arange(len(V), dtype=np.uint32).reshape(-1, 3)
+    return V, N, F
+
+
+def _rotation(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def gem_cluster(width=3840, height=2160, n_gems=2000, groups=1, seed=0, dispersion=0.02, samples=128) -> Scene:
+    """Faceted gem cluster: `n_gems` randomly rotated and scaled convex polyhedra of
+    60-200 triangular facets (hulls of 32-102 points on random ellipsoids), IOR
+    U(1.5, 2.4), roughness U(0, 0.05), per-channel IOR spread `dispersion` (material 'R'),
+    on a 12x12 diffuse plane, lit by 8 area lights of random size and colour; the gems
+    are grouped into `groups` meshes by square tiles of the cluster (one mesh by
+    default: with several world leaves the reference's world-leaf overwrite makes the
+    last leaf's hit win, so grouping changes the image as well as the traversal cost)."""
+    rng = np.random.default_rng(seed)
+    mats = [Material("P", color=(0.8, 0.8, 0.8), roughness=1.0, specular=0.0)]
+    meshes = []
+    Vp, Np, Fp = plane(12.0, 0.0)
+    meshes.append(_mesh(Vp, Np, Fp, 0))
+    # positions first, then spatially coherent groups (tiles of a square grid, so the
+    # group meshes' boxes do not all overlap)
+    rad = 3.2 * np.sqrt(rng.uniform(size=n_gems))
+    ang = rng.uniform(0, 2 * np.pi, n_gems)
+    xy = np.stack([rad * np.cos(ang), rad * np.sin(ang)], 1)
+    side = max(1, int(round(np.sqrt(groups))))
+    cell = np.clip(((xy + 3.2) / 6.4 * side).astype(int), 0, side - 1)
+    gid = cell[:, 0] * side + cell[:, 1]
+    for g in range(side * side):
+        members = np.nonzero(gid == g)[0]
+        if len(members) == 0:
+            continue
+        Vs, Ns, Fs, Ms = [], [], [], []
+        base = 0
+        slots = []
+        for k in members:
+            V, N, F = _convex_gem(rng, int(rng.integers(32, 103)))
+            R = _rotation(rng)
+            scale = rng.uniform(0.06, 0.22)
+            pos = np.array([xy[k, 0], xy[k, 1], 0.0])
+            V = (V @ R.T) * scale
+            pos[2] = -V[:, 2].min() + 0.002
+            Vs.append((V + pos).astype(np.float32))
+            Ns.append(N @ R.T)
+            Fs.append(F + base)
+            base += len(V)
+            mats.append(Material("R", color=(1, 1, 1), ior=float(rng.uniform(1.5, 2.4)),
+                                 roughness=float(rng.uniform(0.0, 0.05)), specular=dispersion))
+            slots.append(len(mats) - 1)
+            Ms.append(np.full(len(F), len(slots) - 1, np.int16))
+        V = np.concatenate(Vs)
+        N = _normals_i16(np.concatenate(Ns))
+        F = np.concatenate(Fs).astype(np.uint32)
+        meshes.append(Mesh(V, N, F, np.concatenate(Ms), slots, np.eye(4, dtype=np.float32)))
+    lights = []
+    for i in range(8):
+        a = 2 * np.pi * i / 8 + rng.uniform(-0.2, 0.2)
+        rr = rng.uniform(1.5, 4.0)
+        hue = rng.uniform(0, 1)
+        col = tuple(float(0.6 + 0.4 * np.cos(2 * np.pi * (hue + o))) for o in (0.0, 1 / 3, 2 / 3))
+        w = rng.uniform(0.3, 1.5)
+        lights.append(Light("A", color=col, position=(rr * np.cos(a), rr * np.sin(a), rng.uniform(4.5, 6.5)),
+                            width=w, height=w * rng.uniform(0.5, 1.5), power=float(rng.uniform(6.0, 14.0))))
+    cam = look_at_camera(width, height, (0.0, -8.5, 6.0), (0.0, 0.0, 0.0), (0, 0, 1), 42.0)
+    return Scene(meshes, mats, lights, cam, samples=samples, base_radius=0.0012, radius_reduction=0.75,
+                 name="gem_cluster")
 
 
 WORKLOADS = {
