@@ -286,6 +286,32 @@ def gem_cluster(width=3840, height=2160, n_gems=2000, groups=1, seed=0, dispersi
                  name="gem_cluster")
 
 
+def batch_scene(seed: int, width=512, height=512):
+    """One scene of the 64-scene batch: a refracting height field of log-uniform
+    [1k, 2M] triangles, IOR U(1.3, 1.8), roughness U(0, 0.1), over a diffuse floor, lit
+    by 1-4 area lights; photons per iteration log-uniform [256k, 8M].
+    Returns (scene, photons_per_iter)."""
+    rng = np.random.default_rng(1000 + seed)
+    tris = float(np.exp(rng.uniform(np.log(1e3), np.log(2e6))))
+    grid = max(4, int(round(np.sqrt(tris / 2.0))) + 1)
+    photons = int(np.exp(rng.uniform(np.log(256 * 1024), np.log(8 * 1024 * 1024))))
+    mats = [Material("R", color=(1, 1, 1), ior=float(rng.uniform(1.3, 1.8)), roughness=float(rng.uniform(0.0, 0.1))),
+            Material("P", color=(0.8, 0.8, 0.8), roughness=1.0, specular=0.0)]
+    Vw, Nw, Fw = water_heightfield(grid, size=6.0, waves=16, seed=seed)
+    Vf, Nf, Ff = plane(6.0, -1.0)
+    meshes = [_mesh(Vw, Nw, Fw, 0), _mesh(Vf, Nf, Ff, 1)]
+    lights = []
+    for i in range(int(rng.integers(1, 5))):
+        w = float(rng.uniform(0.5, 2.0))
+        lights.append(Light("A", color=tuple(float(c) for c in rng.uniform(0.6, 1.0, 3)),
+                            position=(float(rng.uniform(-1.5, 1.5)), float(rng.uniform(-1.5, 1.5)),
+                                      float(rng.uniform(3.0, 5.0))),
+                            width=w, height=w, power=float(rng.uniform(10.0, 30.0))))
+    cam = look_at_camera(width, height, (0.0, -4.5, 3.5), (0.0, 0.0, -1.0), (0, 0, 1), 50.0)
+    sc = Scene(meshes, mats, lights, cam, samples=4, base_radius=0.002, radius_reduction=0.75, name=f"batch{seed}")
+    return sc, photons
+
+
 WORKLOADS = {
     "glass_sphere_point": dict(scene=glass_sphere_point, photons_per_iter=1 << 20, iterations=16, max_path_length=8),
     "water_pool": dict(scene=water_pool, photons_per_iter=16 << 20, iterations=64, max_path_length=8),
