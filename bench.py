@@ -222,7 +222,7 @@ def run_ours(args):
     e2e_s = time.perf_counter() - t0
     lib.rc_release()
     h2d = sum(m.verts.nbytes + m.normals.nbytes + m.tris.nbytes for m in sc.meshes)
-    d2h = args.width * args.height * 3 * 8
+    d2h = img.nbytes            # the FP32 mean image read back each step
     e2e_rank = paths * args.steps / e2e_s
 
     vals = [value_rank]

@@ -77,6 +77,7 @@ struct DeviceState {
     DevBuf<uint2> qstart;
     DevBuf<unsigned char> qscratch;
     DevBuf<double> accum;
+    DevBuf<float> image;          // FP32 mean for readback
     // learned emission proposal
     std::unique_ptr<MlpStore> mlp;
     DevBuf<float4> prop, train_pos, train_dir;
@@ -112,6 +113,7 @@ struct DeviceState {
         tp0.release(); tp1.release(); tp2.release(); qorder.release(); qstart.release(); qscratch.release();
         box_lo.release(); box_hi.release();
         accum.release();
+        image.release();
         mlp.reset();
         prop.release(); train_pos.release(); train_dir.release(); contrib.release(); train_wsum.release();
         train_count.release();
@@ -836,12 +838,19 @@ int read_image(float* rgb, int w, int h) {
     if (!g_scene) { g_err = "no scene"; return RC_E_NO_SCENE; }
     if (!rgb || w != g_scene->camera.width || h != g_scene->camera.height) { g_err = "bad image buffer"; return RC_E_INVALID; }
     size_t n = 3 * (size_t)w * h;
-    std::vector<double> acc(n, 0.0);
-    if (g_dev.accum.p && g_dev.accum.n >= n)
-        RC_CUDA(cudaMemcpy(acc.data(), g_dev.accum.p, n * sizeof(double), cudaMemcpyDeviceToHost));
-    int it = g_dev.iterations_done;
-    double sc = it > 0 ? 1.0 / it : 0.0;
-    for (size_t i = 0; i < n; ++i) rgb[i] = (float)(acc[i] * sc);
+    DeviceState& d = g_dev;
+    if (!d.accum.p || d.accum.n < n || !d.stream) {
+        std::memset(rgb, 0, n * sizeof(float));
+        return RC_OK;
+    }
+    // mean on the device, then one FP32 copy (half the bytes of the FP64 sum)
+    const int it = d.iterations_done;
+    const double sc = it > 0 ? 1.0 / it : 0.0;
+    RC_CUDA(d.image.reserve(n));
+    launch_image_mean(d.accum.p, d.image.p, (long long)n, sc, d.stream);
+    RC_CUDA(cudaGetLastError());
+    RC_CUDA(cudaMemcpyAsync(rgb, d.image.p, n * sizeof(float), cudaMemcpyDeviceToHost, d.stream));
+    RC_CUDA(cudaStreamSynchronize(d.stream));
     return RC_OK;
 }
 

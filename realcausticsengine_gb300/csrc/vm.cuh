@@ -90,6 +90,8 @@ void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next
 // Debug view `mode` (2 normals, 3 facing, 4 materials with IOR `ior`) added into the
 // FP64 image accumulation.
 void launch_debug_view(const VMParams& p, int mode, float ior, double* accum, cudaStream_t s);
+// FP32 mean image (n floats) from the FP64 running sum.
+void launch_image_mean(const double* acc, float* out, long long n, double scale, cudaStream_t s);
 void launch_trace_rays(const SceneView& s, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st);
 void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaStream_t s);

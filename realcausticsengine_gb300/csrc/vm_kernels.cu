@@ -418,6 +418,18 @@ void launch_debug_view(const VMParams& p, int mode, float ior, double* accum, cu
     k_debug_view<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, mode, ior, accum);
 }
 
+// Running FP64 sum -> FP32 mean image (Vertex_Merging::run's final scale,
+// src/Vertex_Merging.cpp:367-379, done at readback).
+__global__ void k_image_mean(const double* __restrict__ acc, float* __restrict__ out, long long n, double scale) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)(acc[i] * scale);
+}
+
+void launch_image_mean(const double* acc, float* out, long long n, double scale, cudaStream_t s) {
+    if (n <= 0) return;
+    k_image_mean<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(acc, out, n, scale);
+}
+
 void launch_trace_rays(const SceneView& sv, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st) {
     if (n <= 0) return;
