@@ -47,7 +47,7 @@ METRIC = "photons/s"
 # bytes per unit of the gather (algorithmic): photon record read once, query record
 # read once, FP64 RGB pixel read+write once per query
 PHOTON_BYTES, QUERY_BYTES, PIXEL_BYTES = 40, 80, 48
-GATHER_TRAFFIC_OVER_ALGORITHMIC = 1.225
+GATHER_TRAFFIC_OVER_ALGORITHMIC = 1.253
 
 
 def dist_env():
@@ -245,7 +245,7 @@ def run_ours(args):
     achieved = gather_bytes / (gather_ms_mean / 1000.0) / 1e9 if gather_ms_mean > 0 else 0.0
     # DRAM bytes per gather launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of one
     # launch on the 960x540 / 4M-path case (profiles/k_gather_water_pool_960x540.md) is
-    # 1.225x that launch's algorithmic bytes; scaled to this workload's launch by its
+    # 1.253x that launch's algorithmic bytes; scaled to this workload's launch by its
     # algorithmic bytes (photon and query records both scale with their counts)
     traffic = GATHER_TRAFFIC_OVER_ALGORITHMIC * gather_bytes
     line = {
