@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <utility>
 
 namespace rc {
@@ -95,32 +96,69 @@ struct TmpNode {
     Box box;
     bool leaf = false;
     int left = -1, right = -1;     // indices into the temporary node pool
-    std::vector<uint32_t> items;   // leaf contents in order
+    uint32_t first = 0, count = 0; // leaf contents: prims [first, first + count) in order
 };
 
 // The recursive binned SAH build shared by both levels.  `world` selects the world
 // variant (per-mesh traversal-cost weights, leaf cost summed over the first 11
 // buckets, src/BVH/BVH_world.cpp:25-159) instead of the mesh variant
 // (src/BVH/BVH_mesh.cpp:28-155).
+// Subtrees of at least kParallelPrims primitives, down to kParallelDepth levels of
+// splitting, are built concurrently (up to 2^kParallelDepth threads).
+constexpr size_t kParallelPrims = 16384;
+constexpr int kParallelDepth = 4;
+thread_local int g_par_depth = 0;
+
+// Order-independent reduction (box unions, counts) over [start, end) on several
+// threads for large ranges: `acc(R&, i)` folds item i, `merge(R&, const R&)` joins.
+constexpr size_t kParallelLoop = 131072;
+template <class R, class Acc, class Merge>
+R par_reduce(size_t start, size_t end, const R& init, Acc&& acc, Merge&& merge) {
+    const size_t n = end - start;
+    static const unsigned hw = std::thread::hardware_concurrency();   // queried once
+    const unsigned nt = hw < 1 ? 1 : (hw > 16 ? 16 : hw);
+    if (n < kParallelLoop || nt == 1) {
+        R r = init;
+        for (size_t i = start; i < end; ++i) acc(r, i);
+        return r;
+    }
+    std::vector<R> part(nt, init);
+    std::vector<std::thread> ts;
+    for (unsigned t = 0; t < nt; ++t)
+        ts.emplace_back([&, t]() {
+            const size_t a = start + n * t / nt, b = start + n * (t + 1) / nt;
+            R local = init;   // thread-local accumulator (no shared cache lines while folding)
+            for (size_t i = a; i < b; ++i) acc(local, i);
+            part[t] = local;
+        });
+    for (auto& t : ts) t.join();
+    R r = init;
+    for (const R& q : part) merge(r, q);
+    return r;
+}
+
 int sah_recurse(std::vector<Prim>& p, size_t start, size_t end, bool world, std::vector<TmpNode>& pool) {
-    Box bbox;
-    for (size_t i = start; i < end; ++i) bbox = box_union(bbox, p[i].box);
+    const Box bbox = par_reduce(start, end, Box{}, [&](Box& b, size_t i) { b = box_union(b, p[i].box); },
+                                [](Box& a, const Box& b) { a = box_union(a, b); });
     size_t n = end - start;
     int me = (int)pool.size();
     pool.emplace_back();
     pool[me].box = bbox;
     if (n == 1) {
         pool[me].leaf = true;
-        pool[me].items.push_back(p[start].index);
+        pool[me].first = (uint32_t)start;
+        pool[me].count = 1;
         return me;
     }
-    Box cb;
-    for (size_t i = start; i < end; ++i) cb = box_union(cb, p[i].center);
+    const Box cb = par_reduce(start, end, Box{}, [&](Box& b, size_t i) { b = box_union(b, p[i].center); },
+                              [](Box& a, const Box& b) { a = box_union(a, b); });
     int dim = max_extent(cb);
     size_t mid = (start + end) / 2;
     auto make_leaf = [&]() {
+        // the range is final: later splits only permute other (disjoint) ranges
         pool[me].leaf = true;
-        for (size_t i = start; i < end; ++i) pool[me].items.push_back(p[i].index);
+        pool[me].first = (uint32_t)start;
+        pool[me].count = (uint32_t)n;
         return me;
     };
     if (comp(cb.mx, dim) == comp(cb.mn, dim)) return make_leaf();
@@ -131,11 +169,25 @@ int sah_recurse(std::vector<Prim>& p, size_t start, size_t end, bool world, std:
         int count[nb] = {0};
         Box bb[nb];
         float travers[nb] = {0};
-        for (size_t i = start; i < end; ++i) {
-            int b = bucket_of(cb, p[i].center, dim);
-            count[b]++;
-            bb[b] = box_union(bb[b], p[i].box);
-            if (world) travers[b] += p[i].cost;
+        if (world || n < kParallelLoop) {
+            for (size_t i = start; i < end; ++i) {
+                int b = bucket_of(cb, p[i].center, dim);
+                count[b]++;
+                bb[b] = box_union(bb[b], p[i].box);
+                if (world) travers[b] += p[i].cost;   // float sums: kept sequential
+            }
+        } else {
+            struct Bins { int count[nb]; Box bb[nb]; };
+            Bins z{};
+            for (int k = 0; k < nb; ++k) z.bb[k] = Box{};
+            const Bins r = par_reduce(start, end, z, [&](Bins& bs, size_t i) {
+                const int b = bucket_of(cb, p[i].center, dim);
+                bs.count[b]++;
+                bs.bb[b] = box_union(bs.bb[b], p[i].box);
+            }, [](Bins& a, const Bins& b) {
+                for (int k = 0; k < nb; ++k) { a.count[k] += b.count[k]; a.bb[k] = box_union(a.bb[k], b.bb[k]); }
+            });
+            for (int k = 0; k < nb; ++k) { count[k] = r.count[k]; bb[k] = r.bb[k]; }
         }
         float cost[nb - 1];
         float sa = surface_area(bbox);
@@ -175,8 +227,34 @@ int sah_recurse(std::vector<Prim>& p, size_t start, size_t end, bool world, std:
             return make_leaf();
         }
     }
-    int l = sah_recurse(p, start, mid, world, pool);
-    int r = sah_recurse(p, mid, end, world, pool);
+    int l, r;
+    if (n >= kParallelPrims && g_par_depth < kParallelDepth) {
+        // the two halves touch disjoint ranges of `p`: build the left one on another
+        // thread into its own pool, then splice it in (child links re-based); node
+        // numbering in the pool does not reach the output, which flatten() orders by
+        // the tree's own pre-order
+        std::vector<TmpNode> lpool;
+        lpool.reserve((mid - start) * 2);
+        int lroot = -1;
+        const int depth = g_par_depth + 1;
+        std::thread t([&]() {
+            g_par_depth = depth;
+            lroot = sah_recurse(p, start, mid, world, lpool);
+        });
+        g_par_depth = depth;
+        r = sah_recurse(p, mid, end, world, pool);
+        g_par_depth = depth - 1;
+        t.join();
+        const int base = (int)pool.size();
+        for (TmpNode& tn : lpool) {
+            if (!tn.leaf) { tn.left += base; tn.right += base; }
+            pool.push_back(std::move(tn));
+        }
+        l = lroot + base;
+    } else {
+        l = sah_recurse(p, start, mid, world, pool);
+        r = sah_recurse(p, mid, end, world, pool);
+    }
     pool[me].left = l;
     pool[me].right = r;
     return me;
@@ -184,22 +262,22 @@ int sah_recurse(std::vector<Prim>& p, size_t start, size_t end, bool world, std:
 
 // Depth-first flattening (populate_cache_friendly_bvh, src/BVH/BVH_mesh.cpp:199-261):
 // pre-order node numbering, left child = parent + 1, 1-based item list.
-void flatten(const std::vector<TmpNode>& pool, int t, uint32_t& idx_nodes, uint32_t& idx_items,
-             std::vector<BvhNode>& nodes, std::vector<int>& items) {
+void flatten(const std::vector<TmpNode>& pool, const std::vector<Prim>& prims, int t, uint32_t& idx_nodes,
+             uint32_t& idx_items, std::vector<BvhNode>& nodes, std::vector<int>& items) {
     const TmpNode& n = pool[t];
     uint32_t cur = idx_nodes;
     nodes[cur].box = n.box;
     if (!n.leaf) {
         uint32_t l = ++idx_nodes;
-        flatten(pool, n.left, idx_nodes, idx_items, nodes, items);
+        flatten(pool, prims, n.left, idx_nodes, idx_items, nodes, items);
         uint32_t r = ++idx_nodes;
-        flatten(pool, n.right, idx_nodes, idx_items, nodes, items);
+        flatten(pool, prims, n.right, idx_nodes, idx_items, nodes, items);
         nodes[cur].w0 = l;
         nodes[cur].w1 = r;
     } else {
-        nodes[cur].w0 = 0x80000000u | (uint32_t)n.items.size();
+        nodes[cur].w0 = 0x80000000u | n.count;
         nodes[cur].w1 = idx_items;
-        for (uint32_t it : n.items) items[++idx_items] = (int)it;
+        for (uint32_t k = 0; k < n.count; ++k) items[++idx_items] = (int)prims[n.first + k].index;
     }
 }
 
@@ -209,11 +287,11 @@ void build_flat(std::vector<Prim>& prims, bool world, std::vector<BvhNode>& node
     int root = sah_recurse(prims, 0, prims.size(), world, pool);
     root_box = pool[root].box;
     size_t nitems = 0;
-    for (const TmpNode& t : pool) nitems += t.items.size();
+    for (const TmpNode& t : pool) nitems += t.count;
     nodes.assign(pool.size(), BvhNode{});
     items.assign(nitems + 1, 0);
     uint32_t in = 0, ii = 0;
-    flatten(pool, root, in, ii, nodes, items);
+    flatten(pool, prims, root, in, ii, nodes, items);
 }
 
 // Inverse (src/matrix.cpp:4-63): cofactor expansion in double, rounded to float.

@@ -86,13 +86,15 @@ class Renderer:
         check(self.L.rc_light_photons(int(iteration), out.ctypes.data, n.value, C.byref(n)), "rc_light_photons")
         return out[: n.value]
 
-    def host_mesh_bvh(self, mesh: int, cap: int = 1 << 22):
+    def host_mesh_bvh(self, mesh: int, cap: int = 1 << 22, with_index: bool = False):
         nodes = np.zeros((cap, 8), np.uint32)
         idx = np.zeros(cap + 1, np.int32)
         cost = C.c_float()
         n = self.L.rc_host_mesh_bvh(mesh, nodes.ctypes.data, cap, idx.ctypes.data, cap + 1, C.byref(cost))
         if n < 0:
             check(n, "rc_host_mesh_bvh")
+        if with_index:
+            return nodes[:n], cost.value, idx
         return nodes[:n], cost.value
 
     def release(self):

@@ -59,8 +59,12 @@ def test_host_scene_matches_golden(golden):
 
 
 @pytest.mark.parametrize("maker", [lambda: scenes.test_scene(40, 30, subdiv=3), scenes.sun_scene,
-                                   lambda: scenes.glass_sphere_point(32, 32, subdiv=5)])
+                                   lambda: scenes.glass_sphere_point(32, 32, subdiv=5),
+                                   # 178,802 triangles: the multi-threaded build paths
+                                   lambda: scenes.water_pool(64, 48, grid=300)])
 def test_host_bvh_matches_reference(ref, in_tmpdir, maker):
+    """Host SAH BVH (multi-threaded above 16k primitives) node arrays, triangle lists and
+    traversal costs bit-identical to the reference's sequential build."""
     sc = maker()
     args = InitArgs(sc)
     args.call(ref.init)
@@ -70,13 +74,15 @@ def test_host_bvh_matches_reference(ref, in_tmpdir, maker):
     info = r.prepare_host()
     assert (np.array(info_r, np.float32).view(np.uint32) == info.view(np.uint32)).all()
     for m in range(len(sc.meshes)):
-        cap = 1 << 16
+        cap = 1 << 19
         nr = np.zeros((cap, 8), np.uint32)
         tr = np.zeros(cap, np.int32)
         cr = C.c_float()
         n = ref.ref_mesh_bvh(m, nr.ctypes.data, cap, tr.ctypes.data, cap, C.byref(cr))
-        nodes, cost = r.host_mesh_bvh(m, cap)
+        nodes, cost, idx = r.host_mesh_bvh(m, cap, with_index=True)
         assert (nodes == nr[:n]).all() and np.float32(cost) == np.float32(cr.value)
+        nt = len(sc.meshes[m].tris)
+        assert (idx[:nt + 1] == tr[:nt + 1]).all()
     ref.ref_release()
     r.release()
 
