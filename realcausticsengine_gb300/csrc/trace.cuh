@@ -40,21 +40,16 @@ struct SceneView {
 
 constexpr int kStackSize = 64;   // BVH_STACK_SIZE in the reference
 
-// Traversal stacks.  LocalStack: a per-thread array (local memory).  SharedStack: the
-// thread's column of a [kStackSize][block size] shared-memory array (entry k of thread
-// t at k * stride + t: the lanes of a warp touch consecutive banks).
+// Traversal stacks.  LocalStack: a per-thread array (local memory), declared by each
+// mesh traversal when the caller passes the CallStack tag, so that its lifetime is the
+// traversal.  (Stacks held for a whole persistent kernel, or kept in shared memory as
+// [kStackSize][block] columns, measured 1.5-3.6x slower on the water workload.)  Any
+// type with int& operator[] can serve as the stack of mesh_traverse.
 struct LocalStack {
     int s[kStackSize];
     __device__ __forceinline__ int& operator[](int i) { return s[i]; }
 };
-// Tag: each mesh traversal declares its own LocalStack (the array's lifetime is the
-// traversal, which lets the compiler keep it tight).
 struct CallStack {};
-struct SharedStack {
-    int* base;     // &array[0][threadIdx.x]
-    int stride;    // threads per block
-    __device__ __forceinline__ int& operator[](int i) { return base[i * stride]; }
-};
 
 struct HitRec {
     float t, u, v;

@@ -107,26 +107,12 @@ __device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& 
     return true;
 }
 
-// Traversal-stack placement for the persistent passes: in shared memory (a
-// [kStackSize][block] int array, dynamic) or per-thread local memory.
-template <bool kSharedStack>
-struct PassStack;
-template <>
-struct PassStack<true> {
-    SharedStack st;
-    __device__ __forceinline__ PassStack(int* smem) : st{smem + threadIdx.x, (int)blockDim.x} {}
-};
-template <>
-struct PassStack<false> {
-    CallStack st;
-    __device__ __forceinline__ PassStack(int*) {}
-};
-
-template <int kBlock, bool kSharedStack>
-__global__ void __launch_bounds__(kBlock) k_light_pass_persistent(const VMParams P, PhotonBuf ph,
-                                                                   unsigned long long* __restrict__ next_path) {
-    extern __shared__ int pass_smem[];
-    PassStack<kSharedStack> stk(pass_smem);
+// kMinBlocks caps the registers per thread (resident blocks per SM the allocation must
+// allow); traversal stacks are per-traversal local-memory arrays.
+template <int kBlock, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_light_pass_persistent(const VMParams P, PhotonBuf ph,
+                                                                               unsigned long long* __restrict__ next_path) {
+    CallStack stk;
     const int lane = threadIdx.x & 31;
     LightPath s;
     bool alive = false;
@@ -145,7 +131,7 @@ __global__ void __launch_bounds__(kBlock) k_light_pass_persistent(const VMParams
             if (base + __popc(need) >= (unsigned long long)P.num_light_paths) pool_left = false;
         }
         if (!__any_sync(0xffffffffu, alive)) break;
-        if (alive) alive = light_path_bounce(P, ph, s, stk.st);
+        if (alive) alive = light_path_bounce(P, ph, s, stk);
     }
 }
 
@@ -229,11 +215,10 @@ __device__ __forceinline__ bool camera_path_bounce(const VMParams& P, QueryBuf& 
     return true;
 }
 
-template <int kBlock, bool kSharedStack>
-__global__ void __launch_bounds__(kBlock) k_camera_pass_persistent(const VMParams P, QueryBuf qb,
-                                                                    unsigned long long* __restrict__ next_pixel) {
-    extern __shared__ int pass_smem[];
-    PassStack<kSharedStack> stk(pass_smem);
+template <int kBlock, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_camera_pass_persistent(const VMParams P, QueryBuf qb,
+                                                                                unsigned long long* __restrict__ next_pixel) {
+    CallStack stk;
     const int lane = threadIdx.x & 31;
     const long long npix = (long long)P.camera.width * P.camera.height;
     CameraPath s;
@@ -253,7 +238,7 @@ __global__ void __launch_bounds__(kBlock) k_camera_pass_persistent(const VMParam
             need = __ballot_sync(0xffffffffu, !alive);   // samples outside the buffer: draw again
         }
         if (!__any_sync(0xffffffffu, alive)) break;
-        if (alive) alive = camera_path_bounce(P, qb, s, stk.st);
+        if (alive) alive = camera_path_bounce(P, qb, s, stk);
     }
 }
 
@@ -311,41 +296,42 @@ unsigned persistent_grid(K kernel, int block, size_t smem, long long work_items)
     return (unsigned)(need < blocks ? need : blocks);
 }
 
-template <int B, bool SH>
+template <int B, int MB>
 void launch_light_t(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s) {
-    const size_t smem = SH ? (size_t)kStackSize * B * sizeof(int) : 0;
     static unsigned grid_cache = 0;
     static long long grid_for = -1;
     if (grid_for != p.num_light_paths) {
-        grid_cache = persistent_grid(k_light_pass_persistent<B, SH>, B, smem, p.num_light_paths);
+        grid_cache = persistent_grid(k_light_pass_persistent<B, MB>, B, 0, p.num_light_paths);
         grid_for = p.num_light_paths;
     }
     cudaMemsetAsync(next_path, 0, sizeof(unsigned long long), s);
-    k_light_pass_persistent<B, SH><<<grid_cache, B, smem, s>>>(p, ph, next_path);
+    k_light_pass_persistent<B, MB><<<grid_cache, B, 0, s>>>(p, ph, next_path);
 }
 
-template <int B, bool SH>
+template <int B, int MB>
 void launch_camera_t(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s) {
     const long long n = (long long)p.camera.width * p.camera.height;
-    const size_t smem = SH ? (size_t)kStackSize * B * sizeof(int) : 0;
     static unsigned grid_cache = 0;
     static long long grid_for = -1;
     if (grid_for != n) {
-        grid_cache = persistent_grid(k_camera_pass_persistent<B, SH>, B, smem, n);
+        grid_cache = persistent_grid(k_camera_pass_persistent<B, MB>, B, 0, n);
         grid_for = n;
     }
     cudaMemsetAsync(next_pixel, 0, sizeof(unsigned long long), s);
-    k_camera_pass_persistent<B, SH><<<grid_cache, B, smem, s>>>(p, qb, next_pixel);
+    k_camera_pass_persistent<B, MB><<<grid_cache, B, 0, s>>>(p, qb, next_pixel);
 }
 
 }  // namespace
 
-int pass_variants() { return 4; }
+int pass_variants() { return 5; }
 
 const char* pass_variant_name(int v) {
-    static const char* names[4] = {"256 threads, local-memory stack", "256 threads, shared-memory stack",
-                                   "128 threads, local-memory stack", "128 threads, shared-memory stack"};
-    return (v >= 0 && v < 4) ? names[v] : "?";
+    static const char* names[5] = {"256 threads, >= 3 blocks/SM (<= 85 registers)",
+                                   "128 threads, >= 7 blocks/SM (<= 73 registers)",
+                                   "128 threads, >= 8 blocks/SM (<= 64 registers)",
+                                   "128 threads, >= 5 blocks/SM (<= 102 registers)",
+                                   "128 threads, >= 10 blocks/SM (<= 51 registers)"};
+    return (v >= 0 && v < 5) ? names[v] : "?";
 }
 
 void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant) {
@@ -353,10 +339,11 @@ void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next
     if (n <= 0) return;
     if (!next_path) return;
     switch (variant) {
-    case 1: launch_light_t<256, true>(p, ph, next_path, s); break;
-    case 2: launch_light_t<128, false>(p, ph, next_path, s); break;
-    case 3: launch_light_t<128, true>(p, ph, next_path, s); break;
-    default: launch_light_t<256, false>(p, ph, next_path, s); break;
+    case 1: launch_light_t<128, 7>(p, ph, next_path, s); break;
+    case 2: launch_light_t<128, 8>(p, ph, next_path, s); break;
+    case 3: launch_light_t<128, 5>(p, ph, next_path, s); break;
+    case 4: launch_light_t<128, 10>(p, ph, next_path, s); break;
+    default: launch_light_t<256, 3>(p, ph, next_path, s); break;
     }
 }
 
@@ -365,10 +352,11 @@ void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next
     if (n <= 0) return;
     if (!next_pixel) return;
     switch (variant) {
-    case 1: launch_camera_t<256, true>(p, qb, next_pixel, s); break;
-    case 2: launch_camera_t<128, false>(p, qb, next_pixel, s); break;
-    case 3: launch_camera_t<128, true>(p, qb, next_pixel, s); break;
-    default: launch_camera_t<256, false>(p, qb, next_pixel, s); break;
+    case 1: launch_camera_t<128, 7>(p, qb, next_pixel, s); break;
+    case 2: launch_camera_t<128, 8>(p, qb, next_pixel, s); break;
+    case 3: launch_camera_t<128, 5>(p, qb, next_pixel, s); break;
+    case 4: launch_camera_t<128, 10>(p, qb, next_pixel, s); break;
+    default: launch_camera_t<256, 3>(p, qb, next_pixel, s); break;
     }
 }
 
