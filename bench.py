@@ -189,7 +189,8 @@ def run_ours(args):
     paths = args.photons
 
     # ---- device-resident throughput
-    r = Renderer(sc, max_path_length=MAX_PATH, photons_per_iter=paths, seed=rank)
+    r = Renderer(sc, max_path_length=MAX_PATH, photons_per_iter=paths, seed=rank,
+                 graph_replay=not args.no_graph_replay)
     r.prepare()
     r.render(args.warmup)
     dev = np.zeros(4, np.float64)
@@ -210,6 +211,7 @@ def run_ours(args):
     cfg.photons_per_iter = paths
     cfg.seed = rank
     cfg.write_exr = 0
+    cfg.graph_replay = 0 if args.no_graph_replay else 1
     lib.rc_set_config(C.byref(cfg))
     img = np.zeros((args.height, args.width, 3), np.float32)
     t0 = time.perf_counter()
@@ -347,6 +349,7 @@ def run_batch(args):
         cfg = abi.RcConfig()
         lib.rc_default_config(C.byref(cfg))
         cfg.max_path_length, cfg.photons_per_iter, cfg.seed, cfg.write_exr = MAX_PATH, paths, seed, 0
+        cfg.graph_replay = 0 if args.no_graph_replay else 1
         lib.rc_set_config(C.byref(cfg))
         ia = InitArgs(sc)
         ia.call(lib.init)
@@ -385,6 +388,8 @@ def main():
     ap.add_argument("--cpu-cores", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-graph-replay", action="store_true",
+                    help="every iteration reads its counts back (no asynchronous CUDA-graph replay)")
     ap.add_argument("--workload", default="water_pool", choices=["water_pool", "batch"])
     ap.add_argument("--batch", type=int, default=64)
     args = ap.parse_args()

@@ -118,10 +118,20 @@ typedef struct rc_config {
      * Two renders with the same camera_seed and different seeds share their merge
      * queries and differ only in their photons. */
     unsigned long long camera_seed;
-    /* 1 (default): the first iteration of each query-count class times the gather's
-     * launch shapes (resident blocks per SM x queries per warp) on a scratch image and
-     * keeps the fastest; 0: the fixed default shape. */
+    /* 1 (default): the first iteration of each size class times the launch shapes of
+     * the light pass, the camera pass (block size x register cap) and the gather
+     * (resident blocks per SM x queries per warp) and keeps the fastest for the process;
+     * 0: the fixed default shapes. */
     int autotune;
+    /* 1 (default): with the uniform sampler and no learned proposal, when an iteration
+     * takes under 20 ms of device time, the iterations after the first of a
+     * configuration are enqueued without host round trips (fixed photon and query
+     * capacities from the previous counts, KD tree over the padded photon capacity) and
+     * replayed as an updated CUDA graph; an iteration whose counts outgrow the
+     * capacities is rendered again at the end of the call.  0: every iteration reads its
+     * counts back.  2: as 1 with capacities equal to the measured counts and no time
+     * limit (tests: exercises the re-render of overflowed iterations). */
+    int graph_replay;
 } rc_config;
 
 int rc_default_config(rc_config* cfg);

@@ -260,8 +260,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const
                                                                          const uint32_t* __restrict__ order,
                                                                          const uint2* __restrict__ start_nodes,
                                                                          long long nq, double* __restrict__ accum,
-                                                                         unsigned long long* __restrict__ counters) {
+                                                                         unsigned long long* __restrict__ counters,
+                                                                         const unsigned long long* __restrict__ nq_dev,
+                                                                         const int* __restrict__ skip) {
     constexpr int kQueriesPerWarp = QPW;
+    // device-side count (bounded by the capacity nq) and an iteration-wide skip flag,
+    // for iterations enqueued without a host round trip
+    if (skip && *skip) return;
+    if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
     __shared__ uint32_t pend[kWarpsPerBlock][64];
     __shared__ uint2 stk[kWarpsPerBlock][kRootStack];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -367,10 +373,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_kd_query(const KdNav t,
 // branches: the shallowest node on the near path with (q[axis] - split)^2 < r^2.  Above
 // it the traversal only follows near sides and tests no median photon, so starting
 // there visits exactly the same photons.  start_nodes[i] = (node, first position).
-__global__ void k_query_cells(const KdNav t, const float* __restrict__ qpos, int stride, long long nq, int level,
+__global__ void k_query_cells(const KdNav t, const float* __restrict__ qpos, int stride, long long nq,
+                              const unsigned long long* __restrict__ nq_dev, int level,
                               float r2, uint32_t* __restrict__ keys, uint32_t* __restrict__ counts,
                               uint2* __restrict__ start_nodes) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
     if (i >= nq) return;
     F3 q = f3(qpos[stride * i], qpos[stride * i + 1], qpos[stride * i + 2]);
     uint32_t e = 1;
@@ -456,9 +464,11 @@ __global__ void __launch_bounds__(1024) k_scan_counts(uint32_t* counts, long lon
     }
 }
 
-__global__ void k_scatter_queries(const uint32_t* __restrict__ keys, long long nq, uint32_t* __restrict__ cursor,
+__global__ void k_scatter_queries(const uint32_t* __restrict__ keys, long long nq,
+                                  const unsigned long long* __restrict__ nq_dev, uint32_t* __restrict__ cursor,
                                   uint32_t* __restrict__ order) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
     if (i >= nq) return;
     uint32_t pos = atomicAdd(&cursor[keys[i]], 1u);
     order[pos] = (uint32_t)i;
@@ -562,7 +572,8 @@ size_t query_order_scratch_bytes(long long nq, const KdTree& tree) {
 }
 
 void launch_query_order(const KdTree& tree, const float* qpos, int stride, long long nq, float r2, void* scratch,
-                        uint32_t* order, uint2* start_nodes, int* launches, cudaStream_t s) {
+                        uint32_t* order, uint2* start_nodes, int* launches, cudaStream_t s,
+                        const unsigned long long* nq_dev) {
     if (nq <= 0) return;
     int lq = query_order_level(nq, tree);
     uint32_t* keys = (uint32_t*)scratch;
@@ -570,9 +581,9 @@ void launch_query_order(const KdTree& tree, const float* qpos, int stride, long 
     long long m = 1LL << lq;
     cudaMemsetAsync(counts, 0, 4 * (size_t)m, s);
     unsigned g = (unsigned)((nq + 255) / 256);
-    k_query_cells<<<g, 256, 0, s>>>(nav_of(tree), qpos, stride, nq, lq, r2, keys, counts, start_nodes);
+    k_query_cells<<<g, 256, 0, s>>>(nav_of(tree), qpos, stride, nq, nq_dev, lq, r2, keys, counts, start_nodes);
     k_scan_counts<<<1, 1024, 0, s>>>(counts, m);
-    k_scatter_queries<<<g, 256, 0, s>>>(keys, nq, counts, order);
+    k_scatter_queries<<<g, 256, 0, s>>>(keys, nq, nq_dev, counts, order);
     if (launches) *launches += 3;
 }
 
@@ -584,10 +595,10 @@ void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaS
 template <int MB, int QPW>
 void launch_gather_t(const VMParams& p, const KdNav& nav, TreePhotons tp, QueryBuf qb, const uint32_t* order,
                      const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters,
-                     cudaStream_t s) {
+                     cudaStream_t s, const unsigned long long* nq_dev, const int* skip) {
     const long long warps = (nq + QPW - 1) / QPW;
     k_gather<MB, QPW><<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
-        p, nav, tp, qb, order, start_nodes, nq, accum, counters);
+        p, nav, tp, qb, order, start_nodes, nq, accum, counters, nq_dev, skip);
 }
 
 int gather_variants() { return 6; }
@@ -601,16 +612,16 @@ const char* gather_variant_name(int v) {
 
 void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
                    const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters, cudaStream_t s,
-                   int variant) {
+                   int variant, const unsigned long long* nq_dev, const int* skip) {
     if (nq <= 0) return;
     const KdNav nav = nav_of(tree);
     switch (variant) {
-    case 0: launch_gather_t<2, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
-    case 1: launch_gather_t<2, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
-    case 2: launch_gather_t<3, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
-    case 4: launch_gather_t<4, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
-    case 5: launch_gather_t<4, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
-    default: launch_gather_t<3, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s); break;
+    case 0: launch_gather_t<2, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
+    case 1: launch_gather_t<2, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
+    case 2: launch_gather_t<3, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
+    case 4: launch_gather_t<4, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
+    case 5: launch_gather_t<4, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
+    default: launch_gather_t<3, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
     }
 }
 

@@ -628,7 +628,11 @@ int kd_build(const float4* pos4, long long n, KdTree& tree, void* scratch, size_
         nl++;
     }
     size_t smem = SmemLayout::total;
-    cudaFuncSetAttribute(k_smem_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static bool attr_set = false;   // once: later builds may be recorded into a CUDA graph
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_smem_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_set = true;
+    }
     k_smem_build<<<(unsigned)(1LL << l0), kSmemThreads, smem, stream>>>(B, cur, l0, n, tree.nodes);
     nl++;
     if (launches) *launches = nl;

@@ -92,6 +92,13 @@ struct DeviceState {
     int camera_variant[64] = {};
     double gather_variant_ms[64][8];
     DevBuf<double> tune_accum;
+    // asynchronous iterations (graph replay): fixed capacities, launch shapes and a
+    // per-iteration overflow flag; the instantiated graph is updated in place
+    long long async_pcap = 0, async_qcap = 0;
+    int async_lvar = 0, async_cvar = 0, async_gvar = 3;
+    DevBuf<int> async_flags;
+    cudaGraphExec_t graph_exec = nullptr;
+    unsigned long long last_photons = 0, last_queries = 0;
     int mlp_rounds = 0;          // training rounds done (the proposal is used after the first)
     double mlp_last_rows = 0;    // training samples collected in the last round
     int iterations_done = 0;
@@ -100,7 +107,7 @@ struct DeviceState {
     float stats_mlt_visible = 0.0f;
     // accumulated over a timed render call
     double acc_gather_ms = 0, acc_gather_bytes = 0, acc_launches = 0;
-    int acc_iters = 0;
+    int acc_iters = 0, acc_async = 0;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
 
     void release() {
@@ -120,6 +127,9 @@ struct DeviceState {
         mlp_rounds = 0;
         mlp_last_rows = 0;
         tune_accum.release();   // the chosen shapes stay: they are kept for the process
+        async_flags.release();
+        if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+        async_pcap = async_qcap = 0;
         for (auto& e : evm) if (e) { cudaEventDestroy(e); e = nullptr; }
         for (auto& e : evg) if (e) { cudaEventDestroy(e); e = nullptr; }
         for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
@@ -149,6 +159,7 @@ void default_config(rc_config* c) {
     c->train_steps = 64;
     c->learning_rate = 1e-3f;
     c->autotune = 1;
+    c->graph_replay = 1;
 }
 
 const rc_config& cfg() {
@@ -323,8 +334,21 @@ VMParams make_params(const HostScene& sc, int iteration) {
 
 float ms_between(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0.0f;
-    cudaEventElapsedTime(&ms, a, b);
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        cudaGetLastError();   // a timing that is not available is reported as 0
+        ms = 0.0f;
+    }
     return ms;
+}
+
+// Event record usable for timing both in eager and in recorded (graph) iterations:
+// during stream capture it becomes an external event node, which records the event
+// like an ordinary record each time the graph runs.
+cudaError_t record(cudaEvent_t e, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cs);
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal)
+                                               : cudaEventRecord(e, s);
 }
 
 ProposalCtx proposal_ctx(const HostScene& sc, const VMParams& p) {
@@ -422,10 +446,13 @@ int autotune_variants(int nvariants, Run&& run, const char* what, long long size
 
 int size_class(long long n) { return n > 0 ? 63 - __builtin_clzll((unsigned long long)n) : 0; }
 
-int render_iteration(HostScene& sc) {
+// One progressive iteration with host round trips (counts read back, buffers grown on
+// overflow).  redo_iteration >= 0 renders that iteration index again without counting
+// it (an iteration an asynchronous replay had to skip).
+int render_iteration(HostScene& sc, int redo_iteration = -1) {
     DeviceState& d = g_dev;
     cudaStream_t s = d.stream;
-    const int it = d.iterations_done;
+    const int it = redo_iteration >= 0 ? redo_iteration : d.iterations_done;
     VMParams p = make_params(sc, it);
     const bool learned = cfg().learned_proposal && cfg().sampler == RC_SAMPLER_UNIFORM;
     const bool train = learned && it < cfg().train_iterations;
@@ -608,7 +635,9 @@ int render_iteration(HostScene& sc) {
         r = check_errors();
         if (r) return r;
     }
-    d.iterations_done++;
+    if (redo_iteration < 0) d.iterations_done++;
+    d.last_photons = nph;
+    d.last_queries = nq;
     double* st = d.stats;
     st[0] = (double)p.num_light_paths;
     st[1] = (double)nph;
@@ -638,6 +667,234 @@ int render_iteration(HostScene& sc) {
                     "\"merged\": %llu, \"tests\": %llu, \"buckets\": %llu, \"nodes\": %llu, "
                     "\"light_ms\": %.3f, \"kd_ms\": %.3f, \"camera_ms\": %.3f, \"gather_ms\": %.3f}\n",
                     it, p.num_light_paths, nph, nq, gc[0], gc[1], gc[2], gc[3], st[4], st[5], st[6], st[7]);
+    return RC_OK;
+}
+
+// ---------------------------------------------------------------- asynchronous iterations
+// After one iteration with host round trips has fixed the sizes, further iterations of
+// the uniform sampler are enqueued without any: photon and query capacities are fixed
+// (the KD tree is built over the whole photon capacity, unused slots padded far away,
+// which leaves every radius query's answer unchanged), the query order and the gather
+// read the query count on the device, and a per-iteration flag records a count that
+// overflowed its capacity (that iteration's gather is skipped and the iteration is
+// rendered again with host round trips at the end).  Each iteration is captured as a
+// CUDA graph; the instantiated graph is updated in place with the next iteration's
+// parameters and replayed.
+constexpr double kReplayMaxIterationMs = 20.0;
+
+bool async_eligible() {
+    return cfg().graph_replay && cfg().sampler == RC_SAMPLER_UNIFORM && !cfg().learned_proposal;
+}
+
+int async_setup(const HostScene& sc) {
+    DeviceState& d = g_dev;
+    const long long npix = (long long)sc.camera.width * sc.camera.height;
+    // capacities: the last measured counts with a 2% + 4096 margin, 1024-aligned (the
+    // counts of a configuration vary by ~0.1% between iterations)
+    // (graph_replay 2, for tests: the counts themselves, so that iterations that store
+    // more photons or queries than the measured one overflow and are rendered again)
+    const bool tight = cfg().graph_replay == 2;
+    auto capacity = [tight](unsigned long long c) {
+        return tight ? (long long)c : (long long)(((c + c / 50 + 4096) + 1023) / 1024 * 1024);
+    };
+    d.async_pcap = capacity(d.last_photons);
+    d.async_qcap = capacity(d.last_queries);
+    RC_CUDA(d.ph_pos.reserve(d.async_pcap)); RC_CUDA(d.ph_dir.reserve(d.async_pcap));
+    RC_CUDA(d.ph_tp.reserve(d.async_pcap)); RC_CUDA(d.ph_path.reserve(d.async_pcap));
+    RC_CUDA(d.q0.reserve(d.async_qcap)); RC_CUDA(d.q1.reserve(d.async_qcap)); RC_CUDA(d.q2.reserve(d.async_qcap));
+    RC_CUDA(d.q3.reserve(d.async_qcap)); RC_CUDA(d.q4.reserve(d.async_qcap));
+    const long long n = d.async_pcap;
+    RC_CUDA(d.kd_nodes.reserve(std::max<long long>(kd_node_array_len(n), 2)));
+    RC_CUDA(d.kd_x.reserve(n)); RC_CUDA(d.kd_y.reserve(n)); RC_CUDA(d.kd_z.reserve(n)); RC_CUDA(d.kd_id.reserve(n));
+    RC_CUDA(d.kd_scratch.reserve(kd_scratch_bytes(n)));
+    RC_CUDA(d.tp0.reserve(n)); RC_CUDA(d.tp1.reserve(n)); RC_CUDA(d.tp2.reserve(n));
+    const int bl = kd_box_levels(n);
+    if (bl > 0) { RC_CUDA(d.box_lo.reserve((size_t)1 << bl)); RC_CUDA(d.box_hi.reserve((size_t)1 << bl)); }
+    KdTree t{};
+    t.n = n;
+    t.levels = n > 0 ? 63 - __builtin_clzll((unsigned long long)n) : 0;
+    RC_CUDA(d.qorder.reserve(d.async_qcap)); RC_CUDA(d.qstart.reserve(d.async_qcap));
+    RC_CUDA(d.qscratch.reserve(query_order_scratch_bytes(d.async_qcap, t)));
+    RC_CUDA(d.accum.reserve(3 * npix));
+    auto var = [](int v, int dflt) { return v >= 0 ? v : dflt; };
+    d.async_lvar = var(d.light_variant[size_class(cfg().photons_per_iter > 0 ? cfg().photons_per_iter : npix)], 0);
+    d.async_cvar = var(d.camera_variant[size_class(npix)], 0);
+    d.async_gvar = var(d.gather_variant[size_class((long long)d.last_queries)], 3);
+    if (!cfg().autotune) d.async_lvar = d.async_cvar = 0, d.async_gvar = 3;
+    return RC_OK;
+}
+
+// Enqueue iteration `it` (no host synchronisation); `flag` receives the overflow flag.
+int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
+    DeviceState& d = g_dev;
+    cudaStream_t s = d.stream;
+    VMParams p = make_params(sc, it);
+    const long long pc = d.async_pcap, qc = d.async_qcap;
+    RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
+    PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, pc, d.counters.p};
+    RC_CUDA(record(d.ev[0], s));
+    launch_light_pass(p, ph, d.counters.p + 6, s, d.async_lvar);
+    RC_CUDA(record(d.ev[1], s));
+    // pads one scene extent (plus four base radii) beyond the scene's +x face: outside
+    // every merge radius, and close enough that the KD build's largest-extent rule
+    // separates them from the stored photons along x within a few levels
+    const float ext = std::max(std::max(sc.bounds.mx.x - sc.bounds.mn.x, sc.bounds.mx.y - sc.bounds.mn.y),
+                               sc.bounds.mx.z - sc.bounds.mn.z);
+    const float4 pad = make_float4(sc.bounds.mx.x + ext + 4.0f * sc.base_radius + 1.0f,
+                                   0.5f * (sc.bounds.mn.y + sc.bounds.mx.y), 0.5f * (sc.bounds.mn.z + sc.bounds.mx.z),
+                                   0.0f);
+    launch_pad_photons(d.ph_pos.p, d.counters.p, pc, pad, s);
+    KdTree tree{};
+    tree.nodes = d.kd_nodes.p; tree.x = d.kd_x.p; tree.y = d.kd_y.p; tree.z = d.kd_z.p; tree.id = d.kd_id.p;
+    RC_CUDA(record(d.ev[2], s));
+    int kl = 0;
+    if (kd_build(d.ph_pos.p, pc, tree, d.kd_scratch.p, d.kd_scratch.n, s, &kl, d.errors.p + ERR_KD)) {
+        g_err = "KD scratch too small"; return RC_E_CAPACITY;
+    }
+    TreePhotons tph{d.tp0.p, d.tp1.p, d.tp2.p};
+    tree.box_levels = kd_box_levels(pc);
+    if (tree.box_levels > 0) {
+        tree.box_lo = d.box_lo.p; tree.box_hi = d.box_hi.p;
+        launch_kd_boxes(tree, s, nullptr);
+    }
+    launch_tree_records(PhotonBuf{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, pc, d.counters.p}, tree, tph, s);
+    RC_CUDA(record(d.ev[3], s));
+    QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qc, d.counters.p + 1};
+    RC_CUDA(record(d.ev[4], s));
+    launch_camera_pass(p, qb, d.counters.p + 7, s, d.async_cvar);
+    RC_CUDA(record(d.ev[5], s));
+    launch_check_counts(d.counters.p, pc, d.counters.p + 1, qc, flag, s);
+    RC_CUDA(record(d.ev[6], s));
+    launch_query_order(tree, reinterpret_cast<const float*>(d.q0.p), 4, qc, p.radius_sqr, d.qscratch.p, d.qorder.p,
+                       d.qstart.p, nullptr, s, d.counters.p + 1);
+    RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
+    RC_CUDA(record(d.evg[0], s));
+    launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, qc, d.accum.p, d.counters.p + 2, s, d.async_gvar,
+                  d.counters.p + 1, flag);
+    RC_CUDA(record(d.evg[1], s));
+    RC_CUDA(record(d.ev[7], s));
+    return RC_OK;
+}
+
+// Capture iteration `it` as a graph, update the instantiated graph with it (or
+// instantiate it) and launch it.
+int launch_async_iteration(HostScene& sc, int it, int* flag) {
+    DeviceState& d = g_dev;
+    cudaStream_t s = d.stream;
+    RC_CUDA(cudaGetLastError());
+    RC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    int r = enqueue_async_iteration(sc, it, flag);
+    const cudaError_t le = cudaGetLastError();   // launch errors recorded during capture
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (r) { if (graph) cudaGraphDestroy(graph); return r; }
+    if (le != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        g_err = std::string("kernel launch while recording an iteration: ") + cudaGetErrorString(le);
+        return RC_E_CUDA;
+    }
+    if (e != cudaSuccess) { g_err = std::string("graph capture: ") + cudaGetErrorString(e); return RC_E_CUDA; }
+    if (d.graph_exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(d.graph_exec, graph, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(d.graph_exec);
+            d.graph_exec = nullptr;
+        }
+    }
+    if (!d.graph_exec) {
+        e = cudaGraphInstantiate(&d.graph_exec, graph, 0);
+        if (e != cudaSuccess) { cudaGraphDestroy(graph); g_err = std::string("graph instantiate: ") + cudaGetErrorString(e); return RC_E_CUDA; }
+    }
+    cudaGraphDestroy(graph);
+    RC_CUDA(cudaGraphLaunch(d.graph_exec, s));
+    RC_CUDA(cudaGetLastError());
+    return RC_OK;
+}
+
+// `iterations` progressive iterations: the first with host round trips, the rest
+// replayed asynchronously when eligible; overflowed iterations are rendered again.
+int render_iterations(HostScene& sc, int iterations) {
+    DeviceState& d = g_dev;
+    int r = RC_OK;
+    int i = 0;
+    if (!async_eligible()) {
+        for (; i < iterations && !r; ++i) r = render_iteration(sc);
+        return r;
+    }
+    if (d.async_pcap == 0 && i < iterations) {
+        r = render_iteration(sc);
+        ++i;
+        if (r) return r;
+        // Replay pays where host round trips and launch gaps are a visible share of an
+        // iteration; for long iterations the KD tree over the padded capacity costs more
+        // than it saves (measured: 64-scene batch +6%, 37 ms water-pool iterations -2%).
+        if (d.stats[9] > kReplayMaxIterationMs && cfg().graph_replay != 2) d.async_pcap = -1;
+        else {
+            r = async_setup(sc);
+            if (r) return r;
+        }
+    }
+    if (d.async_pcap < 0) {
+        for (; i < iterations && !r; ++i) r = render_iteration(sc);
+        return r;
+    }
+    const int n_async = iterations - i;
+    if (n_async <= 0) return RC_OK;
+    RC_CUDA(d.async_flags.reserve(n_async));
+    const int first_it = d.iterations_done;
+    for (int k = 0; k < n_async; ++k) {
+        r = launch_async_iteration(sc, first_it + k, d.async_flags.p + k);
+        if (r) return r;
+        d.iterations_done++;
+    }
+    std::vector<int> flags(n_async, 0);
+    RC_CUDA(cudaMemcpyAsync(flags.data(), d.async_flags.p, sizeof(int) * n_async, cudaMemcpyDeviceToHost, d.stream));
+    RC_CUDA(cudaStreamSynchronize(d.stream));
+    r = check_errors();
+    if (r) return r;
+    // stats of the last replayed iteration
+    unsigned long long cnt[6] = {0, 0, 0, 0, 0, 0};
+    RC_CUDA(cudaMemcpy(cnt, d.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
+    VMParams p = make_params(sc, d.iterations_done - 1);
+    double* st = d.stats;
+    st[0] = (double)p.num_light_paths;
+    st[1] = (double)cnt[0];
+    st[2] = (double)cnt[1];
+    st[3] = (double)cnt[2];
+    st[14] = (double)cnt[3];
+    st[15] = (double)cnt[4];
+    st[4] = ms_between(d.ev[0], d.ev[1]);
+    st[5] = ms_between(d.ev[2], d.ev[3]);
+    st[6] = ms_between(d.ev[4], d.ev[5]);
+    st[7] = ms_between(d.ev[6], d.ev[7]);
+    st[8] = 0.0;
+    st[9] = st[4] + st[5] + st[6] + st[7];
+    st[10] = d.iterations_done;
+    st[11] = sc.scene_radius;
+    st[12] = std::sqrt(p.radius_sqr);
+    const double gms = ms_between(d.evg[0], d.evg[1]);
+    d.acc_gather_ms += gms * n_async;    // the last replay's gather time stands for each
+    d.acc_gather_bytes += (40.0 * (double)cnt[0] + 128.0 * (double)cnt[1]) * n_async;
+    d.acc_iters += n_async;
+    d.acc_async += n_async;
+    d.acc_launches += (d.stats[13] + 2.0) * n_async;   // an eager iteration's kernels + pad + check
+    bool regrow = false;
+    for (int k = 0; k < n_async; ++k) {
+        if (!flags[k]) continue;
+        regrow = true;
+        r = render_iteration(sc, first_it + k);   // the skipped iteration, with round trips
+        if (r) return r;
+    }
+    if (regrow) {
+        // counts outgrew the capacities: size them again from the last measured counts
+        if (d.graph_exec) { cudaGraphExecDestroy(d.graph_exec); d.graph_exec = nullptr; }
+        r = async_setup(sc);
+        if (r) return r;
+    }
+    if (cfg().verbose)
+        std::printf("{\"replayed_iterations\": %d, \"redone\": %d, \"photon_capacity\": %lld, \"query_capacity\": %lld}\n",
+                    n_async, (int)std::count(flags.begin(), flags.end(), 1), d.async_pcap, d.async_qcap);
     return RC_OK;
 }
 
@@ -934,8 +1191,7 @@ int main(void) {
         // averaging), 5 = BVH dump to OBJ files (not provided here)
         const int mode = g_scene->debug_test;
         if (mode == 1) {
-            int iters = g_scene->samples;
-            for (int i = 0; i < iters && !r; ++i) r = render_iteration(*g_scene);
+            r = render_iterations(*g_scene, g_scene->samples);
         } else if (mode >= 2 && mode <= 4) {
             r = render_debug(*g_scene, mode);
         } else {
@@ -981,9 +1237,13 @@ int rc_set_config(const rc_config* c) {
             g_err = "large_step_prob must be in (0, 1]"; return RC_E_INVALID;
         }
     }
+    if (c->graph_replay < 0 || c->graph_replay > 2) { g_err = "graph_replay must be 0, 1 or 2"; return RC_E_INVALID; }
     g_cfg = *c;
     g_cfg.exr_path[sizeof(g_cfg.exr_path) - 1] = 0;
     g_cfg_set = true;
+    // sizes and shapes of asynchronous iterations are re-derived under the new settings
+    g_dev.async_pcap = g_dev.async_qcap = 0;
+    if (g_dev.graph_exec) { cudaGraphExecDestroy(g_dev.graph_exec); g_dev.graph_exec = nullptr; }
     return RC_OK;
 }
 
@@ -1020,7 +1280,7 @@ int rc_host_world_bvh(unsigned* nodes, int cap, int* index, int index_cap) {
 int rc_render(int iterations) {
     if (iterations < 0) { g_err = "iterations < 0"; return RC_E_INVALID; }
     int r = prepare();
-    for (int i = 0; i < iterations && !r; ++i) r = render_iteration(*g_scene);
+    if (!r) r = render_iterations(*g_scene, iterations);
     return r;
 }
 
@@ -1040,9 +1300,10 @@ int rc_render_timed(int iterations, double* out) {
     DeviceState& d = g_dev;
     d.acc_gather_ms = d.acc_gather_bytes = d.acc_launches = 0;
     d.acc_iters = 0;
+    d.acc_async = 0;
     RC_CUDA(cudaStreamSynchronize(d.stream));
     RC_CUDA(cudaEventRecord(d.t0, d.stream));
-    for (int i = 0; i < iterations && !r; ++i) r = render_iteration(*g_scene);
+    r = render_iterations(*g_scene, iterations);
     if (r) return r;
     RC_CUDA(cudaEventRecord(d.t1, d.stream));
     RC_CUDA(cudaEventSynchronize(d.t1));

@@ -92,6 +92,14 @@ void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next
 void launch_debug_view(const VMParams& p, int mode, float ior, double* accum, cudaStream_t s);
 // FP32 mean image (n floats) from the FP64 running sum.
 void launch_image_mean(const double* acc, float* out, long long n, double scale, cudaStream_t s);
+// Photon slots [*count, capacity) get position `pad` (chosen outside the scene by more
+// than any merge radius: a KD tree over the full capacity then answers the same radius
+// queries as one over the stored photons), and *flag = 1 when a count overflowed its
+// capacity.
+void launch_pad_photons(float4* pos, const unsigned long long* count, long long capacity, float4 pad,
+                        cudaStream_t s);
+void launch_check_counts(const unsigned long long* photons, long long photon_cap, const unsigned long long* queries,
+                         long long query_cap, int* flag, cudaStream_t s);
 void launch_trace_rays(const SceneView& s, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st);
 void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaStream_t s);
@@ -103,15 +111,19 @@ void launch_kd_boxes(const KdTree& tree, cudaStream_t s, int* launches);
 // indices grouped by KD cell.  scratch: query_order_scratch_bytes(nq, tree).
 size_t query_order_scratch_bytes(long long nq, const KdTree& tree);
 void launch_query_order(const KdTree& tree, const float* qpos, int stride, long long nq, float r2, void* scratch,
-                        uint32_t* order, uint2* start_nodes, int* launches, cudaStream_t s);
+                        uint32_t* order, uint2* start_nodes, int* launches, cudaStream_t s,
+                        const unsigned long long* nq_dev = nullptr);
 // start_nodes[i]: the node where query i's traversal first branches (from launch_query_order).
 // counters (optional, 4 u64 accumulated): accepted photon-query pairs, photon tests
 // (lanes x staged photons), buckets visited, inner nodes visited
 // `variant` picks the gather's launch shape (see gather_variant_name); 3 is the default
 // the autotuner starts from.
+// With nq_dev the query count is read on the device (bounded by num_queries, the
+// capacity the grid is sized for) and a non-zero *skip makes the launch a no-op.
 void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
                    const uint2* start_nodes, long long num_queries, double* accum, unsigned long long* counters,
-                   cudaStream_t s, int variant = 3);
+                   cudaStream_t s, int variant = 3, const unsigned long long* nq_dev = nullptr,
+                   const int* skip = nullptr);
 int gather_variants();
 // Launch shapes of the persistent light and camera passes (block size x traversal-stack
 // placement), chosen by the autotuner; 0 is the default.

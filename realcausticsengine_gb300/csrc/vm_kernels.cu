@@ -418,6 +418,28 @@ void launch_image_mean(const double* acc, float* out, long long n, double scale,
     k_image_mean<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(acc, out, n, scale);
 }
 
+__global__ void k_pad_photons(float4* __restrict__ pos, const unsigned long long* __restrict__ count, long long cap,
+                              float4 pad) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= cap || (unsigned long long)i < *count) return;
+    pos[i] = pad;
+}
+
+__global__ void k_check_counts(const unsigned long long* photons, long long pcap, const unsigned long long* queries,
+                               long long qcap, int* flag) {
+    *flag = (*photons > (unsigned long long)pcap || *queries > (unsigned long long)qcap) ? 1 : 0;
+}
+
+void launch_pad_photons(float4* pos, const unsigned long long* count, long long capacity, float4 pad, cudaStream_t s) {
+    if (capacity <= 0) return;
+    k_pad_photons<<<(unsigned)((capacity + 255) / 256), 256, 0, s>>>(pos, count, capacity, pad);
+}
+
+void launch_check_counts(const unsigned long long* photons, long long photon_cap, const unsigned long long* queries,
+                         long long query_cap, int* flag, cudaStream_t s) {
+    k_check_counts<<<1, 1, 0, s>>>(photons, photon_cap, queries, query_cap, flag);
+}
+
 void launch_trace_rays(const SceneView& sv, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st) {
     if (n <= 0) return;

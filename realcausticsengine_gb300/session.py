@@ -24,7 +24,7 @@ class Renderer:
     def __init__(self, scene: Scene, max_path_length: int = 6, photons_per_iter: int = 0, seed: int = 0,
                  sampler: int = abi.SAMPLER_UNIFORM, verbose: bool = False, learned_proposal: bool = False,
                  train_iterations: int = 8, train_steps: int = 64, learning_rate: float = 1e-3,
-                 camera_seed: int = 0, autotune: bool = True):
+                 camera_seed: int = 0, autotune: bool = True, graph_replay: bool = True):
         self.scene = scene
         self.L = lib()
         cfg = abi.RcConfig()
@@ -41,6 +41,7 @@ class Renderer:
         cfg.learning_rate = learning_rate
         cfg.camera_seed = camera_seed
         cfg.autotune = int(autotune)
+        cfg.graph_replay = int(graph_replay)
         check(self.L.rc_set_config(C.byref(cfg)), "rc_set_config")
         self.args = InitArgs(scene)
         self.args.call(self.L.init)

@@ -392,3 +392,31 @@ def test_main_runs_debug_view(tmp_path):
     assert (tmp_path / "dbg.exr").stat().st_size > 32 * 24 * 12
     InitArgs(sc, debug_test=5).call(L.init)
     assert L.main() != 0 and b"debug_test" in L.rc_last_error()
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_graph_replay_matches_round_trips(mode):
+    """Iterations replayed as CUDA graphs (fixed capacities, KD tree over the padded
+    photon capacity, device-side counts) render the same image as iterations with host
+    round trips (the photon sets are the same; only FP32 summation order differs).
+    mode 2 sizes the capacities to the first iteration's counts, so iterations that
+    store more photons or queries overflow and are rendered again at the end."""
+    sc = scenes.test_scene(64, 48, subdiv=2)
+    imgs = []
+    for replay in (0, mode):
+        r = Renderer(sc, max_path_length=6, photons_per_iter=60000, seed=21, graph_replay=bool(replay))
+        if replay == 2:
+            from realcausticsengine_gb300 import abi
+            cfg = abi.RcConfig()
+            r.L.rc_default_config(C.byref(cfg))
+            cfg.max_path_length, cfg.photons_per_iter, cfg.seed, cfg.write_exr, cfg.graph_replay = 6, 60000, 21, 0, 2
+            assert r.L.rc_set_config(C.byref(cfg)) == 0
+        r.render(3)
+        r.render(5)
+        imgs.append(r.image().astype(np.float64))
+        st = r.stats()
+        r.release()
+        assert st["iterations"] == 8
+    a, b = imgs
+    assert a.max() > 0
+    assert np.abs(a - b).max() <= 1e-4 * a.max(), np.abs(a - b).max()
