@@ -76,7 +76,7 @@ enum {
     RC_E_NO_SCENE = -1,      /* init() was not called, or main() already released it */
     RC_E_INVALID = -2,       /* bad argument (null pointer, zero size, bad index)    */
     RC_E_CUDA = -3,          /* CUDA runtime error (message in rc_last_error)        */
-    RC_E_UNSUPPORTED = -4,   /* feature outside this build                           */
+    RC_E_UNSUPPORTED = -4,   /* feature this library does not provide                */
     RC_E_CAPACITY = -5,      /* a fixed-size buffer or queue would overflow          */
     RC_E_TIMEOUT = -6,       /* a bounded device-side wait expired                   */
     RC_E_IO = -7             /* output file could not be written                     */

@@ -476,7 +476,7 @@ int convert_lights(HostScene& scene, std::string& err) {
         V3 color = {pl.color[0], pl.color[1], pl.color[2]};
         if (pl.type == 'P') {
             // Point_Light::sample_light is a stub in the reference (src/Lights.h:78-81);
-            // this build emits isotropically from the position.
+            // here it emits isotropically from the position.
             L.type = LIGHT_POINT;
             V3 c = mul(color, pl.power);
             L.cr = c.x; L.cg = c.y; L.cb = c.z;

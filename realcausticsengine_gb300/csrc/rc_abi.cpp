@@ -411,7 +411,7 @@ int proposal_train(const HostScene& sc, const VMParams& p) {
     RC_CUDA(cudaStreamSynchronize(s));
     const int total = (int)std::min<unsigned>(rows, (unsigned)kTrainCapacity);
     d.mlp_last_rows = total;
-    if (total < 256) return RC_OK;   // too few merged paths to learn from this round
+    if (total < 256) return RC_OK;   // too few merged paths to learn from in this pass
     mlp_normalize_weights(d.train_dir.p, total, d.train_wsum.p, s);
     if (mlp_train(d.mlp->p, d.mlp->b, d.train_pos.p, d.train_dir.p, total, cfg().train_steps, cfg().learning_rate, s,
                   d.errors.p + ERR_MLP)) {
