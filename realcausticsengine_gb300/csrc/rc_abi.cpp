@@ -38,12 +38,15 @@ template <class T>
 struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
+    // Grows with 1/16 headroom: per-iteration counts fluctuate, and each reallocation
+    // (cudaFree synchronises the device) would stall an iteration.
     cudaError_t reserve(size_t count) {
         if (count <= n && p) return cudaSuccess;
         if (p) cudaFree(p);
         p = nullptr; n = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
-        if (e == cudaSuccess) n = count;
+        const size_t want = std::max<size_t>(count + count / 16, 1);
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e == cudaSuccess) n = want;
         return e;
     }
     void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
