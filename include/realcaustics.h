@@ -132,6 +132,11 @@ typedef struct rc_config {
      * counts back.  2: as 1 with capacities equal to the measured counts and no time
      * limit (tests: exercises the re-render of overflowed iterations). */
     int graph_replay;
+    /* 1 (default): the per-mesh BVHs (Scene::update_bvh, src/Scene.cpp:110-152) are built
+     * on the device by a binned SAH build whose node arrays, triangle order and traversal
+     * costs are bit-identical to the host build; meshes with non-finite or -0.0 box
+     * coordinates, or without triangles, fall back to the host build.  0: host build. */
+    int gpu_bvh;
 } rc_config;
 
 int rc_default_config(rc_config* cfg);
@@ -152,6 +157,20 @@ int rc_prepare_host(float* info);
  * Returns the node count (copies at most cap nodes / index_cap indices). */
 int rc_host_mesh_bvh(int mesh, unsigned* nodes, int cap, int* index, int index_cap, float* cost);
 int rc_host_world_bvh(unsigned* nodes, int cap, int* index, int index_cap);
+
+/* The scene arrays as the kernels read them (after rc_prepare), for comparing the
+ * device and host BVH builds.  which: 0 = mesh BVH nodes (8 words per node: min xyz |
+ * word0, max xyz | word1, global indices), 1 = triangles in leaf order (24 words: v0 |
+ * triangle id, e1 | material, e2 | mesh, three normals), 2 = world BVH nodes (8 words),
+ * 3 = world leaf mesh list followed by each mesh's root node index.  Copies at most
+ * `cap` words; *words receives the full size.  No counterpart in the reference. */
+int rc_scene_dump(int which, unsigned* out, long long cap, long long* words);
+
+/* Timing of the last rc_prepare: out[0] = mesh BVH build ms (host or device, uploads
+ * included), out[1] = 1 if the device built the mesh BVHs, out[2] = world BVH + light
+ * + material conversion + remaining uploads ms, out[3] = mesh BVH nodes, out[4] = device
+ * level passes (segments above the per-warp size).  Returns the number written. */
+int rc_prepare_stats(double* out, int n);
 
 /* Render `iterations` more progressive iterations into the FP64 running mean. */
 int rc_render(int iterations);

@@ -55,6 +55,8 @@ def lib() -> C.CDLL:
     L.rc_render_debug.argtypes = [C.c_int]
     L.rc_save_state.argtypes = [C.c_char_p]
     L.rc_load_state.argtypes = [C.c_char_p]
+    L.rc_scene_dump.argtypes = [C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
+    L.rc_prepare_stats.argtypes = [C.c_void_p, C.c_int]
     _lib = L
     return L
 
@@ -70,4 +72,4 @@ EXPORTS = ["init", "main", "rc_default_config", "rc_set_config", "rc_prepare", "
            "rc_last_error", "rc_get_stats", "rc_trace_rays", "rc_trace_rays_full", "rc_kd_query",
            "rc_kd_build_nodes", "rc_light_photons", "rc_render_timed", "rc_kd_build_noalloc",
            "rc_kd_noalloc_last_error", "rc_proposal_state", "rc_render_debug",
-           "rc_save_state", "rc_load_state"]
+           "rc_save_state", "rc_load_state", "rc_scene_dump", "rc_prepare_stats"]

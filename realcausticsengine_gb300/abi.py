@@ -47,7 +47,7 @@ class RcConfig(C.Structure):
                 ("write_exr", C.c_int), ("exr_path", C.c_char * 256), ("verbose", C.c_int),
                 ("learned_proposal", C.c_int), ("train_iterations", C.c_int), ("train_steps", C.c_int),
                 ("learning_rate", C.c_float), ("camera_seed", C.c_ulonglong),
-                ("autotune", C.c_int), ("graph_replay", C.c_int)]
+                ("autotune", C.c_int), ("graph_replay", C.c_int), ("gpu_bvh", C.c_int)]
 
 
 SAMPLER_UNIFORM, SAMPLER_HYBRID, SAMPLER_PSSMLT = 0, 1, 2

@@ -35,6 +35,7 @@ SOURCES = [
     ("vm_mlt.cu", "nvcc"),
     ("tc_selftest.cu", "nvcc"),
     ("mlp.cu", "nvcc"),
+    ("bvh_build.cu", "nvcc"),
 ]
 
 

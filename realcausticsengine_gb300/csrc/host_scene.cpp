@@ -8,6 +8,7 @@
 #include "host_scene.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -135,6 +136,19 @@ R par_reduce(size_t start, size_t end, const R& init, Acc&& acc, Merge&& merge) 
     R r = init;
     for (const R& q : part) merge(r, q);
     return r;
+}
+
+// fn(begin, end) over [0, n) in contiguous pieces on several threads for large n
+// (per-element work only: the results do not depend on the split).
+template <class Fn>
+void par_for(size_t n, Fn&& fn) {
+    static const unsigned hw = std::thread::hardware_concurrency();
+    const unsigned nt = hw < 1 ? 1 : (hw > 16 ? 16 : hw);
+    if (n < kParallelLoop || nt == 1) { fn(0, n); return; }
+    std::vector<std::thread> ts;
+    for (unsigned t = 1; t < nt; ++t) ts.emplace_back([&, t]() { fn(n * t / nt, n * (t + 1) / nt); });
+    fn(0, n / nt);
+    for (auto& t : ts) t.join();
 }
 
 int sah_recurse(std::vector<Prim>& p, size_t start, size_t end, bool world, std::vector<TmpNode>& pool) {
@@ -388,7 +402,8 @@ int ingest_mesh(HostMesh& out, const void* blender_mesh, unsigned nverts, unsign
     const float* I = out.inv;
     out.wpos.resize(nverts);
     out.wnrm.resize(nverts);
-    for (unsigned v = 0; v < nverts; ++v) {
+    par_for(nverts, [&](size_t v0, size_t v1) {
+    for (size_t v = v0; v < v1; ++v) {
         const char* mv = mvert + 20 * (size_t)v;     // MVert: co f32[3] @0, no i16[3] @12
         float co[3]; int16_t no[3];
         std::memcpy(co, mv, 12);
@@ -406,21 +421,26 @@ int ingest_mesh(HostMesh& out, const void* blender_mesh, unsigned nverts, unsign
                 I[2] * nx + I[6] * ny + I[10] * nz};
         out.wnrm[v] = normalize(n);
     }
+    });
     out.tri.resize(3 * (size_t)ntris);
     out.mat.resize(ntris);
-    for (unsigned t = 0; t < ntris; ++t) {
-        const char* mp = mpoly + 12 * (size_t)t;    // MPoly: loopstart i32 @0, mat_nr i16 @8
-        int32_t ls; int16_t mat_nr;
-        std::memcpy(&ls, mp, 4);
-        std::memcpy(&mat_nr, mp + 8, 2);
-        for (int k = 0; k < 3; ++k) {
-            uint32_t vi;
-            std::memcpy(&vi, mloop + 8 * ((size_t)ls + k), 4);   // MLoop: v u32 @0
-            if (vi >= nverts) { err = "loop vertex index out of range"; return RC_E_INVALID; }
-            out.tri[3 * (size_t)t + k] = vi;
+    std::atomic<bool> bad_index{false};
+    par_for(ntris, [&](size_t t0, size_t t1) {
+        for (size_t t = t0; t < t1; ++t) {
+            const char* mp = mpoly + 12 * t;    // MPoly: loopstart i32 @0, mat_nr i16 @8
+            int32_t ls; int16_t mat_nr;
+            std::memcpy(&ls, mp, 4);
+            std::memcpy(&mat_nr, mp + 8, 2);
+            for (int k = 0; k < 3; ++k) {
+                uint32_t vi;
+                std::memcpy(&vi, mloop + 8 * ((size_t)ls + k), 4);   // MLoop: v u32 @0
+                if (vi >= nverts) { bad_index = true; vi = 0; }
+                out.tri[3 * t + k] = vi;
+            }
+            out.mat[t] = (uint32_t)material_indices[mat_nr];
         }
-        out.mat[t] = (uint32_t)material_indices[mat_nr];
-    }
+    });
+    if (bad_index) { err = "loop vertex index out of range"; return RC_E_INVALID; }
     return RC_OK;
 }
 

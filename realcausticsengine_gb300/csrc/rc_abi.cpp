@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "bvh_build.h"
 #include "host_scene.h"
 #include "mlp.cuh"
 #include "realcaustics.h"
@@ -58,6 +59,7 @@ struct DeviceState {
     cudaEvent_t ev[8] = {};
     // scene
     DevBuf<float4> node_lo, node_hi, wnode_lo, wnode_hi, tri_v0, tri_e1, tri_e2, tri_n0, tri_n1, tri_n2;
+    long long num_mesh_nodes = 0, num_tris = 0;
     DevBuf<int> world_mesh, mesh_root;
     DevBuf<DevLight> lights;
     DevBuf<float> cdf;
@@ -163,6 +165,7 @@ void default_config(rc_config* c) {
     c->learning_rate = 1e-3f;
     c->autotune = 1;
     c->graph_replay = 1;
+    c->gpu_bvh = 1;
 }
 
 const rc_config& cfg() {
@@ -183,7 +186,8 @@ inline float4 f4(float x, float y, float z, uint32_t w) {
     return make_float4(x, y, z, wf);
 }
 
-int upload_scene(HostScene& sc) {
+// Stream, events and the process-lifetime autotuner tables.
+int ensure_device() {
     DeviceState& d = g_dev;
     if (!d.stream) {
         RC_CUDA(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
@@ -200,8 +204,14 @@ int upload_scene(HostScene& sc) {
         RC_CUDA(cudaEventCreate(&d.t0));
         RC_CUDA(cudaEventCreate(&d.t1));
     }
+    return RC_OK;
+}
+
+// Mesh BVH nodes and triangle records from the host build, packed and uploaded.
+int upload_meshes_host(HostScene& sc, std::vector<int>& mesh_root) {
+    DeviceState& d = g_dev;
     std::vector<float4> nlo, nhi, v0, e1, e2, n0, n1, n2;
-    std::vector<int> mesh_root;
+    mesh_root.clear();
     uint32_t node_base = 0, tri_base = 0, tri_global = 0;
     for (size_t m = 0; m < sc.meshes.size(); ++m) {
         HostMesh& hm = sc.meshes[m];
@@ -232,6 +242,20 @@ int upload_scene(HostScene& sc) {
         tri_base += (uint32_t)(hm.bvh.index.size() - 1);
         tri_global += hm.num_tris;
     }
+    cudaStream_t s = d.stream;
+    int r;
+    if ((r = upload(d.node_lo, nlo, s)) || (r = upload(d.node_hi, nhi, s)) || (r = upload(d.tri_v0, v0, s)) ||
+        (r = upload(d.tri_e1, e1, s)) || (r = upload(d.tri_e2, e2, s)) || (r = upload(d.tri_n0, n0, s)) ||
+        (r = upload(d.tri_n1, n1, s)) || (r = upload(d.tri_n2, n2, s)))
+        return r;
+    d.num_mesh_nodes = (long long)nlo.size();
+    d.num_tris = (long long)v0.size();
+    return RC_OK;
+}
+
+// World BVH, mesh roots, lights and materials; the scene view the kernels read.
+int upload_scene_rest(HostScene& sc, const std::vector<int>& mesh_root) {
+    DeviceState& d = g_dev;
     std::vector<float4> wlo, whi;
     for (const BvhNode& nd : sc.world.nodes) {
         wlo.push_back(f4(nd.box.mn.x, nd.box.mn.y, nd.box.mn.z, nd.w0));
@@ -240,10 +264,8 @@ int upload_scene(HostScene& sc) {
     std::vector<int> wm(sc.world.index.begin() + 1, sc.world.index.end());
     cudaStream_t s = d.stream;
     int r;
-    if ((r = upload(d.node_lo, nlo, s)) || (r = upload(d.node_hi, nhi, s)) || (r = upload(d.wnode_lo, wlo, s)) ||
-        (r = upload(d.wnode_hi, whi, s)) || (r = upload(d.tri_v0, v0, s)) || (r = upload(d.tri_e1, e1, s)) ||
-        (r = upload(d.tri_e2, e2, s)) || (r = upload(d.tri_n0, n0, s)) || (r = upload(d.tri_n1, n1, s)) ||
-        (r = upload(d.tri_n2, n2, s)) || (r = upload(d.world_mesh, wm, s)) || (r = upload(d.mesh_root, mesh_root, s)) ||
+    if ((r = upload(d.wnode_lo, wlo, s)) || (r = upload(d.wnode_hi, whi, s)) ||
+        (r = upload(d.world_mesh, wm, s)) || (r = upload(d.mesh_root, mesh_root, s)) ||
         (r = upload(d.lights, sc.lights, s)) || (r = upload(d.cdf, sc.light_cdf, s)) ||
         (r = upload(d.materials, sc.materials, s)))
         return r;
@@ -264,15 +286,10 @@ int upload_scene(HostScene& sc) {
 }
 
 bool g_host_ready = false;
+double g_prep[5] = {};   // rc_prepare_stats
 
-// Host half of the pre-render steps of main() (src/main.cpp:150-168).
-int prepare_host() {
-    if (!g_scene) { g_err = "no scene: init() was not called"; return RC_E_NO_SCENE; }
-    HostScene& sc = *g_scene;
-    if (g_host_ready) return RC_OK;
-    if (sc.meshes.empty()) { g_err = "scene has no meshes"; return RC_E_INVALID; }
-    // Scene::update_bvh (src/Scene.cpp:110-152)
-    for (HostMesh& m : sc.meshes) build_mesh_bvh(m);
+// The host steps of main() after the mesh BVHs (src/main.cpp:150-168).
+int finish_host(HostScene& sc) {
     build_world_bvh(sc);
     // init_lights + update_pdf_distribution (src/main.cpp:160-163)
     int r = convert_lights(sc, g_err);
@@ -284,13 +301,99 @@ int prepare_host() {
     return RC_OK;
 }
 
-int prepare() {
-    int r = prepare_host();
+// Host half of the pre-render steps of main() (src/main.cpp:150-168).
+int prepare_host() {
+    if (!g_scene) { g_err = "no scene: init() was not called"; return RC_E_NO_SCENE; }
+    HostScene& sc = *g_scene;
+    if (g_host_ready) return RC_OK;
+    if (sc.meshes.empty()) { g_err = "scene has no meshes"; return RC_E_INVALID; }
+    // Scene::update_bvh (src/Scene.cpp:110-152)
+    for (HostMesh& m : sc.meshes) build_mesh_bvh(m);
+    return finish_host(sc);
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// Mesh BVHs built on the device (bvh_build.cu) straight into the scene arrays.  Leaves
+// sc.prepared false when the input needs the host build.
+int prepare_device_bvh(HostScene& sc) {
+    DeviceState& d = g_dev;
+    if (sc.meshes.empty()) return RC_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    int r = ensure_device();
     if (r) return r;
+    std::vector<GpuMeshSrc> src;
+    for (const HostMesh& hm : sc.meshes)
+        src.push_back({hm.wpos.data(), hm.wnrm.data(), hm.tri.data(), hm.mat.data(), hm.num_verts, hm.num_tris});
+    // scratch kept for the process (grow-only): a batch of scenes allocates it once;
+    // never destroyed (no device frees during static destruction at exit)
+    static GpuBvhBuilder& bld = *new GpuBvhBuilder();
+    bool supported = false;
+    std::string err;
+    r = bld.build(src, d.stream, supported, err);
+    if (r) { g_err = err; return r; }
+    if (!supported) return RC_OK;
+    RC_CUDA(d.node_lo.reserve(bld.num_nodes())); RC_CUDA(d.node_hi.reserve(bld.num_nodes()));
+    DevBuf<float4>* tb[] = {&d.tri_v0, &d.tri_e1, &d.tri_e2, &d.tri_n0, &d.tri_n1, &d.tri_n2};
+    for (auto* b : tb) RC_CUDA(b->reserve(bld.num_tris()));
+    r = bld.emit(d.node_lo.p, d.node_hi.p, d.tri_v0.p, d.tri_e1.p, d.tri_e2.p, d.tri_n0.p, d.tri_n1.p, d.tri_n2.p,
+                 d.stream, err);
+    if (r) { g_err = err; return r; }
+    d.num_mesh_nodes = bld.num_nodes();
+    d.num_tris = bld.num_tris();
+    for (size_t m = 0; m < sc.meshes.size(); ++m) {
+        MeshBvh& b = sc.meshes[m].bvh;
+        const float* f = &bld.mesh_box[6 * m];
+        b.bounds.mn = {f[0], f[1], f[2]};
+        b.bounds.mx = {f[3], f[4], f[5]};
+        b.cost = bld.mesh_cost[m];
+        b.nodes.clear();   // the host copy is built on demand (rc_host_mesh_bvh)
+        b.index.clear();
+    }
+    const std::vector<int> roots = bld.mesh_root;
+    const int levels = bld.levels;
+    g_prep[0] = ms_since(t0);
+    g_prep[1] = 1.0;
+    g_prep[3] = (double)d.num_mesh_nodes;
+    g_prep[4] = levels;
+    const auto t1 = std::chrono::steady_clock::now();
+    r = finish_host(sc);
+    if (r) return r;
+    r = upload_scene_rest(sc, roots);
+    if (r) return r;
+    g_prep[2] = ms_since(t1);
+    sc.prepared = true;
+    return RC_OK;
+}
+
+int prepare() {
+    if (!g_scene) { g_err = "no scene: init() was not called"; return RC_E_NO_SCENE; }
     HostScene& sc = *g_scene;
     if (sc.prepared) return RC_OK;
-    r = upload_scene(sc);
+    if (cfg().gpu_bvh && !g_host_ready) {
+        int r = prepare_device_bvh(sc);
+        if (r) return r;
+        if (sc.prepared) return RC_OK;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    const bool built_here = !g_host_ready;
+    int r = prepare_host();
     if (r) return r;
+    r = ensure_device();
+    if (r) return r;
+    std::vector<int> roots;
+    r = upload_meshes_host(sc, roots);
+    if (r) return r;
+    g_prep[0] = built_here ? ms_since(t0) : 0.0;
+    g_prep[1] = 0.0;
+    g_prep[3] = (double)g_dev.num_mesh_nodes;
+    g_prep[4] = 0.0;
+    const auto t1 = std::chrono::steady_clock::now();
+    r = upload_scene_rest(sc, roots);
+    if (r) return r;
+    g_prep[2] = ms_since(t1);
     sc.prepared = true;
     return RC_OK;
 }
@@ -1241,6 +1344,7 @@ int rc_set_config(const rc_config* c) {
         }
     }
     if (c->graph_replay < 0 || c->graph_replay > 2) { g_err = "graph_replay must be 0, 1 or 2"; return RC_E_INVALID; }
+    if (c->gpu_bvh < 0 || c->gpu_bvh > 1) { g_err = "gpu_bvh must be 0 or 1"; return RC_E_INVALID; }
     g_cfg = *c;
     g_cfg.exr_path[sizeof(g_cfg.exr_path) - 1] = 0;
     g_cfg_set = true;
@@ -1268,7 +1372,9 @@ int rc_host_mesh_bvh(int mesh, unsigned* nodes, int cap, int* index, int index_c
     int r = prepare_host();
     if (r) return r;
     if (mesh < 0 || mesh >= (int)g_scene->meshes.size() || !nodes || !index) { g_err = "bad mesh index"; return RC_E_INVALID; }
-    const MeshBvh& b = g_scene->meshes[mesh].bvh;
+    HostMesh& hm = g_scene->meshes[mesh];
+    if (hm.bvh.nodes.empty()) build_mesh_bvh(hm);   // the device built this scene's meshes
+    const MeshBvh& b = hm.bvh;
     if (cost) *cost = b.cost;
     return dump_bvh(b.nodes, b.index, nodes, cap, index, index_cap);
 }
@@ -1278,6 +1384,56 @@ int rc_host_world_bvh(unsigned* nodes, int cap, int* index, int index_cap) {
     if (r) return r;
     if (!nodes || !index) { g_err = "null output"; return RC_E_INVALID; }
     return dump_bvh(g_scene->world.nodes, g_scene->world.index, nodes, cap, index, index_cap);
+}
+
+int rc_scene_dump(int which, unsigned* out, long long cap, long long* words) {
+    if (!g_scene || !g_scene->prepared) { g_err = "rc_scene_dump: scene not prepared"; return RC_E_NO_SCENE; }
+    if (!words || (cap > 0 && !out) || cap < 0) { g_err = "rc_scene_dump: bad arguments"; return RC_E_INVALID; }
+    DeviceState& d = g_dev;
+    struct Part { const void* p; long long words; };
+    std::vector<Part> parts;
+    const long long wn = d.view.num_world_nodes;
+    const long long nm = (long long)g_scene->meshes.size();
+    const long long nw = (long long)g_scene->world.index.size() - 1;
+    switch (which) {
+        case 0: parts = {{d.node_lo.p, 4 * d.num_mesh_nodes}, {d.node_hi.p, 4 * d.num_mesh_nodes}}; break;
+        case 1:
+            parts = {{d.tri_v0.p, 4 * d.num_tris}, {d.tri_e1.p, 4 * d.num_tris}, {d.tri_e2.p, 4 * d.num_tris},
+                     {d.tri_n0.p, 4 * d.num_tris}, {d.tri_n1.p, 4 * d.num_tris}, {d.tri_n2.p, 4 * d.num_tris}};
+            break;
+        case 2: parts = {{d.wnode_lo.p, 4 * wn}, {d.wnode_hi.p, 4 * wn}}; break;
+        case 3: parts = {{d.world_mesh.p, nw}, {d.mesh_root.p, nm}}; break;
+        default: g_err = "rc_scene_dump: which must be 0..3"; return RC_E_INVALID;
+    }
+    // 0 and 2 are interleaved per node as (lo, hi); 1 per triangle as (v0, e1, e2, n0, n1, n2)
+    const int k = (int)parts.size();
+    const long long per = which == 3 ? 0 : 4;
+    long long total = 0;
+    for (const Part& q : parts) total += q.words;
+    *words = total;
+    std::vector<unsigned> host((size_t)total);
+    long long off = 0;
+    for (const Part& q : parts) {
+        if (q.words) RC_CUDA(cudaMemcpy(host.data() + off, q.p, 4 * (size_t)q.words, cudaMemcpyDeviceToHost));
+        off += q.words;
+    }
+    if (per) {
+        const long long items = total / (per * k);
+        std::vector<unsigned> il((size_t)total);
+        for (long long i = 0; i < items; ++i)
+            for (int j = 0; j < k; ++j)
+                std::memcpy(&il[(size_t)((i * k + j) * per)], &host[(size_t)(j * items * per + i * per)], 4 * per);
+        host.swap(il);
+    }
+    if (cap > 0) std::memcpy(out, host.data(), 4 * (size_t)std::min(cap, total));
+    return RC_OK;
+}
+
+int rc_prepare_stats(double* out, int n) {
+    if (!out || n < 0) { g_err = "rc_prepare_stats: bad arguments"; return RC_E_INVALID; }
+    const int k = std::min(n, 5);
+    for (int i = 0; i < k; ++i) out[i] = g_prep[i];
+    return k;
 }
 
 int rc_render(int iterations) {

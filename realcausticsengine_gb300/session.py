@@ -24,7 +24,7 @@ class Renderer:
     def __init__(self, scene: Scene, max_path_length: int = 6, photons_per_iter: int = 0, seed: int = 0,
                  sampler: int = abi.SAMPLER_UNIFORM, verbose: bool = False, learned_proposal: bool = False,
                  train_iterations: int = 8, train_steps: int = 64, learning_rate: float = 1e-3,
-                 camera_seed: int = 0, autotune: bool = True, graph_replay: bool = True):
+                 camera_seed: int = 0, autotune: bool = True, graph_replay: bool = True, gpu_bvh: bool = True):
         self.scene = scene
         self.L = lib()
         cfg = abi.RcConfig()
@@ -42,6 +42,7 @@ class Renderer:
         cfg.camera_seed = camera_seed
         cfg.autotune = int(autotune)
         cfg.graph_replay = int(graph_replay)
+        cfg.gpu_bvh = int(gpu_bvh)
         check(self.L.rc_set_config(C.byref(cfg)), "rc_set_config")
         self.args = InitArgs(scene)
         self.args.call(self.L.init)
@@ -56,6 +57,20 @@ class Renderer:
         info = (C.c_float * 9)()
         check(self.L.rc_prepare_host(info), "rc_prepare_host")
         return np.array(info, np.float32)
+
+    def scene_dump(self, which: int) -> np.ndarray:
+        """The scene arrays the kernels read (rc_scene_dump) as uint32 words."""
+        n = C.c_longlong(0)
+        check(self.L.rc_scene_dump(which, None, 0, C.byref(n)), "rc_scene_dump")
+        out = np.zeros(n.value, np.uint32)
+        check(self.L.rc_scene_dump(which, out.ctypes.data, n.value, C.byref(n)), "rc_scene_dump")
+        return out
+
+    def prepare_stats(self) -> dict:
+        a = np.zeros(5, np.float64)
+        self.L.rc_prepare_stats(a.ctypes.data, 5)
+        return {"mesh_bvh_ms": a[0], "device_bvh": bool(a[1]), "rest_ms": a[2], "mesh_nodes": int(a[3]),
+                "level_passes": int(a[4])}
 
     def render(self, iterations: int):
         check(self.L.rc_render(int(iterations)), "rc_render")
