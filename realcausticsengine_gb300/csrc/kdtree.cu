@@ -126,12 +126,20 @@ __global__ void __launch_bounds__(kThreads) k_bbox(Buffers B, int cur, int level
     __syncthreads();
     int mn[2][3], mx[2][3];
     for (int q = 0; q < 2; ++q) for (int k = 0; k < 3; ++k) { mn[q][k] = 0x7fffffff; mx[q][k] = (int)0x80000000; }
-    for (int it = 0; it < kItems; ++it) {
+    float px[kItems], py[kItems], pz[kItems];
+    int wh[kItems];
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {   // loads of all rounds in flight together
         long long i = a + it * kThreads + threadIdx.x;
-        if (i >= n) break;
-        int w = which(i, cn);
+        wh[it] = i < n ? which(i, cn) : -1;
+        const long long j = wh[it] >= 0 ? i : a;
+        px[it] = B.x[cur][j]; py[it] = B.y[cur][j]; pz[it] = B.z[cur][j];
+    }
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+        const int w = wh[it];
         if (w < 0) continue;
-        int vx = f2ord(B.x[cur][i]), vy = f2ord(B.y[cur][i]), vz = f2ord(B.z[cur][i]);
+        int vx = f2ord(px[it]), vy = f2ord(py[it]), vz = f2ord(pz[it]);
         if (w == 0) {
             mn[0][0] = min(mn[0][0], vx); mn[0][1] = min(mn[0][1], vy); mn[0][2] = min(mn[0][2], vz);
             mx[0][0] = max(mx[0][0], vx); mx[0][1] = max(mx[0][1], vy); mx[0][2] = max(mx[0][2], vz);
@@ -193,14 +201,29 @@ __global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level
     for (int k = threadIdx.x; k < 512; k += kThreads) (&sh[0][0])[k] = 0;
     __syncthreads();
     const int shift = 24 - 8 * pass;
+    // all rounds' coordinates first (independent loads in flight together), then bins
+    float val[kItems];
+    int wh[kItems];
+#pragma unroll
     for (int it = 0; it < kItems; ++it) {
         long long i = a + it * kThreads + threadIdx.x;
-        if (i >= n) break;
-        int w = which(i, cn);
-        if (w < 0) continue;
-        uint32_t key = f2key(coord(B, cur, i, ax[w]));
-        if (pass > 0 && (key >> (shift + 8)) != (pre[w] >> (shift + 8))) continue;
-        atomicAdd(&sh[w][(key >> shift) & 255u], 1u);
+        wh[it] = i < n ? which(i, cn) : -1;
+        val[it] = wh[it] >= 0 ? coord(B, cur, i, ax[wh[it]]) : 0.0f;
+    }
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {   // every lane runs every round (full-warp match)
+        unsigned slot = 0xffffffffu;
+        const int w = wh[it];
+        if (w >= 0) {
+            uint32_t key = f2key(val[it]);
+            if (pass == 0 || (key >> (shift + 8)) == (pre[w] >> (shift + 8)))
+                slot = (unsigned)w * 256u + ((key >> shift) & 255u);
+        }
+        // lanes with the same bin add once (the top digits of nearby coordinates
+        // coincide, so per-lane atomics would serialise on a few bins)
+        const unsigned peers = __match_any_sync(0xffffffffu, slot);
+        if (slot != 0xffffffffu && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1))
+            atomicAdd(&(&sh[0][0])[slot], (uint32_t)__popc(peers));
     }
     __syncthreads();
     for (int k = threadIdx.x; k < 512; k += kThreads) {
@@ -258,40 +281,13 @@ __global__ void k_select(long long count, long long first, int level, long long 
     }
 }
 
-// Block-wide exclusive scan of 6 per-thread counters.
-__device__ __forceinline__ void block_scan6(int (&v)[6], int (&excl)[6], int (&total)[6]) {
-    __shared__ int warp_sums[kThreads / 32][6];
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int incl[6];
-    for (int q = 0; q < 6; ++q) {
-        int x = v[q];
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        incl[q] = x;
-        if (lane == 31) warp_sums[wid][q] = x;
-    }
-    __syncthreads();
-    for (int q = 0; q < 6; ++q) {
-        int before = 0, tot = 0;
-        for (int w = 0; w < kThreads / 32; ++w) {
-            int s = warp_sums[w][q];
-            if (w < wid) before += s;
-            tot += s;
-        }
-        excl[q] = before + incl[q] - v[q];
-        total[q] = tot;
-    }
-    __syncthreads();
-}
-
 __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int level, long long n, long long first,
                                                         NodeSel* sel, uint2* nodes, int* err) {
     __shared__ ChunkNodes cn;
     __shared__ int ax[2], krem[2], eq[2];
     __shared__ uint32_t med[2];
     __shared__ int base[6];
+    __shared__ int woff[kItems][kThreads / 32][6];
     long long a = blockIdx.x * (long long)kChunk;
     if (threadIdx.x == 0) {
         chunk_nodes(a, level, n, cn);
@@ -304,44 +300,71 @@ __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int 
     }
     __syncthreads();
     const int dst = cur ^ 1;
-    // each thread owns kItems consecutive positions (deterministic ranks inside the CTA)
-    long long my0 = a + (long long)threadIdx.x * kItems;
-    int cnt[6] = {0, 0, 0, 0, 0, 0};
-    int cls[kItems];
+    // coalesced rounds of kThreads consecutive positions; the rank of a photon in its
+    // class (node A/B x below/equal/above) follows position order inside the CTA:
+    // ballots within a warp, then per-(round, warp) offsets
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    // the photons of all rounds are loaded once, up front (independent loads in flight
+    // together); position past n: -2, ancestor median (stays in place): -1
+    float px[kItems], py[kItems], pz[kItems];
+    uint32_t pid[kItems];
+    int cls[kItems], rank[kItems];
+#pragma unroll
     for (int it = 0; it < kItems; ++it) {
-        long long i = my0 + it;
-        cls[it] = -1;
-        if (i >= n) continue;
-        int w = which(i, cn);
-        if (w < 0) continue;
-        uint32_t key = f2key(coord(B, cur, i, ax[w]));
-        int c = key < med[w] ? 0 : (key == med[w] ? 1 : 2);
-        cls[it] = w * 3 + c;
-        cnt[w * 3 + c]++;
+        const long long i = a + it * kThreads + threadIdx.x;
+        const long long j = i < n ? i : a;
+        px[it] = B.x[cur][j]; py[it] = B.y[cur][j]; pz[it] = B.z[cur][j]; pid[it] = B.id[cur][j];
+        cls[it] = i < n ? which(i, cn) : -2;
     }
-    int excl[6], total[6];
-    block_scan6(cnt, excl, total);
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+        const int w = cls[it];   // node A (0) / B (1), or -1 / -2 as above
+        int q = w;
+        if (w >= 0) {
+            const int axw = ax[w];
+            const uint32_t key = f2key(axw == 0 ? px[it] : (axw == 1 ? py[it] : pz[it]));
+            q = w * 3 + (key < med[w] ? 0 : (key == med[w] ? 1 : 2));
+        }
+        cls[it] = q;
+        rank[it] = 0;
+#pragma unroll
+        for (int cq = 0; cq < 6; ++cq) {
+            const unsigned m = __ballot_sync(0xffffffffu, q == cq);
+            if (q == cq) rank[it] = __popc(m & lt_mask);
+            if (lane == 0) woff[it][wid][cq] = __popc(m);
+        }
+    }
+    __syncthreads();
     if (threadIdx.x < 6) {
-        int q = threadIdx.x;
+        const int q = threadIdx.x;
+        int run = 0;
+        for (int it = 0; it < kItems; ++it)
+            for (int w = 0; w < kThreads / 32; ++w) {
+                const int v = woff[it][w][q];
+                woff[it][w][q] = run;
+                run += v;
+            }
         long long e = q < 3 ? cn.eA : cn.eB;
-        base[q] = (e && total[q]) ? atomicAdd(&sel[e - first].cnt[q % 3], total[q]) : 0;
+        base[q] = (e && run) ? atomicAdd(&sel[e - first].cnt[q % 3], run) : 0;
     }
     __syncthreads();
     const long long c = cn.c;
     const long long k = c >> 1, odd = c & 1;
+#pragma unroll
     for (int it = 0; it < kItems; ++it) {
-        long long i = my0 + it;
-        if (i >= n) break;
+        long long i = a + it * kThreads + threadIdx.x;
         int q = cls[it];
-        float xv = B.x[cur][i], yv = B.y[cur][i], zv = B.z[cur][i];
-        uint32_t idv = B.id[cur][i];
+        if (q == -2) continue;
+        const float xv = px[it], yv = py[it], zv = pz[it];
+        const uint32_t idv = pid[it];
         long long d;
         if (q < 0) {
             d = i;   // ancestor median: stays in place
         } else {
             int w = q / 3, cl = q % 3;
             long long s = w == 0 ? cn.sA : cn.sB;
-            long long r = base[q] + excl[q]++;
+            long long r = base[q] + woff[it][wid][q] + rank[it];
             long long kl = krem[w];
             long long lt = k - kl;
             if (cl == 0) d = s + r;
