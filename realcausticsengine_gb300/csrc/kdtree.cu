@@ -401,21 +401,30 @@ __global__ void k_copy_medians(Buffers B, int src, int level0, long long n) {
 }
 
 // Shared-memory subtree builder: one CTA per node on level0 (at most kSmemSeg photons).
+// The photons are sorted once along x, y and z (three index lists; bitonic on the key
+// (coordinate, local index)).  Every level then reads each sub-node's extents (first
+// and last entry of each list) and its median (middle entry of the chosen axis's list)
+// off the lists, and splits all three lists stably into left / median / right.  A
+// sub-node of c photons has exactly c/2 photons on each side, so the rank of a photon
+// inside its sub-node's class is a block-wide prefix count minus s * (c/2).
 struct SmemLayout {
-    static constexpr size_t xs = 0;
+    static constexpr size_t xs = 0;                                  // photons by local index
     static constexpr size_t ys = xs + 4 * kSmemSeg;
     static constexpr size_t zs = ys + 4 * kSmemSeg;
     static constexpr size_t ids = zs + 4 * kSmemSeg;
-    static constexpr size_t tx = ids + 4 * kSmemSeg;              // temp copies
-    static constexpr size_t ty = tx + 4 * kSmemSeg;
-    static constexpr size_t tz = ty + 4 * kSmemSeg;
-    static constexpr size_t tid = tz + 4 * kSmemSeg;
-    static constexpr size_t v = tid + 4 * kSmemSeg;               // 2*kSmemSeg uint64 keys
-    static constexpr size_t box = v + 8 * 2 * kSmemSeg;           // kSmemSeg/2 * 6 ints
-    static constexpr size_t segs = box + 4 * 6 * (kSmemSeg / 2);  // sub-node starts: up to kSmemSeg (leaf level)
-    static constexpr size_t axes = segs + 4 * kSmemSeg;           // kSmemSeg/2 axes (levels with >= 2 photons)
-    static constexpr size_t total = axes + 4 * (kSmemSeg / 2);
+    static constexpr size_t v = ids + 4 * kSmemSeg;                  // 3 x kSmemSeg uint64 sort keys,
+    static constexpr size_t lists = v;                               // then 3 x kSmemSeg uint32 lists
+    static constexpr size_t temp = v + 4 * 3 * kSmemSeg;             // and 3 x kSmemSeg uint32 split output
+    static constexpr size_t cls = v + 8 * 3 * kSmemSeg;              // class per photon (0 left, 1 median, 2 right)
+    static constexpr size_t segs = cls + 4 * kSmemSeg;               // sub-node starts (up to kSmemSeg)
+    static constexpr size_t axes = segs + 4 * kSmemSeg;              // split axis per sub-node (up to kSmemSeg / 2)
+    static constexpr size_t warp = axes + 4 * (kSmemSeg / 2);        // block scan scratch
+    static constexpr size_t total = warp + 4 * 6 * (kSmemThreads / 32);
 };
+
+__device__ __forceinline__ float axis_coord(const float* X, const float* Y, const float* Z, int a, uint32_t q) {
+    return a == 0 ? X[q] : (a == 1 ? Y[q] : Z[q]);
+}
 
 __global__ void __launch_bounds__(kSmemThreads) k_smem_build(Buffers B, int src, int level0, long long n, uint2* nodes) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -423,27 +432,68 @@ __global__ void __launch_bounds__(kSmemThreads) k_smem_build(Buffers B, int src,
     float* Y = (float*)(smem + SmemLayout::ys);
     float* Z = (float*)(smem + SmemLayout::zs);
     uint32_t* I = (uint32_t*)(smem + SmemLayout::ids);
-    float* TX = (float*)(smem + SmemLayout::tx);
-    float* TY = (float*)(smem + SmemLayout::ty);
-    float* TZ = (float*)(smem + SmemLayout::tz);
-    uint32_t* TI = (uint32_t*)(smem + SmemLayout::tid);
     unsigned long long* V = (unsigned long long*)(smem + SmemLayout::v);
-    int* box = (int*)(smem + SmemLayout::box);
+    uint32_t* L = (uint32_t*)(smem + SmemLayout::lists);   // L[a * kSmemSeg + p]
+    uint32_t* T = (uint32_t*)(smem + SmemLayout::temp);
+    int* cls = (int*)(smem + SmemLayout::cls);
     int* segs = (int*)(smem + SmemLayout::segs);
     int* axes = (int*)(smem + SmemLayout::axes);
+    int (*wsum)[6] = (int (*)[6])(smem + SmemLayout::warp);
 
     const long long e0 = (1LL << level0) + blockIdx.x;
     const long long s0 = kd_node_start(e0, level0, n);
     const int c0 = (int)(n >> level0);
     const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, wid = tid >> 5;
     for (int i = tid; i < c0; i += nt) {
         X[i] = B.x[src][s0 + i]; Y[i] = B.y[src][s0 + i]; Z[i] = B.z[src][s0 + i]; I[i] = B.id[src][s0 + i];
     }
     __syncthreads();
+    // three sorted lists (padding keys ~0 sort last)
+    int pw = 1;
+    while (pw < c0) pw <<= 1;
+    const int nv3 = 3 * pw;
+    for (int v = tid; v < nv3; v += nt) {
+        const int a = v / pw, p = v - a * pw;
+        V[v] = p < c0 ? ((unsigned long long)f2key(axis_coord(X, Y, Z, a, p)) << 32) | (unsigned)p : ~0ull;
+    }
+    __syncthreads();
+    for (int k = 2; k <= pw; k <<= 1) {
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int i = tid; i < nv3; i += nt) {
+                const int l = i ^ jj;   // same list: pw is a power of two and lists are pw-aligned
+                if (l > i) {
+                    const bool up = ((i & k) == 0) || (k == pw);
+                    const unsigned long long a = V[i], b = V[l];
+                    if ((a > b) == up) { V[i] = b; V[l] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    {
+        // keys -> index lists (the lists overlay the keys: read all, then write)
+        constexpr int kPer = 3 * kSmemSeg / kSmemThreads;
+        uint32_t tmp[kPer];
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+            const int v = tid + r * nt;
+            tmp[r] = v < nv3 ? (uint32_t)(V[v] & 0xffffffffu) : 0u;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+            const int v = tid + r * nt;
+            if (v < nv3) {
+                const int a = v / pw, p = v - a * pw;
+                if (p < c0) L[a * kSmemSeg + p] = tmp[r];
+            }
+        }
+        __syncthreads();
+    }
     for (int j = 0;; ++j) {
         const int c = c0 >> j;
         const int nsub = 1 << j;
-        // sub-node starts (local)
         for (int s = tid; s < nsub; s += nt) {
             int st = 0, cc = c0;
             for (int b = j - 1; b >= 0; --b) {
@@ -455,117 +505,103 @@ __global__ void __launch_bounds__(kSmemThreads) k_smem_build(Buffers B, int src,
         }
         __syncthreads();
         if (c <= 1) {
-            for (int s = tid; s < nsub; s += nt) {
-                long long e = (e0 << j) + s;
-                nodes[e] = make_uint2(I[segs[s]], 0u);
-            }
+            for (int s = tid; s < nsub; s += nt) nodes[(e0 << j) + s] = make_uint2(I[L[segs[s]]], 0u);
             break;
         }
-        // extents per sub-node: a warp per sub-node when nodes are wide, a thread
-        // per sub-node when they are narrower than a warp
-        {
-            const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
-            if (c >= 32) {
-                for (int s = wid; s < nsub; s += nw) {
-                    int st = segs[s];
-                    int mn0 = 0x7fffffff, mn1 = 0x7fffffff, mn2 = 0x7fffffff;
-                    int mx0 = (int)0x80000000, mx1 = (int)0x80000000, mx2 = (int)0x80000000;
-                    for (int i = lane; i < c; i += 32) {
-                        int p = st + i;
-                        int a = f2ord(X[p]), b = f2ord(Y[p]), d = f2ord(Z[p]);
-                        mn0 = min(mn0, a); mn1 = min(mn1, b); mn2 = min(mn2, d);
-                        mx0 = max(mx0, a); mx1 = max(mx1, b); mx2 = max(mx2, d);
-                    }
-                    for (int o = 16; o > 0; o >>= 1) {
-                        mn0 = min(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
-                        mn1 = min(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
-                        mn2 = min(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
-                        mx0 = max(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
-                        mx1 = max(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
-                        mx2 = max(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
-                    }
-                    if (lane == 0) {
-                        int* b = box + 6 * s;
-                        b[0] = mn0; b[1] = mn1; b[2] = mn2; b[3] = mx0; b[4] = mx1; b[5] = mx2;
-                    }
-                }
-            } else {
-                for (int s = tid; s < nsub; s += nt) {
-                    int st = segs[s];
-                    int mn0 = 0x7fffffff, mn1 = 0x7fffffff, mn2 = 0x7fffffff;
-                    int mx0 = (int)0x80000000, mx1 = (int)0x80000000, mx2 = (int)0x80000000;
-                    for (int i = 0; i < c; ++i) {
-                        int p = st + i;
-                        int a = f2ord(X[p]), b = f2ord(Y[p]), d = f2ord(Z[p]);
-                        mn0 = min(mn0, a); mn1 = min(mn1, b); mn2 = min(mn2, d);
-                        mx0 = max(mx0, a); mx1 = max(mx1, b); mx2 = max(mx2, d);
-                    }
-                    int* b = box + 6 * s;
-                    b[0] = mn0; b[1] = mn1; b[2] = mn2; b[3] = mx0; b[4] = mx1; b[5] = mx2;
-                }
-            }
-        }
-        __syncthreads();
+        const int k = c >> 1, odd = c & 1;
+        // node records: extents and median read off the lists
         for (int s = tid; s < nsub; s += nt) {
-            const int* b = box + 6 * s;
-            axes[s] = biggest_axis(ord2f(b[3]) - ord2f(b[0]), ord2f(b[4]) - ord2f(b[1]), ord2f(b[5]) - ord2f(b[2]));
+            const int st = segs[s];
+            const float ex = X[L[st + c - 1]] - X[L[st]];
+            const float ey = Y[L[kSmemSeg + st + c - 1]] - Y[L[kSmemSeg + st]];
+            const float ez = Z[L[2 * kSmemSeg + st + c - 1]] - Z[L[2 * kSmemSeg + st]];
+            const int a = biggest_axis(ex, ey, ez);
+            const uint32_t q = L[a * kSmemSeg + st + k];
+            const float m = axis_coord(X, Y, Z, a, q);
+            const long long e = (e0 << j) + s;
+            if (odd) nodes[e] = make_uint2(I[q] | odd_mask(a), __float_as_uint(m));
+            else nodes[e] = make_uint2(even_mask(a), __float_as_uint(m + kSplitBias));
+            axes[s] = a;
         }
         __syncthreads();
-        // keys into the padded virtual array: nsub blocks of pw entries
-        int pw = 1;
-        while (pw < c) pw <<= 1;
-        const int nv = nsub * pw;
+        // class of every photon (0 left, 1 median, 2 right) from its place in its
+        // sub-node's axis list
+        const int nv = nsub * c;
         for (int v = tid; v < nv; v += nt) {
-            int s = v / pw, off = v % pw;
-            unsigned long long key = ~0ull;
-            if (off < c) {
-                int p = segs[s] + off;
-                int a = axes[s];
-                float f = a == 0 ? X[p] : (a == 1 ? Y[p] : Z[p]);
-                key = ((unsigned long long)f2key(f) << 32) | (unsigned)p;
-            }
-            V[v] = key;
+            const int s = v / c, off = v - s * c;
+            cls[L[axes[s] * kSmemSeg + segs[s] + off]] = off < k ? 0 : ((odd && off == k) ? 1 : 2);
         }
         __syncthreads();
-        // bitonic sort of each pw block, ascending
-        for (int k = 2; k <= pw; k <<= 1) {
-            for (int jj = k >> 1; jj > 0; jj >>= 1) {
-                for (int i = tid; i < nv; i += nt) {
-                    int l = i ^ jj;
-                    if (l > i) {
-                        bool up = ((i & k) == 0) || (k == pw);
-                        unsigned long long a = V[i], b = V[l];
-                        if ((a > b) == up) { V[i] = b; V[l] = a; }
-                    }
+        // stable split of the three lists: thread t takes positions v = 4t..4t+3 of the
+        // level's index space v -> (sub-node s = v / c, offset v % c)
+        int cnt[6] = {0, 0, 0, 0, 0, 0};
+        int cl[3][4];
+        uint32_t qq[3][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int v = 4 * tid + r;
+            const int s = v / c, off = v - s * c;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                cl[a][r] = -1;
+                if (v < nv) {
+                    const uint32_t q = L[a * kSmemSeg + segs[s] + off];
+                    qq[a][r] = q;
+                    cl[a][r] = cls[q];
+                    cnt[2 * a] += cl[a][r] == 0;
+                    cnt[2 * a + 1] += cl[a][r] == 2;
                 }
-                __syncthreads();
             }
         }
-        // node records (split from the rank-c/2 key) and the new order
-        for (int s = tid; s < nsub; s += nt) {
-            int k = c >> 1;
-            unsigned long long km = V[s * pw + k];
-            float m = key2f((uint32_t)(km >> 32));
-            long long e = (e0 << j) + s;
-            uint32_t p = (uint32_t)(km & 0xffffffffu);
-            if (c & 1) nodes[e] = make_uint2(I[p] | odd_mask(axes[s]), __float_as_uint(m));
-            else nodes[e] = make_uint2(even_mask(axes[s]), __float_as_uint(m + kSplitBias));
+        // block-wide exclusive prefix of the 6 counters
+        int excl[6];
+#pragma unroll
+        for (int u = 0; u < 6; ++u) {
+            int x = cnt[u];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            excl[u] = x - cnt[u];
+            if (lane == 31) wsum[wid][u] = x;
         }
-        for (int i = tid; i < c0; i += nt) { TX[i] = X[i]; TY[i] = Y[i]; TZ[i] = Z[i]; TI[i] = I[i]; }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 6; ++u) {
+            int before = 0;
+            for (int w = 0; w < wid; ++w) before += wsum[w][u];
+            excl[u] += before;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int v = 4 * tid + r;
+            if (v >= nv) break;
+            const int s = v / c;
+            const int st = segs[s];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const int c2 = cl[a][r];
+                int dst;
+                if (c2 == 0) dst = st + (excl[2 * a]++ - s * k);
+                else if (c2 == 1) dst = st + k;
+                else dst = st + k + odd + (excl[2 * a + 1]++ - s * k);
+                T[a * kSmemSeg + dst] = qq[a][r];
+            }
+        }
         __syncthreads();
         for (int v = tid; v < nv; v += nt) {
-            int s = v / pw, off = v % pw;
-            if (off < c) {
-                int p = segs[s] + off;
-                uint32_t q = (uint32_t)(V[v] & 0xffffffffu);
-                X[p] = TX[q]; Y[p] = TY[q]; Z[p] = TZ[q]; I[p] = TI[q];
-            }
+            const int s = v / c, p = segs[s] + (v - s * c);
+            L[p] = T[p];
+            L[kSmemSeg + p] = T[kSmemSeg + p];
+            L[2 * kSmemSeg + p] = T[2 * kSmemSeg + p];
         }
         __syncthreads();
     }
     __syncthreads();
     for (int i = tid; i < c0; i += nt) {
-        B.x[0][s0 + i] = X[i]; B.y[0][s0 + i] = Y[i]; B.z[0][s0 + i] = Z[i]; B.id[0][s0 + i] = I[i];
+        const uint32_t q = L[i];
+        B.x[0][s0 + i] = X[q]; B.y[0][s0 + i] = Y[q]; B.z[0][s0 + i] = Z[q]; B.id[0][s0 + i] = I[q];
     }
 }
 
