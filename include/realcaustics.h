@@ -166,6 +166,20 @@ int rc_host_world_bvh(unsigned* nodes, int cap, int* index, int index_cap);
  * `cap` words; *words receives the full size.  No counterpart in the reference. */
 int rc_scene_dump(int which, unsigned* out, long long cap, long long* words);
 
+/* Contexts (no counterpart in the reference, whose state is one global `scene`).  Every
+ * entry point acts on the context bound to the calling thread, or on the process's
+ * default context when the thread has bound none - so a caller that never binds sees
+ * the reference's single global scene, from any thread.  A thread that binds its own
+ * context holds its own scene, configuration, last error and device buffers (and a CUDA
+ * stream): scenes in different contexts render concurrently from different threads.
+ * Autotuner choices are shared by all contexts.  rc_context_bind(NULL) returns the
+ * thread to the default context.  rc_context_destroy releases the context's scene and
+ * device memory; it must not be bound or in use on another thread. */
+typedef struct rc_context rc_context;
+rc_context* rc_context_create(void);
+int rc_context_bind(rc_context* ctx);
+int rc_context_destroy(rc_context* ctx);
+
 /* Timing of the last rc_prepare: out[0] = mesh BVH build ms (host or device, uploads
  * included), out[1] = 1 if the device built the mesh BVHs, out[2] = world BVH + light
  * + material conversion + remaining uploads ms, out[3] = mesh BVH nodes, out[4] = device

@@ -57,6 +57,10 @@ def lib() -> C.CDLL:
     L.rc_load_state.argtypes = [C.c_char_p]
     L.rc_scene_dump.argtypes = [C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_prepare_stats.argtypes = [C.c_void_p, C.c_int]
+    L.rc_context_create.restype = C.c_void_p
+    L.rc_context_create.argtypes = []
+    L.rc_context_bind.argtypes = [C.c_void_p]
+    L.rc_context_destroy.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -72,4 +76,5 @@ EXPORTS = ["init", "main", "rc_default_config", "rc_set_config", "rc_prepare", "
            "rc_last_error", "rc_get_stats", "rc_trace_rays", "rc_trace_rays_full", "rc_kd_query",
            "rc_kd_build_nodes", "rc_light_photons", "rc_render_timed", "rc_kd_build_noalloc",
            "rc_kd_noalloc_last_error", "rc_proposal_state", "rc_render_debug",
-           "rc_save_state", "rc_load_state", "rc_scene_dump", "rc_prepare_stats"]
+           "rc_save_state", "rc_load_state", "rc_scene_dump", "rc_prepare_stats",
+           "rc_context_create", "rc_context_bind", "rc_context_destroy"]

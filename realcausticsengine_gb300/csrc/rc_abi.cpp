@@ -3,11 +3,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -21,16 +23,12 @@ namespace rc {
 
 namespace {
 
-std::string g_err;
-std::unique_ptr<HostScene> g_scene;
-rc_config g_cfg;
-bool g_cfg_set = false;
 
 #define RC_CUDA(call)                                                                   \
     do {                                                                                \
         cudaError_t e_ = (call);                                                        \
         if (e_ != cudaSuccess) {                                                        \
-            g_err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+            ctx().err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
             return RC_E_CUDA;                                                           \
         }                                                                               \
     } while (0)
@@ -90,12 +88,6 @@ struct DeviceState {
     DevBuf<unsigned> train_count;
     cudaEvent_t evm[2] = {};
     cudaEvent_t evg[2] = {};    // around the gather kernel alone
-    // gather autotuner: chosen launch variant per query-count class (log2), -1 = untuned;
-    // kept for the life of the process (a new scene reuses the choices)
-    int gather_variant[64] = {};
-    int light_variant[64] = {};
-    int camera_variant[64] = {};
-    double gather_variant_ms[64][8];
     DevBuf<double> tune_accum;
     // asynchronous iterations (graph replay): fixed capacities, launch shapes and a
     // per-iteration overflow flag; the instantiated graph is updated in place
@@ -146,7 +138,37 @@ struct DeviceState {
     }
 };
 
-DeviceState g_dev;
+// Autotuner choices: launch variant per size class (log2 of light paths, pixels or
+// queries), -1 = untuned.  Kept for the process and shared by every context (a new
+// scene, or a scene in another context, reuses them).
+struct TuneTables {
+    std::atomic<int> light[64], camera[64], gather[64];
+    TuneTables() {
+        for (int i = 0; i < 64; ++i) { light[i] = -1; camera[i] = -1; gather[i] = -1; }
+    }
+};
+TuneTables g_tune;
+
+// Everything one scene needs: the reference's global `scene` plus the device state.
+// Entry points act on the context bound to the calling thread (rc_context_bind), or on
+// the process's default context when none is bound.
+struct Context {
+    std::string err;
+    std::unique_ptr<HostScene> scene;
+    rc_config cfg;
+    bool cfg_set = false;
+    DeviceState dev;
+    bool host_ready = false;
+    double prep[5] = {};                   // rc_prepare_stats
+    std::unique_ptr<GpuBvhBuilder> bvh;    // device BVH scratch, kept for the context (grow-only)
+};
+
+Context& default_ctx() {
+    static Context* c = new Context();   // never destroyed: no device frees at exit
+    return *c;
+}
+thread_local Context* t_bound = nullptr;
+Context& ctx() { return t_bound ? *t_bound : default_ctx(); }
 
 void default_config(rc_config* c) {
     std::memset(c, 0, sizeof(*c));
@@ -169,8 +191,8 @@ void default_config(rc_config* c) {
 }
 
 const rc_config& cfg() {
-    if (!g_cfg_set) { default_config(&g_cfg); g_cfg_set = true; }
-    return g_cfg;
+    if (!ctx().cfg_set) { default_config(&ctx().cfg); ctx().cfg_set = true; }
+    return ctx().cfg;
 }
 
 template <class T>
@@ -188,19 +210,12 @@ inline float4 f4(float x, float y, float z, uint32_t w) {
 
 // Stream, events and the process-lifetime autotuner tables.
 int ensure_device() {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     if (!d.stream) {
         RC_CUDA(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
         for (auto& e : d.ev) RC_CUDA(cudaEventCreate(&e));
         for (auto& e : d.evm) RC_CUDA(cudaEventCreate(&e));
         for (auto& e : d.evg) RC_CUDA(cudaEventCreate(&e));
-        static bool tables_ready = false;   // autotuner choices live for the process
-        if (!tables_ready) {
-            for (int& v : d.gather_variant) v = -1;
-            for (int& v : d.light_variant) v = -1;
-            for (int& v : d.camera_variant) v = -1;
-            tables_ready = true;
-        }
         RC_CUDA(cudaEventCreate(&d.t0));
         RC_CUDA(cudaEventCreate(&d.t1));
     }
@@ -209,7 +224,7 @@ int ensure_device() {
 
 // Mesh BVH nodes and triangle records from the host build, packed and uploaded.
 int upload_meshes_host(HostScene& sc, std::vector<int>& mesh_root) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     std::vector<float4> nlo, nhi, v0, e1, e2, n0, n1, n2;
     mesh_root.clear();
     uint32_t node_base = 0, tri_base = 0, tri_global = 0;
@@ -255,7 +270,7 @@ int upload_meshes_host(HostScene& sc, std::vector<int>& mesh_root) {
 
 // World BVH, mesh roots, lights and materials; the scene view the kernels read.
 int upload_scene_rest(HostScene& sc, const std::vector<int>& mesh_root) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     std::vector<float4> wlo, whi;
     for (const BvhNode& nd : sc.world.nodes) {
         wlo.push_back(f4(nd.box.mn.x, nd.box.mn.y, nd.box.mn.z, nd.w0));
@@ -285,28 +300,26 @@ int upload_scene_rest(HostScene& sc, const std::vector<int>& mesh_root) {
     return RC_OK;
 }
 
-bool g_host_ready = false;
-double g_prep[5] = {};   // rc_prepare_stats
 
 // The host steps of main() after the mesh BVHs (src/main.cpp:150-168).
 int finish_host(HostScene& sc) {
     build_world_bvh(sc);
     // init_lights + update_pdf_distribution (src/main.cpp:160-163)
-    int r = convert_lights(sc, g_err);
+    int r = convert_lights(sc, ctx().err);
     if (r) return r;
     convert_materials(sc);
     // base_radius *= SceneRadius (src/main.cpp:166-168)
     sc.base_radius *= sc.scene_radius;
-    g_host_ready = true;
+    ctx().host_ready = true;
     return RC_OK;
 }
 
 // Host half of the pre-render steps of main() (src/main.cpp:150-168).
 int prepare_host() {
-    if (!g_scene) { g_err = "no scene: init() was not called"; return RC_E_NO_SCENE; }
-    HostScene& sc = *g_scene;
-    if (g_host_ready) return RC_OK;
-    if (sc.meshes.empty()) { g_err = "scene has no meshes"; return RC_E_INVALID; }
+    if (!ctx().scene) { ctx().err = "no scene: init() was not called"; return RC_E_NO_SCENE; }
+    HostScene& sc = *ctx().scene;
+    if (ctx().host_ready) return RC_OK;
+    if (sc.meshes.empty()) { ctx().err = "scene has no meshes"; return RC_E_INVALID; }
     // Scene::update_bvh (src/Scene.cpp:110-152)
     for (HostMesh& m : sc.meshes) build_mesh_bvh(m);
     return finish_host(sc);
@@ -319,7 +332,7 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 // Mesh BVHs built on the device (bvh_build.cu) straight into the scene arrays.  Leaves
 // sc.prepared false when the input needs the host build.
 int prepare_device_bvh(HostScene& sc) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     if (sc.meshes.empty()) return RC_OK;
     const auto t0 = std::chrono::steady_clock::now();
     int r = ensure_device();
@@ -327,20 +340,21 @@ int prepare_device_bvh(HostScene& sc) {
     std::vector<GpuMeshSrc> src;
     for (const HostMesh& hm : sc.meshes)
         src.push_back({hm.wpos.data(), hm.wnrm.data(), hm.tri.data(), hm.mat.data(), hm.num_verts, hm.num_tris});
-    // scratch kept for the process (grow-only): a batch of scenes allocates it once;
-    // never destroyed (no device frees during static destruction at exit)
-    static GpuBvhBuilder& bld = *new GpuBvhBuilder();
+    // scratch kept for the context (grow-only): a batch of scenes loaded one after the
+    // other into one context allocates it once
+    if (!ctx().bvh) ctx().bvh = std::make_unique<GpuBvhBuilder>();
+    GpuBvhBuilder& bld = *ctx().bvh;
     bool supported = false;
     std::string err;
     r = bld.build(src, d.stream, supported, err);
-    if (r) { g_err = err; return r; }
+    if (r) { ctx().err = err; return r; }
     if (!supported) return RC_OK;
     RC_CUDA(d.node_lo.reserve(bld.num_nodes())); RC_CUDA(d.node_hi.reserve(bld.num_nodes()));
     DevBuf<float4>* tb[] = {&d.tri_v0, &d.tri_e1, &d.tri_e2, &d.tri_n0, &d.tri_n1, &d.tri_n2};
     for (auto* b : tb) RC_CUDA(b->reserve(bld.num_tris()));
     r = bld.emit(d.node_lo.p, d.node_hi.p, d.tri_v0.p, d.tri_e1.p, d.tri_e2.p, d.tri_n0.p, d.tri_n1.p, d.tri_n2.p,
                  d.stream, err);
-    if (r) { g_err = err; return r; }
+    if (r) { ctx().err = err; return r; }
     d.num_mesh_nodes = bld.num_nodes();
     d.num_tris = bld.num_tris();
     for (size_t m = 0; m < sc.meshes.size(); ++m) {
@@ -354,31 +368,31 @@ int prepare_device_bvh(HostScene& sc) {
     }
     const std::vector<int> roots = bld.mesh_root;
     const int levels = bld.levels;
-    g_prep[0] = ms_since(t0);
-    g_prep[1] = 1.0;
-    g_prep[3] = (double)d.num_mesh_nodes;
-    g_prep[4] = levels;
+    ctx().prep[0] = ms_since(t0);
+    ctx().prep[1] = 1.0;
+    ctx().prep[3] = (double)d.num_mesh_nodes;
+    ctx().prep[4] = levels;
     const auto t1 = std::chrono::steady_clock::now();
     r = finish_host(sc);
     if (r) return r;
     r = upload_scene_rest(sc, roots);
     if (r) return r;
-    g_prep[2] = ms_since(t1);
+    ctx().prep[2] = ms_since(t1);
     sc.prepared = true;
     return RC_OK;
 }
 
 int prepare() {
-    if (!g_scene) { g_err = "no scene: init() was not called"; return RC_E_NO_SCENE; }
-    HostScene& sc = *g_scene;
+    if (!ctx().scene) { ctx().err = "no scene: init() was not called"; return RC_E_NO_SCENE; }
+    HostScene& sc = *ctx().scene;
     if (sc.prepared) return RC_OK;
-    if (cfg().gpu_bvh && !g_host_ready) {
+    if (cfg().gpu_bvh && !ctx().host_ready) {
         int r = prepare_device_bvh(sc);
         if (r) return r;
         if (sc.prepared) return RC_OK;
     }
     const auto t0 = std::chrono::steady_clock::now();
-    const bool built_here = !g_host_ready;
+    const bool built_here = !ctx().host_ready;
     int r = prepare_host();
     if (r) return r;
     r = ensure_device();
@@ -386,33 +400,33 @@ int prepare() {
     std::vector<int> roots;
     r = upload_meshes_host(sc, roots);
     if (r) return r;
-    g_prep[0] = built_here ? ms_since(t0) : 0.0;
-    g_prep[1] = 0.0;
-    g_prep[3] = (double)g_dev.num_mesh_nodes;
-    g_prep[4] = 0.0;
+    ctx().prep[0] = built_here ? ms_since(t0) : 0.0;
+    ctx().prep[1] = 0.0;
+    ctx().prep[3] = (double)ctx().dev.num_mesh_nodes;
+    ctx().prep[4] = 0.0;
     const auto t1 = std::chrono::steady_clock::now();
     r = upload_scene_rest(sc, roots);
     if (r) return r;
-    g_prep[2] = ms_since(t1);
+    ctx().prep[2] = ms_since(t1);
     sc.prepared = true;
     return RC_OK;
 }
 
 int check_errors() {
     int h[ERR_COUNT];
-    RC_CUDA(cudaMemcpy(h, g_dev.errors.p, sizeof(h), cudaMemcpyDeviceToHost));
-    if (h[ERR_STACK]) { g_err = "BVH traversal stack overflow (depth > 64)"; return RC_E_CAPACITY; }
-    if (h[ERR_MATERIAL]) { g_err = "triangle material index out of range"; return RC_E_INVALID; }
-    if (h[ERR_KD]) { g_err = "KD-tree build found inconsistent counts"; return RC_E_INVALID; }
-    if (h[ERR_MLP]) { g_err = "tensor-core pipeline wait timed out in the MLP"; return RC_E_CUDA; }
+    RC_CUDA(cudaMemcpy(h, ctx().dev.errors.p, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h[ERR_STACK]) { ctx().err = "BVH traversal stack overflow (depth > 64)"; return RC_E_CAPACITY; }
+    if (h[ERR_MATERIAL]) { ctx().err = "triangle material index out of range"; return RC_E_INVALID; }
+    if (h[ERR_KD]) { ctx().err = "KD-tree build found inconsistent counts"; return RC_E_INVALID; }
+    if (h[ERR_MLP]) { ctx().err = "tensor-core pipeline wait timed out in the MLP"; return RC_E_CUDA; }
     return RC_OK;
 }
 
 VMParams make_params(const HostScene& sc, int iteration) {
     VMParams p{};
-    p.scene = g_dev.view;
-    p.lights = LightsView{g_dev.lights.p, g_dev.cdf.p, (int)sc.lights.size(), sc.light_integral};
-    p.materials = g_dev.materials.p;
+    p.scene = ctx().dev.view;
+    p.lights = LightsView{ctx().dev.lights.p, ctx().dev.cdf.p, (int)sc.lights.size(), sc.light_integral};
+    p.materials = ctx().dev.materials.p;
     p.num_materials = (int)sc.materials.size();
     const HostCamera& c = sc.camera;
     p.camera.width = c.width; p.camera.height = c.height;
@@ -434,7 +448,7 @@ VMParams make_params(const HostScene& sc, int iteration) {
     float radius_sqr = radius * radius;
     p.radius_sqr = radius_sqr;
     p.vm_norm = 1.0f / (PI * radius_sqr * light_paths_count);
-    p.error = g_dev.errors.p;
+    p.error = ctx().dev.errors.p;
     return p;
 }
 
@@ -478,20 +492,20 @@ constexpr int kTrainCapacity = 1 << 20;
 // Before the light pass: make sure the network exists and, once it has been trained,
 // write every light path's proposed emission direction and weight.
 int proposal_before(const HostScene& sc, VMParams& p, bool train) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
     const long long n = p.num_light_paths;
     if (!d.mlp) {
         d.mlp = std::make_unique<MlpStore>();
-        if (!d.mlp->setup(kTrainBatchRows)) { g_err = "MLP allocation failed"; return RC_E_CUDA; }
-        if (mlp_init(d.mlp->p, cfg().seed ^ 0x9E3779B97F4A7C15ull, s)) { g_err = "MLP init failed"; return RC_E_CUDA; }
+        if (!d.mlp->setup(kTrainBatchRows)) { ctx().err = "MLP allocation failed"; return RC_E_CUDA; }
+        if (mlp_init(d.mlp->p, cfg().seed ^ 0x9E3779B97F4A7C15ull, s)) { ctx().err = "MLP init failed"; return RC_E_CUDA; }
         RC_CUDA(d.train_pos.reserve(kTrainCapacity)); RC_CUDA(d.train_dir.reserve(kTrainCapacity));
         RC_CUDA(d.train_count.reserve(1)); RC_CUDA(d.train_wsum.reserve(1));
     }
     if (d.mlp_rounds > 0) {
         RC_CUDA(d.prop.reserve(std::max<long long>(n, 1)));
         if (mlp_proposal(d.mlp->p, proposal_ctx(sc, p), n, d.prop.p, s, d.errors.p + ERR_MLP)) {
-            g_err = "proposal launch failed"; return RC_E_CUDA;
+            ctx().err = "proposal launch failed"; return RC_E_CUDA;
         }
         p.proposal = d.prop.p;
     }
@@ -507,7 +521,7 @@ int proposal_before(const HostScene& sc, VMParams& p, bool train) {
 // After the gather: collect (position, direction, weight) of the paths that reached the
 // image and take Adam steps on them.
 int proposal_train(const HostScene& sc, const VMParams& p) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
     unsigned rows = 0;
     mlp_collect(proposal_ctx(sc, p), p.num_light_paths, d.contrib.p, p.proposal, kTrainCapacity, d.train_pos.p,
@@ -521,7 +535,7 @@ int proposal_train(const HostScene& sc, const VMParams& p) {
     mlp_normalize_weights(d.train_dir.p, total, d.train_wsum.p, s);
     if (mlp_train(d.mlp->p, d.mlp->b, d.train_pos.p, d.train_dir.p, total, cfg().train_steps, cfg().learning_rate, s,
                   d.errors.p + ERR_MLP)) {
-        g_err = "MLP training launch failed"; return RC_E_CUDA;
+        ctx().err = "MLP training launch failed"; return RC_E_CUDA;
     }
     RC_CUDA(cudaGetLastError());
     d.mlp_rounds++;
@@ -532,7 +546,7 @@ int proposal_train(const HostScene& sc, const VMParams& p) {
 // `run(v)` must reset whatever the pass appends to) and return the fastest.
 template <class Run>
 int autotune_variants(int nvariants, Run&& run, const char* what, long long size) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     float best = 1e30f;
     int best_v = 0;
     for (int v = 0; v < nvariants; ++v) {
@@ -556,7 +570,7 @@ int size_class(long long n) { return n > 0 ? 63 - __builtin_clzll((unsigned long
 // overflow).  redo_iteration >= 0 renders that iteration index again without counting
 // it (an iteration an asynchronous replay had to skip).
 int render_iteration(HostScene& sc, int redo_iteration = -1) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
     const int it = redo_iteration >= 0 ? redo_iteration : d.iterations_done;
     VMParams p = make_params(sc, it);
@@ -589,13 +603,13 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         }
         int lvar = 0;
         if (sampler == RC_SAMPLER_UNIFORM && cfg().autotune) {
-            int& slot = d.light_variant[size_class(p.num_light_paths)];
-            if (slot < 0)
+            std::atomic<int>& slot = g_tune.light[size_class(p.num_light_paths)];
+            if (slot.load() < 0)
                 slot = autotune_variants(pass_variants(), [&](int v) {
                     cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s);
                     launch_light_pass(p, ph, d.counters.p + 6, s, v);
                 }, "light pass", p.num_light_paths);
-            lvar = slot;
+            lvar = slot.load();
             RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         }
         RC_CUDA(cudaEventRecord(d.ev[0], s));
@@ -611,7 +625,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         if (learned) t_mlp = ms_between(d.evm[0], d.evm[1]);
         if ((long long)nph <= cap) break;
         cap = (long long)nph + nph / 8 + 1024;
-        if (attempt == 2) { g_err = "photon buffer overflow"; return RC_E_CAPACITY; }
+        if (attempt == 2) { ctx().err = "photon buffer overflow"; return RC_E_CAPACITY; }
     }
     int r = check_errors();
     if (r) return r;
@@ -634,7 +648,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     int kd_launches = 0;
     RC_CUDA(cudaEventRecord(d.ev[2], s));
     if (kd_build(d.ph_pos.p, n, tree, d.kd_scratch.p, d.kd_scratch.n, s, &kd_launches, d.errors.p + ERR_KD)) {
-        g_err = "KD scratch too small"; return RC_E_CAPACITY;
+        ctx().err = "KD scratch too small"; return RC_E_CAPACITY;
     }
     RC_CUDA(cudaGetLastError());
     RC_CUDA(d.tp0.reserve(std::max<long long>(n, 1))); RC_CUDA(d.tp1.reserve(std::max<long long>(n, 1)));
@@ -666,13 +680,13 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qcap, d.counters.p + 1};
         int cvar = 0;
         if (cfg().autotune) {
-            int& slot = d.camera_variant[size_class(npix)];
-            if (slot < 0)
+            std::atomic<int>& slot = g_tune.camera[size_class(npix)];
+            if (slot.load() < 0)
                 slot = autotune_variants(pass_variants(), [&](int v) {
                     cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s);
                     launch_camera_pass(p, qb, d.counters.p + 7, s, v);
                 }, "camera pass", npix);
-            cvar = slot;
+            cvar = slot.load();
             RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s));
         }
         RC_CUDA(cudaEventRecord(d.ev[4], s));
@@ -684,7 +698,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         t_cam = ms_between(d.ev[4], d.ev[5]);
         if ((long long)nq <= qcap) break;
         qcap = (long long)nq + nq / 8 + 1024;
-        if (attempt == 2) { g_err = "query buffer overflow"; return RC_E_CAPACITY; }
+        if (attempt == 2) { ctx().err = "query buffer overflow"; return RC_E_CAPACITY; }
     }
     r = check_errors();
     if (r) return r;
@@ -699,7 +713,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     int variant = 3;
     if (cfg().autotune && nq > 0) {
         const int cls = 63 - __builtin_clzll((unsigned long long)nq);
-        if (d.gather_variant[cls] < 0) {
+        if (g_tune.gather[cls].load() < 0) {
             // time every launch shape on this iteration's queries into a scratch image
             // (warm-up launch first: the first launch of a shape loads its code)
             RC_CUDA(d.tune_accum.reserve(std::max<long long>(3 * npix, 1)));
@@ -712,15 +726,14 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
                 RC_CUDA(cudaEventRecord(d.evm[1], s));
                 RC_CUDA(cudaEventSynchronize(d.evm[1]));
                 const float ms = ms_between(d.evm[0], d.evm[1]);
-                if (v < 8) d.gather_variant_ms[cls][v] = ms;
                 if (ms < best) { best = ms; best_v = v; }
             }
-            d.gather_variant[cls] = best_v;
+            g_tune.gather[cls] = best_v;
             if (cfg().verbose)
                 std::printf("{\"autotune\": \"gather\", \"queries\": %llu, \"variant\": \"%s\", \"ms\": %.3f}\n",
                             nq, gather_variant_name(best_v), best);
         }
-        variant = d.gather_variant[cls];
+        variant = g_tune.gather[cls].load();
     }
     RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
     RC_CUDA(cudaEventRecord(d.evg[0], s));
@@ -793,7 +806,7 @@ bool async_eligible() {
 }
 
 int async_setup(const HostScene& sc) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     const long long npix = (long long)sc.camera.width * sc.camera.height;
     // capacities: the last measured counts with a 2% + 4096 margin, 1024-aligned (the
     // counts of a configuration vary by ~0.1% between iterations)
@@ -823,16 +836,16 @@ int async_setup(const HostScene& sc) {
     RC_CUDA(d.qscratch.reserve(query_order_scratch_bytes(d.async_qcap, t)));
     RC_CUDA(d.accum.reserve(3 * npix));
     auto var = [](int v, int dflt) { return v >= 0 ? v : dflt; };
-    d.async_lvar = var(d.light_variant[size_class(cfg().photons_per_iter > 0 ? cfg().photons_per_iter : npix)], 0);
-    d.async_cvar = var(d.camera_variant[size_class(npix)], 0);
-    d.async_gvar = var(d.gather_variant[size_class((long long)d.last_queries)], 3);
+    d.async_lvar = var(g_tune.light[size_class(cfg().photons_per_iter > 0 ? cfg().photons_per_iter : npix)].load(), 0);
+    d.async_cvar = var(g_tune.camera[size_class(npix)].load(), 0);
+    d.async_gvar = var(g_tune.gather[size_class((long long)d.last_queries)].load(), 3);
     if (!cfg().autotune) d.async_lvar = d.async_cvar = 0, d.async_gvar = 3;
     return RC_OK;
 }
 
 // Enqueue iteration `it` (no host synchronisation); `flag` receives the overflow flag.
 int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
     VMParams p = make_params(sc, it);
     const long long pc = d.async_pcap, qc = d.async_qcap;
@@ -855,7 +868,7 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     RC_CUDA(record(d.ev[2], s));
     int kl = 0;
     if (kd_build(d.ph_pos.p, pc, tree, d.kd_scratch.p, d.kd_scratch.n, s, &kl, d.errors.p + ERR_KD)) {
-        g_err = "KD scratch too small"; return RC_E_CAPACITY;
+        ctx().err = "KD scratch too small"; return RC_E_CAPACITY;
     }
     TreePhotons tph{d.tp0.p, d.tp1.p, d.tp2.p};
     tree.box_levels = kd_box_levels(pc);
@@ -885,7 +898,7 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
 // Capture iteration `it` as a graph, update the instantiated graph with it (or
 // instantiate it) and launch it.
 int launch_async_iteration(HostScene& sc, int it, int* flag) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
     RC_CUDA(cudaGetLastError());
     RC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
@@ -896,10 +909,10 @@ int launch_async_iteration(HostScene& sc, int it, int* flag) {
     if (r) { if (graph) cudaGraphDestroy(graph); return r; }
     if (le != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
-        g_err = std::string("kernel launch while recording an iteration: ") + cudaGetErrorString(le);
+        ctx().err = std::string("kernel launch while recording an iteration: ") + cudaGetErrorString(le);
         return RC_E_CUDA;
     }
-    if (e != cudaSuccess) { g_err = std::string("graph capture: ") + cudaGetErrorString(e); return RC_E_CUDA; }
+    if (e != cudaSuccess) { ctx().err = std::string("graph capture: ") + cudaGetErrorString(e); return RC_E_CUDA; }
     if (d.graph_exec) {
         cudaGraphExecUpdateResultInfo info;
         if (cudaGraphExecUpdate(d.graph_exec, graph, &info) != cudaSuccess) {
@@ -910,7 +923,7 @@ int launch_async_iteration(HostScene& sc, int it, int* flag) {
     }
     if (!d.graph_exec) {
         e = cudaGraphInstantiate(&d.graph_exec, graph, 0);
-        if (e != cudaSuccess) { cudaGraphDestroy(graph); g_err = std::string("graph instantiate: ") + cudaGetErrorString(e); return RC_E_CUDA; }
+        if (e != cudaSuccess) { cudaGraphDestroy(graph); ctx().err = std::string("graph instantiate: ") + cudaGetErrorString(e); return RC_E_CUDA; }
     }
     cudaGraphDestroy(graph);
     RC_CUDA(cudaGraphLaunch(d.graph_exec, s));
@@ -921,7 +934,7 @@ int launch_async_iteration(HostScene& sc, int it, int* flag) {
 // `iterations` progressive iterations: the first with host round trips, the rest
 // replayed asynchronously when eligible; overflowed iterations are rendered again.
 int render_iterations(HostScene& sc, int iterations) {
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     int r = RC_OK;
     int i = 0;
     if (!async_eligible()) {
@@ -1006,8 +1019,8 @@ int render_iterations(HostScene& sc, int iterations) {
 
 // Debug view `mode` (2-4) into the image accumulation, counted as one iteration.
 int render_debug(HostScene& sc, int mode) {
-    if (mode < 2 || mode > 4) { g_err = "debug view must be 2 (normals), 3 (facing) or 4 (materials)"; return RC_E_INVALID; }
-    DeviceState& d = g_dev;
+    if (mode < 2 || mode > 4) { ctx().err = "debug view must be 2 (normals), 3 (facing) or 4 (materials)"; return RC_E_INVALID; }
+    DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
     VMParams p = make_params(sc, 0);
     const long long npix = (long long)sc.camera.width * sc.camera.height;
@@ -1061,10 +1074,10 @@ struct StateHeader {
 };
 
 int save_state(const char* path) {
-    if (!g_scene || !g_scene->prepared) { g_err = "save_state: no prepared scene"; return RC_E_NO_SCENE; }
-    if (!path) { g_err = "save_state: null path"; return RC_E_INVALID; }
-    const HostScene& sc = *g_scene;
-    DeviceState& d = g_dev;
+    if (!ctx().scene || !ctx().scene->prepared) { ctx().err = "save_state: no prepared scene"; return RC_E_NO_SCENE; }
+    if (!path) { ctx().err = "save_state: null path"; return RC_E_INVALID; }
+    const HostScene& sc = *ctx().scene;
+    DeviceState& d = ctx().dev;
     const size_t npix = (size_t)sc.camera.width * sc.camera.height;
     StateHeader h{};
     std::memcpy(h.magic, kStateMagic, 8);
@@ -1085,25 +1098,25 @@ int save_state(const char* path) {
     if (d.accum.p && d.accum.n >= 3 * npix)
         RC_CUDA(cudaMemcpy(acc.data(), d.accum.p, acc.size() * sizeof(double), cudaMemcpyDeviceToHost));
     std::vector<float> ml(h.mlp_floats);
-    if (h.mlp_floats && mlp_export(d.mlp->p, ml.data())) { g_err = "save_state: MLP read-back failed"; return RC_E_CUDA; }
+    if (h.mlp_floats && mlp_export(d.mlp->p, ml.data())) { ctx().err = "save_state: MLP read-back failed"; return RC_E_CUDA; }
     FILE* f = std::fopen(path, "wb");
-    if (!f) { g_err = std::string("cannot open ") + path; return RC_E_IO; }
+    if (!f) { ctx().err = std::string("cannot open ") + path; return RC_E_IO; }
     bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
               std::fwrite(acc.data(), sizeof(double), acc.size(), f) == acc.size() &&
               std::fwrite(ml.data(), sizeof(float), ml.size(), f) == ml.size();
     ok = (std::fclose(f) == 0) && ok;
-    if (!ok) { g_err = std::string("write failed: ") + path; return RC_E_IO; }
+    if (!ok) { ctx().err = std::string("write failed: ") + path; return RC_E_IO; }
     return RC_OK;
 }
 
 int load_state(const char* path) {
     int r = prepare();
     if (r) return r;
-    if (!path) { g_err = "load_state: null path"; return RC_E_INVALID; }
-    const HostScene& sc = *g_scene;
-    DeviceState& d = g_dev;
+    if (!path) { ctx().err = "load_state: null path"; return RC_E_INVALID; }
+    const HostScene& sc = *ctx().scene;
+    DeviceState& d = ctx().dev;
     FILE* f = std::fopen(path, "rb");
-    if (!f) { g_err = std::string("cannot open ") + path; return RC_E_IO; }
+    if (!f) { ctx().err = std::string("cannot open ") + path; return RC_E_IO; }
     StateHeader h{};
     const size_t npix = (size_t)sc.camera.width * sc.camera.height;
     bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kStateMagic, 8) == 0;
@@ -1111,7 +1124,7 @@ int load_state(const char* path) {
                h.accum_doubles != 3 * npix || (h.mlp_floats && h.mlp_floats != mlp_state_floats()) ||
                h.iterations_done < 0)) {
         std::fclose(f);
-        g_err = "load_state: the state was saved for another scene";
+        ctx().err = "load_state: the state was saved for another scene";
         return RC_E_INVALID;
     }
     std::vector<double> acc(ok ? h.accum_doubles : 0);
@@ -1119,7 +1132,7 @@ int load_state(const char* path) {
     ok = ok && std::fread(acc.data(), sizeof(double), acc.size(), f) == acc.size() &&
          std::fread(ml.data(), sizeof(float), ml.size(), f) == ml.size();
     std::fclose(f);
-    if (!ok) { g_err = std::string("load_state: unreadable or truncated state file ") + path; return RC_E_IO; }
+    if (!ok) { ctx().err = std::string("load_state: unreadable or truncated state file ") + path; return RC_E_IO; }
     // sampling configuration continues as saved
     rc_config c = cfg();
     c.seed = h.seed;
@@ -1128,7 +1141,7 @@ int load_state(const char* path) {
     c.max_path_length = h.max_path_length;
     c.sampler = h.sampler;
     c.learned_proposal = h.learned;
-    g_cfg = c;
+    ctx().cfg = c;
     RC_CUDA(d.accum.reserve(std::max<size_t>(acc.size(), 1)));
     RC_CUDA(cudaMemcpy(d.accum.p, acc.data(), acc.size() * sizeof(double), cudaMemcpyHostToDevice));
     d.iterations_done = h.iterations_done;
@@ -1136,11 +1149,11 @@ int load_state(const char* path) {
     if (h.mlp_floats) {
         if (!d.mlp) {
             d.mlp = std::make_unique<MlpStore>();
-            if (!d.mlp->setup(kTrainBatchRows)) { g_err = "MLP allocation failed"; return RC_E_CUDA; }
+            if (!d.mlp->setup(kTrainBatchRows)) { ctx().err = "MLP allocation failed"; return RC_E_CUDA; }
             RC_CUDA(d.train_pos.reserve(kTrainCapacity)); RC_CUDA(d.train_dir.reserve(kTrainCapacity));
             RC_CUDA(d.train_count.reserve(1)); RC_CUDA(d.train_wsum.reserve(1));
         }
-        if (mlp_import(d.mlp->p, ml.data(), h.adam_step, d.stream)) { g_err = "MLP upload failed"; return RC_E_CUDA; }
+        if (mlp_import(d.mlp->p, ml.data(), h.adam_step, d.stream)) { ctx().err = "MLP upload failed"; return RC_E_CUDA; }
         d.mlp_rounds = h.mlp_rounds;
     }
     return RC_OK;
@@ -1149,7 +1162,7 @@ int load_state(const char* path) {
 // Minimal single-part scanline OpenEXR writer: FP32 RGB, no compression.
 int write_exr(const char* path, const float* rgb, int w, int h) {
     FILE* f = std::fopen(path, "wb");
-    if (!f) { g_err = std::string("cannot open ") + path; return RC_E_IO; }
+    if (!f) { ctx().err = std::string("cannot open ") + path; return RC_E_IO; }
     std::vector<unsigned char> hdr;
     auto put = [&](const void* p, size_t n) { const unsigned char* c = (const unsigned char*)p; hdr.insert(hdr.end(), c, c + n); };
     auto put_i32 = [&](int32_t v) { put(&v, 4); };
@@ -1193,15 +1206,15 @@ int write_exr(const char* path, const float* rgb, int w, int h) {
              std::fwrite(line.data(), 4, line.size(), f) == line.size();
     }
     ok = (std::fclose(f) == 0) && ok;
-    if (!ok) { g_err = std::string("write failed: ") + path; return RC_E_IO; }
+    if (!ok) { ctx().err = std::string("write failed: ") + path; return RC_E_IO; }
     return RC_OK;
 }
 
 int read_image(float* rgb, int w, int h) {
-    if (!g_scene) { g_err = "no scene"; return RC_E_NO_SCENE; }
-    if (!rgb || w != g_scene->camera.width || h != g_scene->camera.height) { g_err = "bad image buffer"; return RC_E_INVALID; }
+    if (!ctx().scene) { ctx().err = "no scene"; return RC_E_NO_SCENE; }
+    if (!rgb || w != ctx().scene->camera.width || h != ctx().scene->camera.height) { ctx().err = "bad image buffer"; return RC_E_INVALID; }
     size_t n = 3 * (size_t)w * h;
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     if (!d.accum.p || d.accum.n < n || !d.stream) {
         std::memset(rgb, 0, n * sizeof(float));
         return RC_OK;
@@ -1218,9 +1231,9 @@ int read_image(float* rgb, int w, int h) {
 }
 
 void release_all() {
-    g_dev.release();
-    g_scene.reset();
-    g_host_ready = false;
+    ctx().dev.release();
+    ctx().scene.reset();
+    ctx().host_ready = false;
 }
 
 int dump_bvh(const std::vector<BvhNode>& nodes, const std::vector<int>& index, unsigned* out, int cap, int* idx, int idx_cap) {
@@ -1249,7 +1262,7 @@ void init(int samples, float base_radius, float radius_reduction, long long* mes
           rc_python_light* lights, unsigned int number_of_lights, rc_python_material* materials,
           unsigned int number_of_materials, int** materials_indices, int debug_test, rc_debug_stuff debug_stuff) {
     release_all();
-    g_err.clear();
+    ctx().err.clear();
     auto sc = std::make_unique<HostScene>();
     sc->samples = samples;
     sc->base_radius = base_radius;
@@ -1258,18 +1271,18 @@ void init(int samples, float base_radius, float radius_reduction, long long* mes
     sc->debug_ior = debug_stuff.specular;   // src/main.cpp:116 (read by run_debug_materials)
     if (number_of_meshes && (!meshes_pointers || !mesh_matrices || !meshes_number_of_verts ||
                              !meshes_number_of_tris || !materials_indices)) {
-        g_err = "init: null mesh arrays";
+        ctx().err = "init: null mesh arrays";
         return;
     }
     sc->meshes.resize(number_of_meshes);
     for (unsigned i = 0; i < number_of_meshes; ++i) {
         int r = ingest_mesh(sc->meshes[i], (const void*)meshes_pointers[i], meshes_number_of_verts[i],
-                            meshes_number_of_tris[i], mesh_matrices[i], materials_indices[i], g_err);
+                            meshes_number_of_tris[i], mesh_matrices[i], materials_indices[i], ctx().err);
         if (r) return;
     }
     for (unsigned i = 0; i < number_of_meshes; ++i)
         for (uint32_t m : sc->meshes[i].mat)
-            if (m >= number_of_materials) { g_err = "init: material index out of range"; return; }
+            if (m >= number_of_materials) { ctx().err = "init: material index out of range"; return; }
     // Camera(camera_x, camera_y, position, corners...) (src/Camera.h:21-26)
     HostCamera& c = sc->camera;
     c.width = (int)camera_x;
@@ -1281,39 +1294,39 @@ void init(int samples, float base_radius, float radius_reduction, long long* mes
     // The reference keeps the caller's light array and converts it in main()
     // (src/main.cpp:134,163); the records are copied here so that the caller may free
     // them after init (converted at prepare time all the same).
-    if (number_of_lights && !lights) { g_err = "init: null lights"; return; }
+    if (number_of_lights && !lights) { ctx().err = "init: null lights"; return; }
     sc->py_lights.assign(lights, lights + number_of_lights);
     sc->num_lights = number_of_lights;
-    if (number_of_materials && !materials) { g_err = "init: null materials"; return; }
+    if (number_of_materials && !materials) { ctx().err = "init: null materials"; return; }
     sc->py_materials.assign(materials, materials + number_of_materials);
-    g_scene = std::move(sc);
+    ctx().scene = std::move(sc);
 }
 
 int main(void) {
-    if (!g_scene) { g_err = "main: no scene (init was not called or failed: " + g_err + ")"; return RC_E_NO_SCENE; }
+    if (!ctx().scene) { ctx().err = "main: no scene (init was not called or failed: " + ctx().err + ")"; return RC_E_NO_SCENE; }
     int r = prepare();
     if (!r) {
         // src/main.cpp:170-186: 1 = vertex merging, 2-4 = debug views (one pass, no
         // averaging), 5 = BVH dump to OBJ files (not provided here)
-        const int mode = g_scene->debug_test;
+        const int mode = ctx().scene->debug_test;
         if (mode == 1) {
-            r = render_iterations(*g_scene, g_scene->samples);
+            r = render_iterations(*ctx().scene, ctx().scene->samples);
         } else if (mode >= 2 && mode <= 4) {
-            r = render_debug(*g_scene, mode);
+            r = render_debug(*ctx().scene, mode);
         } else {
-            g_err = "debug_test must be 1 (render) or 2-4 (debug views); 5 (BVH OBJ dump) is not provided";
+            ctx().err = "debug_test must be 1 (render) or 2-4 (debug views); 5 (BVH OBJ dump) is not provided";
             r = RC_E_UNSUPPORTED;
         }
     }
     if (!r && cfg().write_exr) {
-        int w = g_scene->camera.width, h = g_scene->camera.height;
+        int w = ctx().scene->camera.width, h = ctx().scene->camera.height;
         std::vector<float> img(3 * (size_t)w * h);
         r = read_image(img.data(), w, h);
         if (!r) r = write_exr(cfg().exr_path, img.data(), w, h);
     }
-    std::string keep = g_err;
+    std::string keep = ctx().err;
     release_all();
-    g_err = keep;
+    ctx().err = keep;
     return r;
 }
 
@@ -1324,33 +1337,33 @@ int rc_default_config(rc_config* c) {
 }
 
 int rc_set_config(const rc_config* c) {
-    if (!c) { g_err = "null config"; return RC_E_INVALID; }
-    if (c->max_path_length < 0 || c->max_path_length > 30) { g_err = "max_path_length out of range [0, 30]"; return RC_E_INVALID; }
-    if (c->photons_per_iter < 0) { g_err = "photons_per_iter < 0"; return RC_E_INVALID; }
+    if (!c) { ctx().err = "null config"; return RC_E_INVALID; }
+    if (c->max_path_length < 0 || c->max_path_length > 30) { ctx().err = "max_path_length out of range [0, 30]"; return RC_E_INVALID; }
+    if (c->photons_per_iter < 0) { ctx().err = "photons_per_iter < 0"; return RC_E_INVALID; }
     if (c->sampler != RC_SAMPLER_UNIFORM && c->sampler != RC_SAMPLER_HYBRID && c->sampler != RC_SAMPLER_PSSMLT) {
-        g_err = "unknown sampler"; return RC_E_INVALID;
+        ctx().err = "unknown sampler"; return RC_E_INVALID;
     }
     if (c->learned_proposal) {
-        if (c->sampler != RC_SAMPLER_UNIFORM) { g_err = "learned_proposal requires the uniform sampler"; return RC_E_UNSUPPORTED; }
+        if (c->sampler != RC_SAMPLER_UNIFORM) { ctx().err = "learned_proposal requires the uniform sampler"; return RC_E_UNSUPPORTED; }
         if (c->train_iterations < 0 || c->train_steps < 0 || !(c->learning_rate > 0.0f && c->learning_rate < 1.0f)) {
-            g_err = "learned proposal: train_iterations/train_steps >= 0, learning_rate in (0, 1)"; return RC_E_INVALID;
+            ctx().err = "learned proposal: train_iterations/train_steps >= 0, learning_rate in (0, 1)"; return RC_E_INVALID;
         }
     }
     if (c->sampler != RC_SAMPLER_UNIFORM) {
-        if (c->mlt_chains <= 0) { g_err = "mlt_chains must be positive"; return RC_E_INVALID; }
-        if (c->max_path_length > kMltMaxPathLength) { g_err = "Metropolis samplers support max_path_length <= 12"; return RC_E_UNSUPPORTED; }
+        if (c->mlt_chains <= 0) { ctx().err = "mlt_chains must be positive"; return RC_E_INVALID; }
+        if (c->max_path_length > kMltMaxPathLength) { ctx().err = "Metropolis samplers support max_path_length <= 12"; return RC_E_UNSUPPORTED; }
         if (c->sampler == RC_SAMPLER_PSSMLT && !(c->large_step_prob > 0.0f && c->large_step_prob <= 1.0f)) {
-            g_err = "large_step_prob must be in (0, 1]"; return RC_E_INVALID;
+            ctx().err = "large_step_prob must be in (0, 1]"; return RC_E_INVALID;
         }
     }
-    if (c->graph_replay < 0 || c->graph_replay > 2) { g_err = "graph_replay must be 0, 1 or 2"; return RC_E_INVALID; }
-    if (c->gpu_bvh < 0 || c->gpu_bvh > 1) { g_err = "gpu_bvh must be 0 or 1"; return RC_E_INVALID; }
-    g_cfg = *c;
-    g_cfg.exr_path[sizeof(g_cfg.exr_path) - 1] = 0;
-    g_cfg_set = true;
+    if (c->graph_replay < 0 || c->graph_replay > 2) { ctx().err = "graph_replay must be 0, 1 or 2"; return RC_E_INVALID; }
+    if (c->gpu_bvh < 0 || c->gpu_bvh > 1) { ctx().err = "gpu_bvh must be 0 or 1"; return RC_E_INVALID; }
+    ctx().cfg = *c;
+    ctx().cfg.exr_path[sizeof(ctx().cfg.exr_path) - 1] = 0;
+    ctx().cfg_set = true;
     // sizes and shapes of asynchronous iterations are re-derived under the new settings
-    g_dev.async_pcap = g_dev.async_qcap = 0;
-    if (g_dev.graph_exec) { cudaGraphExecDestroy(g_dev.graph_exec); g_dev.graph_exec = nullptr; }
+    ctx().dev.async_pcap = ctx().dev.async_qcap = 0;
+    if (ctx().dev.graph_exec) { cudaGraphExecDestroy(ctx().dev.graph_exec); ctx().dev.graph_exec = nullptr; }
     return RC_OK;
 }
 
@@ -1359,7 +1372,7 @@ int rc_prepare(void) { return prepare(); }
 int rc_prepare_host(float* info) {
     int r = prepare_host();
     if (r) return r;
-    const HostScene& sc = *g_scene;
+    const HostScene& sc = *ctx().scene;
     if (info) {
         info[0] = sc.bounds.mn.x; info[1] = sc.bounds.mn.y; info[2] = sc.bounds.mn.z;
         info[3] = sc.bounds.mx.x; info[4] = sc.bounds.mx.y; info[5] = sc.bounds.mx.z;
@@ -1371,8 +1384,8 @@ int rc_prepare_host(float* info) {
 int rc_host_mesh_bvh(int mesh, unsigned* nodes, int cap, int* index, int index_cap, float* cost) {
     int r = prepare_host();
     if (r) return r;
-    if (mesh < 0 || mesh >= (int)g_scene->meshes.size() || !nodes || !index) { g_err = "bad mesh index"; return RC_E_INVALID; }
-    HostMesh& hm = g_scene->meshes[mesh];
+    if (mesh < 0 || mesh >= (int)ctx().scene->meshes.size() || !nodes || !index) { ctx().err = "bad mesh index"; return RC_E_INVALID; }
+    HostMesh& hm = ctx().scene->meshes[mesh];
     if (hm.bvh.nodes.empty()) build_mesh_bvh(hm);   // the device built this scene's meshes
     const MeshBvh& b = hm.bvh;
     if (cost) *cost = b.cost;
@@ -1382,19 +1395,19 @@ int rc_host_mesh_bvh(int mesh, unsigned* nodes, int cap, int* index, int index_c
 int rc_host_world_bvh(unsigned* nodes, int cap, int* index, int index_cap) {
     int r = prepare_host();
     if (r) return r;
-    if (!nodes || !index) { g_err = "null output"; return RC_E_INVALID; }
-    return dump_bvh(g_scene->world.nodes, g_scene->world.index, nodes, cap, index, index_cap);
+    if (!nodes || !index) { ctx().err = "null output"; return RC_E_INVALID; }
+    return dump_bvh(ctx().scene->world.nodes, ctx().scene->world.index, nodes, cap, index, index_cap);
 }
 
 int rc_scene_dump(int which, unsigned* out, long long cap, long long* words) {
-    if (!g_scene || !g_scene->prepared) { g_err = "rc_scene_dump: scene not prepared"; return RC_E_NO_SCENE; }
-    if (!words || (cap > 0 && !out) || cap < 0) { g_err = "rc_scene_dump: bad arguments"; return RC_E_INVALID; }
-    DeviceState& d = g_dev;
+    if (!ctx().scene || !ctx().scene->prepared) { ctx().err = "rc_scene_dump: scene not prepared"; return RC_E_NO_SCENE; }
+    if (!words || (cap > 0 && !out) || cap < 0) { ctx().err = "rc_scene_dump: bad arguments"; return RC_E_INVALID; }
+    DeviceState& d = ctx().dev;
     struct Part { const void* p; long long words; };
     std::vector<Part> parts;
     const long long wn = d.view.num_world_nodes;
-    const long long nm = (long long)g_scene->meshes.size();
-    const long long nw = (long long)g_scene->world.index.size() - 1;
+    const long long nm = (long long)ctx().scene->meshes.size();
+    const long long nw = (long long)ctx().scene->world.index.size() - 1;
     switch (which) {
         case 0: parts = {{d.node_lo.p, 4 * d.num_mesh_nodes}, {d.node_hi.p, 4 * d.num_mesh_nodes}}; break;
         case 1:
@@ -1403,7 +1416,7 @@ int rc_scene_dump(int which, unsigned* out, long long cap, long long* words) {
             break;
         case 2: parts = {{d.wnode_lo.p, 4 * wn}, {d.wnode_hi.p, 4 * wn}}; break;
         case 3: parts = {{d.world_mesh.p, nw}, {d.mesh_root.p, nm}}; break;
-        default: g_err = "rc_scene_dump: which must be 0..3"; return RC_E_INVALID;
+        default: ctx().err = "rc_scene_dump: which must be 0..3"; return RC_E_INVALID;
     }
     // 0 and 2 are interleaved per node as (lo, hi); 1 per triangle as (v0, e1, e2, n0, n1, n2)
     const int k = (int)parts.size();
@@ -1429,17 +1442,36 @@ int rc_scene_dump(int which, unsigned* out, long long cap, long long* words) {
     return RC_OK;
 }
 
+rc_context* rc_context_create(void) { return reinterpret_cast<rc_context*>(new (std::nothrow) Context()); }
+
+int rc_context_bind(rc_context* c) {
+    t_bound = reinterpret_cast<Context*>(c);
+    return RC_OK;
+}
+
+int rc_context_destroy(rc_context* c) {
+    if (!c) { ctx().err = "rc_context_destroy: null context"; return RC_E_INVALID; }
+    Context* x = reinterpret_cast<Context*>(c);
+    Context* prev = t_bound;
+    t_bound = x;
+    release_all();   // the scene and its device buffers
+    x->bvh.reset();
+    t_bound = prev == x ? nullptr : prev;
+    delete x;
+    return RC_OK;
+}
+
 int rc_prepare_stats(double* out, int n) {
-    if (!out || n < 0) { g_err = "rc_prepare_stats: bad arguments"; return RC_E_INVALID; }
+    if (!out || n < 0) { ctx().err = "rc_prepare_stats: bad arguments"; return RC_E_INVALID; }
     const int k = std::min(n, 5);
-    for (int i = 0; i < k; ++i) out[i] = g_prep[i];
+    for (int i = 0; i < k; ++i) out[i] = ctx().prep[i];
     return k;
 }
 
 int rc_render(int iterations) {
-    if (iterations < 0) { g_err = "iterations < 0"; return RC_E_INVALID; }
+    if (iterations < 0) { ctx().err = "iterations < 0"; return RC_E_INVALID; }
     int r = prepare();
-    if (!r) r = render_iterations(*g_scene, iterations);
+    if (!r) r = render_iterations(*ctx().scene, iterations);
     return r;
 }
 
@@ -1449,20 +1481,20 @@ int rc_load_state(const char* path) { return load_state(path); }
 int rc_render_debug(int mode) {
     int r = prepare();
     if (r) return r;
-    return render_debug(*g_scene, mode);
+    return render_debug(*ctx().scene, mode);
 }
 
 int rc_render_timed(int iterations, double* out) {
-    if (iterations < 0 || !out) { g_err = "bad arguments"; return RC_E_INVALID; }
+    if (iterations < 0 || !out) { ctx().err = "bad arguments"; return RC_E_INVALID; }
     int r = prepare();
     if (r) return r;
-    DeviceState& d = g_dev;
+    DeviceState& d = ctx().dev;
     d.acc_gather_ms = d.acc_gather_bytes = d.acc_launches = 0;
     d.acc_iters = 0;
     d.acc_async = 0;
     RC_CUDA(cudaStreamSynchronize(d.stream));
     RC_CUDA(cudaEventRecord(d.t0, d.stream));
-    r = render_iterations(*g_scene, iterations);
+    r = render_iterations(*ctx().scene, iterations);
     if (r) return r;
     RC_CUDA(cudaEventRecord(d.t1, d.stream));
     RC_CUDA(cudaEventSynchronize(d.t1));
@@ -1483,17 +1515,17 @@ int rc_release(void) {
     return RC_OK;
 }
 
-const char* rc_last_error(void) { return g_err.c_str(); }
+const char* rc_last_error(void) { return ctx().err.c_str(); }
 
 int rc_get_stats(double* out, int n) {
     if (!out || n < 0) return RC_E_INVALID;
-    for (int i = 0; i < n && i < 16; ++i) out[i] = g_dev.stats[i];
+    for (int i = 0; i < n && i < 16; ++i) out[i] = ctx().dev.stats[i];
     return RC_OK;
 }
 
 int rc_proposal_state(long long n, float* prop4, float* contrib) {
-    if (n < 0) { g_err = "n < 0"; return RC_E_INVALID; }
-    DeviceState& d = g_dev;
+    if (n < 0) { ctx().err = "n < 0"; return RC_E_INVALID; }
+    DeviceState& d = ctx().dev;
     if (prop4) {
         std::memset(prop4, 0, sizeof(float) * 4 * (size_t)n);
         const long long m = std::min<long long>(n, (long long)d.prop.n);
@@ -1510,9 +1542,9 @@ int rc_proposal_state(long long n, float* prop4, float* contrib) {
 int rc_light_photons(int iteration, float* out, long long cap, long long* count) {
     int r = prepare();
     if (r) return r;
-    if (iteration < 0 || (cap > 0 && !out)) { g_err = "bad photon output"; return RC_E_INVALID; }
-    HostScene& sc = *g_scene;
-    DeviceState& d = g_dev;
+    if (iteration < 0 || (cap > 0 && !out)) { ctx().err = "bad photon output"; return RC_E_INVALID; }
+    HostScene& sc = *ctx().scene;
+    DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
     VMParams p = make_params(sc, iteration);
     long long pcap = std::max<long long>(p.num_light_paths * 2, 1024);
@@ -1557,15 +1589,15 @@ int rc_light_photons(int iteration, float* out, long long cap, long long* count)
 int rc_trace_rays(int n, const float* origins, const float* directions, float tmin, unsigned* out) {
     int r = prepare();
     if (r) return r;
-    if (n < 0 || (n > 0 && (!origins || !directions || !out))) { g_err = "bad ray arrays"; return RC_E_INVALID; }
+    if (n < 0 || (n > 0 && (!origins || !directions || !out))) { ctx().err = "bad ray arrays"; return RC_E_INVALID; }
     if (n == 0) return RC_OK;
-    cudaStream_t s = g_dev.stream;
+    cudaStream_t s = ctx().dev.stream;
     DevBuf<float> o, d;
     DevBuf<unsigned> w;
     RC_CUDA(o.reserve(3 * (size_t)n)); RC_CUDA(d.reserve(3 * (size_t)n)); RC_CUDA(w.reserve(8 * (size_t)n));
     RC_CUDA(cudaMemcpyAsync(o.p, origins, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
     RC_CUDA(cudaMemcpyAsync(d.p, directions, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
-    launch_trace_rays(g_dev.view, n, o.p, d.p, tmin, nullptr, w.p, g_dev.errors.p, s);
+    launch_trace_rays(ctx().dev.view, n, o.p, d.p, tmin, nullptr, w.p, ctx().dev.errors.p, s);
     RC_CUDA(cudaGetLastError());
     RC_CUDA(cudaMemcpyAsync(out, w.p, 32 * (size_t)n, cudaMemcpyDeviceToHost, s));
     RC_CUDA(cudaStreamSynchronize(s));
@@ -1576,14 +1608,14 @@ int rc_trace_rays(int n, const float* origins, const float* directions, float tm
 int rc_trace_rays_full(int n, const float* origins, const float* directions, float tmin, float* out) {
     int r = prepare();
     if (r) return r;
-    if (n < 0 || (n > 0 && (!origins || !directions || !out))) { g_err = "bad ray arrays"; return RC_E_INVALID; }
+    if (n < 0 || (n > 0 && (!origins || !directions || !out))) { ctx().err = "bad ray arrays"; return RC_E_INVALID; }
     if (n == 0) return RC_OK;
-    cudaStream_t s = g_dev.stream;
+    cudaStream_t s = ctx().dev.stream;
     DevBuf<float> o, d, f;
     RC_CUDA(o.reserve(3 * (size_t)n)); RC_CUDA(d.reserve(3 * (size_t)n)); RC_CUDA(f.reserve(16 * (size_t)n));
     RC_CUDA(cudaMemcpyAsync(o.p, origins, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
     RC_CUDA(cudaMemcpyAsync(d.p, directions, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
-    launch_trace_rays(g_dev.view, n, o.p, d.p, tmin, f.p, nullptr, g_dev.errors.p, s);
+    launch_trace_rays(ctx().dev.view, n, o.p, d.p, tmin, f.p, nullptr, ctx().dev.errors.p, s);
     RC_CUDA(cudaGetLastError());
     RC_CUDA(cudaMemcpyAsync(out, f.p, 64 * (size_t)n, cudaMemcpyDeviceToHost, s));
     RC_CUDA(cudaStreamSynchronize(s));
@@ -1607,7 +1639,7 @@ static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, Dev
     RC_CUDA(z.reserve(std::max(n, 1))); RC_CUDA(id.reserve(std::max(n, 1)));
     RC_CUDA(scratch.reserve(kd_scratch_bytes(n)));
     tree.nodes = nodes.p; tree.x = x.p; tree.y = y.p; tree.z = z.p; tree.id = id.p;
-    if (kd_build(pos.p, n, tree, scratch.p, scratch.n, s, nullptr, err.p)) { g_err = "KD scratch"; return RC_E_CAPACITY; }
+    if (kd_build(pos.p, n, tree, scratch.p, scratch.n, s, nullptr, err.p)) { ctx().err = "KD scratch"; return RC_E_CAPACITY; }
     RC_CUDA(cudaGetLastError());
     tree.box_levels = kd_box_levels(n);
     if (tree.box_levels > 0) {
@@ -1621,13 +1653,13 @@ static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, Dev
     RC_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     RC_CUDA(cudaStreamSynchronize(s));
     err.release();
-    if (h) { g_err = "KD-tree build found inconsistent counts"; return RC_E_INVALID; }
+    if (h) { ctx().err = "KD-tree build found inconsistent counts"; return RC_E_INVALID; }
     return RC_OK;
 }
 
 int rc_kd_query(int n, const float* positions, int q, const float* queries, float r2, int* counts, int* idx,
                 long long cap, long long* total) {
-    if (n < 0 || q < 0 || (n > 0 && !positions) || (q > 0 && (!queries || !counts))) { g_err = "bad KD arrays"; return RC_E_INVALID; }
+    if (n < 0 || q < 0 || (n > 0 && !positions) || (q > 0 && (!queries || !counts))) { ctx().err = "bad KD arrays"; return RC_E_INVALID; }
     cudaStream_t s = nullptr;
     RC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     DevBuf<float4> pos; DevBuf<uint2> nodes; DevBuf<float> x, y, z, qp; DevBuf<uint32_t> id;
@@ -1671,7 +1703,7 @@ int rc_kd_query(int n, const float* positions, int q, const float* queries, floa
 }
 
 int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes_out, long long cap, long long* num_nodes) {
-    if (n < 0 || (n > 0 && !positions)) { g_err = "bad KD arrays"; return RC_E_INVALID; }
+    if (n < 0 || (n > 0 && !positions)) { ctx().err = "bad KD arrays"; return RC_E_INVALID; }
     cudaStream_t s = nullptr;
     RC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     DevBuf<float4> pos; DevBuf<uint2> nodes; DevBuf<float> x, y, z; DevBuf<uint32_t> id; DevBuf<unsigned char> scratch;
@@ -1685,7 +1717,7 @@ int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes_out, long l
             long long m = std::min(nn, cap);
             cudaError_t e = cudaMemcpyAsync(nodes_out, nodes.p, 8 * (size_t)m, cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) { g_err = cudaGetErrorString(e); r = RC_E_CUDA; }
+            if (e != cudaSuccess) { ctx().err = cudaGetErrorString(e); r = RC_E_CUDA; }
         }
     }
     pos.release(); nodes.release(); x.release(); y.release(); z.release(); id.release(); scratch.release();

@@ -298,8 +298,9 @@ unsigned persistent_grid(K kernel, int block, size_t smem, long long work_items)
 
 template <int B, int MB>
 void launch_light_t(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s) {
-    static unsigned grid_cache = 0;
-    static long long grid_for = -1;
+    // per host thread: contexts on different threads launch concurrently
+    static thread_local unsigned grid_cache = 0;
+    static thread_local long long grid_for = -1;
     if (grid_for != p.num_light_paths) {
         grid_cache = persistent_grid(k_light_pass_persistent<B, MB>, B, 0, p.num_light_paths);
         grid_for = p.num_light_paths;
@@ -311,8 +312,9 @@ void launch_light_t(const VMParams& p, PhotonBuf ph, unsigned long long* next_pa
 template <int B, int MB>
 void launch_camera_t(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s) {
     const long long n = (long long)p.camera.width * p.camera.height;
-    static unsigned grid_cache = 0;
-    static long long grid_for = -1;
+    // per host thread: contexts on different threads launch concurrently
+    static thread_local unsigned grid_cache = 0;
+    static thread_local long long grid_for = -1;
     if (grid_for != n) {
         grid_cache = persistent_grid(k_camera_pass_persistent<B, MB>, B, 0, n);
         grid_for = n;

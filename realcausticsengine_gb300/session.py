@@ -17,6 +17,38 @@ STAT_NAMES = ["light_paths", "photons", "queries", "merged", "light_ms", "kd_ms"
               "buckets_visited"]
 
 
+class Context:
+    """A library context (rc_context_create).  Bound on a thread (`with ctx:` or
+    bind()), it holds that thread's scene, settings, last error and device buffers, so
+    scenes in different contexts render concurrently from different threads; threads
+    that bind nothing share the default context."""
+
+    def __init__(self):
+        self.L = lib()
+        self.handle = self.L.rc_context_create()
+        if not self.handle:
+            raise MemoryError("rc_context_create failed")
+
+    def bind(self):
+        check(self.L.rc_context_bind(self.handle), "rc_context_bind")
+
+    @staticmethod
+    def unbind():
+        lib().rc_context_bind(None)
+
+    def __enter__(self):
+        self.bind()
+        return self
+
+    def __exit__(self, *exc):
+        self.unbind()
+
+    def destroy(self):
+        if self.handle:
+            check(self.L.rc_context_destroy(self.handle), "rc_context_destroy")
+            self.handle = None
+
+
 class Renderer:
     """One scene loaded into the library (the library holds one scene at a time,
     like the reference's global `scene`)."""

@@ -1,0 +1,86 @@
+"""Library contexts: a thread that binds its own context holds its own scene, settings
+and last error; threads that bind none share the default context (the reference's one
+global scene)."""
+import threading
+
+import numpy as np
+import pytest
+
+from realcausticsengine_gb300 import _native, scenes
+from realcausticsengine_gb300.session import Context, Renderer
+
+
+def _host_info(sc):
+    r = Renderer(sc)
+    info = r.prepare_host()
+    r.release()
+    return info
+
+
+def test_contexts_hold_separate_scenes_and_errors():
+    lib = _native.lib()
+    a, b = scenes.test_scene(), scenes.glass_sphere_point(32, 32, subdiv=2)
+    want = [_host_info(a), _host_info(b)]          # default context, one after the other
+    got, errs = [None, None], [None, None]
+    start = threading.Barrier(2)
+
+    def worker(k, sc):
+        ctx = Context()
+        with ctx:
+            r = Renderer(sc)
+            start.wait()                            # both scenes loaded before either prepares
+            got[k] = r.prepare_host()
+            assert lib.rc_render(-1) != 0           # an error in this context only
+            errs[k] = lib.rc_last_error()
+            r.release()
+        ctx.destroy()
+
+    ts = [threading.Thread(target=worker, args=(k, sc)) for k, sc in enumerate((a, b))]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    for k in range(2):
+        assert (got[k].view(np.uint32) == want[k].view(np.uint32)).all()
+        assert b"iterations < 0" in errs[k]
+    # the default context saw neither scene nor error
+    assert lib.rc_prepare_host(None) != 0 and b"no scene" in lib.rc_last_error()
+
+
+def test_destroy_rejects_null():
+    lib = _native.lib()
+    assert lib.rc_context_destroy(None) != 0
+
+
+@pytest.mark.gpu
+def test_concurrent_contexts_render_like_sequential():
+    """Two scenes rendered at the same time from two threads, each in its own context,
+    give the images the default context renders for them one after the other (up to the
+    FP64 summation order of the merges)."""
+    scs = [scenes.test_scene(64, 48), scenes.glass_sphere_point(64, 64, subdiv=3, light="area")]
+    kw = dict(max_path_length=6, photons_per_iter=65536, seed=3)
+
+    def render(sc):
+        r = Renderer(sc, **kw)
+        r.render(4)
+        img = r.image()
+        r.release()
+        return img
+
+    want = [render(sc) for sc in scs]
+    got = [None, None]
+
+    def worker(k):
+        ctx = Context()
+        with ctx:
+            got[k] = render(scs[k])
+        ctx.destroy()
+
+    ts = [threading.Thread(target=worker, args=(k,)) for k in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    for g, w in zip(got, want):
+        assert w.sum() > 0
+        np.testing.assert_allclose(g, w, rtol=1e-5, atol=1e-7)
