@@ -59,6 +59,21 @@ __device__ __forceinline__ bool in_radius(F3 q, float px, float py, float pz, fl
 // query accepts.  `stack` is this warp's shared-memory stack (kStack (e, start) pairs).
 struct VisitCounts { unsigned nodes, buckets, tests; };
 
+// Hand the first 32 pending entries to `flush` once there are 32 or more, and move the
+// rest (at most 31) to the front, so that every flush but a warp's last is a full one.
+template <class Flush>
+__device__ __forceinline__ void drain32(uint32_t* pend, int& np, Flush& flush) {
+    if (np < 32) return;
+    flush(32, pend);
+    __syncwarp();
+    const int lane = threadIdx.x & 31, rest = np - 32;
+    const uint32_t v = lane < rest ? pend[32 + lane] : 0u;
+    __syncwarp();
+    if (lane < rest) pend[lane] = v;
+    np = rest;
+    __syncwarp();
+}
+
 // One query per warp.  The traversal is the reference's descent for that single query
 // (uniform across the warp): near side first, far side and an odd node's median photon
 // only when (q[axis] - split)^2 < r^2.  The stack lives in registers spread over the
@@ -69,7 +84,7 @@ struct VisitCounts { unsigned nodes, buckets, tests; };
 // and once at the end, so the per-photon work is spread over the lanes.
 template <class Flush>
 __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend,
-                                              VisitCounts& vc, Flush&& flush) {
+                                              int& np, uint32_t tag, VisitCounts& vc, Flush&& flush) {
     const int lane = threadIdx.x & 31;
     if (t.n <= 0) return;
     uint32_t se0 = 0, ss0 = 0, se1 = 0, ss1 = 0;   // stack entries lane and lane+32
@@ -80,7 +95,6 @@ __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, ui
             return;
     }
     int sp = 1;
-    int np = 0;   // pending entries (uniform)
     const uint32_t n32 = (uint32_t)t.n;   // photon counts stay below 2^28 (28-bit index field)
     while (sp) {
         --sp;
@@ -102,10 +116,10 @@ __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, ui
                     acc = in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2);
                 }
                 const unsigned m = __ballot_sync(0xffffffffu, acc);
-                if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = start + i;
+                if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = (start + i) | tag;
                 np += __popc(m);
                 __syncwarp();
-                if (np >= 32) { flush(np, pend); np = 0; __syncwarp(); }
+                drain32(pend, np, flush);
             }
             continue;
         }
@@ -121,10 +135,10 @@ __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, ui
         if (odd && within) {
             const uint32_t p = start + half;
             const bool a = in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2);
-            if (a && lane == 0) pend[np] = p;
+            if (a && lane == 0) pend[np] = p | tag;
             np += a ? 1 : 0;
             __syncwarp();
-            if (np >= 32) { flush(np, pend); np = 0; __syncwarp(); }
+            drain32(pend, np, flush);
         }
         const uint32_t le = 2u * e, ls = start;
         const uint32_t re = 2u * e + 1u, rs = start + half + odd;
@@ -140,7 +154,6 @@ __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, ui
             ++sp;
         }
     }
-    if (np > 0) flush(np, pend);
     __syncwarp();
 }
 
@@ -160,7 +173,7 @@ constexpr int kRootStack = 256;
 
 template <class Flush>
 __device__ __forceinline__ void kd_query_expand(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend,
-                                                uint2* stk, VisitCounts& vc, Flush&& flush) {
+                                                uint2* stk, int& np, uint32_t tag, VisitCounts& vc, Flush&& flush) {
     const int lane = threadIdx.x & 31;
     if (t.n <= 0) return;
     const uint32_t n32 = (uint32_t)t.n;
@@ -169,13 +182,12 @@ __device__ __forceinline__ void kd_query_expand(const KdNav& t, F3 q, float r2, 
         const int l0 = 31 - __clz(start_node.x);
         if (l0 <= Lb && box_outside(q, __ldg(&t.box_lo[start_node.x]), __ldg(&t.box_hi[start_node.x]), r2)) return;
     }
-    int np = 0;
     auto append = [&](bool acc, uint32_t p) {
         const unsigned m = __ballot_sync(0xffffffffu, acc);
-        if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = p;
+        if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = p | tag;
         np += __popc(m);
         __syncwarp();
-        if (np >= 32) { flush(np, pend); np = 0; __syncwarp(); }
+        drain32(pend, np, flush);
     };
     if (lane == 0) stk[0] = start_node;
     __syncwarp();
@@ -241,15 +253,17 @@ __device__ __forceinline__ void kd_query_expand(const KdNav& t, F3 q, float r2, 
             __syncwarp();
         }
     }
-    if (np > 0) flush(np, pend);
     __syncwarp();
 }
 
+// Accepted tree positions go to the warp's pending list `pend` (count `np`, uniform,
+// carried across the queries of a warp) with `tag` in their top bits; the list is
+// handed to `flush` whenever it holds 32 or more entries.  The caller flushes the rest.
 template <class Flush>
 __device__ __forceinline__ void kd_query(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend, uint2* stk,
-                                         VisitCounts& vc, Flush&& flush) {
-    if (t.box_levels > 0) kd_query_expand(t, q, r2, start_node, pend, stk, vc, flush);
-    else kd_query_warp(t, q, r2, start_node, pend, vc, flush);
+                                         int& np, uint32_t tag, VisitCounts& vc, Flush&& flush) {
+    if (t.box_levels > 0) kd_query_expand(t, q, r2, start_node, pend, stk, np, tag, vc, flush);
+    else kd_query_warp(t, q, r2, start_node, pend, np, tag, vc, flush);
 }
 
 // MinBlocks (resident blocks per SM the register allocation must allow) and QPW
@@ -264,37 +278,48 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const
                                                                          const unsigned long long* __restrict__ nq_dev,
                                                                          const int* __restrict__ skip) {
     constexpr int kQueriesPerWarp = QPW;
+    static_assert(QPW <= 16, "a pending entry keeps its query slot in its top 4 bits");
     // device-side count (bounded by the capacity nq) and an iteration-wide skip flag,
     // for iterations enqueued without a host round trip
     if (skip && *skip) return;
     if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
     __shared__ uint32_t pend[kWarpsPerBlock][64];
     __shared__ uint2 stk[kWarpsPerBlock][kRootStack];
+    // the warp's queries (position | camera dVM, shading normal | material, geometric
+    // normal | pixel, throughput, outgoing direction | dispersion channel) and their sums
+    __shared__ float4 qrec[kWarpsPerBlock][QPW][5];
+    __shared__ float qcol[kWarpsPerBlock][QPW][3];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long w = blockIdx.x * (long long)kWarpsPerBlock + warp;
     const long long first = w * kQueriesPerWarp;
     if (first >= nq) return;
     const long long last = first + kQueriesPerWarp < nq ? first + kQueriesPerWarp : nq;
+    const int nslots = (int)(last - first);
     VisitCounts vc{0u, 0u, 0u};
     unsigned accepted = 0;
-    for (long long slot = first; slot < last; ++slot) {
-        const long long qi = __ldg(&order[slot]);
-        const uint2 sn = __ldg(&start_nodes[qi]);
-        const float4 a = qb.q0[qi], b = qb.q1[qi], c = qb.q2[qi], ww = qb.q3[qi], e = qb.q4[qi];
-        const F3 q = xyz(a), ng = xyz(c);
-        const float cam_dVM = a.w;
-        Bsdf bs;
-        const DevMaterial& qm = P.materials[__float_as_int(b.w)];
-        const int channel = __float_as_int(e.w);   // the camera path's dispersion channel
-        bs.init(qm, xyz(b), xyz(e), true, (qm.disp > 0.0f && channel >= 0) ? (float)(channel - 1) * qm.disp : 0.0f);
-        // per-query constants of the merge evaluation
-        const float wo_ng = dot(bs.fr.to_world(bs.wo), ng);
-        const float fwo = (bs.kind == BSDF_K_PLASTIC_GGX || bs.kind == BSDF_K_PLASTIC_SMOOTH)
-                              ? fresnel_reflectance(fabsf(bs.wo.z), bs.s) : 0.0f;
-        F3 color = f3(0.0f);
-        kd_query(t, q, P.radius_sqr, sn, pend[warp], stk[warp], vc, [&](int n, const uint32_t* list) {
-            for (int j = lane; j < n; j += 32) {
-                const uint32_t p = list[j];
+    // Merges of all the warp's queries share the pending list (entry = query slot << 28
+    // | tree position), so the lanes of a flush evaluate merges of several queries; the
+    // list is in slot order, and a segmented scan over the lanes sums each query's
+    // merges in a fixed order (the same image every run).
+    auto flush = [&](int n, const uint32_t* list) {
+        for (int j0 = 0; j0 < n; j0 += 32) {
+            const int j = j0 + lane;
+            const bool valid = j < n;
+            const uint32_t entry = valid ? list[j] : 0u;
+            const int k = valid ? (int)(entry >> 28) : -1;
+            F3 cpair = f3(0.0f);
+            if (valid) {
+                const uint32_t p = entry & 0x0fffffffu;
+                const float4 a = qrec[warp][k][0], b = qrec[warp][k][1], c = qrec[warp][k][2];
+                const float4 e = qrec[warp][k][4];
+                const F3 ng = xyz(c);
+                Bsdf bs;
+                const DevMaterial& qm = P.materials[__float_as_int(b.w)];
+                const int channel = __float_as_int(e.w);   // the camera path's dispersion channel
+                bs.init(qm, xyz(b), xyz(e), true, (qm.disp > 0.0f && channel >= 0) ? (float)(channel - 1) * qm.disp : 0.0f);
+                const float wo_ng = dot(bs.fr.to_world(bs.wo), ng);
+                const float fwo = (bs.kind == BSDF_K_PLASTIC_GGX || bs.kind == BSDF_K_PLASTIC_SMOOTH)
+                                      ? fresnel_reflectance(fabsf(bs.wo.z), bs.s) : 0.0f;
                 const float4 p0 = __ldg(&tp.t0[p]);
                 const float4 p1 = __ldg(&tp.t1[p]);
                 const float2 p2 = __ldg(&tp.t2[p]);
@@ -302,34 +327,57 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const
                 float fwd, rev;
                 F3 ev;
                 bs.eval_pdf(wi, ng, wo_ng, fwo, ev, fwd, rev);
-                const float weight = 1.0f / (1.0f + cam_dVM * rev + p0.w * fwd);
-                const F3 cpair = ev * f3(p1.w, p2.x, p2.y) * weight;
-                color = color + cpair;
+                const float weight = 1.0f / (1.0f + a.w * rev + p0.w * fwd);
+                cpair = ev * f3(p1.w, p2.x, p2.y) * weight;
                 if (P.path_contrib) {
                     // learned-proposal training signal: the squared luminance this merge adds
                     // to its pixel, summed per light path
-                    const F3 img = xyz(ww) * cpair;
+                    const F3 img = xyz(qrec[warp][k][3]) * cpair;
                     const float lum = (fabsf(img.x) + fabsf(img.y) + fabsf(img.z)) * (1.0f / 3.0f);
                     if (lum > 0.0f)
                         atomicAdd(&P.path_contrib[__ldg(&P.photon_path[__ldg(&t.id[p])])], lum * lum);
                 }
             }
-            accepted += (unsigned)n;
-        });
-        // warp sum of the per-lane partial colours
-        for (int o = 16; o > 0; o >>= 1) {
-            color.x += __shfl_xor_sync(0xffffffffu, color.x, o);
-            color.y += __shfl_xor_sync(0xffffffffu, color.y, o);
-            color.z += __shfl_xor_sync(0xffffffffu, color.z, o);
-        }
-        if (lane == 0) {
-            const F3 r = xyz(ww) * color;
-            if (r.x != 0.0f || r.y != 0.0f || r.z != 0.0f) {
-                const long long pixel = __float_as_int(c.w);
-                atomicAdd(&accum[3 * pixel + 0], (double)r.x);
-                atomicAdd(&accum[3 * pixel + 1], (double)r.y);
-                atomicAdd(&accum[3 * pixel + 2], (double)r.z);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float x = __shfl_up_sync(0xffffffffu, cpair.x, o);
+                const float y = __shfl_up_sync(0xffffffffu, cpair.y, o);
+                const float z = __shfl_up_sync(0xffffffffu, cpair.z, o);
+                const int ko = __shfl_up_sync(0xffffffffu, k, o);
+                if (lane >= o && ko == k) { cpair.x += x; cpair.y += y; cpair.z += z; }
             }
+            const int knext = __shfl_down_sync(0xffffffffu, k, 1);
+            if (valid && (lane == 31 || knext != k)) {   // last lane of its slot's run
+                qcol[warp][k][0] += cpair.x;
+                qcol[warp][k][1] += cpair.y;
+                qcol[warp][k][2] += cpair.z;
+            }
+            __syncwarp();
+        }
+        accepted += (unsigned)n;
+    };
+    int np = 0;
+    for (int k = 0; k < nslots; ++k) {
+        const long long qi = __ldg(&order[first + k]);
+        const uint2 sn = __ldg(&start_nodes[qi]);
+        if (lane < 5) {
+            const float4* src = lane == 0 ? qb.q0 : (lane == 1 ? qb.q1 : (lane == 2 ? qb.q2 : (lane == 3 ? qb.q3 : qb.q4)));
+            qrec[warp][k][lane] = src[qi];
+        }
+        if (lane < 3) qcol[warp][k][lane] = 0.0f;
+        const float4 a = qb.q0[qi];
+        __syncwarp();
+        kd_query(t, xyz(a), P.radius_sqr, sn, pend[warp], stk[warp], np, (uint32_t)k << 28, vc, flush);
+    }
+    if (np > 0) flush(np, pend[warp]);
+    __syncwarp();
+    if (lane < nslots) {
+        const F3 r = xyz(qrec[warp][lane][3]) * f3(qcol[warp][lane][0], qcol[warp][lane][1], qcol[warp][lane][2]);
+        if (r.x != 0.0f || r.y != 0.0f || r.z != 0.0f) {
+            const long long pixel = __float_as_int(qrec[warp][lane][2].w);
+            atomicAdd(&accum[3 * pixel + 0], (double)r.x);
+            atomicAdd(&accum[3 * pixel + 1], (double)r.y);
+            atomicAdd(&accum[3 * pixel + 2], (double)r.z);
         }
     }
     if (counters && lane == 0) {
@@ -356,12 +404,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_kd_query(const KdNav t,
         const long long j = order[slot];
         const F3 p = f3(qpos[3 * j], qpos[3 * j + 1], qpos[3 * j + 2]);
         const long long off = offsets ? offsets[j] : 0;
-        int n = 0;
-        kd_query(t, p, r2, start_nodes[j], pend[warp], stk[warp], vc, [&](int cnt, const uint32_t* list) {
+        int n = 0, np = 0;
+        auto flush = [&](int cnt, const uint32_t* list) {
             if (idx)
                 for (int k = lane; k < cnt; k += 32) idx[off + n + k] = (int)__ldg(&t.id[list[k]]);
             n += cnt;
-        });
+        };
+        kd_query(t, p, r2, start_nodes[j], pend[warp], stk[warp], np, 0u, vc, flush);
+        if (np > 0) flush(np, pend[warp]);
+        __syncwarp();
         if (lane == 0) counts[j] = n;
     }
 }

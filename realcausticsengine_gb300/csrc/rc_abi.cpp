@@ -627,6 +627,11 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         cap = (long long)nph + nph / 8 + 1024;
         if (attempt == 2) { ctx().err = "photon buffer overflow"; return RC_E_CAPACITY; }
     }
+    if (nph >= (1ull << 28)) {
+        // the KD node word holds a photon index in 28 bits (src/KD_Tree.h:13-32)
+        ctx().err = "more than 2^28 photons stored in one iteration";
+        return RC_E_CAPACITY;
+    }
     int r = check_errors();
     if (r) return r;
     if (sampler != RC_SAMPLER_UNIFORM) {
@@ -816,7 +821,7 @@ int async_setup(const HostScene& sc) {
     auto capacity = [tight](unsigned long long c) {
         return tight ? (long long)c : (long long)(((c + c / 50 + 4096) + 1023) / 1024 * 1024);
     };
-    d.async_pcap = capacity(d.last_photons);
+    d.async_pcap = std::min<long long>(capacity(d.last_photons), (1ll << 28) - 1);   // 28-bit photon index
     d.async_qcap = capacity(d.last_queries);
     RC_CUDA(d.ph_pos.reserve(d.async_pcap)); RC_CUDA(d.ph_dir.reserve(d.async_pcap));
     RC_CUDA(d.ph_tp.reserve(d.async_pcap)); RC_CUDA(d.ph_path.reserve(d.async_pcap));
