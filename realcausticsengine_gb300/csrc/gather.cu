@@ -266,18 +266,20 @@ __device__ __forceinline__ void kd_query(const KdNav& t, F3 q, float r2, uint2 s
     else kd_query_warp(t, q, r2, start_node, pend, np, tag, vc, flush);
 }
 
-// MinBlocks (resident blocks per SM the register allocation must allow) and QPW
-// (consecutive sorted queries per warp) are the autotuned shape parameters.
+// Traversal half of the gather.  MinBlocks (resident blocks per SM the register
+// allocation must allow) and QPW (consecutive sorted queries per warp) are the autotuned
+// shape parameters.  The warp's queries share the pending list (entry = query slot << 28
+// | tree position); every 32 accepted photons become 32 pairs (query index, position) in
+// the merge buffer, in query order.
 template <int MinBlocks, int QPW>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const VMParams P, const KdNav t,
-                                                                         TreePhotons tp, QueryBuf qb,
+                                                                         QueryBuf qb,
                                                                          const uint32_t* __restrict__ order,
                                                                          const uint2* __restrict__ start_nodes,
-                                                                         long long nq, double* __restrict__ accum,
+                                                                         long long nq, MergeBuf mb,
                                                                          unsigned long long* __restrict__ counters,
                                                                          const unsigned long long* __restrict__ nq_dev,
                                                                          const int* __restrict__ skip) {
-    constexpr int kQueriesPerWarp = QPW;
     static_assert(QPW <= 16, "a pending entry keeps its query slot in its top 4 bits");
     // device-side count (bounded by the capacity nq) and an iteration-wide skip flag,
     // for iterations enqueued without a host round trip
@@ -285,106 +287,120 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const
     if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
     __shared__ uint32_t pend[kWarpsPerBlock][64];
     __shared__ uint2 stk[kWarpsPerBlock][kRootStack];
-    // the warp's queries (position | camera dVM, shading normal | material, geometric
-    // normal | pixel, throughput, outgoing direction | dispersion channel) and their sums
-    __shared__ float4 qrec[kWarpsPerBlock][QPW][5];
-    __shared__ float qcol[kWarpsPerBlock][QPW][3];
+    __shared__ uint32_t qidx[kWarpsPerBlock][QPW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long w = blockIdx.x * (long long)kWarpsPerBlock + warp;
-    const long long first = w * kQueriesPerWarp;
+    const long long first = w * QPW;
     if (first >= nq) return;
-    const long long last = first + kQueriesPerWarp < nq ? first + kQueriesPerWarp : nq;
-    const int nslots = (int)(last - first);
+    const int nslots = (int)((first + QPW < nq ? first + QPW : nq) - first);
     VisitCounts vc{0u, 0u, 0u};
     unsigned accepted = 0;
-    // Merges of all the warp's queries share the pending list (entry = query slot << 28
-    // | tree position), so the lanes of a flush evaluate merges of several queries; the
-    // list is in slot order, and a segmented scan over the lanes sums each query's
-    // merges in a fixed order (the same image every run).
     auto flush = [&](int n, const uint32_t* list) {
-        for (int j0 = 0; j0 < n; j0 += 32) {
-            const int j = j0 + lane;
-            const bool valid = j < n;
-            const uint32_t entry = valid ? list[j] : 0u;
-            const int k = valid ? (int)(entry >> 28) : -1;
-            F3 cpair = f3(0.0f);
-            if (valid) {
-                const uint32_t p = entry & 0x0fffffffu;
-                const float4 a = qrec[warp][k][0], b = qrec[warp][k][1], c = qrec[warp][k][2];
-                const float4 e = qrec[warp][k][4];
-                const F3 ng = xyz(c);
-                Bsdf bs;
-                const DevMaterial& qm = P.materials[__float_as_int(b.w)];
-                const int channel = __float_as_int(e.w);   // the camera path's dispersion channel
-                bs.init(qm, xyz(b), xyz(e), true, (qm.disp > 0.0f && channel >= 0) ? (float)(channel - 1) * qm.disp : 0.0f);
-                const float wo_ng = dot(bs.fr.to_world(bs.wo), ng);
-                const float fwo = (bs.kind == BSDF_K_PLASTIC_GGX || bs.kind == BSDF_K_PLASTIC_SMOOTH)
-                                      ? fresnel_reflectance(fabsf(bs.wo.z), bs.s) : 0.0f;
-                const float4 p0 = __ldg(&tp.t0[p]);
-                const float4 p1 = __ldg(&tp.t1[p]);
-                const float2 p2 = __ldg(&tp.t2[p]);
-                const F3 wi = xyz(p1);
-                float fwd, rev;
-                F3 ev;
-                bs.eval_pdf(wi, ng, wo_ng, fwo, ev, fwd, rev);
-                const float weight = 1.0f / (1.0f + a.w * rev + p0.w * fwd);
-                cpair = ev * f3(p1.w, p2.x, p2.y) * weight;
-                if (P.path_contrib) {
-                    // learned-proposal training signal: the squared luminance this merge adds
-                    // to its pixel, summed per light path
-                    const F3 img = xyz(qrec[warp][k][3]) * cpair;
-                    const float lum = (fabsf(img.x) + fabsf(img.y) + fabsf(img.z)) * (1.0f / 3.0f);
-                    if (lum > 0.0f)
-                        atomicAdd(&P.path_contrib[__ldg(&P.photon_path[__ldg(&t.id[p])])], lum * lum);
-                }
-            }
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const float x = __shfl_up_sync(0xffffffffu, cpair.x, o);
-                const float y = __shfl_up_sync(0xffffffffu, cpair.y, o);
-                const float z = __shfl_up_sync(0xffffffffu, cpair.z, o);
-                const int ko = __shfl_up_sync(0xffffffffu, k, o);
-                if (lane >= o && ko == k) { cpair.x += x; cpair.y += y; cpair.z += z; }
-            }
-            const int knext = __shfl_down_sync(0xffffffffu, k, 1);
-            if (valid && (lane == 31 || knext != k)) {   // last lane of its slot's run
-                qcol[warp][k][0] += cpair.x;
-                qcol[warp][k][1] += cpair.y;
-                qcol[warp][k][2] += cpair.z;
-            }
-            __syncwarp();
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(mb.count, (unsigned long long)n);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        for (int j = lane; j < n; j += 32) {
+            const unsigned long long at = base + (unsigned long long)j;
+            const uint32_t entry = list[j];
+            if (at < (unsigned long long)mb.cap) mb.pairs[at] = make_uint2(qidx[warp][entry >> 28], entry & 0x0fffffffu);
         }
         accepted += (unsigned)n;
     };
     int np = 0;
     for (int k = 0; k < nslots; ++k) {
-        const long long qi = __ldg(&order[first + k]);
+        const uint32_t qi = __ldg(&order[first + k]);
+        if (lane == 0) qidx[warp][k] = qi;
         const uint2 sn = __ldg(&start_nodes[qi]);
-        if (lane < 5) {
-            const float4* src = lane == 0 ? qb.q0 : (lane == 1 ? qb.q1 : (lane == 2 ? qb.q2 : (lane == 3 ? qb.q3 : qb.q4)));
-            qrec[warp][k][lane] = src[qi];
-        }
-        if (lane < 3) qcol[warp][k][lane] = 0.0f;
         const float4 a = qb.q0[qi];
         __syncwarp();
         kd_query(t, xyz(a), P.radius_sqr, sn, pend[warp], stk[warp], np, (uint32_t)k << 28, vc, flush);
     }
     if (np > 0) flush(np, pend[warp]);
-    __syncwarp();
-    if (lane < nslots) {
-        const F3 r = xyz(qrec[warp][lane][3]) * f3(qcol[warp][lane][0], qcol[warp][lane][1], qcol[warp][lane][2]);
-        if (r.x != 0.0f || r.y != 0.0f || r.z != 0.0f) {
-            const long long pixel = __float_as_int(qrec[warp][lane][2].w);
-            atomicAdd(&accum[3 * pixel + 0], (double)r.x);
-            atomicAdd(&accum[3 * pixel + 1], (double)r.y);
-            atomicAdd(&accum[3 * pixel + 2], (double)r.z);
-        }
-    }
     if (counters && lane == 0) {
         atomicAdd(&counters[0], (unsigned long long)accepted);
         atomicAdd(&counters[1], (unsigned long long)vc.tests);
         atomicAdd(&counters[2], (unsigned long long)vc.buckets);
         atomicAdd(&counters[3], (unsigned long long)vc.nodes);
+    }
+}
+
+// Merge half of the gather (Path_Vertices::get_contrib, src/Path_Vertices.h:46-68): per
+// pair, the camera vertex's BSDF at the photon's direction, the MIS weight
+// 1 / (1 + dVM_cam pdf_rev + dVM_light pdf_fwd), times the photon throughput.  A
+// warp's pairs come in runs of one query (each traversal flush writes its pairs in query
+// order), so a segmented scan over the lanes sums each run and its last lane adds the
+// run, times the camera throughput, to the pixel's FP64 sum.
+constexpr int kMergeThreads = 256;
+__global__ void __launch_bounds__(kMergeThreads) k_merge(const VMParams P, TreePhotons tp, QueryBuf qb,
+                                                         const uint32_t* __restrict__ tree_id, MergeBuf mb,
+                                                         double* __restrict__ accum, const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    const unsigned long long n = *mb.count;
+    if (n > (unsigned long long)mb.cap) {
+        if (mb.overflow && blockIdx.x == 0 && threadIdx.x == 0) *mb.overflow = 1;
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const unsigned long long stride = (unsigned long long)gridDim.x * kMergeThreads;
+    // whole warps step together (the scan below needs every lane)
+    for (unsigned long long i0 = (unsigned long long)blockIdx.x * kMergeThreads + (threadIdx.x & ~31u); i0 < n;
+         i0 += stride) {
+        const unsigned long long i = i0 + (unsigned long long)lane;
+        const bool valid = i < n;
+        const uint2 pr = valid ? mb.pairs[i] : make_uint2(0xffffffffu, 0u);
+        const uint32_t qi = pr.x;
+        F3 cpair = f3(0.0f);
+        if (valid) {
+            const uint32_t p = pr.y;
+            const float4 a = qb.q0[qi], b = qb.q1[qi], c = qb.q2[qi], e = qb.q4[qi];
+            const F3 ng = xyz(c);
+            Bsdf bs;
+            const DevMaterial& qm = P.materials[__float_as_int(b.w)];
+            const int channel = __float_as_int(e.w);   // the camera path's dispersion channel
+            bs.init(qm, xyz(b), xyz(e), true, (qm.disp > 0.0f && channel >= 0) ? (float)(channel - 1) * qm.disp : 0.0f);
+            const float wo_ng = dot(bs.fr.to_world(bs.wo), ng);
+            const float fwo = (bs.kind == BSDF_K_PLASTIC_GGX || bs.kind == BSDF_K_PLASTIC_SMOOTH)
+                                  ? fresnel_reflectance(fabsf(bs.wo.z), bs.s) : 0.0f;
+            const float4 p0 = __ldg(&tp.t0[p]);
+            const float4 p1 = __ldg(&tp.t1[p]);
+            const float2 p2 = __ldg(&tp.t2[p]);
+            float fwd, rev;
+            F3 ev;
+            bs.eval_pdf(xyz(p1), ng, wo_ng, fwo, ev, fwd, rev);
+            const float weight = 1.0f / (1.0f + a.w * rev + p0.w * fwd);
+            cpair = ev * f3(p1.w, p2.x, p2.y) * weight;
+            if (P.path_contrib) {
+                // learned-proposal training signal: the squared luminance this merge adds
+                // to its pixel, summed per light path
+                const F3 img = xyz(qb.q3[qi]) * cpair;
+                const float lum = (fabsf(img.x) + fabsf(img.y) + fabsf(img.z)) * (1.0f / 3.0f);
+                if (lum > 0.0f) atomicAdd(&P.path_contrib[__ldg(&P.photon_path[__ldg(&tree_id[p])])], lum * lum);
+            }
+        }
+        // runs of equal query index, numbered by their heads: a query's pairs may form two
+        // runs in one window (its warp's flushes need not be adjacent in the buffer), and
+        // the scan must not join them across another query's run
+        const uint32_t qprev = __shfl_up_sync(0xffffffffu, qi, 1);
+        const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || qprev != qi);
+        const int run = __popc(heads & ((2u << lane) - 1u));
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float x = __shfl_up_sync(0xffffffffu, cpair.x, o);
+            const float y = __shfl_up_sync(0xffffffffu, cpair.y, o);
+            const float z = __shfl_up_sync(0xffffffffu, cpair.z, o);
+            const int ro = __shfl_up_sync(0xffffffffu, run, o);
+            if (lane >= o && ro == run) { cpair.x += x; cpair.y += y; cpair.z += z; }
+        }
+        const uint32_t qnext = __shfl_down_sync(0xffffffffu, qi, 1);
+        if (valid && (lane == 31 || qnext != qi)) {   // last lane of its query's run
+            const F3 r = xyz(qb.q3[qi]) * cpair;
+            if (r.x != 0.0f || r.y != 0.0f || r.z != 0.0f) {
+                const long long pixel = __float_as_int(qb.q2[qi].w);
+                atomicAdd(&accum[3 * pixel + 0], (double)r.x);
+                atomicAdd(&accum[3 * pixel + 1], (double)r.y);
+                atomicAdd(&accum[3 * pixel + 2], (double)r.z);
+            }
+        }
     }
 }
 
@@ -644,12 +660,24 @@ void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaS
 }
 
 template <int MB, int QPW>
-void launch_gather_t(const VMParams& p, const KdNav& nav, TreePhotons tp, QueryBuf qb, const uint32_t* order,
-                     const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters,
+void launch_gather_t(const VMParams& p, const KdNav& nav, QueryBuf qb, const uint32_t* order,
+                     const uint2* start_nodes, long long nq, MergeBuf mb, unsigned long long* counters,
                      cudaStream_t s, const unsigned long long* nq_dev, const int* skip) {
     const long long warps = (nq + QPW - 1) / QPW;
     k_gather<MB, QPW><<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
-        p, nav, tp, qb, order, start_nodes, nq, accum, counters, nq_dev, skip);
+        p, nav, qb, order, start_nodes, nq, mb, counters, nq_dev, skip);
+}
+
+unsigned merge_grid() {
+    static thread_local unsigned g = 0;
+    if (!g) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_merge, kMergeThreads, 0);
+        g = (unsigned)(sms * (per_sm > 0 ? per_sm : 1));
+    }
+    return g;
 }
 
 int gather_variants() { return 6; }
@@ -662,18 +690,20 @@ const char* gather_variant_name(int v) {
 }
 
 void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
-                   const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters, cudaStream_t s,
-                   int variant, const unsigned long long* nq_dev, const int* skip) {
+                   const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters, MergeBuf mb,
+                   cudaStream_t s, int variant, const unsigned long long* nq_dev, const int* skip) {
     if (nq <= 0) return;
     const KdNav nav = nav_of(tree);
+    cudaMemsetAsync(mb.count, 0, sizeof(unsigned long long), s);
     switch (variant) {
-    case 0: launch_gather_t<2, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
-    case 1: launch_gather_t<2, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
-    case 2: launch_gather_t<3, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
-    case 4: launch_gather_t<4, 8>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
-    case 5: launch_gather_t<4, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
-    default: launch_gather_t<3, 16>(p, nav, tp, qb, order, start_nodes, nq, accum, counters, s, nq_dev, skip); break;
+    case 0: launch_gather_t<2, 8>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 1: launch_gather_t<2, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 2: launch_gather_t<3, 8>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 4: launch_gather_t<4, 8>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 5: launch_gather_t<4, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    default: launch_gather_t<3, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
     }
+    k_merge<<<merge_grid(), kMergeThreads, 0, s>>>(p, tp, qb, tree.id, mb, accum, skip);
 }
 
 void launch_kd_query(const KdTree& tree, int q, const float* qpos, const uint32_t* order, const uint2* start_nodes,

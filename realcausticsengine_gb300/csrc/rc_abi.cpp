@@ -81,6 +81,11 @@ struct DeviceState {
     DevBuf<unsigned char> qscratch;
     DevBuf<double> accum;
     DevBuf<float> image;          // FP32 mean for readback
+    // photon-query merge pairs between the gather's traversal and its merge evaluation
+    DevBuf<uint2> merges;
+    DevBuf<unsigned long long> merge_count;
+    unsigned long long last_merges = 0;
+    long long async_mcap = 0;
     // learned emission proposal
     std::unique_ptr<MlpStore> mlp;
     DevBuf<float4> prop, train_pos, train_dir;
@@ -118,6 +123,8 @@ struct DeviceState {
         box_lo.release(); box_hi.release();
         accum.release();
         image.release();
+        merges.release(); merge_count.release();
+        last_merges = 0;
         mlp.reset();
         prop.release(); train_pos.release(); train_dir.release(); contrib.release(); train_wsum.release();
         train_count.release();
@@ -715,8 +722,14 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     int qlaunch = 0;
     launch_query_order(tree, reinterpret_cast<const float*>(d.q0.p), 4, (long long)nq, p.radius_sqr, d.qscratch.p,
                        d.qorder.p, d.qstart.p, &qlaunch, s);
+    // merge pairs: room for the last iteration's count + 1/4, at least 4 per query
+    long long mcap = std::max<long long>({(long long)d.merges.n, (long long)(d.last_merges + d.last_merges / 4) + 65536,
+                                          4 * (long long)nq});
+    RC_CUDA(d.merges.reserve(mcap));
+    RC_CUDA(d.merge_count.reserve(1));
     int variant = 3;
     if (cfg().autotune && nq > 0) {
+        const MergeBuf mb{d.merges.p, (long long)d.merges.n, d.merge_count.p, nullptr};
         const int cls = 63 - __builtin_clzll((unsigned long long)nq);
         if (g_tune.gather[cls].load() < 0) {
             // time every launch shape on this iteration's queries into a scratch image
@@ -725,9 +738,9 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             float best = 1e30f;
             int best_v = 3;
             for (int v = 0; v < gather_variants(); ++v) {
-                launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.tune_accum.p, nullptr, s, v);
+                launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.tune_accum.p, nullptr, mb, s, v);
                 RC_CUDA(cudaEventRecord(d.evm[0], s));
-                launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.tune_accum.p, nullptr, s, v);
+                launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.tune_accum.p, nullptr, mb, s, v);
                 RC_CUDA(cudaEventRecord(d.evm[1], s));
                 RC_CUDA(cudaEventSynchronize(d.evm[1]));
                 const float ms = ms_between(d.evm[0], d.evm[1]);
@@ -740,15 +753,27 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         }
         variant = g_tune.gather[cls].load();
     }
-    RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
-    RC_CUDA(cudaEventRecord(d.evg[0], s));
-    launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.accum.p, d.counters.p + 2, s, variant);
-    RC_CUDA(cudaEventRecord(d.evg[1], s));
-    RC_CUDA(cudaGetLastError());
-    RC_CUDA(cudaEventRecord(d.ev[7], s));
-    unsigned long long gc[4] = {0, 0, 0, 0};
-    RC_CUDA(cudaMemcpyAsync(gc, d.counters.p + 2, sizeof(gc), cudaMemcpyDeviceToHost, s));
-    RC_CUDA(cudaStreamSynchronize(s));
+    unsigned long long gc[4] = {0, 0, 0, 0}, nmerge = 0;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        // the merge evaluation does nothing when the pairs overflowed, so the gather can
+        // simply run again with a larger buffer
+        RC_CUDA(d.merges.reserve(mcap));
+        const MergeBuf mb{d.merges.p, (long long)d.merges.n, d.merge_count.p, nullptr};
+        RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
+        RC_CUDA(cudaEventRecord(d.evg[0], s));
+        launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.accum.p, d.counters.p + 2, mb, s,
+                      variant);
+        RC_CUDA(cudaEventRecord(d.evg[1], s));
+        RC_CUDA(cudaGetLastError());
+        RC_CUDA(cudaEventRecord(d.ev[7], s));
+        RC_CUDA(cudaMemcpyAsync(gc, d.counters.p + 2, sizeof(gc), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(cudaMemcpyAsync(&nmerge, d.merge_count.p, sizeof(nmerge), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(cudaStreamSynchronize(s));
+        if ((long long)nmerge <= (long long)d.merges.n) break;
+        mcap = (long long)(nmerge + nmerge / 8) + 65536;
+        if (attempt == 2) { ctx().err = "merge pair buffer overflow"; return RC_E_CAPACITY; }
+    }
+    d.last_merges = nmerge;
     if (train) {
         RC_CUDA(cudaEventRecord(d.evm[0], s));
         r = proposal_train(sc, p);
@@ -823,6 +848,11 @@ int async_setup(const HostScene& sc) {
     };
     d.async_pcap = std::min<long long>(capacity(d.last_photons), (1ll << 28) - 1);   // 28-bit photon index
     d.async_qcap = capacity(d.last_queries);
+    // merge pairs vary more between iterations than photons and queries: 1/8 margin
+    d.async_mcap = tight ? (long long)std::max<unsigned long long>(d.last_merges, 1)
+                         : (long long)(d.last_merges + d.last_merges / 8) + 65536;
+    RC_CUDA(d.merges.reserve(d.async_mcap));
+    RC_CUDA(d.merge_count.reserve(1));
     RC_CUDA(d.ph_pos.reserve(d.async_pcap)); RC_CUDA(d.ph_dir.reserve(d.async_pcap));
     RC_CUDA(d.ph_tp.reserve(d.async_pcap)); RC_CUDA(d.ph_path.reserve(d.async_pcap));
     RC_CUDA(d.q0.reserve(d.async_qcap)); RC_CUDA(d.q1.reserve(d.async_qcap)); RC_CUDA(d.q2.reserve(d.async_qcap));
@@ -893,7 +923,8 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
                        d.qstart.p, nullptr, s, d.counters.p + 1);
     RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
     RC_CUDA(record(d.evg[0], s));
-    launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, qc, d.accum.p, d.counters.p + 2, s, d.async_gvar,
+    const MergeBuf mb{d.merges.p, d.async_mcap, d.merge_count.p, flag};
+    launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, qc, d.accum.p, d.counters.p + 2, mb, s, d.async_gvar,
                   d.counters.p + 1, flag);
     RC_CUDA(record(d.evg[1], s));
     RC_CUDA(record(d.ev[7], s));

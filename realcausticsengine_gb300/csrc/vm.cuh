@@ -48,6 +48,17 @@ struct TreePhotons {
     float2* t2;
 };
 
+// Photon-query merge pairs, written by the gather's traversal and read by its merge
+// evaluation: pairs[i] = (query index, tree position).  *count may exceed cap (the
+// pairs beyond cap are dropped and the evaluation does nothing; *overflow, when given,
+// is set so that the iteration is rendered again).
+struct MergeBuf {
+    uint2* pairs;
+    long long cap;
+    unsigned long long* count;
+    int* overflow;
+};
+
 struct LightsView {
     const DevLight* lights;
     const float* cdf;      // n + 1 entries
@@ -120,9 +131,11 @@ void launch_query_order(const KdTree& tree, const float* qpos, int stride, long 
 // the autotuner starts from.
 // With nq_dev the query count is read on the device (bounded by num_queries, the
 // capacity the grid is sized for) and a non-zero *skip makes the launch a no-op.
+// Two kernels: the traversal writes the accepted photon-query pairs to `mb`, then the
+// merge evaluation (BSDF, MIS weight, FP64 pixel sums) runs over the pairs.
 void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
                    const uint2* start_nodes, long long num_queries, double* accum, unsigned long long* counters,
-                   cudaStream_t s, int variant = 3, const unsigned long long* nq_dev = nullptr,
+                   MergeBuf mb, cudaStream_t s, int variant = 3, const unsigned long long* nq_dev = nullptr,
                    const int* skip = nullptr);
 int gather_variants();
 // Launch shapes of the persistent light and camera passes (block size x traversal-stack
