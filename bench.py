@@ -48,7 +48,7 @@ METRIC = "photons/s"
 # bytes per unit of the gather (algorithmic): photon record read once, query record
 # read once, FP64 RGB pixel read+write once per query
 PHOTON_BYTES, QUERY_BYTES, PIXEL_BYTES = 40, 80, 48
-GATHER_TRAFFIC_OVER_ALGORITHMIC = 1.253
+GATHER_TRAFFIC_OVER_ALGORITHMIC = 1.147
 
 
 def dist_env():
@@ -246,10 +246,11 @@ def run_ours(args):
         return
     peak, peak_kind = measured_peaks()
     achieved = gather_bytes / (gather_ms_mean / 1000.0) / 1e9 if gather_ms_mean > 0 else 0.0
-    # DRAM bytes per gather launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of one
-    # launch on the 960x540 / 4M-path case (profiles/k_gather_water_pool_960x540.md) is
-    # 1.253x that launch's algorithmic bytes; scaled to this workload's launch by its
-    # algorithmic bytes (photon and query records both scale with their counts)
+    # DRAM bytes per gather (traversal + merge kernels): ncu dram__bytes_read.sum +
+    # dram__bytes_write.sum of one gather on the 960x540 / 4M-path case
+    # (profiles/k_gather_water_pool_960x540.md) is 1.147x its algorithmic bytes; scaled to
+    # this workload's gather by its algorithmic bytes (photon and query records both scale
+    # with their counts)
     traffic = GATHER_TRAFFIC_OVER_ALGORITHMIC * gather_bytes
     line = {
         "metric": METRIC, "value": float(vals[0]) if world == 1 else float(vals[0]), "unit": METRIC,
@@ -263,7 +264,7 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": float(e2es[0]), "unit": METRIC, "h2d_bytes_per_step": int(h2d // max(args.steps, 1)),
                 "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"kernel": "k_gather", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"kernel": "k_gather + k_merge (the gather)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes": gather_bytes},
         "gpu_launches": int(dev[3]),

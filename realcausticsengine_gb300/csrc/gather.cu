@@ -680,13 +680,14 @@ unsigned merge_grid() {
     return g;
 }
 
-int gather_variants() { return 6; }
+int gather_variants() { return 8; }
 
 const char* gather_variant_name(int v) {
-    static const char* names[6] = {"blocks/SM>=2, 8 queries/warp", "blocks/SM>=2, 16 queries/warp",
+    static const char* names[8] = {"blocks/SM>=2, 8 queries/warp", "blocks/SM>=2, 16 queries/warp",
                                    "blocks/SM>=3, 8 queries/warp", "blocks/SM>=3, 16 queries/warp",
-                                   "blocks/SM>=4, 8 queries/warp", "blocks/SM>=4, 16 queries/warp"};
-    return (v >= 0 && v < 6) ? names[v] : "?";
+                                   "blocks/SM>=4, 8 queries/warp", "blocks/SM>=4, 16 queries/warp",
+                                   "blocks/SM>=5, 16 queries/warp", "blocks/SM>=6, 16 queries/warp"};
+    return (v >= 0 && v < 8) ? names[v] : "?";
 }
 
 void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
@@ -701,6 +702,8 @@ void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryB
     case 2: launch_gather_t<3, 8>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
     case 4: launch_gather_t<4, 8>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
     case 5: launch_gather_t<4, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 6: launch_gather_t<5, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 7: launch_gather_t<6, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
     default: launch_gather_t<3, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
     }
     k_merge<<<merge_grid(), kMergeThreads, 0, s>>>(p, tp, qb, tree.id, mb, accum, skip);
