@@ -103,13 +103,17 @@ typedef struct rc_config {
     int write_exr;              /* main(): 1 = write EXR (reference behaviour)           */
     char exr_path[256];         /* main(): output file, default "D:\\caustics.exr"       */
     int verbose;                /* 1 = print per-iteration JSON lines to stdout          */
-    /* learned emission proposal (UNIFORM sampler, area and point lights): an MLP maps
-     * the emission position to a 16-lobe von Mises-Fisher mixture over directions, used
-     * in a defensive mixture with the light's own density (fraction 0.2).  It is trained
+    /* learned emission proposal (area and point lights): an MLP maps the emission
+     * position to a 16-lobe von Mises-Fisher mixture over directions, used in a
+     * defensive mixture with the light's own density (fraction 0.2).  It is trained
      * online on the light paths whose photons the camera merged, during the first
      * `train_iterations` iterations (`train_steps` Adam steps of 16384 samples each,
      * learning rate `learning_rate`), and guides emission from the iteration after the
-     * first training round.  No counterpart in the reference. */
+     * first training round.  With the HYBRID or PSSMLT sampler the training iterations
+     * are plain (uniform-sampler) iterations; the chains of the later ones draw their
+     * emission from the network evaluated on a 32 x 32 grid over each light (one extra
+     * primary-sample dimension picks the mixture component).  No counterpart in the
+     * reference. */
     int learned_proposal;
     int train_iterations;       /* default 8                                             */
     int train_steps;            /* default 64                                            */

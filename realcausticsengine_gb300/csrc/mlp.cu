@@ -1,6 +1,7 @@
 // MLP emission proposal: tcgen05 forward / backward kernels, loss, Adam.
 #include "mlp.cuh"
 #include "lights.cuh"
+#include "proposal.cuh"
 #include "tc_gemm.cuh"
 #include "rng.cuh"
 
@@ -13,7 +14,6 @@ namespace rc {
 namespace {
 
 constexpr uint32_t kWait = 1u << 22;
-constexpr float kKappaMin = 0.1f, kKappaMax = 2000.0f;
 
 // sin/cos(2^k pi c) for k = 0..11: sincospi at k = 0, then the double-angle identities
 // sin 2a = 2 sin a cos a, cos 2a = 1 - 2 sin^2 a (rounding error doubles per step:
@@ -204,27 +204,6 @@ struct BatchIO {
 };
 
 // ----------------------------------------------------------------------------- proposal
-__device__ __forceinline__ F3 sample_vmf(F3 mu, float kappa, float u1, float u2) {
-    u1 = fmaxf(u1, 1e-7f);
-    const float w = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * kappa)) / kappa;
-    const float st = sqrtf(fmaxf(0.0f, 1.0f - w * w));
-    Frame f;
-    f.set_from_z(mu);
-    float sp, cp;
-    sincosf(kPI2 * u2, &sp, &cp);
-    return f.x * (st * cp) + f.y * (st * sp) + mu * w;
-}
-
-// Fast-intrinsic vMF density for the proposal weights (relative error ~1e-6 against
-// the sampler's own density: a bias of that order in p_light / q).
-__device__ __forceinline__ float vmf_pdf_fast(float kappa, float cosang) {
-    return kappa * __expf(kappa * (cosang - 1.0f)) / (kPI2 * (1.0f - __expf(-2.0f * kappa)));
-}
-__device__ __forceinline__ float kappa_of(float raw) {
-    const float sp = raw > 20.0f ? raw : __logf(1.0f + __expf(raw));
-    return fminf(kKappaMin + sp, kKappaMax);
-}
-
 struct ProposalIO {
     struct State {
         int light;
@@ -290,6 +269,52 @@ struct ProposalIO {
         }
         const float q = kMlpDefensive * pl + (1.0f - kMlpDefensive) * (S / sum);
         prop[row] = make_float4(w.x, w.y, w.z, (pl > 0.0f && q > 0.0f) ? pl / q : 0.0f);
+    }
+};
+
+// The tabulated proposal (proposal.cuh): one row per (light, cell); the cell centre's
+// position in, the mixture (cumulative lobe weights, unit means, concentrations) out.
+struct TableIO {
+    struct State {};
+    ProposalCtx c;
+    int res;
+    float* cells;
+    __device__ __forceinline__ void input(long long row, bool valid, float* x, State&) const {
+        if (!valid) {
+#pragma unroll
+            for (int i = 0; i < kMlpIn; ++i) x[i] = 0.0f;
+            return;
+        }
+        const int cells_per_light = res * res;
+        const int li = (int)(row / cells_per_light), cell = (int)(row % cells_per_light);
+        const DevLight& l = c.lights.lights[li];
+        const float u1 = ((cell % res) + 0.5f) / (float)res, u2 = ((cell / res) + 0.5f) / (float)res;
+        F3 o;
+        if (l.type == LIGHT_POINT) o = ld3(l.pos);
+        else o = ld3(l.bl) + ld3(l.hz) * u1 + ld3(l.vt) * u2;   // light_position's area/sun mapping
+        encode((o.x - c.bmin[0]) * c.binv[0], (o.y - c.bmin[1]) * c.binv[1], (o.z - c.bmin[2]) * c.binv[2], x);
+    }
+    __device__ __forceinline__ void output(long long row, bool valid, const float* o, const State&) const {
+        if (!valid) return;
+        float mxl = -INFINITY;
+#pragma unroll
+        for (int k = 0; k < kMlpLobes; ++k) mxl = fmaxf(mxl, o[5 * k]);
+        float e[kMlpLobes], sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kMlpLobes; ++k) { e[k] = __expf(o[5 * k] - mxl); sum += e[k]; }
+        float* out = cells + (size_t)row * kProposalCellFloats;
+        float cum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kMlpLobes; ++k) {
+            cum += e[k];
+            const float x = o[5 * k + 1], y = o[5 * k + 2], z = o[5 * k + 3];
+            const float len = fmaxf(sqrtf(x * x + y * y + z * z), 1e-6f);
+            out[5 * k + 0] = k == kMlpLobes - 1 ? 1.0f : cum / sum;   // sampling and density agree
+            out[5 * k + 1] = x / len;
+            out[5 * k + 2] = y / len;
+            out[5 * k + 3] = z / len;
+            out[5 * k + 4] = kappa_of(o[5 * k + 4]);
+        }
     }
 };
 
@@ -733,6 +758,22 @@ int mlp_proposal(const MlpParams& p, const ProposalCtx& c, long long n, float4* 
     const long long tiles = (n + 127) / 128;
     const int grid = (int)(tiles < forward_blocks() ? tiles : forward_blocks());
     k_mlp_forward<ProposalIO><<<grid, 128, smem, s>>>(p, io, n, err);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int mlp_proposal_table(const MlpParams& p, const ProposalCtx& c, int res, float* cells, cudaStream_t s, int* err) {
+    const long long n = (long long)c.lights.count * res * res;
+    if (n <= 0) return 0;
+    TableIO io{c, res, cells};
+    const size_t smem = SmemFwd::total;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_mlp_forward<TableIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    const long long tiles = (n + 127) / 128;
+    const int grid = (int)(tiles < forward_blocks() ? tiles : forward_blocks());
+    k_mlp_forward<TableIO><<<grid, 128, smem, s>>>(p, io, n, err);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

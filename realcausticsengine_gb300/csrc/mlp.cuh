@@ -81,6 +81,9 @@ struct ProposalCtx {
 
 size_t mlp_param_floats();
 int mlp_proposal(const MlpParams& p, const ProposalCtx& c, long long n, float4* prop, cudaStream_t s, int* err);
+// The tabulated proposal for the Metropolis samplers (proposal.cuh): the mixture at the
+// centres of res x res cells per light, written to cells (lights x res x res x 80 floats).
+int mlp_proposal_table(const MlpParams& p, const ProposalCtx& c, int res, float* cells, cudaStream_t s, int* err);
 // Training samples from the light paths that contributed to the image (contrib > 0,
 // contrib = the gather's per-path sum of squared per-merge luminance):
 // pos4 = (normalised emission position, p_light(dir)), dir4 = (dir, sqrt(contrib)),

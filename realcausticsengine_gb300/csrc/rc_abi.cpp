@@ -16,6 +16,7 @@
 #include "bvh_build.h"
 #include "host_scene.h"
 #include "mlp.cuh"
+#include "proposal.cuh"
 #include "realcaustics.h"
 #include "vm.cuh"
 
@@ -89,6 +90,7 @@ struct DeviceState {
     // learned emission proposal
     std::unique_ptr<MlpStore> mlp;
     DevBuf<float4> prop, train_pos, train_dir;
+    DevBuf<float> prop_table;   // tabulated proposal for the Metropolis samplers
     DevBuf<float> contrib, train_wsum;
     DevBuf<unsigned> train_count;
     cudaEvent_t evm[2] = {};
@@ -127,6 +129,7 @@ struct DeviceState {
         last_merges = 0;
         mlp.reset();
         prop.release(); train_pos.release(); train_dir.release(); contrib.release(); train_wsum.release();
+        prop_table.release();
         train_count.release();
         mlp_rounds = 0;
         mlp_last_rows = 0;
@@ -581,8 +584,14 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     cudaStream_t s = d.stream;
     const int it = redo_iteration >= 0 ? redo_iteration : d.iterations_done;
     VMParams p = make_params(sc, it);
-    const bool learned = cfg().learned_proposal && cfg().sampler == RC_SAMPLER_UNIFORM;
+    // With a Metropolis sampler and the learned proposal, the first train_iterations
+    // iterations are plain ones that train the network; the chains of the later ones
+    // draw their emission from the network's table (proposal.cuh).
+    const bool train_phase = cfg().learned_proposal && it < cfg().train_iterations;
+    const int sampler = (cfg().sampler != RC_SAMPLER_UNIFORM && train_phase) ? RC_SAMPLER_UNIFORM : cfg().sampler;
+    const bool learned = cfg().learned_proposal && sampler == RC_SAMPLER_UNIFORM;
     const bool train = learned && it < cfg().train_iterations;
+    const bool tabulated = cfg().learned_proposal && sampler != RC_SAMPLER_UNIFORM && d.mlp && d.mlp_rounds > 0;
     float t_mlp = 0.0f;
     const long long npix = (long long)sc.camera.width * sc.camera.height;
     if (d.accum.n < (size_t)(3 * npix)) {
@@ -596,7 +605,17 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     unsigned long long nph = 0;
     unsigned long long mlt[2] = {0, 0};
     float t_light = 0.0f;
-    const int sampler = cfg().sampler;
+    if (tabulated) {
+        RC_CUDA(cudaEventRecord(d.evm[0], s));
+        RC_CUDA(d.prop_table.reserve((size_t)sc.lights.size() * kProposalRes * kProposalRes * kProposalCellFloats));
+        if (mlp_proposal_table(d.mlp->p, proposal_ctx(sc, p), kProposalRes, d.prop_table.p, s, d.errors.p + ERR_MLP)) {
+            ctx().err = "proposal table launch failed";
+            return RC_E_CUDA;
+        }
+        RC_CUDA(cudaEventRecord(d.evm[1], s));
+        p.proposal_table = d.prop_table.p;
+        p.proposal_table_res = kProposalRes;
+    }
     for (int attempt = 0; attempt < 3; ++attempt) {
         RC_CUDA(d.ph_pos.reserve(cap)); RC_CUDA(d.ph_dir.reserve(cap));
         RC_CUDA(d.ph_tp.reserve(cap)); RC_CUDA(d.ph_path.reserve(cap));
@@ -629,7 +648,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             RC_CUDA(cudaMemcpyAsync(mlt, d.counters.p + 2, sizeof(mlt), cudaMemcpyDeviceToHost, s));
         RC_CUDA(cudaStreamSynchronize(s));
         t_light = ms_between(d.ev[0], d.ev[1]);
-        if (learned) t_mlp = ms_between(d.evm[0], d.evm[1]);
+        if (learned || tabulated) t_mlp = ms_between(d.evm[0], d.evm[1]);
         if ((long long)nph <= cap) break;
         cap = (long long)nph + nph / 8 + 1024;
         if (attempt == 2) { ctx().err = "photon buffer overflow"; return RC_E_CAPACITY; }
@@ -1380,7 +1399,6 @@ int rc_set_config(const rc_config* c) {
         ctx().err = "unknown sampler"; return RC_E_INVALID;
     }
     if (c->learned_proposal) {
-        if (c->sampler != RC_SAMPLER_UNIFORM) { ctx().err = "learned_proposal requires the uniform sampler"; return RC_E_UNSUPPORTED; }
         if (c->train_iterations < 0 || c->train_steps < 0 || !(c->learning_rate > 0.0f && c->learning_rate < 1.0f)) {
             ctx().err = "learned proposal: train_iterations/train_steps >= 0, learning_rate in (0, 1)"; return RC_E_INVALID;
         }

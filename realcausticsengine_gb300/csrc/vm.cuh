@@ -84,6 +84,9 @@ struct VMParams {
     float* path_contrib;    // gather: per light path, sum over its merges of the squared
                             // luminance each adds to its pixel (proposal training)
     const uint32_t* photon_path;   // photon buffer index -> light path (with path_contrib)
+    // tabulated learned proposal for the Metropolis samplers (proposal.cuh; nullptr: none)
+    const float* proposal_table;
+    int proposal_table_res;
 };
 
 // error flag slots

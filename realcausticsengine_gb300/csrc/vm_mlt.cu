@@ -14,6 +14,11 @@
 //   back to its last state, is mutated, and the mutation is traced and accepted if it
 //   stores a photon.  All stored photons are kept; the estimator scales them by
 //   V/N (visible large steps over light paths), applied here through VM_normalization.
+// With the learned proposal (P.proposal_table), the emission direction is drawn from the
+// tabulated proposal at the emission cell (dims 3, 4 and the extra last dim for the
+// mixture choice) and the path throughput carries p_light / q; the chains then explore
+// the primary-sample space of that emission.
+//
 // RC_SAMPLER_PSSMLT - a visibility-target primary-sample Metropolis chain: each step is
 //   a large step with probability p_large, else a small step; a visible proposal is
 //   accepted, an invisible one rejected.  Every step deposits the current state's
@@ -25,6 +30,7 @@
 #include "vm.cuh"
 #include "bsdf.cuh"
 #include "lights.cuh"
+#include "proposal.cuh"
 #include "rng.cuh"
 
 namespace rc {
@@ -32,7 +38,8 @@ namespace rc {
 namespace {
 
 constexpr int kMltMaxLen = 12;                        // longest path the sample vector covers
-constexpr int kMltDims = 5 + 3 * (kMltMaxLen + 1);    // (max_path_length + 2) * 3 + 2
+// (max_path_length + 2) * 3 + 2 dims as the reference, plus the proposal's mixture choice
+constexpr int kMltDims = 5 + 3 * (kMltMaxLen + 1) + 1;
 constexpr int kPhotonBuf = kMltMaxLen + 2;
 
 struct PhotonRec { float4 pos, dir; float2 tp; };
@@ -42,7 +49,22 @@ struct PhotonRec { float4 pos, dir; float2 tp; };
 // takes them from its global stream).  Returns the number of photons.
 __device__ int trace_light_samples(const VMParams& P, const float* u, const PathRng& rr, int maxlen, PhotonRec* out) {
     F3 o, d, tp;
-    sample_light(P.lights, u[0], u[1], u[2], u[3], u[4], o, d, tp);
+    if (P.proposal_table) {
+        const LightSample ls = light_position(P.lights, u[0], u[1], u[2]);
+        const DevLight& l = P.lights.lights[ls.idx];
+        o = ls.o;
+        tp = ls.tp;
+        if (l.type == LIGHT_SUN) {
+            d = light_direction(l, u[3], u[4]);
+        } else {
+            const float ratio = table_direction(ProposalTable{P.proposal_table, P.proposal_table_res}, l, ls.idx, u[1],
+                                                u[2], u[3], u[4], u[kMltDims - 1], d);
+            if (!(ratio > 0.0f)) return 0;
+            tp = tp * ratio;
+        }
+    } else {
+        sample_light(P.lights, u[0], u[1], u[2], u[3], u[4], o, d, tp);
+    }
     int diffuse = 0, last = EV_DIFFUSE, n = 0, channel = -1;
     float dVM = 0.0f;
     for (int len = 0;; ++len) {

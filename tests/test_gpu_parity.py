@@ -322,16 +322,19 @@ def test_no_photons_is_not_an_error():
     assert st["photons"] == 0 and (img == 0).all()
 
 
-def _render_mean(sc, sampler, chains, iters, paths=0, maxlen=6, seed=3):
+def _render_mean(sc, sampler, chains, iters, paths=0, maxlen=6, seed=3, learned=False, stats=None):
     from realcausticsengine_gb300 import abi
     r = Renderer(sc, max_path_length=maxlen, photons_per_iter=paths, seed=seed)
     cfg = abi.RcConfig()
     r.L.rc_default_config(C.byref(cfg))
     cfg.max_path_length, cfg.photons_per_iter, cfg.seed = maxlen, paths, seed
     cfg.sampler, cfg.mlt_chains, cfg.write_exr = sampler, chains, 0
+    cfg.learned_proposal = int(learned)
     assert r.L.rc_set_config(C.byref(cfg)) == 0, r.L.rc_last_error()
     r.render(iters)
     img = r.image()
+    if stats is not None:
+        stats.update(r.stats())
     r.release()
     return float(img.mean())
 
@@ -420,3 +423,29 @@ def test_graph_replay_matches_round_trips(mode):
     a, b = imgs
     assert a.max() > 0
     assert np.abs(a - b).max() <= 1e-4 * a.max(), np.abs(a - b).max()
+
+
+def test_pssmlt_with_learned_proposal_is_consistent():
+    """PSSMLT with the learned emission proposal: 8 plain iterations train the network,
+    then the chains draw emission from its table (mixture per cell of a 32 x 32 grid on
+    the light, weight p_light / q).  The estimate stays that of plain vertex merging:
+    means within 5% over 60 iterations.  (stats[8] is the proposal time of the last
+    iteration: non-zero only when the table was built, i.e. the network was trained.)"""
+    sc = scenes.glass_sphere_point(48, 36, subdiv=3, light="area")
+    plain = _render_mean(sc, 0, 1, 60, paths=200000, seed=11)
+    st = {}
+    pss = _render_mean(sc, 2, 4096, 60, paths=200000, seed=11, learned=True, stats=st)
+    assert st["accum_ms"] > 0.0, "the proposal table was not used"
+    assert abs(pss / plain - 1.0) < 0.05, (pss, plain)
+
+
+def test_hybrid_with_learned_proposal_runs():
+    """The reference's hybrid Metropolis scheme with the learned proposal: the chains
+    draw from the table after the training iterations.  The hybrid estimate is the
+    reference's own (photons of accepted mutations kept with weight 1, all scaled by the
+    visible fraction of large steps), which is not plain vertex merging's mean, so only
+    a positive image and the table's use are checked here."""
+    sc = scenes.glass_sphere_point(48, 36, subdiv=3, light="area")
+    st = {}
+    hyb = _render_mean(sc, 1, 4096, 12, paths=200000, seed=11, learned=True, stats=st)
+    assert st["accum_ms"] > 0.0 and hyb > 0.0
