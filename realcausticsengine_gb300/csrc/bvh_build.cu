@@ -754,8 +754,8 @@ __global__ void __launch_bounds__(1024) k_scan_add(int* out, int n, const int* t
 }
 
 __global__ void k_emit(const NodeRec* small_pool, long long nsmall, const NodeRec* large_pool, const int* large_count,
-                       int large_cap, const int* prefix, const int* topd, long long nn, float4* node_lo,
-                       float4* node_hi, int* parent, int* flags) {
+                       int large_cap, const int* prefix, const int* topd, long long nn, float4* nodes, int* parent,
+                       int* flags) {
     const long long total = nsmall + min(*large_count, large_cap);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < total;
          r += (long long)gridDim.x * blockDim.x) {
@@ -775,16 +775,16 @@ __global__ void k_emit(const NodeRec* small_pool, long long nsmall, const NodeRe
             parent[right] = (int)pre;
         }
         if (pre < 0 || pre >= nn) { atomicOr(flags, kFlagIndex); continue; }
-        node_lo[pre] = make_float4(rec.lo.x, rec.lo.y, rec.lo.z, __uint_as_float(w0));
-        node_hi[pre] = make_float4(rec.hi.x, rec.hi.y, rec.hi.z, __uint_as_float(w1));
+        nodes[2 * pre] = make_float4(rec.lo.x, rec.lo.y, rec.lo.z, __uint_as_float(w0));
+        nodes[2 * pre + 1] = make_float4(rec.hi.x, rec.hi.y, rec.hi.z, __uint_as_float(w1));
     }
 }
 
 // CostOfTraversing (src/BVH/BVH_mesh.cpp:286-305) bottom-up.
-__global__ void k_cost(const float4* __restrict__ lo, const float4* __restrict__ hi, const int* __restrict__ parent,
-                       long long nn, int* arrive, float* cost, int* flags) {
+__global__ void k_cost(const float4* __restrict__ nodes, const int* __restrict__ parent, long long nn, int* arrive,
+                       float* cost, int* flags) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nn; v += (long long)gridDim.x * blockDim.x) {
-        const uint32_t w0 = __float_as_uint(lo[v].w);
+        const uint32_t w0 = __float_as_uint(nodes[2 * v].w);
         if (!(w0 & 0x80000000u)) continue;
         float c = (float)(w0 & 0x7fffffffu);
         __stcg(&cost[v], c);
@@ -797,12 +797,12 @@ __global__ void k_cost(const float4* __restrict__ lo, const float4* __restrict__
             __threadfence();
             if (atomicAdd(&arrive[p], 1) == 0) break;   // the sibling subtree finishes the parent
             __threadfence();
-            const float4 pl = lo[p], ph = hi[p];
+            const float4 pl = nodes[2 * p], ph = nodes[2 * p + 1];
             const uint32_t l = __float_as_uint(pl.w), r = __float_as_uint(ph.w);
             if (l >= nn || r >= nn) { atomicOr(flags, kFlagIndex); break; }
             const float a = surface_area(pl, ph);
-            const float la = surface_area(lo[l], hi[l]);
-            const float ra = surface_area(lo[r], hi[r]);
+            const float la = surface_area(nodes[2 * l], nodes[2 * l + 1]);
+            const float ra = surface_area(nodes[2 * r], nodes[2 * r + 1]);
             c = (float)(0.16874 + (double)((__ldcg(&cost[l]) * la + __ldcg(&cost[r]) * ra) / a));
             __stcg(&cost[p], c);
             cur = p;
@@ -814,8 +814,8 @@ __global__ void k_cost(const float4* __restrict__ lo, const float4* __restrict__
 __global__ void k_pack_tris(const uint32_t* __restrict__ perm, const float* __restrict__ wpos,
                             const float* __restrict__ wnrm, const uint32_t* __restrict__ tri,
                             const uint32_t* __restrict__ mat, const uint32_t* __restrict__ tri_off,
-                            const uint32_t* __restrict__ vert_off, int M, int N, float4* v0, float4* e1, float4* e2,
-                            float4* n0, float4* n1, float4* n2) {
+                            const uint32_t* __restrict__ vert_off, int M, int N, float4* tris, float4* n0,
+                            float4* n1, float4* n2) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
         const uint32_t t = perm[j];
         const int m = find_mesh(tri_off, M, t);
@@ -824,21 +824,22 @@ __global__ void k_pack_tris(const uint32_t* __restrict__ perm, const float* __re
         const size_t ib = 3 * (size_t)(tri[3 * (size_t)t + 1] + vo);
         const size_t ic = 3 * (size_t)(tri[3 * (size_t)t + 2] + vo);
         const float ax = wpos[ia], ay = wpos[ia + 1], az = wpos[ia + 2];
-        v0[j] = make_float4(ax, ay, az, __uint_as_float(t));
-        e1[j] = make_float4(wpos[ib] - ax, wpos[ib + 1] - ay, wpos[ib + 2] - az, __uint_as_float(mat[t]));
-        e2[j] = make_float4(wpos[ic] - ax, wpos[ic + 1] - ay, wpos[ic + 2] - az, __uint_as_float((uint32_t)m));
+        tris[3 * (size_t)j] = make_float4(ax, ay, az, __uint_as_float(t));
+        tris[3 * (size_t)j + 1] = make_float4(wpos[ib] - ax, wpos[ib + 1] - ay, wpos[ib + 2] - az, __uint_as_float(mat[t]));
+        tris[3 * (size_t)j + 2] =
+            make_float4(wpos[ic] - ax, wpos[ic + 1] - ay, wpos[ic + 2] - az, __uint_as_float((uint32_t)m));
         n0[j] = make_float4(wnrm[ia], wnrm[ia + 1], wnrm[ia + 2], 0.0f);
         n1[j] = make_float4(wnrm[ib], wnrm[ib + 1], wnrm[ib + 2], 0.0f);
         n2[j] = make_float4(wnrm[ic], wnrm[ic + 1], wnrm[ic + 2], 0.0f);
     }
 }
 
-__global__ void k_mesh_results(const uint32_t* tri_off, int M, const int* prefix, const float4* lo, const float4* hi,
+__global__ void k_mesh_results(const uint32_t* tri_off, int M, const int* prefix, const float4* nodes,
                                const float* cost, float* out) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M) return;
     const int root = prefix[tri_off[m]];
-    const float4 l = lo[root], h = hi[root];
+    const float4 l = nodes[2 * (size_t)root], h = nodes[2 * (size_t)root + 1];
     float* o = out + 8 * (size_t)m;
     o[0] = l.x; o[1] = l.y; o[2] = l.z; o[3] = h.x; o[4] = h.y; o[5] = h.z;
     o[6] = cost[root];
@@ -1039,8 +1040,8 @@ int GpuBvhBuilder::build(const std::vector<GpuMeshSrc>& meshes, cudaStream_t s, 
     return RC_OK;
 }
 
-int GpuBvhBuilder::emit(float4* node_lo, float4* node_hi, float4* v0, float4* e1, float4* e2, float4* n0, float4* n1,
-                        float4* n2, cudaStream_t s, std::string& err) {
+int GpuBvhBuilder::emit(float4* nodes, float4* tris, float4* n0, float4* n1, float4* n2, cudaStream_t s,
+                        std::string& err) {
     if (!b_ || num_nodes_ <= 0) { err = "device BVH build: nothing built"; return RC_E_INVALID; }
     Bufs& B = *b_;
     const long long nn = num_nodes_;
@@ -1051,13 +1052,12 @@ int GpuBvhBuilder::emit(float4* node_lo, float4* node_hi, float4* v0, float4* e1
     BVH_CUDA(cudaMemsetAsync(B.parent.p, 0xff, 4 * nn, s));
     BVH_CUDA(cudaMemsetAsync(B.arrive.p, 0, 4 * nn, s));
     k_emit<<<grid_for(2ll * N + B.large_cap, 256), 256, 0, s>>>(B.small_pool.p, 2ll * N, B.large_pool.p, B.ctr.p + 3,
-                                                                 B.large_cap, B.prefix.p, B.topd.p, nn, node_lo, node_hi,
-                                                                 B.parent.p, flags);
-    k_cost<<<grid_for(nn, 256), 256, 0, s>>>(node_lo, node_hi, B.parent.p, nn, B.arrive.p, B.cost.p, flags);
+                                                                 B.large_cap, B.prefix.p, B.topd.p, nn, nodes, B.parent.p,
+                                                                 flags);
+    k_cost<<<grid_for(nn, 256), 256, 0, s>>>(nodes, B.parent.p, nn, B.arrive.p, B.cost.p, flags);
     k_pack_tris<<<grid_for(N, 256), 256, 0, s>>>(B.perm.p, B.wpos.p, B.wnrm.p, B.tri.p, B.mat.p, B.tri_off.p,
-                                                 B.vert_off.p, M, N, v0, e1, e2, n0, n1, n2);
-    k_mesh_results<<<(M + 127) / 128, 128, 0, s>>>(B.tri_off.p, M, B.prefix.p, node_lo, node_hi, B.cost.p,
-                                                   B.results.p);
+                                                 B.vert_off.p, M, N, tris, n0, n1, n2);
+    k_mesh_results<<<(M + 127) / 128, 128, 0, s>>>(B.tri_off.p, M, B.prefix.p, nodes, B.cost.p, B.results.p);
     BVH_CUDA(cudaGetLastError());
     std::vector<float> res(8 * (size_t)M);
     int h_flags = 0;

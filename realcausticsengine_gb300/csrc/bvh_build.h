@@ -35,13 +35,13 @@ public:
     int build(const std::vector<GpuMeshSrc>& meshes, cudaStream_t s, bool& supported, std::string& err);
     long long num_nodes() const { return num_nodes_; }
     long long num_tris() const { return num_tris_; }
-    // Writes the flattened nodes (mesh after mesh, pre-order, the device format:
-    // lo = (min, word0), hi = (max, word1); inner word0/word1 = global child indices,
-    // leaf word0 = 0x80000000 | count, word1 = first triangle slot) and the triangle
-    // records in leaf order (v0 | global triangle id, e1 | material, e2 | mesh, and the
-    // three vertex normals), then fills mesh_root, mesh_box and mesh_cost.
-    int emit(float4* node_lo, float4* node_hi, float4* v0, float4* e1, float4* e2, float4* n0, float4* n1,
-             float4* n2, cudaStream_t s, std::string& err);
+    // Writes the flattened nodes (mesh after mesh, pre-order, the device format: node i
+    // at nodes[2i] = (min, word0), nodes[2i+1] = (max, word1); inner word0/word1 = global
+    // child indices, leaf word0 = 0x80000000 | count, word1 = first triangle slot) and
+    // the triangle records in leaf order (slot j at tris[3j..3j+2] = v0 | global triangle
+    // id, e1 | material, e2 | mesh; the three vertex normals in n0..n2), then fills
+    // mesh_root, mesh_box and mesh_cost.
+    int emit(float4* nodes, float4* tris, float4* n0, float4* n1, float4* n2, cudaStream_t s, std::string& err);
     std::vector<int> mesh_root;       // global index of each mesh's root node
     std::vector<float> mesh_box;      // 6 floats per mesh: min xyz, max xyz
     std::vector<float> mesh_cost;     // CostOfTraversing of the root

@@ -57,7 +57,7 @@ struct DeviceState {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
     // scene
-    DevBuf<float4> node_lo, node_hi, wnode_lo, wnode_hi, tri_v0, tri_e1, tri_e2, tri_n0, tri_n1, tri_n2;
+    DevBuf<float4> nodes, wnode_lo, wnode_hi, tris, tri_n0, tri_n1, tri_n2;   // layouts: trace.cuh SceneView
     long long num_mesh_nodes = 0, num_tris = 0;
     DevBuf<int> world_mesh, mesh_root;
     DevBuf<DevLight> lights;
@@ -115,7 +115,7 @@ struct DeviceState {
     cudaEvent_t t0 = nullptr, t1 = nullptr;
 
     void release() {
-        DevBuf<float4>* f4[] = {&node_lo, &node_hi, &wnode_lo, &wnode_hi, &tri_v0, &tri_e1, &tri_e2, &tri_n0,
+        DevBuf<float4>* f4[] = {&nodes, &wnode_lo, &wnode_hi, &tris, &tri_n0,
                                 &tri_n1, &tri_n2, &ph_pos, &ph_dir, &q0, &q1, &q2, &q3, &q4};
         for (auto* b : f4) b->release();
         world_mesh.release(); mesh_root.release(); lights.release(); cdf.release(); materials.release();
@@ -235,7 +235,7 @@ int ensure_device() {
 // Mesh BVH nodes and triangle records from the host build, packed and uploaded.
 int upload_meshes_host(HostScene& sc, std::vector<int>& mesh_root) {
     DeviceState& d = ctx().dev;
-    std::vector<float4> nlo, nhi, v0, e1, e2, n0, n1, n2;
+    std::vector<float4> nod, trs, n0, n1, n2;
     mesh_root.clear();
     uint32_t node_base = 0, tri_base = 0, tri_global = 0;
     for (size_t m = 0; m < sc.meshes.size(); ++m) {
@@ -245,17 +245,17 @@ int upload_meshes_host(HostScene& sc, std::vector<int>& mesh_root) {
             uint32_t w0 = nd.w0, w1 = nd.w1;
             if (w0 & 0x80000000u) w1 = tri_base + w1;
             else { w0 += node_base; w1 += node_base; }
-            nlo.push_back(f4(nd.box.mn.x, nd.box.mn.y, nd.box.mn.z, w0));
-            nhi.push_back(f4(nd.box.mx.x, nd.box.mx.y, nd.box.mx.z, w1));
+            nod.push_back(f4(nd.box.mn.x, nd.box.mn.y, nd.box.mn.z, w0));
+            nod.push_back(f4(nd.box.mx.x, nd.box.mx.y, nd.box.mx.z, w1));
         }
         for (size_t k = 1; k < hm.bvh.index.size(); ++k) {
             uint32_t t = (uint32_t)hm.bvh.index[k];
             const V3& a = hm.wpos[hm.tri[3 * t]];
             const V3& b = hm.wpos[hm.tri[3 * t + 1]];
             const V3& c = hm.wpos[hm.tri[3 * t + 2]];
-            v0.push_back(f4(a.x, a.y, a.z, tri_global + t));
-            e1.push_back(f4(b.x - a.x, b.y - a.y, b.z - a.z, hm.mat[t]));
-            e2.push_back(f4(c.x - a.x, c.y - a.y, c.z - a.z, (uint32_t)m));
+            trs.push_back(f4(a.x, a.y, a.z, tri_global + t));
+            trs.push_back(f4(b.x - a.x, b.y - a.y, b.z - a.z, hm.mat[t]));
+            trs.push_back(f4(c.x - a.x, c.y - a.y, c.z - a.z, (uint32_t)m));
             const V3& na = hm.wnrm[hm.tri[3 * t]];
             const V3& nb = hm.wnrm[hm.tri[3 * t + 1]];
             const V3& nc = hm.wnrm[hm.tri[3 * t + 2]];
@@ -269,12 +269,11 @@ int upload_meshes_host(HostScene& sc, std::vector<int>& mesh_root) {
     }
     cudaStream_t s = d.stream;
     int r;
-    if ((r = upload(d.node_lo, nlo, s)) || (r = upload(d.node_hi, nhi, s)) || (r = upload(d.tri_v0, v0, s)) ||
-        (r = upload(d.tri_e1, e1, s)) || (r = upload(d.tri_e2, e2, s)) || (r = upload(d.tri_n0, n0, s)) ||
+    if ((r = upload(d.nodes, nod, s)) || (r = upload(d.tris, trs, s)) || (r = upload(d.tri_n0, n0, s)) ||
         (r = upload(d.tri_n1, n1, s)) || (r = upload(d.tri_n2, n2, s)))
         return r;
-    d.num_mesh_nodes = (long long)nlo.size();
-    d.num_tris = (long long)v0.size();
+    d.num_mesh_nodes = (long long)nod.size() / 2;
+    d.num_tris = (long long)n0.size();
     return RC_OK;
 }
 
@@ -299,10 +298,10 @@ int upload_scene_rest(HostScene& sc, const std::vector<int>& mesh_root) {
     RC_CUDA(cudaMemsetAsync(d.errors.p, 0, sizeof(int) * ERR_COUNT, s));
     RC_CUDA(cudaStreamSynchronize(s));
     SceneView& v = d.view;
-    v.node_lo = d.node_lo.p; v.node_hi = d.node_hi.p;
+    v.nodes = d.nodes.p;
     v.wnode_lo = d.wnode_lo.p; v.wnode_hi = d.wnode_hi.p;
     v.world_mesh = d.world_mesh.p; v.mesh_root = d.mesh_root.p;
-    v.tri_v0 = d.tri_v0.p; v.tri_e1 = d.tri_e1.p; v.tri_e2 = d.tri_e2.p;
+    v.tris = d.tris.p;
     v.tri_n0 = d.tri_n0.p; v.tri_n1 = d.tri_n1.p; v.tri_n2 = d.tri_n2.p;
     v.num_world_nodes = (int)sc.world.nodes.size();
     v.num_meshes = (int)sc.meshes.size();
@@ -359,10 +358,11 @@ int prepare_device_bvh(HostScene& sc) {
     r = bld.build(src, d.stream, supported, err);
     if (r) { ctx().err = err; return r; }
     if (!supported) return RC_OK;
-    RC_CUDA(d.node_lo.reserve(bld.num_nodes())); RC_CUDA(d.node_hi.reserve(bld.num_nodes()));
-    DevBuf<float4>* tb[] = {&d.tri_v0, &d.tri_e1, &d.tri_e2, &d.tri_n0, &d.tri_n1, &d.tri_n2};
+    RC_CUDA(d.nodes.reserve(2 * bld.num_nodes()));
+    RC_CUDA(d.tris.reserve(3 * bld.num_tris()));
+    DevBuf<float4>* tb[] = {&d.tri_n0, &d.tri_n1, &d.tri_n2};
     for (auto* b : tb) RC_CUDA(b->reserve(bld.num_tris()));
-    r = bld.emit(d.node_lo.p, d.node_hi.p, d.tri_v0.p, d.tri_e1.p, d.tri_e2.p, d.tri_n0.p, d.tri_n1.p, d.tri_n2.p,
+    r = bld.emit(d.nodes.p, d.tris.p, d.tri_n0.p, d.tri_n1.p, d.tri_n2.p,
                  d.stream, err);
     if (r) { ctx().err = err; return r; }
     d.num_mesh_nodes = bld.num_nodes();
@@ -1457,24 +1457,23 @@ int rc_scene_dump(int which, unsigned* out, long long cap, long long* words) {
     if (!ctx().scene || !ctx().scene->prepared) { ctx().err = "rc_scene_dump: scene not prepared"; return RC_E_NO_SCENE; }
     if (!words || (cap > 0 && !out) || cap < 0) { ctx().err = "rc_scene_dump: bad arguments"; return RC_E_INVALID; }
     DeviceState& d = ctx().dev;
-    struct Part { const void* p; long long words; };
+    struct Part { const void* p; long long words; int width; };   // width: words per item
     std::vector<Part> parts;
     const long long wn = d.view.num_world_nodes;
     const long long nm = (long long)ctx().scene->meshes.size();
     const long long nw = (long long)ctx().scene->world.index.size() - 1;
     switch (which) {
-        case 0: parts = {{d.node_lo.p, 4 * d.num_mesh_nodes}, {d.node_hi.p, 4 * d.num_mesh_nodes}}; break;
+        case 0: parts = {{d.nodes.p, 8 * d.num_mesh_nodes, 8}}; break;
         case 1:
-            parts = {{d.tri_v0.p, 4 * d.num_tris}, {d.tri_e1.p, 4 * d.num_tris}, {d.tri_e2.p, 4 * d.num_tris},
-                     {d.tri_n0.p, 4 * d.num_tris}, {d.tri_n1.p, 4 * d.num_tris}, {d.tri_n2.p, 4 * d.num_tris}};
+            parts = {{d.tris.p, 12 * d.num_tris, 12}, {d.tri_n0.p, 4 * d.num_tris, 4}, {d.tri_n1.p, 4 * d.num_tris, 4},
+                     {d.tri_n2.p, 4 * d.num_tris, 4}};
             break;
-        case 2: parts = {{d.wnode_lo.p, 4 * wn}, {d.wnode_hi.p, 4 * wn}}; break;
-        case 3: parts = {{d.world_mesh.p, nw}, {d.mesh_root.p, nm}}; break;
+        case 2: parts = {{d.wnode_lo.p, 4 * wn, 4}, {d.wnode_hi.p, 4 * wn, 4}}; break;
+        case 3: parts = {{d.world_mesh.p, nw, 0}, {d.mesh_root.p, nm, 0}}; break;
         default: ctx().err = "rc_scene_dump: which must be 0..3"; return RC_E_INVALID;
     }
-    // 0 and 2 are interleaved per node as (lo, hi); 1 per triangle as (v0, e1, e2, n0, n1, n2)
-    const int k = (int)parts.size();
-    const long long per = which == 3 ? 0 : 4;
+    // 0 and 2 per node as (lo, hi); 1 per triangle as (v0, e1, e2, n0, n1, n2); 3 the
+    // two lists one after the other
     long long total = 0;
     for (const Part& q : parts) total += q.words;
     *words = total;
@@ -1484,12 +1483,19 @@ int rc_scene_dump(int which, unsigned* out, long long cap, long long* words) {
         if (q.words) RC_CUDA(cudaMemcpy(host.data() + off, q.p, 4 * (size_t)q.words, cudaMemcpyDeviceToHost));
         off += q.words;
     }
-    if (per) {
-        const long long items = total / (per * k);
+    if (parts[0].width > 0 && parts.size() > 1) {
+        int stride = 0;
+        for (const Part& q : parts) stride += q.width;
+        const long long items = total / stride;
         std::vector<unsigned> il((size_t)total);
-        for (long long i = 0; i < items; ++i)
-            for (int j = 0; j < k; ++j)
-                std::memcpy(&il[(size_t)((i * k + j) * per)], &host[(size_t)(j * items * per + i * per)], 4 * per);
+        long long src = 0;
+        int col = 0;
+        for (const Part& q : parts) {
+            for (long long i = 0; i < items; ++i)
+                std::memcpy(&il[(size_t)(i * stride + col)], &host[(size_t)(src + i * q.width)], 4 * (size_t)q.width);
+            src += q.words;
+            col += q.width;
+        }
         host.swap(il);
     }
     if (cap > 0) std::memcpy(out, host.data(), 4 * (size_t)std::min(cap, total));

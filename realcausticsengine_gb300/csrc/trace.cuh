@@ -17,20 +17,20 @@
 
 namespace rc {
 
-// Device view of the scene.  Nodes: two float4 per node (min.xyz|w0, max.xyz|w1).
-// Mesh-level inner nodes hold global child indices; mesh-level leaves hold
-// (0x80000000|count, first triangle slot).  World leaves hold
-// (0x80000000|count, first slot in world_mesh).  Triangles are stored in leaf order.
+// Device view of the scene.  Nodes: two float4 per node (min.xyz|w0, max.xyz|w1), the
+// mesh nodes interleaved in one array (node i at nodes[2i], nodes[2i+1]: one 32-byte
+// sector per visit).  Mesh-level inner nodes hold global child indices; mesh-level
+// leaves hold (0x80000000|count, first triangle slot).  World leaves hold
+// (0x80000000|count, first slot in world_mesh).  Triangles are stored in leaf order,
+// the three records a test reads interleaved (slot j at tris[3j .. 3j+2]).
 struct SceneView {
-    const float4* __restrict__ node_lo;
-    const float4* __restrict__ node_hi;
+    const float4* __restrict__ nodes;       // mesh BVH nodes, 2 per node
     const float4* __restrict__ wnode_lo;
     const float4* __restrict__ wnode_hi;
     const int* __restrict__ world_mesh;     // mesh id per world-leaf slot
     const int* __restrict__ mesh_root;      // global root node per mesh
-    const float4* __restrict__ tri_v0;      // v0.xyz | global triangle id
-    const float4* __restrict__ tri_e1;      // (v1 - v0).xyz | material
-    const float4* __restrict__ tri_e2;      // (v2 - v0).xyz | mesh id
+    const float4* __restrict__ tris;        // 3 per triangle: v0.xyz | global triangle id,
+                                            // (v1 - v0).xyz | material, (v2 - v0).xyz | mesh id
     const float4* __restrict__ tri_n0;      // vertex normals (normalised, world space)
     const float4* __restrict__ tri_n1;
     const float4* __restrict__ tri_n2;
@@ -80,9 +80,9 @@ __device__ __forceinline__ bool box_hit(float4 lo, float4 hi, F3 o, F3 inv, floa
 // Möller-Trumbore as src/Triangle.cpp:44-66 computes it.
 __device__ __forceinline__ bool tri_hit(const SceneView& s, int slot, F3 o, F3 d, float tmin, float tmax,
                                         float& t_out, float& u_out, float& v_out) {
-    float4 a = __ldg(&s.tri_v0[slot]);
-    float4 b = __ldg(&s.tri_e1[slot]);
-    float4 c = __ldg(&s.tri_e2[slot]);
+    float4 a = __ldg(&s.tris[3 * slot]);
+    float4 b = __ldg(&s.tris[3 * slot + 1]);
+    float4 c = __ldg(&s.tris[3 * slot + 2]);
     F3 v0 = xyz(a), e1 = xyz(b), e2 = xyz(c);
     F3 pvec = cross(d, e2);
     float det = dot(e1, pvec);
@@ -115,8 +115,8 @@ __device__ __forceinline__ bool mesh_traverse_impl(const SceneView& s, int mesh,
     stack[sp++] = __ldg(&s.mesh_root[mesh]);
     while (sp) {
         int id = stack[--sp];
-        float4 lo = __ldg(&s.node_lo[id]);
-        float4 hi = __ldg(&s.node_hi[id]);
+        float4 lo = __ldg(&s.nodes[2 * id]);
+        float4 hi = __ldg(&s.nodes[2 * id + 1]);
         if (!box_hit(lo, hi, o, inv, tmin, rec.t)) continue;
         uint32_t w0 = __float_as_uint(lo.w), w1 = __float_as_uint(hi.w);
         if (w0 & 0x80000000u) {
@@ -223,9 +223,9 @@ struct Isect {
 };
 
 __device__ __forceinline__ void fill_isect(const SceneView& s, const HitRec& h, F3 o, F3 d, Isect& is) {
-    float4 a = __ldg(&s.tri_v0[h.slot]);
-    float4 b = __ldg(&s.tri_e1[h.slot]);
-    float4 c = __ldg(&s.tri_e2[h.slot]);
+    float4 a = __ldg(&s.tris[3 * h.slot]);
+    float4 b = __ldg(&s.tris[3 * h.slot + 1]);
+    float4 c = __ldg(&s.tris[3 * h.slot + 2]);
     F3 e1 = xyz(b), e2 = xyz(c);
     is.t = h.t; is.u = h.u; is.v = h.v;
     is.ng = normalize(cross(e1, e2));
