@@ -741,9 +741,11 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     int qlaunch = 0;
     launch_query_order(tree, reinterpret_cast<const float*>(d.q0.p), 4, (long long)nq, p.radius_sqr, d.qscratch.p,
                        d.qorder.p, d.qstart.p, &qlaunch, s);
-    // merge pairs: room for the last iteration's count + 1/4, at least 4 per query
-    long long mcap = std::max<long long>({(long long)d.merges.n, (long long)(d.last_merges + d.last_merges / 4) + 65536,
-                                          4 * (long long)nq});
+    // merge pairs: room for the last iteration's count + 1/4; before any count, 16 per
+    // query (the water pool merges 6.9 per query; an overflow only re-runs the gather)
+    long long mcap = std::max<long long>((long long)d.merges.n, d.last_merges
+                                                                   ? (long long)(d.last_merges + d.last_merges / 4) + 65536
+                                                                   : 16 * (long long)nq + 65536);
     RC_CUDA(d.merges.reserve(mcap));
     RC_CUDA(d.merge_count.reserve(1));
     int variant = 3;
