@@ -71,6 +71,39 @@ def _edge_scene():
     return _scene([one, two, three, same, clusters, soup, grid])
 
 
+def _random_meshes_scene(seed=3, count=40):
+    """Many meshes of random sizes (1 to 30,000 triangles): soups of small random
+    triangles, random grids and stretched slabs, so that segments cross the per-warp size
+    at every depth and the world BVH has many leaves."""
+    rng = np.random.default_rng(seed)
+    meshes = []
+    for m in range(count):
+        n = int(np.exp(rng.uniform(0.0, np.log(30000.0))))
+        centre = rng.uniform(-4, 4, 3)
+        scale = rng.uniform(0.05, 2.0, 3)
+        kind = m % 3
+        if kind == 0:   # soup
+            base = centre + rng.uniform(-1, 1, (n, 1, 3)) * scale
+            V = (base + rng.normal(0, 0.02, (n, 3, 3))).reshape(-1, 3)
+            F = np.arange(3 * n).reshape(n, 3)
+        elif kind == 1:  # grid with random heights
+            g = max(2, int(np.sqrt(n / 2)) + 1)
+            xs, ys = np.meshgrid(np.linspace(-1, 1, g), np.linspace(-1, 1, g))
+            V = np.stack([xs.ravel(), ys.ravel(), rng.normal(0, 0.05, g * g)], 1) * scale + centre
+            F = []
+            for i in range(g - 1):
+                for j in range(g - 1):
+                    a = i * g + j
+                    F += [[a, a + 1, a + g], [a + 1, a + g + 1, a + g]]
+            F = np.asarray(F)
+        else:            # thin slab: flat on one axis
+            V = rng.uniform(-1, 1, (3 * n, 3)) * scale + centre
+            V[:, m % 3 - 1] = centre[m % 3 - 1]
+            F = np.arange(3 * n).reshape(n, 3)
+        meshes.append(_mesh(V, F, m % 2))
+    return _scene(meshes)
+
+
 SCENES = {
     "test_scene": lambda: scenes.test_scene(),
     "glass_sphere": lambda: scenes.glass_sphere_point(64, 64, subdiv=5),
@@ -79,6 +112,7 @@ SCENES = {
     "batch_0": lambda: scenes.batch_scene(0, 32, 32)[0],
     "batch_5": lambda: scenes.batch_scene(5, 32, 32)[0],
     "edges": _edge_scene,
+    "random_meshes": _random_meshes_scene,
 }
 
 
