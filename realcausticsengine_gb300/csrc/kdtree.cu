@@ -15,6 +15,7 @@
 #include "kdtree.cuh"
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 
 namespace rc {
 
@@ -687,11 +688,10 @@ int kd_build(const float4* pos4, long long n, KdTree& tree, void* scratch, size_
         nl++;
     }
     size_t smem = SmemLayout::total;
-    static bool attr_set = false;   // once: later builds may be recorded into a CUDA graph
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_smem_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_set = true;
-    }
+    // once per process: later builds may be recorded into a CUDA graph, and contexts on
+    // several threads build concurrently
+    static std::once_flag attr_set;
+    std::call_once(attr_set, [&] { cudaFuncSetAttribute(k_smem_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
     k_smem_build<<<(unsigned)(1LL << l0), kSmemThreads, smem, stream>>>(B, cur, l0, n, tree.nodes);
     nl++;
     if (launches) *launches = nl;
