@@ -654,6 +654,10 @@ void launch_query_order(const KdTree& tree, const float* qpos, int stride, long 
     if (launches) *launches += 3;
 }
 
+void launch_scan_counts(uint32_t* counts, long long m, cudaStream_t s) {
+    if (m > 0) k_scan_counts<<<1, 1024, 0, s>>>(counts, m);
+}
+
 void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaStream_t s) {
     if (tree.n <= 0) return;
     k_tree_records<<<(unsigned)((tree.n + 255) / 256), 256, 0, s>>>(ph, tree.id, tree.n, tp);

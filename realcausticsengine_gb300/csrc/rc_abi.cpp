@@ -82,6 +82,9 @@ struct DeviceState {
     DevBuf<unsigned char> qscratch;
     DevBuf<double> accum;
     DevBuf<float> image;          // FP32 mean for readback
+    // light-path processing order (launch_light_order) and its scratch
+    DevBuf<uint32_t> path_order;
+    DevBuf<unsigned char> order_scratch;
     // photon-query merge pairs between the gather's traversal and its merge evaluation
     DevBuf<uint2> merges;
     DevBuf<unsigned long long> merge_count;
@@ -126,6 +129,7 @@ struct DeviceState {
         accum.release();
         image.release();
         merges.release(); merge_count.release();
+        path_order.release(); order_scratch.release();
         last_merges = 0;
         mlp.reset();
         prop.release(); train_pos.release(); train_dir.release(); contrib.release(); train_wsum.release();
@@ -627,6 +631,14 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             if (r) return r;
             RC_CUDA(cudaEventRecord(d.evm[1], s));
         }
+        RC_CUDA(cudaEventRecord(d.ev[0], s));
+        if (sampler == RC_SAMPLER_UNIFORM && !p.proposal && attempt == 0) {
+            // coherent processing order of the light paths (their samples unchanged)
+            RC_CUDA(d.path_order.reserve(std::max<long long>(p.num_light_paths, 1)));
+            RC_CUDA(d.order_scratch.reserve(light_order_scratch_bytes(p.num_light_paths)));
+            launch_light_order(p, d.order_scratch.p, d.path_order.p, s);
+            p.path_order = d.path_order.p;
+        }
         int lvar = 0;
         if (sampler == RC_SAMPLER_UNIFORM && cfg().autotune) {
             std::atomic<int>& slot = g_tune.light[size_class(p.num_light_paths)];
@@ -638,7 +650,6 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             lvar = slot.load();
             RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         }
-        RC_CUDA(cudaEventRecord(d.ev[0], s));
         if (sampler == RC_SAMPLER_UNIFORM) launch_light_pass(p, ph, d.counters.p + 6, s, lvar);
         else launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
         RC_CUDA(cudaGetLastError());
@@ -876,6 +887,11 @@ int async_setup(const HostScene& sc) {
     RC_CUDA(d.merge_count.reserve(1));
     RC_CUDA(d.ph_pos.reserve(d.async_pcap)); RC_CUDA(d.ph_dir.reserve(d.async_pcap));
     RC_CUDA(d.ph_tp.reserve(d.async_pcap)); RC_CUDA(d.ph_path.reserve(d.async_pcap));
+    {
+        const long long paths = cfg().photons_per_iter > 0 ? cfg().photons_per_iter : npix;
+        RC_CUDA(d.path_order.reserve(std::max<long long>(paths, 1)));
+        RC_CUDA(d.order_scratch.reserve(light_order_scratch_bytes(paths)));
+    }
     RC_CUDA(d.q0.reserve(d.async_qcap)); RC_CUDA(d.q1.reserve(d.async_qcap)); RC_CUDA(d.q2.reserve(d.async_qcap));
     RC_CUDA(d.q3.reserve(d.async_qcap)); RC_CUDA(d.q4.reserve(d.async_qcap));
     const long long n = d.async_pcap;
@@ -908,6 +924,8 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
     PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, pc, d.counters.p};
     RC_CUDA(record(d.ev[0], s));
+    launch_light_order(p, d.order_scratch.p, d.path_order.p, s);
+    p.path_order = d.path_order.p;
     launch_light_pass(p, ph, d.counters.p + 6, s, d.async_lvar);
     RC_CUDA(record(d.ev[1], s));
     // pads one scene extent (plus four base radii) beyond the scene's +x face: outside

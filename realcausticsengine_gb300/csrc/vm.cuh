@@ -87,6 +87,7 @@ struct VMParams {
     // tabulated learned proposal for the Metropolis samplers (proposal.cuh; nullptr: none)
     const float* proposal_table;
     int proposal_table_res;
+    const uint32_t* path_order;    // light-path processing order (launch_light_order; nullptr: index order)
 };
 
 // error flag slots
@@ -98,6 +99,14 @@ enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERF
 constexpr int kMltMaxPathLength = 12;
 void launch_mlt_pass(const VMParams& p, PhotonBuf ph, int sampler, int chains, float p_large,
                      unsigned long long* stats, cudaStream_t s);
+// Processing order of the light paths (p.num_light_paths of them) for p.path_order:
+// indices sorted by the 4D Morton cell (32 per axis) of their own emission samples (area
+// u, v, direction u, v), so that each warp of the persistent pass starts coherent rays.
+// Every path keeps its samples and index: only the order of tracing changes.
+size_t light_order_scratch_bytes(long long n);
+void launch_light_order(const VMParams& p, void* scratch, uint32_t* order, cudaStream_t s);
+// Exclusive scan of m counters in one block (m up to a few million).
+void launch_scan_counts(uint32_t* counts, long long m, cudaStream_t s);
 // next_path: device counter for the persistent kernel (nullptr: one thread per path)
 void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant = 0);
 void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s, int variant = 0);

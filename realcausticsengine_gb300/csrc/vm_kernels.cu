@@ -107,6 +107,36 @@ __device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& 
     return true;
 }
 
+// Light-path order: 4D Morton key of a path's emission samples (the same Philox draws
+// light_path_start reads), counting-sorted.
+constexpr int kOrderBits = 5;                      // cells per axis: 32
+constexpr int kOrderCells = 1 << (4 * kOrderBits);
+
+__global__ void k_light_keys(const VMParams P, uint32_t* __restrict__ keys, uint32_t* __restrict__ counts) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= P.num_light_paths) return;
+    PathRng g;
+    g.init(P.seed, (uint64_t)i, P.iteration, STREAM_LIGHT);
+    const U4 b0 = g.block(0), b1 = g.block(1);
+    const float u[4] = {u01(b0.b), u01(b0.c), u01(b0.d), u01(b1.a)};
+    uint32_t key = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t c = min((uint32_t)(u[k] * (float)(1 << kOrderBits)), (uint32_t)((1 << kOrderBits) - 1));
+#pragma unroll
+        for (int bit = 0; bit < kOrderBits; ++bit) key |= ((c >> bit) & 1u) << (4 * bit + k);
+    }
+    keys[i] = key;
+    atomicAdd(&counts[key], 1u);
+}
+
+__global__ void k_light_scatter(const uint32_t* __restrict__ keys, long long n, uint32_t* __restrict__ cursor,
+                                uint32_t* __restrict__ order) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    order[atomicAdd(&cursor[keys[i]], 1u)] = (uint32_t)i;
+}
+
 // kMinBlocks caps the registers per thread (resident blocks per SM the allocation must
 // allow); traversal stacks are per-traversal local-memory arrays.
 template <int kBlock, int kMinBlocks>
@@ -126,7 +156,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_light_pass_persistent(co
             base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
             if (!alive) {
                 const unsigned long long mine = base + __popc(need & ((1u << lane) - 1u));
-                if (mine < (unsigned long long)P.num_light_paths) alive = light_path_start(P, (long long)mine, s);
+                if (mine < (unsigned long long)P.num_light_paths)
+                    alive = light_path_start(P, P.path_order ? (long long)__ldg(&P.path_order[mine]) : (long long)mine,
+                                             s);
             }
             if (base + __popc(need) >= (unsigned long long)P.num_light_paths) pool_left = false;
         }
@@ -324,6 +356,20 @@ void launch_camera_t(const VMParams& p, QueryBuf qb, unsigned long long* next_pi
 }
 
 }  // namespace
+
+size_t light_order_scratch_bytes(long long n) { return 4 * (size_t)(n > 0 ? n : 1) + 4 * (size_t)kOrderCells + 256; }
+
+void launch_light_order(const VMParams& p, void* scratch, uint32_t* order, cudaStream_t s) {
+    const long long n = p.num_light_paths;
+    if (n <= 0) return;
+    uint32_t* keys = static_cast<uint32_t*>(scratch);
+    uint32_t* counts = keys + ((n + 63) & ~63LL);
+    cudaMemsetAsync(counts, 0, 4 * (size_t)kOrderCells, s);
+    const unsigned g = (unsigned)((n + 255) / 256);
+    k_light_keys<<<g, 256, 0, s>>>(p, keys, counts);
+    launch_scan_counts(counts, kOrderCells, s);
+    k_light_scatter<<<g, 256, 0, s>>>(keys, n, counts, order);
+}
 
 int pass_variants() { return 5; }
 
