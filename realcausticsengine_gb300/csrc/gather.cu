@@ -531,6 +531,46 @@ __global__ void __launch_bounds__(1024) k_scan_counts(uint32_t* counts, long lon
     }
 }
 
+// Multi-block form of the same scan for large m: each block scans one 8192-counter tile
+// in place and writes its total, one block scans the totals, a third pass adds them.
+constexpr long long kScanTile = 1024 * 8;
+__global__ void __launch_bounds__(1024) k_scan_tile(uint32_t* counts, long long m, uint32_t* tile_sums) {
+    __shared__ uint32_t warp_sums[32];
+    const long long base = blockIdx.x * kScanTile;
+    uint32_t v[8];
+    uint32_t sum = 0;
+    const long long i0 = base + (long long)threadIdx.x * 8;
+    for (int k = 0; k < 8; ++k) { v[k] = (i0 + k < m) ? counts[i0 + k] : 0u; sum += v[k]; }
+    uint32_t incl = sum;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = warp_sums[lane], wi = w;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        warp_sums[lane] = wi - w;
+        if (lane == 31) tile_sums[blockIdx.x] = wi;
+    }
+    __syncthreads();
+    uint32_t run = warp_sums[wid] + incl - sum;
+    for (int k = 0; k < 8; ++k) {
+        if (i0 + k < m) counts[i0 + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void k_scan_tile_add(uint32_t* counts, long long m, const uint32_t* __restrict__ tile_offsets) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < m) counts[i] += tile_offsets[i / kScanTile];
+}
+
 __global__ void k_scatter_queries(const uint32_t* __restrict__ keys, long long nq,
                                   const unsigned long long* __restrict__ nq_dev, uint32_t* __restrict__ cursor,
                                   uint32_t* __restrict__ order) {
@@ -635,7 +675,7 @@ int query_order_level(long long nq, const KdTree& tree) {
 
 size_t query_order_scratch_bytes(long long nq, const KdTree& tree) {
     int lq = query_order_level(nq, tree);
-    return 4 * (size_t)(nq > 0 ? nq : 1) + 4 * ((size_t)1 << lq) + 256;
+    return 4 * (size_t)(nq > 0 ? nq : 1) + 4 * ((size_t)1 << lq) + 4 * scan_scratch_words(1LL << lq) + 512;
 }
 
 void launch_query_order(const KdTree& tree, const float* qpos, int stride, long long nq, float r2, void* scratch,
@@ -649,13 +689,20 @@ void launch_query_order(const KdTree& tree, const float* qpos, int stride, long 
     cudaMemsetAsync(counts, 0, 4 * (size_t)m, s);
     unsigned g = (unsigned)((nq + 255) / 256);
     k_query_cells<<<g, 256, 0, s>>>(nav_of(tree), qpos, stride, nq, nq_dev, lq, r2, keys, counts, start_nodes);
-    k_scan_counts<<<1, 1024, 0, s>>>(counts, m);
+    launch_scan_counts(counts, m, counts + ((m + 63) & ~63LL), s);
     k_scatter_queries<<<g, 256, 0, s>>>(keys, nq, nq_dev, counts, order);
-    if (launches) *launches += 3;
+    if (launches) *launches += m > 4 * kScanTile ? 5 : 3;
 }
 
-void launch_scan_counts(uint32_t* counts, long long m, cudaStream_t s) {
-    if (m > 0) k_scan_counts<<<1, 1024, 0, s>>>(counts, m);
+size_t scan_scratch_words(long long m) { return (size_t)(m / kScanTile + 2); }
+
+void launch_scan_counts(uint32_t* counts, long long m, uint32_t* tile_scratch, cudaStream_t s) {
+    if (m <= 0) return;
+    if (m <= 4 * kScanTile || !tile_scratch) { k_scan_counts<<<1, 1024, 0, s>>>(counts, m); return; }
+    const long long tiles = (m + kScanTile - 1) / kScanTile;
+    k_scan_tile<<<(unsigned)tiles, 1024, 0, s>>>(counts, m, tile_scratch);
+    k_scan_counts<<<1, 1024, 0, s>>>(tile_scratch, tiles);
+    k_scan_tile_add<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(counts, m, tile_scratch);
 }
 
 void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaStream_t s) {

@@ -105,8 +105,10 @@ void launch_mlt_pass(const VMParams& p, PhotonBuf ph, int sampler, int chains, f
 // Every path keeps its samples and index: only the order of tracing changes.
 size_t light_order_scratch_bytes(long long n);
 void launch_light_order(const VMParams& p, void* scratch, uint32_t* order, cudaStream_t s);
-// Exclusive scan of m counters in one block (m up to a few million).
-void launch_scan_counts(uint32_t* counts, long long m, cudaStream_t s);
+// Exclusive scan of m counters in place; large m in three passes over 8192-counter tiles
+// with tile_scratch (scan_scratch_words(m) words) for the tile totals.
+size_t scan_scratch_words(long long m);
+void launch_scan_counts(uint32_t* counts, long long m, uint32_t* tile_scratch, cudaStream_t s);
 // next_path: device counter for the persistent kernel (nullptr: one thread per path)
 void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant = 0);
 void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s, int variant = 0);

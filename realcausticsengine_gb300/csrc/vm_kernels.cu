@@ -357,7 +357,9 @@ void launch_camera_t(const VMParams& p, QueryBuf qb, unsigned long long* next_pi
 
 }  // namespace
 
-size_t light_order_scratch_bytes(long long n) { return 4 * (size_t)(n > 0 ? n : 1) + 4 * (size_t)kOrderCells + 256; }
+size_t light_order_scratch_bytes(long long n) {
+    return 4 * (size_t)(n > 0 ? n : 1) + 4 * (size_t)kOrderCells + 4 * scan_scratch_words(kOrderCells) + 512;
+}
 
 void launch_light_order(const VMParams& p, void* scratch, uint32_t* order, cudaStream_t s) {
     const long long n = p.num_light_paths;
@@ -367,7 +369,7 @@ void launch_light_order(const VMParams& p, void* scratch, uint32_t* order, cudaS
     cudaMemsetAsync(counts, 0, 4 * (size_t)kOrderCells, s);
     const unsigned g = (unsigned)((n + 255) / 256);
     k_light_keys<<<g, 256, 0, s>>>(p, keys, counts);
-    launch_scan_counts(counts, kOrderCells, s);
+    launch_scan_counts(counts, kOrderCells, counts + kOrderCells, s);
     k_light_scatter<<<g, 256, 0, s>>>(keys, n, counts, order);
 }
 
