@@ -137,6 +137,8 @@ __global__ void k_light_scatter(const uint32_t* __restrict__ keys, long long n, 
     order[atomicAdd(&cursor[keys[i]], 1u)] = (uint32_t)i;
 }
 
+constexpr int kRefillLanes = 24;
+
 // kMinBlocks caps the registers per thread (resident blocks per SM the allocation must
 // allow); traversal stacks are per-traversal local-memory arrays.
 template <int kBlock, int kMinBlocks>
@@ -148,9 +150,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_light_pass_persistent(co
     bool alive = false;
     bool pool_left = true;
     while (true) {
-        // refill lanes without a path
+        // refill lanes without a path, once at least kRefillLanes are free (or none has
+        // a path): lanes refilled together take consecutive, coherent paths (the order
+        // sorts paths by their emission samples), so a warp keeps groups of coherent
+        // paths together for several bounces (measured on the water pool: refilling at
+        // any free lane 14.2 ms, at 16 free 13.6, at 20-24 free 13.4, at 32 free 14.5)
         const unsigned need = __ballot_sync(0xffffffffu, !alive);
-        if (need && pool_left) {
+        if (need && pool_left && (__popc(need) >= kRefillLanes || need == 0xffffffffu)) {
             unsigned long long base = 0;
             if (lane == __ffs(need) - 1) base = atomicAdd(next_path, (unsigned long long)__popc(need));
             base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
@@ -257,8 +263,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_camera_pass_persistent(c
     bool alive = false;
     bool pool_left = true;
     while (true) {
+        // refill as in the light pass: once kRefillLanes lanes are free (2.43 -> 2.35 ms on
+        // the water pool), drawing again for samples that fall outside the buffer
         unsigned need = __ballot_sync(0xffffffffu, !alive);
-        while (need && pool_left) {
+        while (need && pool_left && (__popc(need) >= kRefillLanes || need == 0xffffffffu)) {
             unsigned long long base = 0;
             if (lane == __ffs(need) - 1) base = atomicAdd(next_pixel, (unsigned long long)__popc(need));
             base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
