@@ -159,16 +159,19 @@ __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, ui
 
 // Lane-parallel variant of the same query, used when node boxes exist down to the bucket
 // level Lb (every node at level Lb holds n >> Lb <= kBucket photons).  A subtree root at
-// level L < Lb is expanded k = min(5, Lb - L) levels at once: lane j box-tests the j-th
-// descendant at level L + k and survivors are pushed as new roots, while lanes test the
-// median photons of the 2^k - 1 inner nodes in between (odd counts only).  Roots at
+// level L < Lb is expanded k = min(kExpand, Lb - L) levels at once: lane j box-tests the
+// j-th descendant at level L + k and survivors are pushed as new roots, while lanes test
+// the median photons of the 2^k - 1 inner nodes in between (odd counts only).  Roots at
 // level >= Lb are scanned like buckets.  The accepted set is the reference's: every
 // photon of the start node's range lies in a bucket or is an inner node's median; a
 // culled box holds no photon within the radius (box distance <= photon distance under
 // monotonic rounding), a median outside its node's split slab fails the predicate
 // (its distance >= |q[axis] - split|), and every photon that is tested is tested with
-// the reference's predicate.  DFS over roots keeps at most 31 pending roots per
-// expansion level: with n < 2^28 (Lb <= 27) at most 6 x 31 + 1 = 187 < kRootStack.
+// the reference's predicate.  DFS over roots keeps at most 2^kExpand - 1 pending roots
+// per expansion level: with n < 2^28 (Lb <= 27) at most 7 x 15 + 1 = 106 < kRootStack.
+// (4 levels per step measured best on the water pool: 3 / 4 / 5 levels 8.2 / 6.9 /
+// 7.1 ms per gather.)
+constexpr int kExpand = 4;
 constexpr int kRootStack = 256;
 
 template <class Flush>
@@ -211,7 +214,7 @@ __device__ __forceinline__ void kd_query_expand(const KdNav& t, F3 q, float r2, 
             }
             continue;
         }
-        const int k = (Lb - L) < 5 ? (Lb - L) : 5;
+        const int k = (Lb - L) < kExpand ? (Lb - L) : kExpand;
         const uint32_t m = 1u << k;
         vc.nodes += m - 1;
         {
