@@ -632,7 +632,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             RC_CUDA(cudaEventRecord(d.evm[1], s));
         }
         RC_CUDA(cudaEventRecord(d.ev[0], s));
-        if (sampler == RC_SAMPLER_UNIFORM && !p.proposal && attempt == 0) {
+        if (sampler == RC_SAMPLER_UNIFORM && attempt == 0) {
             // coherent processing order of the light paths (their samples unchanged)
             RC_CUDA(d.path_order.reserve(std::max<long long>(p.num_light_paths, 1)));
             RC_CUDA(d.order_scratch.reserve(light_order_scratch_bytes(p.num_light_paths)));

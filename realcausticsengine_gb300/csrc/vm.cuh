@@ -101,7 +101,8 @@ void launch_mlt_pass(const VMParams& p, PhotonBuf ph, int sampler, int chains, f
                      unsigned long long* stats, cudaStream_t s);
 // Processing order of the light paths (p.num_light_paths of them) for p.path_order:
 // indices sorted by the 4D Morton cell (32 per axis) of their own emission samples (area
-// u, v, direction u, v), so that each warp of the persistent pass starts coherent rays.
+// u, v, direction u, v; with p.proposal, the proposed direction's octahedral coordinates
+// for the direction), so that each warp of the persistent pass starts coherent rays.
 // Every path keeps its samples and index: only the order of tracing changes.
 size_t light_order_scratch_bytes(long long n);
 void launch_light_order(const VMParams& p, void* scratch, uint32_t* order, cudaStream_t s);

@@ -108,7 +108,8 @@ __device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& 
 }
 
 // Light-path order: 4D Morton key of a path's emission samples (the same Philox draws
-// light_path_start reads), counting-sorted.
+// light_path_start reads; with the learned proposal, the area samples and the proposed
+// direction), counting-sorted.
 constexpr int kOrderBits = 5;                      // cells per axis: 32
 constexpr int kOrderCells = 1 << (4 * kOrderBits);
 
@@ -118,7 +119,20 @@ __global__ void k_light_keys(const VMParams P, uint32_t* __restrict__ keys, uint
     PathRng g;
     g.init(P.seed, (uint64_t)i, P.iteration, STREAM_LIGHT);
     const U4 b0 = g.block(0), b1 = g.block(1);
-    const float u[4] = {u01(b0.b), u01(b0.c), u01(b0.d), u01(b1.a)};
+    float u[4] = {u01(b0.b), u01(b0.c), u01(b0.d), u01(b1.a)};
+    if (P.proposal) {
+        // the learned proposal gives the direction: its octahedral coordinates instead
+        const float4 pr = __ldg(&P.proposal[i]);
+        const float l1 = fabsf(pr.x) + fabsf(pr.y) + fabsf(pr.z);
+        float ox = l1 > 0.0f ? pr.x / l1 : 0.0f, oy = l1 > 0.0f ? pr.y / l1 : 0.0f;
+        if (pr.z < 0.0f) {
+            const float tx = (1.0f - fabsf(oy)) * (ox < 0.0f ? -1.0f : 1.0f);
+            oy = (1.0f - fabsf(ox)) * (oy < 0.0f ? -1.0f : 1.0f);
+            ox = tx;
+        }
+        u[2] = 0.5f * (ox + 1.0f);
+        u[3] = 0.5f * (oy + 1.0f);
+    }
     uint32_t key = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
