@@ -84,3 +84,54 @@ def test_concurrent_contexts_render_like_sequential():
     for g, w in zip(got, want):
         assert w.sum() > 0
         np.testing.assert_allclose(g, w, rtol=1e-5, atol=1e-7)
+
+
+def test_new_entry_points_validate_arguments():
+    """gpu_bvh is 0 or 1; the scene dump needs a prepared scene and a known selector;
+    the prepare statistics copy at most what they hold."""
+    import ctypes as C
+    from realcausticsengine_gb300 import abi
+    lib = _native.lib()
+    lib.rc_release()
+    cfg = abi.RcConfig()
+    lib.rc_default_config(C.byref(cfg))
+    assert cfg.gpu_bvh == 1
+    cfg.gpu_bvh = 2
+    assert lib.rc_set_config(C.byref(cfg)) != 0 and b"gpu_bvh" in lib.rc_last_error()
+    cfg.gpu_bvh = 0
+    assert lib.rc_set_config(C.byref(cfg)) == 0
+    n = C.c_longlong(-1)
+    assert lib.rc_scene_dump(0, None, 0, C.byref(n)) != 0 and b"not prepared" in lib.rc_last_error()
+    out = np.full(8, -1.0)
+    assert lib.rc_prepare_stats(out.ctypes.data, 2) == 2 and (out[2:] == -1.0).all()
+    lib.rc_default_config(C.byref(cfg))
+    assert lib.rc_set_config(C.byref(cfg)) == 0
+
+
+def test_unbound_threads_share_the_default_context():
+    """A thread that never binds (and one that binds and unbinds) sees the default
+    context: a scene loaded there on one thread is visible from another, as with the
+    reference's single global scene."""
+    lib = _native.lib()
+    sc = scenes.test_scene()
+    r = Renderer(sc)                        # default context, main thread
+    seen = []
+
+    def worker():
+        ctx = Context()
+        ctx.bind()
+        ctx.unbind()                        # back to the default context
+        info = (np.zeros(9, np.float32))
+        seen.append(lib.rc_prepare_host(info.ctypes.data_as(_ctypes_float_p())))
+        ctx.destroy()
+
+    t = threading.Thread(target=worker)
+    t.start()
+    t.join()
+    assert seen == [0]
+    r.release()
+
+
+def _ctypes_float_p():
+    import ctypes as C
+    return C.POINTER(C.c_float)
