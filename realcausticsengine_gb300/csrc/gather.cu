@@ -159,22 +159,22 @@ __device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, ui
 
 // Lane-parallel variant of the same query, used when node boxes exist down to the bucket
 // level Lb (every node at level Lb holds n >> Lb <= kBucket photons).  A subtree root at
-// level L < Lb is expanded k = min(kExpand, Lb - L) levels at once: lane j box-tests the
-// j-th descendant at level L + k and survivors are pushed as new roots, while lanes test
-// the median photons of the 2^k - 1 inner nodes in between (odd counts only).  Roots at
+// level L < Lb is expanded k = min(E, Lb - L) levels at once (E = 4 or 5, a launch-shape
+// parameter): lane j box-tests the j-th descendant at level L + k and survivors are
+// pushed as new roots, while lanes test the median photons of the 2^k - 1 inner nodes in
+// between (odd counts only).  Roots at
 // level >= Lb are scanned like buckets.  The accepted set is the reference's: every
 // photon of the start node's range lies in a bucket or is an inner node's median; a
 // culled box holds no photon within the radius (box distance <= photon distance under
 // monotonic rounding), a median outside its node's split slab fails the predicate
 // (its distance >= |q[axis] - split|), and every photon that is tested is tested with
-// the reference's predicate.  DFS over roots keeps at most 2^kExpand - 1 pending roots
-// per expansion level: with n < 2^28 (Lb <= 27) at most 7 x 15 + 1 = 106 < kRootStack.
-// (4 levels per step measured best on the water pool: 3 / 4 / 5 levels 8.2 / 6.9 /
-// 7.1 ms per gather.)
-constexpr int kExpand = 4;
+// the reference's predicate.  DFS over roots keeps at most 2^E - 1 pending roots per
+// expansion level: with n < 2^28 (Lb <= 27) at most 6 x 31 + 1 = 187 (E = 5) or
+// 7 x 15 + 1 = 106 (E = 4) < kRootStack.  (On the 1920x1080 water pool 4 levels per
+// step beat 5; 3 lost to both: 6.9 / 7.1 / 8.2 ms per gather.)
 constexpr int kRootStack = 256;
 
-template <class Flush>
+template <int E, class Flush>
 __device__ __forceinline__ void kd_query_expand(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend,
                                                 uint2* stk, int& np, uint32_t tag, VisitCounts& vc, Flush&& flush) {
     const int lane = threadIdx.x & 31;
@@ -214,7 +214,7 @@ __device__ __forceinline__ void kd_query_expand(const KdNav& t, F3 q, float r2, 
             }
             continue;
         }
-        const int k = (Lb - L) < kExpand ? (Lb - L) : kExpand;
+        const int k = (Lb - L) < E ? (Lb - L) : E;
         const uint32_t m = 1u << k;
         vc.nodes += m - 1;
         {
@@ -262,10 +262,10 @@ __device__ __forceinline__ void kd_query_expand(const KdNav& t, F3 q, float r2, 
 // Accepted tree positions go to the warp's pending list `pend` (count `np`, uniform,
 // carried across the queries of a warp) with `tag` in their top bits; the list is
 // handed to `flush` whenever it holds 32 or more entries.  The caller flushes the rest.
-template <class Flush>
+template <int E = 5, class Flush>
 __device__ __forceinline__ void kd_query(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend, uint2* stk,
                                          int& np, uint32_t tag, VisitCounts& vc, Flush&& flush) {
-    if (t.box_levels > 0) kd_query_expand(t, q, r2, start_node, pend, stk, np, tag, vc, flush);
+    if (t.box_levels > 0) kd_query_expand<E>(t, q, r2, start_node, pend, stk, np, tag, vc, flush);
     else kd_query_warp(t, q, r2, start_node, pend, np, tag, vc, flush);
 }
 
@@ -274,7 +274,7 @@ __device__ __forceinline__ void kd_query(const KdNav& t, F3 q, float r2, uint2 s
 // shape parameters.  The warp's queries share the pending list (entry = query slot << 28
 // | tree position); every 32 accepted photons become 32 pairs (query index, position) in
 // the merge buffer, in query order.
-template <int MinBlocks, int QPW>
+template <int MinBlocks, int QPW, int E>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const VMParams P, const KdNav t,
                                                                          QueryBuf qb,
                                                                          const uint32_t* __restrict__ order,
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const
         const uint2 sn = __ldg(&start_nodes[qi]);
         const float4 a = qb.q0[qi];
         __syncwarp();
-        kd_query(t, xyz(a), P.radius_sqr, sn, pend[warp], stk[warp], np, (uint32_t)k << 28, vc, flush);
+        kd_query<E>(t, xyz(a), P.radius_sqr, sn, pend[warp], stk[warp], np, (uint32_t)k << 28, vc, flush);
     }
     if (np > 0) flush(np, pend[warp]);
     if (counters && lane == 0) {
@@ -713,12 +713,12 @@ void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaS
     k_tree_records<<<(unsigned)((tree.n + 255) / 256), 256, 0, s>>>(ph, tree.id, tree.n, tp);
 }
 
-template <int MB, int QPW>
+template <int MB, int QPW, int E>
 void launch_gather_t(const VMParams& p, const KdNav& nav, QueryBuf qb, const uint32_t* order,
                      const uint2* start_nodes, long long nq, MergeBuf mb, unsigned long long* counters,
                      cudaStream_t s, const unsigned long long* nq_dev, const int* skip) {
     const long long warps = (nq + QPW - 1) / QPW;
-    k_gather<MB, QPW><<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
+    k_gather<MB, QPW, E><<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
         p, nav, qb, order, start_nodes, nq, mb, counters, nq_dev, skip);
 }
 
@@ -737,10 +737,11 @@ unsigned merge_grid() {
 int gather_variants() { return 8; }
 
 const char* gather_variant_name(int v) {
-    static const char* names[8] = {"blocks/SM>=2, 8 queries/warp", "blocks/SM>=2, 16 queries/warp",
-                                   "blocks/SM>=3, 8 queries/warp", "blocks/SM>=3, 16 queries/warp",
-                                   "blocks/SM>=4, 8 queries/warp", "blocks/SM>=4, 16 queries/warp",
-                                   "blocks/SM>=5, 16 queries/warp", "blocks/SM>=6, 16 queries/warp"};
+    static const char* names[8] = {
+        "blocks/SM>=2, 8 queries/warp, 5-level steps", "blocks/SM>=2, 16 queries/warp, 5-level steps",
+        "blocks/SM>=3, 8 queries/warp, 5-level steps", "blocks/SM>=3, 16 queries/warp, 5-level steps",
+        "blocks/SM>=4, 8 queries/warp, 5-level steps", "blocks/SM>=4, 16 queries/warp, 5-level steps",
+        "blocks/SM>=3, 8 queries/warp, 4-level steps", "blocks/SM>=4, 8 queries/warp, 4-level steps"};
     return (v >= 0 && v < 8) ? names[v] : "?";
 }
 
@@ -751,14 +752,14 @@ void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryB
     const KdNav nav = nav_of(tree);
     cudaMemsetAsync(mb.count, 0, sizeof(unsigned long long), s);
     switch (variant) {
-    case 0: launch_gather_t<2, 8>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 1: launch_gather_t<2, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 2: launch_gather_t<3, 8>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 4: launch_gather_t<4, 8>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 5: launch_gather_t<4, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 6: launch_gather_t<5, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 7: launch_gather_t<6, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    default: launch_gather_t<3, 16>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 0: launch_gather_t<2, 8, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 1: launch_gather_t<2, 16, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 2: launch_gather_t<3, 8, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 4: launch_gather_t<4, 8, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 5: launch_gather_t<4, 16, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 6: launch_gather_t<3, 8, 4>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    case 7: launch_gather_t<4, 8, 4>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
+    default: launch_gather_t<3, 16, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
     }
     k_merge<<<merge_grid(), kMergeThreads, 0, s>>>(p, tp, qb, tree.id, mb, accum, skip);
 }
