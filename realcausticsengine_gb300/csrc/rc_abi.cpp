@@ -56,6 +56,10 @@ struct DeviceState {
     bool ready = false;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
+    // the camera pass's stream, beside the light pass and the KD build: fork and join
+    // events (timing disabled)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     // scene
     DevBuf<float4> nodes, wnode_lo, wnode_hi, tris, tri_n0, tri_n1, tri_n2;   // layouts: trace.cuh SceneView
     long long num_mesh_nodes = 0, num_tris = 0;
@@ -146,6 +150,9 @@ struct DeviceState {
         for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
         if (t0) { cudaEventDestroy(t0); t0 = nullptr; }
         if (t1) { cudaEventDestroy(t1); t1 = nullptr; }
+        if (fork) { cudaEventDestroy(fork); fork = nullptr; }
+        if (join) { cudaEventDestroy(join); join = nullptr; }
+        if (side) { cudaStreamDestroy(side); side = nullptr; }
         if (stream) { cudaStreamDestroy(stream); stream = nullptr; }
         ready = false;
         iterations_done = 0;
@@ -232,6 +239,9 @@ int ensure_device() {
         for (auto& e : d.evg) RC_CUDA(cudaEventCreate(&e));
         RC_CUDA(cudaEventCreate(&d.t0));
         RC_CUDA(cudaEventCreate(&d.t1));
+        RC_CUDA(cudaStreamCreateWithFlags(&d.side, cudaStreamNonBlocking));
+        RC_CUDA(cudaEventCreateWithFlags(&d.fork, cudaEventDisableTiming));
+        RC_CUDA(cudaEventCreateWithFlags(&d.join, cudaEventDisableTiming));
     }
     return RC_OK;
 }
@@ -620,10 +630,26 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         p.proposal_table = d.prop_table.p;
         p.proposal_table_res = kProposalRes;
     }
+    // With uniformly sampled light paths the camera pass reads nothing that the light
+    // pass writes (a Metropolis sampler scales vm_norm by the light pass's visibility).
+    // Once its launch shape is tuned it then runs on the side stream, issued right
+    // behind the light pass: its blocks take the SMs that the light pass's tail frees
+    // and run through the host's read-back of the photon count and the KD build's
+    // launches; it joins the main stream before the query order.
+    long long qcap = std::max<long long>((long long)d.q0.n, npix * 2);
+    unsigned long long nq = 0;
+    float t_cam = 0.0f;
+    const bool cam_side = sampler == RC_SAMPLER_UNIFORM && !learned &&
+                          (!cfg().autotune || g_tune.camera[size_class(npix)].load() >= 0);
+    const int cam_var = cfg().autotune ? std::max(g_tune.camera[size_class(npix)].load(), 0) : 0;
+    if (cam_side) {
+        RC_CUDA(d.q0.reserve(qcap)); RC_CUDA(d.q1.reserve(qcap)); RC_CUDA(d.q2.reserve(qcap));
+        RC_CUDA(d.q3.reserve(qcap)); RC_CUDA(d.q4.reserve(qcap));
+    }
     for (int attempt = 0; attempt < 3; ++attempt) {
         RC_CUDA(d.ph_pos.reserve(cap)); RC_CUDA(d.ph_dir.reserve(cap));
         RC_CUDA(d.ph_tp.reserve(cap)); RC_CUDA(d.ph_path.reserve(cap));
-        RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
+        RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, cap, d.counters.p};
         if (learned) {
             RC_CUDA(cudaEventRecord(d.evm[0], s));
@@ -650,10 +676,22 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             lvar = slot.load();
             RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         }
+        if (cam_side && attempt == 0) RC_CUDA(cudaEventRecord(d.fork, s));
         if (sampler == RC_SAMPLER_UNIFORM) launch_light_pass(p, ph, d.counters.p + 6, s, lvar);
         else launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaEventRecord(d.ev[1], s));
+        if (cam_side && attempt == 0) {
+            // (its count is read at the join: a read into pageable memory would wait here)
+            RC_CUDA(cudaStreamWaitEvent(d.side, d.fork, 0));
+            RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), d.side));
+            QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qcap, d.counters.p + 1};
+            RC_CUDA(cudaEventRecord(d.ev[4], d.side));
+            launch_camera_pass(p, qb, d.counters.p + 7, d.side, cam_var);
+            RC_CUDA(cudaGetLastError());
+            RC_CUDA(cudaEventRecord(d.ev[5], d.side));
+            RC_CUDA(cudaEventRecord(d.join, d.side));
+        }
         RC_CUDA(cudaMemcpyAsync(&nph, d.counters.p, sizeof(nph), cudaMemcpyDeviceToHost, s));
         if (sampler != RC_SAMPLER_UNIFORM)
             RC_CUDA(cudaMemcpyAsync(mlt, d.counters.p + 2, sizeof(mlt), cudaMemcpyDeviceToHost, s));
@@ -710,12 +748,18 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         RC_CUDA(cudaGetLastError());
     }
     RC_CUDA(cudaEventRecord(d.ev[3], s));
-    // camera pass -> merge queries
-    long long qcap = (long long)d.q0.n;
-    if (qcap < npix * 2) qcap = npix * 2;
-    unsigned long long nq = 0;
-    float t_cam = 0.0f;
-    for (int attempt = 0; attempt < 3; ++attempt) {
+    // camera pass -> merge queries (joined from the side stream, or run here: untuned
+    // launch shape, a Metropolis sampler, the learned proposal, or a query overflow)
+    bool cam_done = false;
+    if (cam_side) {
+        RC_CUDA(cudaMemcpyAsync(&nq, d.counters.p + 1, sizeof(nq), cudaMemcpyDeviceToHost, d.side));
+        RC_CUDA(cudaStreamSynchronize(d.side));
+        RC_CUDA(cudaStreamWaitEvent(s, d.join, 0));
+        t_cam = ms_between(d.ev[4], d.ev[5]);
+        cam_done = (long long)nq <= qcap;
+        if (!cam_done) qcap = (long long)nq + nq / 8 + 1024;
+    }
+    for (int attempt = 0; attempt < 3 && !cam_done; ++attempt) {
         RC_CUDA(d.q0.reserve(qcap)); RC_CUDA(d.q1.reserve(qcap)); RC_CUDA(d.q2.reserve(qcap));
         RC_CUDA(d.q3.reserve(qcap)); RC_CUDA(d.q4.reserve(qcap));
         RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s));
@@ -923,11 +967,20 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     const long long pc = d.async_pcap, qc = d.async_qcap;
     RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
     PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, pc, d.counters.p};
+    QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qc, d.counters.p + 1};
+    // the camera pass on a branch of its own beside the light pass and the KD build
+    // (it reads nothing they write), joined before the count check
+    RC_CUDA(cudaEventRecord(d.fork, s));
+    RC_CUDA(cudaStreamWaitEvent(d.side, d.fork, 0));
     RC_CUDA(record(d.ev[0], s));
     launch_light_order(p, d.order_scratch.p, d.path_order.p, s);
     p.path_order = d.path_order.p;
     launch_light_pass(p, ph, d.counters.p + 6, s, d.async_lvar);
     RC_CUDA(record(d.ev[1], s));
+    RC_CUDA(record(d.ev[4], d.side));
+    launch_camera_pass(p, qb, d.counters.p + 7, d.side, d.async_cvar);
+    RC_CUDA(record(d.ev[5], d.side));
+    RC_CUDA(cudaEventRecord(d.join, d.side));
     // pads one scene extent (plus four base radii) beyond the scene's +x face: outside
     // every merge radius, and close enough that the KD build's largest-extent rule
     // separates them from the stored photons along x within a few levels
@@ -952,10 +1005,7 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     }
     launch_tree_records(PhotonBuf{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, pc, d.counters.p}, tree, tph, s);
     RC_CUDA(record(d.ev[3], s));
-    QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qc, d.counters.p + 1};
-    RC_CUDA(record(d.ev[4], s));
-    launch_camera_pass(p, qb, d.counters.p + 7, s, d.async_cvar);
-    RC_CUDA(record(d.ev[5], s));
+    RC_CUDA(cudaStreamWaitEvent(s, d.join, 0));
     launch_check_counts(d.counters.p, pc, d.counters.p + 1, qc, flag, s);
     RC_CUDA(record(d.ev[6], s));
     launch_query_order(tree, reinterpret_cast<const float*>(d.q0.p), 4, qc, p.radius_sqr, d.qscratch.p, d.qorder.p,
