@@ -270,6 +270,8 @@ def run_ours(args):
         "gpu_launches": int(dev[3]),
         "clocks": clk.summary(),
         "phase_ms_per_step": {k: st[k] for k in ("light_ms", "kd_ms", "camera_ms", "gather_ms")},
+        "phase_note": "event windows of the last iteration; the camera pass runs on a second stream "
+                      "beside the light pass and the KD build, its window opening with the light pass",
         "wall_s": wall,
     }
     if not args.no_learned:

@@ -79,6 +79,15 @@ struct Buffers {
     float* x[2]; float* y[2]; float* z[2]; uint32_t* id[2];
 };
 
+// One half of the double buffer, picked with selects: indexing the kernel parameter
+// with a runtime value would copy all of it to local memory in every thread.
+struct Side {
+    float* x; float* y; float* z; uint32_t* id;
+};
+__device__ __forceinline__ Side side(const Buffers& B, int k) {
+    return k ? Side{B.x[1], B.y[1], B.z[1], B.id[1]} : Side{B.x[0], B.y[0], B.z[0], B.id[0]};
+}
+
 // Chunk -> at most two nodes A, B on `level`.
 struct ChunkNodes {
     long long eA, sA, eB, sB, c;
@@ -129,12 +138,13 @@ __global__ void __launch_bounds__(kThreads) k_bbox(Buffers B, int cur, int level
     for (int q = 0; q < 2; ++q) for (int k = 0; k < 3; ++k) { mn[q][k] = 0x7fffffff; mx[q][k] = (int)0x80000000; }
     float px[kItems], py[kItems], pz[kItems];
     int wh[kItems];
+    const Side S = side(B, cur);
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {   // loads of all rounds in flight together
         long long i = a + it * kThreads + threadIdx.x;
         wh[it] = i < n ? which(i, cn) : -1;
         const long long j = wh[it] >= 0 ? i : a;
-        px[it] = B.x[cur][j]; py[it] = B.y[cur][j]; pz[it] = B.z[cur][j];
+        px[it] = S.x[j]; py[it] = S.y[j]; pz[it] = S.z[j];
     }
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
@@ -183,8 +193,8 @@ __global__ void k_axis(long long count, const int* nbox, NodeSel* sel) {
     sel[t].axis = node_axis(nbox, t);
 }
 
-__device__ __forceinline__ float coord(const Buffers& B, int cur, long long i, int axis) {
-    return axis == 0 ? B.x[cur][i] : (axis == 1 ? B.y[cur][i] : B.z[cur][i]);
+__device__ __forceinline__ float coord(const Side& S, long long i, int axis) {
+    return axis == 0 ? S.x[i] : (axis == 1 ? S.y[i] : S.z[i]);
 }
 
 __global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level, long long n, long long first,
@@ -205,11 +215,12 @@ __global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level
     // all rounds' coordinates first (independent loads in flight together), then bins
     float val[kItems];
     int wh[kItems];
+    const Side S = side(B, cur);
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
         long long i = a + it * kThreads + threadIdx.x;
         wh[it] = i < n ? which(i, cn) : -1;
-        val[it] = wh[it] >= 0 ? coord(B, cur, i, ax[wh[it]]) : 0.0f;
+        val[it] = wh[it] >= 0 ? coord(S, i, ax[wh[it]]) : 0.0f;
     }
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {   // every lane runs every round (full-warp match)
@@ -311,11 +322,12 @@ __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int 
     float px[kItems], py[kItems], pz[kItems];
     uint32_t pid[kItems];
     int cls[kItems], rank[kItems];
+    const Side S = side(B, cur), D = side(B, dst);
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
         const long long i = a + it * kThreads + threadIdx.x;
         const long long j = i < n ? i : a;
-        px[it] = B.x[cur][j]; py[it] = B.y[cur][j]; pz[it] = B.z[cur][j]; pid[it] = B.id[cur][j];
+        px[it] = S.x[j]; py[it] = S.y[j]; pz[it] = S.z[j]; pid[it] = S.id[j];
         cls[it] = i < n ? which(i, cn) : -2;
     }
 #pragma unroll
@@ -379,7 +391,7 @@ __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int 
             } else d = s + k + odd + (eq[w] - kl - odd) + r;
             if (d < s || d >= s + c) { atomicOr(err, 2); continue; }   // inconsistent counts
         }
-        B.x[dst][d] = xv; B.y[dst][d] = yv; B.z[dst][d] = zv; B.id[dst][d] = idv;
+        D.x[d] = xv; D.y[d] = yv; D.z[d] = zv; D.id[d] = idv;
     }
 }
 
@@ -398,7 +410,8 @@ __global__ void k_copy_medians(Buffers B, int src, int level0, long long n) {
     long long c = n >> lv;
     if (!(c & 1)) return;
     long long p = kd_node_start(e, lv, n) + (c >> 1);
-    B.x[0][p] = B.x[src][p]; B.y[0][p] = B.y[src][p]; B.z[0][p] = B.z[src][p]; B.id[0][p] = B.id[src][p];
+    const Side S = side(B, src);
+    B.x[0][p] = S.x[p]; B.y[0][p] = S.y[p]; B.z[0][p] = S.z[p]; B.id[0][p] = S.id[p];
 }
 
 // Shared-memory subtree builder: one CTA per node on level0 (at most kSmemSeg photons).
@@ -446,8 +459,9 @@ __global__ void __launch_bounds__(kSmemThreads) k_smem_build(Buffers B, int src,
     const int c0 = (int)(n >> level0);
     const int tid = threadIdx.x, nt = blockDim.x;
     const int lane = tid & 31, wid = tid >> 5;
+    const Side S = side(B, src);
     for (int i = tid; i < c0; i += nt) {
-        X[i] = B.x[src][s0 + i]; Y[i] = B.y[src][s0 + i]; Z[i] = B.z[src][s0 + i]; I[i] = B.id[src][s0 + i];
+        X[i] = S.x[s0 + i]; Y[i] = S.y[s0 + i]; Z[i] = S.z[s0 + i]; I[i] = S.id[s0 + i];
     }
     __syncthreads();
     // three sorted lists (padding keys ~0 sort last)

@@ -495,6 +495,13 @@ cudaError_t record(cudaEvent_t e, cudaStream_t s) {
                                                : cudaEventRecord(e, s);
 }
 
+// Device time from the light pass's start to the later of the KD build's end and the
+// camera pass's end, for an iteration whose camera pass ran on the side stream (its
+// events ev[4], ev[5] overlap the light pass and the KD build).
+double overlapped_ms(const DeviceState& d) {
+    return std::max(ms_between(d.ev[0], d.ev[3]), ms_between(d.ev[0], d.ev[5]));
+}
+
 ProposalCtx proposal_ctx(const HostScene& sc, const VMParams& p) {
     ProposalCtx c{};
     c.lights = p.lights;
@@ -876,7 +883,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     st[6] = t_cam;
     st[7] = ms_between(d.ev[6], d.ev[7]);
     st[8] = t_mlp;           // proposal inference + training
-    st[9] = st[4] + st[5] + st[6] + st[7] + st[8];
+    st[9] = (cam_side ? overlapped_ms(d) : st[4] + st[5] + st[6]) + st[7] + st[8];
     st[10] = d.iterations_done;
     st[11] = sc.scene_radius;
     st[12] = std::sqrt(p.radius_sqr);
@@ -1113,7 +1120,7 @@ int render_iterations(HostScene& sc, int iterations) {
     st[6] = ms_between(d.ev[4], d.ev[5]);
     st[7] = ms_between(d.ev[6], d.ev[7]);
     st[8] = 0.0;
-    st[9] = st[4] + st[5] + st[6] + st[7];
+    st[9] = overlapped_ms(d) + st[7];
     st[10] = d.iterations_done;
     st[11] = sc.scene_radius;
     st[12] = std::sqrt(p.radius_sqr);
