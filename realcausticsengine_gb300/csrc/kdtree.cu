@@ -440,6 +440,20 @@ __device__ __forceinline__ float axis_coord(const float* X, const float* Y, cons
     return a == 0 ? X[q] : (a == 1 ? Y[q] : Z[q]);
 }
 
+// Compare-exchange of a thread's keys E0 < E1 (positions 4t + E0, 4t + E1) in all three
+// lists, ascending where bit k of the position is clear.
+template <int E0, int E1>
+__device__ __forceinline__ void sort_pair(unsigned long long (&key)[3][4], int tid, int k) {
+    const bool up = ((4 * tid + E0) & k) == 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const unsigned long long lo = key[a][E0], hi = key[a][E1];
+        const bool swap = (lo > hi) == up;
+        key[a][E0] = swap ? hi : lo;
+        key[a][E1] = swap ? lo : hi;
+    }
+}
+
 __global__ void __launch_bounds__(kSmemThreads) k_smem_build(Buffers B, int src, int level0, long long n, uint2* nodes) {
     extern __shared__ __align__(16) unsigned char smem[];
     float* X = (float*)(smem + SmemLayout::xs);
@@ -464,48 +478,64 @@ __global__ void __launch_bounds__(kSmemThreads) k_smem_build(Buffers B, int src,
         X[i] = S.x[s0 + i]; Y[i] = S.y[s0 + i]; Z[i] = S.z[s0 + i]; I[i] = S.id[s0 + i];
     }
     __syncthreads();
-    // three sorted lists (padding keys ~0 sort last)
-    int pw = 1;
-    while (pw < c0) pw <<= 1;
-    const int nv3 = 3 * pw;
-    for (int v = tid; v < nv3; v += nt) {
-        const int a = v / pw, p = v - a * pw;
-        V[v] = p < c0 ? ((unsigned long long)f2key(axis_coord(X, Y, Z, a, p)) << 32) | (unsigned)p : ~0ull;
-    }
-    __syncthreads();
-    for (int k = 2; k <= pw; k <<= 1) {
+    // three sorted lists: a bitonic network over kSmemSeg keys (coordinate key, local
+    // index) per list, padding keys ~0 sorting last.  Thread t holds keys 4t..4t+3 of
+    // every list in registers: strides 1 and 2 are exchanged in registers, 4..64 with
+    // warp shuffles (partner lane t ^ stride/4), 128 and up through shared memory.
+    static_assert(kSmemSeg == 4 * kSmemThreads, "four keys per thread and list");
+    unsigned long long key[3][4];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int p = 4 * tid + e;
+            key[a][e] = p < c0 ? ((unsigned long long)f2key(axis_coord(X, Y, Z, a, p)) << 32) | (unsigned)p : ~0ull;
+        }
+    for (int k = 2; k <= kSmemSeg; k <<= 1) {
         for (int jj = k >> 1; jj > 0; jj >>= 1) {
-            for (int i = tid; i < nv3; i += nt) {
-                const int l = i ^ jj;   // same list: pw is a power of two and lists are pw-aligned
-                if (l > i) {
-                    const bool up = ((i & k) == 0) || (k == pw);
-                    const unsigned long long a = V[i], b = V[l];
-                    if ((a > b) == up) { V[i] = b; V[l] = a; }
+            if (jj >= 4) {
+                const bool smem_stage = jj >= 128;
+                if (smem_stage) {
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) V[a * kSmemSeg + 4 * tid + e] = key[a][e];
+                    __syncthreads();
                 }
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int i = 4 * tid + e;
+                    // the lower index of a pair keeps the minimum in an ascending run
+                    const bool keep_min = ((i & jj) == 0) == ((i & k) == 0);
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const unsigned long long other =
+                            smem_stage ? V[a * kSmemSeg + (i ^ jj)]
+                                       : (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)key[a][e], jj >> 2);
+                        const unsigned long long mine = key[a][e];
+                        key[a][e] = keep_min ? (mine < other ? mine : other) : (mine < other ? other : mine);
+                    }
+                }
+                if (smem_stage) __syncthreads();
+            } else if (jj == 2) {
+                sort_pair<0, 2>(key, tid, k);
+                sort_pair<1, 3>(key, tid, k);
+            } else {
+                sort_pair<0, 1>(key, tid, k);
+                sort_pair<2, 3>(key, tid, k);
             }
-            __syncthreads();
         }
     }
-    {
-        // keys -> index lists (the lists overlay the keys: read all, then write)
-        constexpr int kPer = 3 * kSmemSeg / kSmemThreads;
-        uint32_t tmp[kPer];
+    // keys -> index lists (the lists overlay the keys; the last shared-memory stage
+    // ended with a barrier)
 #pragma unroll
-        for (int r = 0; r < kPer; ++r) {
-            const int v = tid + r * nt;
-            tmp[r] = v < nv3 ? (uint32_t)(V[v] & 0xffffffffu) : 0u;
-        }
-        __syncthreads();
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int r = 0; r < kPer; ++r) {
-            const int v = tid + r * nt;
-            if (v < nv3) {
-                const int a = v / pw, p = v - a * pw;
-                if (p < c0) L[a * kSmemSeg + p] = tmp[r];
-            }
+        for (int e = 0; e < 4; ++e) {
+            const int p = 4 * tid + e;
+            if (p < c0) L[a * kSmemSeg + p] = (uint32_t)(key[a][e] & 0xffffffffu);
         }
-        __syncthreads();
-    }
+    __syncthreads();
     for (int j = 0;; ++j) {
         const int c = c0 >> j;
         const int nsub = 1 << j;
