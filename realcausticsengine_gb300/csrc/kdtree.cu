@@ -3,15 +3,17 @@
 // Levels whose nodes hold more than kSmemSeg photons are split with global passes,
 // one pass per step over all photons (SoA x/y/z/id, double buffered):
 //   bbox      per-node extent -> axis (largest extent)
-//   hist x4   8-bit radix select of the rank-count/2 key along the node's axis
+//   hist x4   8-bit radix select of the rank-count/2 key along the node's axis (the
+//             leading digits the node's box fixes are skipped)
 //   partition photons below / equal / above the median key to their halves
 // A CTA covers kChunk consecutive positions; because nodes on these levels hold more
 // than kChunk photons, a chunk meets at most two nodes (and one ancestor median
 // between them), so histograms and counters stay in shared memory and only their
 // totals go to global memory.
 // From the first level with at most kSmemSeg photons per node, one CTA per node
-// loads its photons into shared memory and finishes the whole subtree there with a
-// bitonic sort per level (key, then local index), writing nodes and final order.
+// loads its photons into shared memory and finishes the whole subtree there: one
+// sort along x, y and z (key, then local index), then stable splits of the three
+// lists per level, writing nodes and final order.
 #include "kdtree.cuh"
 #include <cmath>
 #include <cstdio>
@@ -73,6 +75,7 @@ struct NodeSel {
     int eq;            // photons whose key equals the median key
     int axis;
     int cnt[3];        // partition cursors (below / equal / above)
+    int first;         // first digit pass that runs (earlier digits fixed by the node's box)
 };
 
 struct Buffers {
@@ -125,6 +128,7 @@ __global__ void k_level_init(int level, long long first, long long count, int* n
     NodeSel& s = sel[t];
     s.prefix = 0; s.krem = (int)((n >> level) >> 1); s.eq = 0; s.axis = 0;
     s.cnt[0] = s.cnt[1] = s.cnt[2] = 0;
+    s.first = 0;
 }
 
 __global__ void __launch_bounds__(kThreads) k_bbox(Buffers B, int cur, int level, long long n, long long first, int* nbox) {
@@ -187,10 +191,21 @@ __device__ __forceinline__ int node_axis(const int* nbox, long long t) {
     return biggest_axis(ex, ey, ez);
 }
 
+// The node's split axis.  Every key of the node lies between the keys of its box's
+// ends along that axis (both orders are IEEE total order), so the whole leading digits
+// those two keys share are the median's digits too: they go into the prefix, and the
+// radix-select passes over them are skipped (the last pass always runs: it writes the
+// split and the count of keys equal to the median).
 __global__ void k_axis(long long count, const int* nbox, NodeSel* sel) {
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= count) return;
-    sel[t].axis = node_axis(nbox, t);
+    const int a = node_axis(nbox, t);
+    const uint32_t lo = f2key(ord2f(nbox[6 * t + a])), hi = f2key(ord2f(nbox[6 * t + 3 + a]));
+    const int d = min(__clz(lo ^ hi) >> 3, 3);
+    NodeSel& s = sel[t];
+    s.axis = a;
+    s.first = d;
+    s.prefix = lo & ~(0xffffffffu >> (8 * d));
 }
 
 __device__ __forceinline__ float coord(const Side& S, long long i, int axis) {
@@ -203,14 +218,21 @@ __global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level
     __shared__ uint32_t sh[2][256];
     __shared__ uint32_t pre[2];
     __shared__ int ax[2];
+    __shared__ bool live[2];   // the node's digit for this pass is not fixed by its box
     long long a = blockIdx.x * (long long)kChunk;
     if (threadIdx.x == 0) {
         chunk_nodes(a, level, n, cn);
-        ax[0] = sel[cn.eA - first].axis; pre[0] = sel[cn.eA - first].prefix;
-        if (cn.eB) { ax[1] = sel[cn.eB - first].axis; pre[1] = sel[cn.eB - first].prefix; }
+        const NodeSel* sa = sel + (cn.eA - first);
+        ax[0] = sa->axis; pre[0] = sa->prefix; live[0] = pass >= sa->first;
+        live[1] = false;
+        if (cn.eB) {
+            const NodeSel* sb = sel + (cn.eB - first);
+            ax[1] = sb->axis; pre[1] = sb->prefix; live[1] = pass >= sb->first;
+        }
     }
     for (int k = threadIdx.x; k < 512; k += kThreads) (&sh[0][0])[k] = 0;
     __syncthreads();
+    if (!live[0] && !live[1]) return;
     const int shift = 24 - 8 * pass;
     // all rounds' coordinates first (independent loads in flight together), then bins
     float val[kItems];
@@ -219,7 +241,8 @@ __global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
         long long i = a + it * kThreads + threadIdx.x;
-        wh[it] = i < n ? which(i, cn) : -1;
+        const int w = i < n ? which(i, cn) : -1;
+        wh[it] = w >= 0 && live[w] ? w : -1;
         val[it] = wh[it] >= 0 ? coord(S, i, ax[wh[it]]) : 0.0f;
     }
 #pragma unroll
@@ -253,6 +276,7 @@ __global__ void k_select(long long count, long long first, int level, long long 
     long long t = blockIdx.x * (long long)(blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
     if (t >= count) return;
+    if (pass < sel[t].first) return;   // digit fixed by the node's box (k_axis); no counts
     uint32_t* h = hist + t * 256;
     uint32_t v[8];
     uint32_t sum = 0;
@@ -461,8 +485,8 @@ __global__ void __launch_bounds__(kSmemThreads) k_smem_build(Buffers B, int src,
     float* Z = (float*)(smem + SmemLayout::zs);
     uint32_t* I = (uint32_t*)(smem + SmemLayout::ids);
     unsigned long long* V = (unsigned long long*)(smem + SmemLayout::v);
-    uint32_t* L = (uint32_t*)(smem + SmemLayout::lists);   // L[a * kSmemSeg + p]
-    uint32_t* T = (uint32_t*)(smem + SmemLayout::temp);
+    uint32_t* L = (uint32_t*)(smem + SmemLayout::lists);   // current lists: L[a * kSmemSeg + p]
+    uint32_t* T = (uint32_t*)(smem + SmemLayout::temp);    // split output (swapped with L per level)
     int* cls = (int*)(smem + SmemLayout::cls);
     int* segs = (int*)(smem + SmemLayout::segs);
     int* axes = (int*)(smem + SmemLayout::axes);
@@ -632,16 +656,15 @@ __global__ void __launch_bounds__(kSmemThreads) k_smem_build(Buffers B, int src,
                 else if (c2 == 1) dst = st + k;
                 else dst = st + k + odd + (excl[2 * a + 1]++ - s * k);
                 T[a * kSmemSeg + dst] = qq[a][r];
+                // a median keeps its place for good, outside every later sub-node: it
+                // goes into both buffers (this level's reads of L ended at the barrier)
+                if (c2 == 1) L[a * kSmemSeg + dst] = qq[a][r];
             }
         }
         __syncthreads();
-        for (int v = tid; v < nv; v += nt) {
-            const int s = v / c, p = segs[s] + (v - s * c);
-            L[p] = T[p];
-            L[kSmemSeg + p] = T[kSmemSeg + p];
-            L[2 * kSmemSeg + p] = T[2 * kSmemSeg + p];
-        }
-        __syncthreads();
+        uint32_t* const done = L;   // the split lists become the current ones
+        L = T;
+        T = done;
     }
     __syncthreads();
     for (int i = tid; i < c0; i += nt) {
