@@ -216,7 +216,7 @@ const char* rc_last_error(void);
  * [11] scene radius, [12] current merge radius, [13] kernel launches,
  * [14] photon-query distance tests in the gather, [15] 64-photon buckets visited.
  * With the learned proposal, [8] is the proposal inference + training time.
- * With uniformly sampled light paths (and no learned proposal) the camera pass runs on
+ * With uniformly sampled light paths the camera pass runs on
  * a second stream beside the light pass and the KD build: its window [6] opens with the
  * light pass, and [9] counts the overlapped span once. */
 int rc_get_stats(double* out, int n);

@@ -642,11 +642,13 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     // Once its launch shape is tuned it then runs on the side stream, issued right
     // behind the light pass: its blocks take the SMs that the light pass's tail frees
     // and run through the host's read-back of the photon count and the KD build's
-    // launches; it joins the main stream before the query order.
+    // launches; it joins the main stream before the query order.  (With the learned
+    // proposal the network's inference ends before the fork and its training starts
+    // after the join: no tensor-core kernel runs beside it.)
     long long qcap = std::max<long long>((long long)d.q0.n, npix * 2);
     unsigned long long nq = 0;
     float t_cam = 0.0f;
-    const bool cam_side = sampler == RC_SAMPLER_UNIFORM && !learned &&
+    const bool cam_side = sampler == RC_SAMPLER_UNIFORM &&
                           (!cfg().autotune || g_tune.camera[size_class(npix)].load() >= 0);
     const int cam_var = cfg().autotune ? std::max(g_tune.camera[size_class(npix)].load(), 0) : 0;
     if (cam_side) {
@@ -756,7 +758,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     }
     RC_CUDA(cudaEventRecord(d.ev[3], s));
     // camera pass -> merge queries (joined from the side stream, or run here: untuned
-    // launch shape, a Metropolis sampler, the learned proposal, or a query overflow)
+    // launch shape, a Metropolis sampler, or a query overflow)
     bool cam_done = false;
     if (cam_side) {
         RC_CUDA(cudaMemcpyAsync(&nq, d.counters.p + 1, sizeof(nq), cudaMemcpyDeviceToHost, d.side));
