@@ -214,7 +214,7 @@ const char* rc_last_error(void);
  * [4] light-pass ms, [5] KD-build ms, [6] camera-pass ms, [7] gather ms,
  * [8] accumulate ms, [9] total device ms, [10] iterations rendered so far,
  * [11] scene radius, [12] current merge radius, [13] kernel launches,
- * [14] photon-query distance tests in the gather, [15] 64-photon buckets visited.
+ * [14] photon-query distance tests in the gather, [15] 32-photon buckets visited.
  * With the learned proposal, [8] is the proposal inference + training time.
  * With uniformly sampled light paths the camera pass runs on
  * a second stream beside the light pass and the KD build: its window [6] opens with the
