@@ -768,6 +768,9 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         cam_done = (long long)nq <= qcap;
         if (!cam_done) qcap = (long long)nq + nq / 8 + 1024;
     }
+    // a side-stream camera pass of an earlier iteration that returned an error may
+    // still be writing the query buffers (a wait before the event's first record is void)
+    if (!cam_side) RC_CUDA(cudaStreamWaitEvent(s, d.join, 0));
     for (int attempt = 0; attempt < 3 && !cam_done; ++attempt) {
         RC_CUDA(d.q0.reserve(qcap)); RC_CUDA(d.q1.reserve(qcap)); RC_CUDA(d.q2.reserve(qcap));
         RC_CUDA(d.q3.reserve(qcap)); RC_CUDA(d.q4.reserve(qcap));
@@ -1094,6 +1097,9 @@ int render_iterations(HostScene& sc, int iterations) {
     }
     const int n_async = iterations - i;
     if (n_async <= 0) return RC_OK;
+    // the replayed iterations' camera branch writes the query buffers that an eager
+    // iteration's side-stream camera pass may still be writing (after an error return)
+    RC_CUDA(cudaStreamSynchronize(d.side));
     RC_CUDA(d.async_flags.reserve(n_async));
     const int first_it = d.iterations_done;
     for (int k = 0; k < n_async; ++k) {
