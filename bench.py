@@ -55,6 +55,52 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def visible_device(local: int) -> str:
+    """CUDA_VISIBLE_DEVICES value that gives a rank its own GPU: the local-th entry of a
+    device list the launcher set (its only entry when it set one per rank), else the
+    local rank itself."""
+    ids = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    if not ids:
+        return str(local)
+    if len(ids) == 1:
+        return ids[0]
+    if local < len(ids):
+        return ids[local]
+    raise SystemExit(f"local rank {local} has no GPU in CUDA_VISIBLE_DEVICES={','.join(ids)}")
+
+
+class Ranks:
+    """Coordination of the ranks of a multi-process run (one process per GPU, launched by
+    torch.distributed.run): a gloo group for the barriers around the timed regions and
+    the maximum of the timings over ranks.  The ranks are independent replicas, so no
+    data moves between them.  With one rank every call is a no-op."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, *values: float) -> list[float]:
+        if self.dist is None:
+            return [float(v) for v in values]
+        import torch
+        t = torch.tensor(values, dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return t.tolist()
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -183,8 +229,10 @@ def run_ours(args):
     from realcausticsengine_gb300.session import Renderer
     from realcausticsengine_gb300 import abi
 
-    rank, world, local = dist_env()
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+    ranks = Ranks()
+    rank, world, local = ranks.rank, ranks.world, ranks.local
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = visible_device(local)
     lib = _native.lib()
     sc = scenes.water_pool(args.width, args.height, grid=args.grid, samples=args.steps)
     paths = args.photons
@@ -195,14 +243,16 @@ def run_ours(args):
     r.prepare()
     r.render(args.warmup)
     dev = np.zeros(4, np.float64)
+    ranks.barrier()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
+        # synchronises the library's stream before its first event and after its last
         _native.check(lib.rc_render_timed(args.steps, dev.ctypes.data), "rc_render_timed")
         wall = time.perf_counter() - t0
+    ranks.barrier()
     st = r.stats()
     device_ms = dev[0]
     gather_ms_mean, gather_bytes, nq, nph = dev[1], dev[2], st["queries"], st["photons"]
-    value_rank = paths * args.steps / (device_ms / 1000.0)
     r.release()
 
     # ---- end to end through the C ABI with host buffers
@@ -216,34 +266,27 @@ def run_ours(args):
     lib.rc_set_config(C.byref(cfg))
     img = np.zeros((args.height, args.width, 3), np.float32)
     ia = InitArgs(sc)            # the Blender-side structures init() reads
+    ranks.barrier()
     t0 = time.perf_counter()
     ia.call(lib.init)
     _native.check(lib.rc_prepare(), "rc_prepare")
     for _ in range(args.steps):
         _native.check(lib.rc_render(1), "rc_render")
+        # a synchronous read: the step's image is on the host when it returns
         _native.check(lib.rc_read_image(img.ctypes.data, args.width, args.height), "rc_read_image")
     e2e_s = time.perf_counter() - t0
+    ranks.barrier()
     lib.rc_release()
     h2d = sum(m.verts.nbytes + m.normals.nbytes + m.tris.nbytes for m in sc.meshes)
     d2h = img.nbytes            # the FP32 mean image read back each step
-    e2e_rank = paths * args.steps / e2e_s
 
-    vals = [value_rank]
-    e2es = [e2e_rank]
-    dms = [device_ms]
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        t = torch.tensor([device_ms, e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        device_ms, e2e_s = t.tolist()
-        vals = [paths * args.steps * world / (device_ms / 1000.0)]
-        e2es = [paths * args.steps * world / e2e_s]
-        dms = [device_ms]
-        dist.destroy_process_group()
+    # the slowest rank's times; every rank processed `paths * steps` light paths
+    device_ms, e2e_s = ranks.max(device_ms, e2e_s)
+    ranks.close()
     if rank != 0:
         return
+    value = paths * args.steps * world / (device_ms / 1000.0)
+    e2e_value = paths * args.steps * world / e2e_s
     peak, peak_kind = measured_peaks()
     achieved = gather_bytes / (gather_ms_mean / 1000.0) / 1e9 if gather_ms_mean > 0 else 0.0
     # DRAM bytes per gather (traversal + merge kernels): ncu dram__bytes_read.sum +
@@ -253,16 +296,16 @@ def run_ours(args):
     # with their counts)
     traffic = GATHER_TRAFFIC_OVER_ALGORITHMIC * gather_bytes
     line = {
-        "metric": METRIC, "value": float(vals[0]) if world == 1 else float(vals[0]), "unit": METRIC,
+        "metric": METRIC, "value": float(value), "unit": METRIC,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": dms[0] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": device_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{WORKLOAD} {args.width}x{args.height}, {args.grid}x{args.grid}-vertex heightfield "
                                f"({sc.num_tris()} tris), {paths} photons/iter, max depth {MAX_PATH}",
                    "photons_per_iter": paths, "stored_photons_per_iter": nph, "merge_queries_per_iter": nq,
                    "l2": "inputs larger than L2 (photon map and query buffers > 129 MB)",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "e2e": {"value": float(e2es[0]), "unit": METRIC, "h2d_bytes_per_step": int(h2d // max(args.steps, 1)),
+        "e2e": {"value": float(e2e_value), "unit": METRIC, "h2d_bytes_per_step": int(h2d // max(args.steps, 1)),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"kernel": "k_gather + k_merge (the gather)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
@@ -418,7 +461,7 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
-def main():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=8)
@@ -437,7 +480,11 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--batch-threads", type=int, default=2,
                     help="host threads driving the batch's scenes (one library context per scene)")
-    args = ap.parse_args()
+    return ap.parse_args(argv)
+
+
+def main():
+    args = parse_args()
     if args.workload == "batch" and args.impl != "reference":
         run_batch(args)
         return
