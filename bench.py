@@ -45,10 +45,14 @@ WORKLOAD = "water_pool"
 PHOTONS_PER_ITER = 16 << 20
 MAX_PATH = 8
 METRIC = "photons/s"
-# bytes per unit of the gather (algorithmic): photon record read once, query record
-# read once, FP64 RGB pixel read+write once per query
-PHOTON_BYTES, QUERY_BYTES, PIXEL_BYTES = 40, 80, 48
-GATHER_TRAFFIC_OVER_ALGORITHMIC = 1.147
+# bytes per unit of the gather (algorithmic): each stored photon's 40-byte record read
+# once, each merge query's 64-byte record read once, each pixel's FP64 RGB sum read and
+# written once (40 P + 64 Q + 48 X); the "touched" variant reads one photon record per
+# accepted photon-query pair (40 sum k)
+PHOTON_BYTES, QUERY_BYTES, PIXEL_BYTES = 40, 64, 48
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) over algorithmic bytes of one
+# k_gather launch on the 960x540 / 4M-path water pool (profiles/k_gather_water_pool_960x540.md)
+GATHER_TRAFFIC_OVER_ALGORITHMIC = 1.163
 
 
 def dist_env():
@@ -289,12 +293,11 @@ def run_ours(args):
     e2e_value = paths * args.steps * world / e2e_s
     peak, peak_kind = measured_peaks()
     achieved = gather_bytes / (gather_ms_mean / 1000.0) / 1e9 if gather_ms_mean > 0 else 0.0
-    # DRAM bytes per gather (traversal + merge kernels): ncu dram__bytes_read.sum +
-    # dram__bytes_write.sum of one gather on the 960x540 / 4M-path case
-    # (profiles/k_gather_water_pool_960x540.md) is 1.147x its algorithmic bytes; scaled to
-    # this workload's gather by its algorithmic bytes (photon and query records both scale
-    # with their counts)
+    # DRAM bytes of one gather: the ncu capture on the 960x540 / 4M-path case moved
+    # 1.163x its algorithmic bytes; scaled to this workload's launch by its algorithmic
+    # bytes (photon, query and pixel records all scale with their counts)
     traffic = GATHER_TRAFFIC_OVER_ALGORITHMIC * gather_bytes
+    touched = PHOTON_BYTES * st["merged"]
     line = {
         "metric": METRIC, "value": float(value), "unit": METRIC,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -307,9 +310,13 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": float(e2e_value), "unit": METRIC, "h2d_bytes_per_step": int(h2d // max(args.steps, 1)),
                 "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"kernel": "k_gather + k_merge (the gather)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"kernel": "k_gather (fused photon gather: traversal, merge evaluation, FP64 pixel sums)",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes": gather_bytes},
+                     "algorithmic_bytes": gather_bytes,
+                     "bytes_formula": "40 B x stored photons + 64 B x merge queries + 48 B x pixels",
+                     "touched_bytes": touched,
+                     "touched_frac": (touched / (gather_ms_mean / 1000.0) / 1e9) / peak if gather_ms_mean > 0 else 0.0},
         "gpu_launches": int(dev[3]),
         "clocks": clk.summary(),
         "phase_ms_per_step": {k: st[k] for k in ("light_ms", "kd_ms", "camera_ms", "gather_ms")},

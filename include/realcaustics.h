@@ -195,8 +195,8 @@ int rc_render(int iterations);
 
 /* rc_render timed on the device: CUDA events on the library's stream around all
  * `iterations`.  out[0] = elapsed ms, out[1] = mean gather-kernel ms per iteration,
- * out[2] = gather algorithmic bytes per iteration (40 B per photon + 80 B per merge
- * query + 48 B FP64 pixel read/write per query), out[3] = kernel launches. */
+ * out[2] = gather algorithmic bytes per iteration (40 B per stored photon + 64 B per
+ * merge query + 48 B FP64 RGB read/write per pixel), out[3] = kernel launches. */
 int rc_render_timed(int iterations, double* out);
 
 /* Copy the current image (mean over rendered iterations) as FP32 RGB, rows in the
@@ -214,7 +214,8 @@ const char* rc_last_error(void);
  * [4] light-pass ms, [5] KD-build ms, [6] camera-pass ms, [7] gather ms,
  * [8] accumulate ms, [9] total device ms, [10] iterations rendered so far,
  * [11] scene radius, [12] current merge radius, [13] kernel launches,
- * [14] photon-query distance tests in the gather, [15] 32-photon buckets visited.
+ * [14] photon-query distance tests in the gather, [15] photon chunks (of at most 32)
+ * tested by the gather's query groups.
  * With the learned proposal, [8] is the proposal inference + training time.
  * With uniformly sampled light paths the camera pass runs on
  * a second stream beside the light pass and the KD build: its window [6] opens with the
@@ -266,6 +267,12 @@ int rc_trace_rays_full(int n, const float* origins, const float* directions, flo
  * (u32 bits), 0].  *count receives the number stored (may exceed cap). */
 int rc_light_photons(int iteration, float* out, long long cap, long long* count);
 
+/* One camera pass (iteration `iteration`, current config) on the GPU; copies the merge
+ * queries it writes (one per non-delta camera vertex, Vertex_Merging.cpp:309-362), in
+ * storage order, as 4 floats each: [position xyz, camera dVM].  *count receives the
+ * number written (may exceed cap). */
+int rc_camera_queries(int iteration, float* out, long long cap, long long* count);
+
 /* Build the photon KD-tree on the GPU over n photon positions (3 floats each) and
  * answer q radius queries (squared radius r2): counts[j] = number of photons with
  * ((dx*dx + dy*dy) + dz*dz) < r2 (KD_Tree::find_closest_in_radius, src/KD_Tree.cpp:217-280),
@@ -273,6 +280,16 @@ int rc_light_photons(int iteration, float* out, long long cap, long long* count)
  * (capacity cap).  *total receives the total count (may exceed cap). */
 int rc_kd_query(int n, const float* positions, int q, const float* queries, float r2,
                 int* counts, int* idx, long long cap, long long* total);
+
+/* The same radius query run by the render's own gather kernel (KD_Tree::find_closest_in_radius,
+ * src/KD_Tree.cpp:217-280, as the gather of Path_Vertices::get_contrib, src/Path_Vertices.h:46-68,
+ * calls it): the tree's chunk boxes, the KD-cell query order, `variant`'s launch shape
+ * (0 .. rc_gather_variants()-1, -1 = the default; the autotuner picks among the same
+ * shapes) and the pending-pair lists, with a sink that records photon ids where the
+ * render evaluates merges.  rc_kd_query is this call with variant -1. */
+int rc_gather_query(int variant, int n, const float* positions, int q, const float* queries, float r2,
+                    int* counts, int* idx, long long cap, long long* total);
+int rc_gather_variants(void);
 
 /* The GPU-built tree in the reference's node format (8-byte KDTreeNode, heap order,
  * root at 1, src/KD_Tree.h:13-32) for n photon positions; returns the node count in

@@ -45,6 +45,10 @@ def lib() -> C.CDLL:
     L.rc_trace_rays_full.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
     L.rc_kd_query.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
                               C.c_longlong, C.POINTER(C.c_longlong)]
+    L.rc_gather_query.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_void_p,
+                                  C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
+    L.rc_gather_variants.argtypes = []
+    L.rc_camera_queries.argtypes = [C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_kd_build_nodes.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_render_timed.argtypes = [C.c_int, C.c_void_p]
     L.rc_kd_build_noalloc.argtypes = [C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p,
@@ -77,4 +81,5 @@ EXPORTS = ["init", "main", "rc_default_config", "rc_set_config", "rc_prepare", "
            "rc_kd_build_nodes", "rc_light_photons", "rc_render_timed", "rc_kd_build_noalloc",
            "rc_kd_noalloc_last_error", "rc_proposal_state", "rc_render_debug",
            "rc_save_state", "rc_load_state", "rc_scene_dump", "rc_prepare_stats",
-           "rc_context_create", "rc_context_bind", "rc_context_destroy"]
+           "rc_context_create", "rc_context_bind", "rc_context_destroy", "rc_gather_query",
+           "rc_gather_variants", "rc_camera_queries"]

@@ -1,22 +1,38 @@
 // Radius gather at the camera vertices (Path_Vertices::get_contrib,
 // src/Path_Vertices.h:46-68, over KD_Tree::find_closest_in_radius,
-// src/KD_Tree.cpp:217-280), one merge query per warp.
+// src/KD_Tree.cpp:217-280).
 //
-// Queries are first ordered by the KD cell they fall in (launch_query_order), so the
-// queries a warp processes one after another touch the same nodes and photons (L1/L2
-// reuse).  For each query the warp runs the reference's descent uniformly (near side
-// first; far side and an odd node's median photon only when (q[axis] - split)^2 < r^2)
-// and, at a node of at most kBucket photons, tests the whole contiguous tree-order range
-// at once, one photon per lane, with the reference's acceptance predicate
-// ((dx*dx + dy*dy) + dz*dz) < r^2 in FP32 without contraction.  Accepted photons are
-// compacted in shared memory and their MIS-weighted BSDF contributions are evaluated
-// lane-parallel, then summed across the warp.
+// The photons the reference's query returns for a camera vertex q are exactly
+// { p : ((dx*dx + dy*dy) + dz*dz) < r^2 } in FP32 without contraction: its descent
+// prunes a side only when (q[axis] - split)^2 >= r^2, and every photon beyond that
+// plane has a squared distance at least as large (rounding is monotonic), so pruning
+// never drops a photon the predicate accepts.  The set does not depend on the tree's
+// shape, so the gather may walk the photons in any order, as long as it skips only
+// boxes that provably hold no accepted photon and tests every other photon with the
+// reference's predicate.
 //
-// The set of photons a query accepts is exactly the reference's: the descent is the
-// reference's own, a bucket is tested exhaustively, and pruning never drops a photon
-// inside the radius (rounding is monotonic, so |q - p|^2 >= (q[axis] - split)^2 holds in
-// floats too).  Accumulation order differs from the reference's recursion, so
-// contributions agree to FP32 rounding.
+// Layout (launch_kd_boxes).  The photons in tree order are cut into 2^Lc chunks, Lc
+// being the shallowest level whose nodes hold at most 31 photons: chunk i is node
+// (2^Lc + i)'s contiguous range plus the gap before the next chunk's range, which holds
+// at most one inner node's median photon (that of the two nodes' lowest common
+// ancestor), so a chunk holds at most 32 photons.  Each chunk has its photons' bounding
+// box, with its first position and count in the spare .w words; every node above has
+// the union of its children's boxes.
+//
+// Work split (k_gather).  Queries are sorted by Morton code (launch_query_order) and a
+// warp owns G consecutive ones (a group), one per lane.  The warp descends the box hierarchy
+// once for the whole group, E levels per step (lane j tests descendant j's box against
+// the group's bounding box grown by the radius), down to the candidate chunks.  At a
+// chunk each lane tests its own query's sphere against the chunk box (a ballot names the
+// overlapping queries), each lane loads one of the chunk's photons, and for every
+// overlapping query the warp tests all of the chunk's photons at once: a query x photon
+// cross product, one photon per lane, the query broadcast from shared memory.  Accepted
+// (query slot, photon) pairs collect in a per-warp pending list, and every 32 of them
+// go to the sink with all lanes busy.  The render's sink evaluates the merges (the
+// camera vertex's BSDF at the photon's direction, MIS weight, photon throughput) from
+// per-query BSDF state staged in shared memory when the group starts, sums them per
+// query in shared memory, and adds each query's sum into its FP64 pixel once.  The
+// parity hook's sink records photon ids instead; both are the same kernel template.
 #include "vm.cuh"
 #include "bsdf.cuh"
 
@@ -25,474 +41,443 @@ namespace rc {
 namespace {
 
 constexpr int kWarpsPerBlock = 8;
-constexpr int kStack = 64;
-constexpr int kQueriesPerWarp = 16;
-constexpr int kBucket = 32;   // photons tested per bucket (kBucket / 32 per lane)
+constexpr long long kChunkNode = 31;   // photons per chunk-level node (the chunk adds at most one median)
+// DFS stack of subtree roots per warp.  Lc <= 24 for n < 2^28 photons, so a path from
+// the root crosses at most ceil(24 / E) expansion steps, the last of which reaches the
+// chunks (processed at once, never pushed): at most 4 x 31 + 1 = 125 (E = 5) or
+// 5 x 15 + 1 = 76 (E = 4) pending roots.
+constexpr int kRootStack = 128;
+constexpr unsigned kFull = 0xffffffffu;
 
-struct KdNav {
-    const uint2* __restrict__ nodes;
-    const float* __restrict__ x;
-    const float* __restrict__ y;
-    const float* __restrict__ z;
-    const uint32_t* __restrict__ id;
-    const float4* __restrict__ box_lo;   // per node down to the bucket level (nullptr: none)
-    const float4* __restrict__ box_hi;
-    int box_levels;                      // boxes exist for levels [0, box_levels)
-    long long n;
+struct ChunkTree {
+    const float4* __restrict__ lo;    // node boxes, heap order, levels [0, lc]; chunk level: .w = first position
+    const float4* __restrict__ hi;    //                                          chunk level: .w = photon count
+    const float4* __restrict__ pos;   // photon positions in tree order (TreePhotons::t0)
+    int lc;                           // chunk level (-1: no photons)
 };
 
-// Squared distance from q to a box, formed like the acceptance test so that it never
+// Squared distance from q to a box, formed like the acceptance test, so that it never
 // exceeds the squared distance to any photon inside the box (rounding is monotonic).
 __device__ __forceinline__ bool box_outside(F3 q, float4 lo, float4 hi, float r2) {
-    float dx = q.x < lo.x ? lo.x - q.x : (q.x > hi.x ? q.x - hi.x : 0.0f);
-    float dy = q.y < lo.y ? lo.y - q.y : (q.y > hi.y ? q.y - hi.y : 0.0f);
-    float dz = q.z < lo.z ? lo.z - q.z : (q.z > hi.z ? q.z - hi.z : 0.0f);
+    const float dx = q.x < lo.x ? lo.x - q.x : (q.x > hi.x ? q.x - hi.x : 0.0f);
+    const float dy = q.y < lo.y ? lo.y - q.y : (q.y > hi.y ? q.y - hi.y : 0.0f);
+    const float dz = q.z < lo.z ? lo.z - q.z : (q.z > hi.z ? q.z - hi.z : 0.0f);
     return !(dx * dx + dy * dy + dz * dz < r2);
 }
 
+// The same bound between two boxes: never more than the squared distance from any
+// point of the first (a query of the group) to any point of the second (a photon).
+__device__ __forceinline__ bool gap_outside(float4 glo, float4 ghi, float4 lo, float4 hi, float r2) {
+    const float dx = lo.x > ghi.x ? lo.x - ghi.x : (glo.x > hi.x ? glo.x - hi.x : 0.0f);
+    const float dy = lo.y > ghi.y ? lo.y - ghi.y : (glo.y > hi.y ? glo.y - hi.y : 0.0f);
+    const float dz = lo.z > ghi.z ? lo.z - ghi.z : (glo.z > hi.z ? glo.z - hi.z : 0.0f);
+    return !(dx * dx + dy * dy + dz * dz < r2);
+}
+
+// Bounding box of the queries of the lanes with `in` set (all lanes call it).
+__device__ __forceinline__ void warp_box(bool in, F3 q, float4& lo, float4& hi) {
+    float lx = in ? q.x : INFINITY, ly = in ? q.y : INFINITY, lz = in ? q.z : INFINITY;
+    float hx = in ? q.x : -INFINITY, hy = in ? q.y : -INFINITY, hz = in ? q.z : -INFINITY;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o)); ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+        lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o)); hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+        hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o)); hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
+    }
+    lo = make_float4(lx, ly, lz, 0.0f);
+    hi = make_float4(hx, hy, hz, 0.0f);
+}
+
+// Lane holding the largest value (the lowest such lane on ties).
+__device__ __forceinline__ int warp_argmax(float v) {
+    int at = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oa = __shfl_xor_sync(0xffffffffu, at, o);
+        if (ov > v || (ov == v && oa < at)) { v = ov; at = oa; }
+    }
+    return at;
+}
+
+// Surface of a box grown by `g` on every side (a proxy for how many chunk boxes it meets).
+__device__ __forceinline__ float box_surface(float4 lo, float4 hi, float g) {
+    const float ex = hi.x - lo.x + 2.0f * g, ey = hi.y - lo.y + 2.0f * g, ez = hi.z - lo.z + 2.0f * g;
+    return ex * ey + ey * ez + ex * ez;
+}
+
+// The reference's acceptance test (src/KD_Tree.cpp:217-280): ((dx*dx + dy*dy) + dz*dz) < r2.
 __device__ __forceinline__ bool in_radius(F3 q, float px, float py, float pz, float r2) {
-    float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+    const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
     return dx * dx + dy * dy + dz * dz < r2;
 }
 
-// Warp-uniform traversal; fn(tree position) runs on each lane for each photon its
-// query accepts.  `stack` is this warp's shared-memory stack (kStack (e, start) pairs).
-struct VisitCounts { unsigned nodes, buckets, tests; };
+// Camera-vertex state a merge evaluation needs, staged once per query.  29 words: an
+// odd stride, so lanes reading different queries' fields hit different banks.
+struct QState {
+    int kind;
+    float R[3], ior, a2, s;
+    float fx[3], fy[3], fz[3];   // shading frame
+    float wo[3];                 // local direction towards the previous camera vertex
+    float ng[3];
+    float wo_ng, fwo, dvm;       // dot(to_world(wo), Ng), plastic Fresnel at wo, camera dVM
+    float tp[3];                 // camera throughput x VM normalisation
+    float pad;
+};
+static_assert(sizeof(QState) == 29 * 4, "QState must keep an odd word stride");
 
-// Hand the first 32 pending entries to `flush` once there are 32 or more, and move the
-// rest (at most 31) to the front, so that every flush but a warp's last is a full one.
-template <class Flush>
-__device__ __forceinline__ void drain32(uint32_t* pend, int& np, Flush& flush) {
-    if (np < 32) return;
-    flush(32, pend);
-    __syncwarp();
-    const int lane = threadIdx.x & 31, rest = np - 32;
-    const uint32_t v = lane < rest ? pend[32 + lane] : 0u;
-    __syncwarp();
-    if (lane < rest) pend[lane] = v;
-    np = rest;
-    __syncwarp();
-}
+template <bool Eval> struct GroupExtra {};
+template <> struct GroupExtra<true> {
+    QState qs[32];
+    float acc[32][3];            // per-query merge sums (word stride 3: conflict-free)
+};
 
-// One query per warp.  The traversal is the reference's descent for that single query
-// (uniform across the warp): near side first, far side and an odd node's median photon
-// only when (q[axis] - split)^2 < r^2.  The stack lives in registers spread over the
-// lanes (entry k in lane k % 32 of register pair k / 32); push and pop are uniform.
-// A node of at most kBucket photons is a bucket, tested kBucket/32 photons per lane.
-// Accepted tree positions are appended to the warp's pending list in shared memory;
-// `flush(count, list)` runs on all lanes whenever the list holds 32 or more entries
-// and once at the end, so the per-photon work is spread over the lanes.
-template <class Flush>
-__device__ __forceinline__ void kd_query_warp(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend,
-                                              int& np, uint32_t tag, VisitCounts& vc, Flush&& flush) {
-    const int lane = threadIdx.x & 31;
-    if (t.n <= 0) return;
-    uint32_t se0 = 0, ss0 = 0, se1 = 0, ss1 = 0;   // stack entries lane and lane+32
-    if (lane == 0) { se0 = start_node.x; ss0 = start_node.y; }
-    {
-        const int l0 = 31 - __clz(start_node.x);
-        if (l0 < t.box_levels && box_outside(q, __ldg(&t.box_lo[start_node.x]), __ldg(&t.box_hi[start_node.x]), r2))
-            return;
-    }
-    int sp = 1;
-    const uint32_t n32 = (uint32_t)t.n;   // photon counts stay below 2^28 (28-bit index field)
-    while (sp) {
-        --sp;
-        uint32_t e, start;
-        if (sp < 32) { e = __shfl_sync(0xffffffffu, se0, sp); start = __shfl_sync(0xffffffffu, ss0, sp); }
-        else { e = __shfl_sync(0xffffffffu, se1, sp - 32); start = __shfl_sync(0xffffffffu, ss1, sp - 32); }
-        const int level = 31 - __clz(e);
-        const uint32_t c = n32 >> level;
-        if (c <= (uint32_t)kBucket) {
-            if (level < t.box_levels && box_outside(q, __ldg(&t.box_lo[e]), __ldg(&t.box_hi[e]), r2)) continue;
-            vc.buckets++;
-            vc.tests += c;
-#pragma unroll
-            for (int k = 0; k < kBucket / 32; ++k) {
-                const uint32_t i = (uint32_t)(k * 32 + lane);
-                bool acc = false;
-                if (i < c) {
-                    const uint32_t p = start + i;
-                    acc = in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2);
-                }
-                const unsigned m = __ballot_sync(0xffffffffu, acc);
-                if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = (start + i) | tag;
-                np += __popc(m);
-                __syncwarp();
-                drain32(pend, np, flush);
-            }
-            continue;
-        }
-        vc.nodes++;
-        const uint2 nd = __ldg(&t.nodes[e]);
-        const uint32_t ax = nd.x & 0x60000000u;
-        const float split = __uint_as_float(nd.y);
-        const float qa = ax == 0 ? q.x : (ax == 0x20000000u ? q.y : q.z);
-        const float d = qa - split;
-        const uint32_t half = c >> 1, odd = c & 1u;
-        const bool left_near = d < 0;
-        const bool within = d * d < r2;
-        if (odd && within) {
-            const uint32_t p = start + half;
-            const bool a = in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2);
-            if (a && lane == 0) pend[np] = p | tag;
-            np += a ? 1 : 0;
-            __syncwarp();
-            drain32(pend, np, flush);
-        }
-        const uint32_t le = 2u * e, ls = start;
-        const uint32_t re = 2u * e + 1u, rs = start + half + odd;
-        // far side first (when within), then the near side, which is popped next
-        if (within && sp < kStack) {
-            const uint32_t fe = left_near ? re : le, fs = left_near ? rs : ls;
-            if ((sp & 31) == lane) { if (sp < 32) { se0 = fe; ss0 = fs; } else { se1 = fe; ss1 = fs; } }
-            ++sp;
-        }
-        if (sp < kStack) {
-            const uint32_t ne = left_near ? le : re, ns = left_near ? ls : rs;
-            if ((sp & 31) == lane) { if (sp < 32) { se0 = ne; ss0 = ns; } else { se1 = ne; ss1 = ns; } }
-            ++sp;
-        }
-    }
-    __syncwarp();
-}
+template <bool Eval> struct WarpSmem {
+    float4 qp[32];               // query positions (broadcast in the cross product)
+    uint32_t qidx[32];           // query indices of the group's slots
+    uint32_t pend_pos[64];       // accepted pairs: tree position ...
+    uint8_t pend_slot[64];       // ... and query slot
+    uint32_t stk[kRootStack];
+    GroupExtra<Eval> g;
+};
 
-// Lane-parallel variant of the same query, used when node boxes exist down to the bucket
-// level Lb (every node at level Lb holds n >> Lb <= kBucket photons).  A subtree root at
-// level L < Lb is expanded k = min(E, Lb - L) levels at once (E = 4 or 5, a launch-shape
-// parameter): lane j box-tests the j-th descendant at level L + k and survivors are
-// pushed as new roots, while lanes test the median photons of the 2^k - 1 inner nodes in
-// between (odd counts only).  Roots at
-// level >= Lb are scanned like buckets.  The accepted set is the reference's: every
-// photon of the start node's range lies in a bucket or is an inner node's median; a
-// culled box holds no photon within the radius (box distance <= photon distance under
-// monotonic rounding), a median outside its node's split slab fails the predicate
-// (its distance >= |q[axis] - split|), and every photon that is tested is tested with
-// the reference's predicate.  DFS over roots keeps at most 2^E - 1 pending roots per
-// expansion level: with n < 2^28 (Lb <= 27) at most 6 x 31 + 1 = 187 (E = 5) or
-// 7 x 15 + 1 = 106 (E = 4) < kRootStack.  (On the 1920x1080 water pool 4 levels per
-// step beat 5; 3 lost to both: 6.9 / 7.1 / 8.2 ms per gather.)
-constexpr int kRootStack = 256;
+// The render's sink: merge evaluation (Path_Vertices::get_contrib, src/Path_Vertices.h:46-68)
+// and FP64 pixel accumulation.
+struct EvalSink {
+    static constexpr bool kEval = true;
+    VMParams P;
+    QueryBuf qb;
+    TreePhotons tp;
+    const uint32_t* tree_id;
+    double* accum;
 
-template <int E, class Flush>
-__device__ __forceinline__ void kd_query_expand(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend,
-                                                uint2* stk, int& np, uint32_t tag, VisitCounts& vc, Flush&& flush) {
-    const int lane = threadIdx.x & 31;
-    if (t.n <= 0) return;
-    const uint32_t n32 = (uint32_t)t.n;
-    const int Lb = t.box_levels - 1;
-    {
-        const int l0 = 31 - __clz(start_node.x);
-        if (l0 <= Lb && box_outside(q, __ldg(&t.box_lo[start_node.x]), __ldg(&t.box_hi[start_node.x]), r2)) return;
-    }
-    auto append = [&](bool acc, uint32_t p) {
-        const unsigned m = __ballot_sync(0xffffffffu, acc);
-        if (acc) pend[np + __popc(m & ((1u << lane) - 1u))] = p | tag;
-        np += __popc(m);
-        __syncwarp();
-        drain32(pend, np, flush);
-    };
-    if (lane == 0) stk[0] = start_node;
-    __syncwarp();
-    int sp = 1;
-    while (sp) {
-        --sp;
-        const uint2 rt = stk[sp];
-        __syncwarp();
-        const uint32_t e = rt.x, start = rt.y;
-        const int L = 31 - __clz(e);
-        if (L >= Lb) {
-            const uint32_t c = n32 >> L;
-            vc.buckets++;
-            vc.tests += c;
-#pragma unroll
-            for (int k = 0; k < kBucket / 32; ++k) {
-                const uint32_t i = (uint32_t)(k * 32 + lane);
-                bool acc = false;
-                if (i < c) acc = in_radius(q, __ldg(&t.x[start + i]), __ldg(&t.y[start + i]), __ldg(&t.z[start + i]), r2);
-                append(acc, start + i);
-            }
-            continue;
-        }
-        const int k = (Lb - L) < E ? (Lb - L) : E;
-        const uint32_t m = 1u << k;
-        vc.nodes += m - 1;
-        {
-            // median photons of the inner nodes at levels L .. L+k-1 (1-based BFS index)
-            bool acc = false;
-            uint32_t p = 0;
-            if ((uint32_t)lane < m - 1) {
-                const uint32_t i1 = (uint32_t)lane + 1u;
-                const int li = 31 - __clz(i1);
-                const uint32_t pi = i1 - (1u << li);
-                const uint32_t c = n32 >> (L + li);
-                if (c & 1u) {
-                    uint32_t st = start;
-                    for (int b = 0; b < li; ++b) {
-                        const uint32_t cl = n32 >> (L + b);
-                        if ((pi >> (li - 1 - b)) & 1u) st += (cl >> 1) + (cl & 1u);
-                    }
-                    p = st + (c >> 1);
-                    acc = in_radius(q, __ldg(&t.x[p]), __ldg(&t.y[p]), __ldg(&t.z[p]), r2);
-                }
-            }
-            append(acc, p);
-        }
-        {
-            // the 2^k descendants at level L + k: box test, survivors become roots
-            bool keep = false;
-            uint32_t st = start;
-            const uint32_t ce = (e << k) + (uint32_t)lane;
-            if ((uint32_t)lane < m) {
-                for (int b = 0; b < k; ++b) {
-                    const uint32_t cl = n32 >> (L + b);
-                    if (((uint32_t)lane >> (k - 1 - b)) & 1u) st += (cl >> 1) + (cl & 1u);
-                }
-                keep = !box_outside(q, __ldg(&t.box_lo[ce]), __ldg(&t.box_hi[ce]), r2);
-            }
-            const unsigned bm = __ballot_sync(0xffffffffu, keep);
-            if (keep) stk[sp + __popc(bm & ((1u << lane) - 1u))] = make_uint2(ce, st);
-            sp += __popc(bm);
-            __syncwarp();
-        }
-    }
-    __syncwarp();
-}
-
-// Accepted tree positions go to the warp's pending list `pend` (count `np`, uniform,
-// carried across the queries of a warp) with `tag` in their top bits; the list is
-// handed to `flush` whenever it holds 32 or more entries.  The caller flushes the rest.
-template <int E = 5, class Flush>
-__device__ __forceinline__ void kd_query(const KdNav& t, F3 q, float r2, uint2 start_node, uint32_t* pend, uint2* stk,
-                                         int& np, uint32_t tag, VisitCounts& vc, Flush&& flush) {
-    if (t.box_levels > 0) kd_query_expand<E>(t, q, r2, start_node, pend, stk, np, tag, vc, flush);
-    else kd_query_warp(t, q, r2, start_node, pend, np, tag, vc, flush);
-}
-
-// Traversal half of the gather.  MinBlocks (resident blocks per SM the register
-// allocation must allow) and QPW (consecutive sorted queries per warp) are the autotuned
-// shape parameters.  The warp's queries share the pending list (entry = query slot << 28
-// | tree position); every 32 accepted photons become 32 pairs (query index, position) in
-// the merge buffer, in query order.
-template <int MinBlocks, int QPW, int E>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks) k_gather(const VMParams P, const KdNav t,
-                                                                         QueryBuf qb,
-                                                                         const uint32_t* __restrict__ order,
-                                                                         const uint2* __restrict__ start_nodes,
-                                                                         long long nq, MergeBuf mb,
-                                                                         unsigned long long* __restrict__ counters,
-                                                                         const unsigned long long* __restrict__ nq_dev,
-                                                                         const int* __restrict__ skip) {
-    static_assert(QPW <= 16, "a pending entry keeps its query slot in its top 4 bits");
-    // device-side count (bounded by the capacity nq) and an iteration-wide skip flag,
-    // for iterations enqueued without a host round trip
-    if (skip && *skip) return;
-    if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
-    __shared__ uint32_t pend[kWarpsPerBlock][64];
-    __shared__ uint2 stk[kWarpsPerBlock][kRootStack];
-    __shared__ uint32_t qidx[kWarpsPerBlock][QPW];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long w = blockIdx.x * (long long)kWarpsPerBlock + warp;
-    const long long first = w * QPW;
-    if (first >= nq) return;
-    const int nslots = (int)((first + QPW < nq ? first + QPW : nq) - first);
-    VisitCounts vc{0u, 0u, 0u};
-    unsigned accepted = 0;
-    auto flush = [&](int n, const uint32_t* list) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(mb.count, (unsigned long long)n);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        for (int j = lane; j < n; j += 32) {
-            const unsigned long long at = base + (unsigned long long)j;
-            const uint32_t entry = list[j];
-            if (at < (unsigned long long)mb.cap) mb.pairs[at] = make_uint2(qidx[warp][entry >> 28], entry & 0x0fffffffu);
-        }
-        accepted += (unsigned)n;
-    };
-    int np = 0;
-    for (int k = 0; k < nslots; ++k) {
-        const uint32_t qi = __ldg(&order[first + k]);
-        if (lane == 0) qidx[warp][k] = qi;
-        const uint2 sn = __ldg(&start_nodes[qi]);
-        const float4 a = qb.q0[qi];
-        __syncwarp();
-        kd_query<E>(t, xyz(a), P.radius_sqr, sn, pend[warp], stk[warp], np, (uint32_t)k << 28, vc, flush);
-    }
-    if (np > 0) flush(np, pend[warp]);
-    if (counters && lane == 0) {
-        atomicAdd(&counters[0], (unsigned long long)accepted);
-        atomicAdd(&counters[1], (unsigned long long)vc.tests);
-        atomicAdd(&counters[2], (unsigned long long)vc.buckets);
-        atomicAdd(&counters[3], (unsigned long long)vc.nodes);
-    }
-}
-
-// Merge half of the gather (Path_Vertices::get_contrib, src/Path_Vertices.h:46-68): per
-// pair, the camera vertex's BSDF at the photon's direction, the MIS weight
-// 1 / (1 + dVM_cam pdf_rev + dVM_light pdf_fwd), times the photon throughput.  A
-// warp's pairs come in runs of one query (each traversal flush writes its pairs in query
-// order), so a segmented scan over the lanes sums each run and its last lane adds the
-// run, times the camera throughput, to the pixel's FP64 sum.
-constexpr int kMergeThreads = 256;
-__global__ void __launch_bounds__(kMergeThreads) k_merge(const VMParams P, TreePhotons tp, QueryBuf qb,
-                                                         const uint32_t* __restrict__ tree_id, MergeBuf mb,
-                                                         double* __restrict__ accum, const int* __restrict__ skip) {
-    if (skip && *skip) return;
-    const unsigned long long n = *mb.count;
-    if (n > (unsigned long long)mb.cap) {
-        if (mb.overflow && blockIdx.x == 0 && threadIdx.x == 0) *mb.overflow = 1;
-        return;
-    }
-    const int lane = threadIdx.x & 31;
-    const unsigned long long stride = (unsigned long long)gridDim.x * kMergeThreads;
-    // whole warps step together (the scan below needs every lane)
-    for (unsigned long long i0 = (unsigned long long)blockIdx.x * kMergeThreads + (threadIdx.x & ~31u); i0 < n;
-         i0 += stride) {
-        const unsigned long long i = i0 + (unsigned long long)lane;
-        const bool valid = i < n;
-        const uint2 pr = valid ? mb.pairs[i] : make_uint2(0xffffffffu, 0u);
-        const uint32_t qi = pr.x;
-        F3 cpair = f3(0.0f);
-        if (valid) {
-            const uint32_t p = pr.y;
-            const float4 a = qb.q0[qi], b = qb.q1[qi], c = qb.q2[qi], e = qb.q4[qi];
-            const F3 ng = xyz(c);
-            Bsdf bs;
+    __device__ __forceinline__ void setup(WarpSmem<true>& sm, int lane, bool active, uint32_t qi) const {
+        if (active) {
+            const float dvm = qb.q0[qi].w;
+            const float4 b = qb.q1[qi], c = qb.q2[qi], e = qb.q4[qi], g = qb.q3[qi];
             const DevMaterial& qm = P.materials[__float_as_int(b.w)];
             const int channel = __float_as_int(e.w);   // the camera path's dispersion channel
+            Bsdf bs;
             bs.init(qm, xyz(b), xyz(e), true, (qm.disp > 0.0f && channel >= 0) ? (float)(channel - 1) * qm.disp : 0.0f);
-            const float wo_ng = dot(bs.fr.to_world(bs.wo), ng);
-            const float fwo = (bs.kind == BSDF_K_PLASTIC_GGX || bs.kind == BSDF_K_PLASTIC_SMOOTH)
-                                  ? fresnel_reflectance(fabsf(bs.wo.z), bs.s) : 0.0f;
+            QState& st = sm.g.qs[lane];
+            st.kind = bs.kind;
+            st.R[0] = bs.R.x; st.R[1] = bs.R.y; st.R[2] = bs.R.z;
+            st.ior = bs.ior; st.a2 = bs.a2; st.s = bs.s;
+            st.fx[0] = bs.fr.x.x; st.fx[1] = bs.fr.x.y; st.fx[2] = bs.fr.x.z;
+            st.fy[0] = bs.fr.y.x; st.fy[1] = bs.fr.y.y; st.fy[2] = bs.fr.y.z;
+            st.fz[0] = bs.fr.z.x; st.fz[1] = bs.fr.z.y; st.fz[2] = bs.fr.z.z;
+            st.wo[0] = bs.wo.x; st.wo[1] = bs.wo.y; st.wo[2] = bs.wo.z;
+            st.ng[0] = c.x; st.ng[1] = c.y; st.ng[2] = c.z;
+            st.wo_ng = dot(bs.fr.to_world(bs.wo), xyz(c));
+            st.fwo = (bs.kind == BSDF_K_PLASTIC_GGX || bs.kind == BSDF_K_PLASTIC_SMOOTH)
+                         ? fresnel_reflectance(fabsf(bs.wo.z), bs.s) : 0.0f;
+            st.dvm = dvm;
+            st.tp[0] = g.x; st.tp[1] = g.y; st.tp[2] = g.z;
+        }
+        sm.g.acc[lane][0] = 0.0f; sm.g.acc[lane][1] = 0.0f; sm.g.acc[lane][2] = 0.0f;
+    }
+
+    // Evaluate the first `count` pending pairs (lane j: pair j); sum each run of one
+    // query's pairs across the lanes and add it to that query's shared sum.
+    __device__ __forceinline__ void flush(WarpSmem<true>& sm, int lane, int count) const {
+        F3 c = f3(0.0f);
+        int s = -1;
+        if (lane < count) {
+            const uint32_t p = sm.pend_pos[lane];
+            s = sm.pend_slot[lane];
+            const QState& st = sm.g.qs[s];
+            Bsdf bs;
+            bs.kind = st.kind;
+            bs.R = f3(st.R[0], st.R[1], st.R[2]);
+            bs.ior = st.ior; bs.a2 = st.a2; bs.s = st.s; bs.cont = 0.0f;
+            bs.fr.x = f3(st.fx[0], st.fx[1], st.fx[2]);
+            bs.fr.y = f3(st.fy[0], st.fy[1], st.fy[2]);
+            bs.fr.z = f3(st.fz[0], st.fz[1], st.fz[2]);
+            bs.wo = f3(st.wo[0], st.wo[1], st.wo[2]);
+            bs.radiance = true;
             const float4 p0 = __ldg(&tp.t0[p]);
             const float4 p1 = __ldg(&tp.t1[p]);
             const float2 p2 = __ldg(&tp.t2[p]);
-            float fwd, rev;
             F3 ev;
-            bs.eval_pdf(xyz(p1), ng, wo_ng, fwo, ev, fwd, rev);
-            const float weight = 1.0f / (1.0f + a.w * rev + p0.w * fwd);
-            cpair = ev * f3(p1.w, p2.x, p2.y) * weight;
+            float fwd, rev;
+            bs.eval_pdf(xyz(p1), f3(st.ng[0], st.ng[1], st.ng[2]), st.wo_ng, st.fwo, ev, fwd, rev);
+            const float weight = 1.0f / (1.0f + st.dvm * rev + p0.w * fwd);
+            c = ev * f3(p1.w, p2.x, p2.y) * weight;
             if (P.path_contrib) {
                 // learned-proposal training signal: the squared luminance this merge adds
                 // to its pixel, summed per light path
-                const F3 img = xyz(qb.q3[qi]) * cpair;
+                const F3 img = f3(st.tp[0], st.tp[1], st.tp[2]) * c;
                 const float lum = (fabsf(img.x) + fabsf(img.y) + fabsf(img.z)) * (1.0f / 3.0f);
                 if (lum > 0.0f) atomicAdd(&P.path_contrib[__ldg(&P.photon_path[__ldg(&tree_id[p])])], lum * lum);
             }
         }
-        // runs of equal query index, numbered by their heads: a query's pairs may form two
-        // runs in one window (its warp's flushes need not be adjacent in the buffer), and
-        // the scan must not join them across another query's run
-        const uint32_t qprev = __shfl_up_sync(0xffffffffu, qi, 1);
-        const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || qprev != qi);
+        // runs of equal slot, numbered by their heads (one query can form two runs in a
+        // flush: its pairs from two chunks with another query's between them)
+        const int sprev = __shfl_up_sync(kFull, s, 1);
+        const unsigned heads = __ballot_sync(kFull, lane == 0 || sprev != s);
         const int run = __popc(heads & ((2u << lane) - 1u));
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const float x = __shfl_up_sync(0xffffffffu, cpair.x, o);
-            const float y = __shfl_up_sync(0xffffffffu, cpair.y, o);
-            const float z = __shfl_up_sync(0xffffffffu, cpair.z, o);
-            const int ro = __shfl_up_sync(0xffffffffu, run, o);
-            if (lane >= o && ro == run) { cpair.x += x; cpair.y += y; cpair.z += z; }
+            const float x = __shfl_up_sync(kFull, c.x, o);
+            const float y = __shfl_up_sync(kFull, c.y, o);
+            const float z = __shfl_up_sync(kFull, c.z, o);
+            const int ro = __shfl_up_sync(kFull, run, o);
+            if (lane >= o && ro == run) { c.x += x; c.y += y; c.z += z; }
         }
-        const uint32_t qnext = __shfl_down_sync(0xffffffffu, qi, 1);
-        if (valid && (lane == 31 || qnext != qi)) {   // last lane of its query's run
-            const F3 r = xyz(qb.q3[qi]) * cpair;
-            if (r.x != 0.0f || r.y != 0.0f || r.z != 0.0f) {
-                const long long pixel = __float_as_int(qb.q2[qi].w);
-                atomicAdd(&accum[3 * pixel + 0], (double)r.x);
-                atomicAdd(&accum[3 * pixel + 1], (double)r.y);
-                atomicAdd(&accum[3 * pixel + 2], (double)r.z);
+        const int snext = __shfl_down_sync(kFull, s, 1);
+        if (s >= 0 && (lane == 31 || snext != s) && !is_zero(c)) {
+            atomicAdd(&sm.g.acc[s][0], c.x);
+            atomicAdd(&sm.g.acc[s][1], c.y);
+            atomicAdd(&sm.g.acc[s][2], c.z);
+        }
+    }
+
+    __device__ __forceinline__ void finish(WarpSmem<true>& sm, int lane, bool active, uint32_t qi) const {
+        if (!active) return;
+        const QState& st = sm.g.qs[lane];
+        const F3 r = f3(st.tp[0], st.tp[1], st.tp[2]) * f3(sm.g.acc[lane][0], sm.g.acc[lane][1], sm.g.acc[lane][2]);
+        if (is_zero(r)) return;
+        const long long pixel = __float_as_int(qb.q2[qi].w);
+        atomicAdd(&accum[3 * pixel + 0], (double)r.x);
+        atomicAdd(&accum[3 * pixel + 1], (double)r.y);
+        atomicAdd(&accum[3 * pixel + 2], (double)r.z);
+    }
+};
+
+// The parity hook's sink: per query, the ids of the photons it accepts.  Without
+// `offsets` it counts (counts[] zeroed by the caller), with them it writes the ids at
+// offsets[q] + cursor[q]++ (cursor zeroed by the caller).
+struct SetSink {
+    static constexpr bool kEval = false;
+    const uint32_t* tree_id;
+    int* counts;
+    const long long* offsets;
+    int* cursor;
+    int* idx;
+
+    __device__ __forceinline__ void setup(WarpSmem<false>&, int, bool, uint32_t) const {}
+    __device__ __forceinline__ void flush(WarpSmem<false>& sm, int lane, int count) const {
+        if (lane >= count) return;
+        const uint32_t qi = sm.qidx[sm.pend_slot[lane]];
+        const uint32_t p = sm.pend_pos[lane];
+        if (!offsets) atomicAdd(&counts[qi], 1);
+        else idx[offsets[qi] + atomicAdd(&cursor[qi], 1)] = (int)__ldg(&tree_id[p]);
+    }
+    __device__ __forceinline__ void finish(WarpSmem<false>&, int, bool, uint32_t) const {}
+};
+
+// One group of G queries per warp.  MinBlocks (resident blocks per SM the register
+// allocation must allow), G and E (levels per expansion step) are the launch shape the
+// autotuner picks.  counters (optional, 4 u64 accumulated): accepted pairs, photon
+// tests (chunk photons x overlapping queries), chunks tested, boxes tested.
+template <int MinBlocks, int G, int E, class Sink>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, MinBlocks)
+    k_gather(const ChunkTree t, const float* __restrict__ qpos, int qstride, const uint32_t* __restrict__ order,
+             long long nq, const unsigned long long* __restrict__ nq_dev, const int* __restrict__ skip, float r2,
+             const Sink sink, unsigned long long* __restrict__ counters, int* __restrict__ err) {
+    static_assert(G == 16 || G == 32, "a group is a half or a whole warp of queries");
+    static_assert(E >= 1 && E <= 5, "an expansion step tests at most 32 descendants");
+    // device-side count (bounded by the capacity nq) and an iteration-wide skip flag,
+    // for iterations enqueued without a host round trip
+    if (skip && *skip) return;
+    if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
+    __shared__ WarpSmem<Sink::kEval> smem[kWarpsPerBlock];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long first = ((long long)blockIdx.x * kWarpsPerBlock + warp) * G;
+    if (first >= nq || t.lc < 0) return;
+    WarpSmem<Sink::kEval>& sm = smem[warp];
+    const int nslots = (int)min((long long)G, nq - first);
+    const bool active = lane < nslots;
+    const unsigned lt = (1u << lane) - 1u;
+    uint32_t qi = 0;
+    F3 q = f3(0.0f);
+    if (active) {
+        qi = __ldg(&order[first + lane]);
+        const float* qp = qpos + (long long)qstride * qi;
+        q = f3(qp[0], qp[1], qp[2]);
+        sm.qidx[lane] = qi;
+        sm.qp[lane] = make_float4(q.x, q.y, q.z, 0.0f);
+    }
+    sink.setup(sm, lane, active, qi);
+    __syncwarp();
+    // The group is traversed as one or more sub-groups (lane ranges [a, b) of the sorted
+    // queries, `in` = this lane's query belongs to the current one, glo/ghi its box).
+    bool in = false;
+    float4 glo, ghi;
+
+    int np = 0;
+    unsigned n_acc = 0, n_tests = 0, n_chunks = 0, n_boxes = 0;
+
+    // Append one chunk's accepted pairs: this lane's photon (tree position p) is accepted
+    // by the queries whose bits are set in `am`.  Pairs go in query by query (runs of one
+    // query), every 32 to the sink.
+    auto emit = [&](uint32_t am, uint32_t p) {
+        unsigned qa = __reduce_or_sync(kFull, am);
+        while (qa) {
+            const int s = __ffs(qa) - 1;
+            qa &= qa - 1u;
+            const bool acc = (am >> s) & 1u;
+            const unsigned m = __ballot_sync(kFull, acc);
+            if (acc) {
+                const int at = np + __popc(m & lt);
+                sm.pend_pos[at] = p;
+                sm.pend_slot[at] = (uint8_t)s;
+            }
+            np += __popc(m);
+            __syncwarp();
+            if (np >= 32) {
+                sink.flush(sm, lane, 32);
+                n_acc += 32;
+                __syncwarp();
+                const int rest = np - 32;
+                uint32_t vp = 0;
+                uint8_t vs = 0;
+                if (lane < rest) { vp = sm.pend_pos[32 + lane]; vs = sm.pend_slot[32 + lane]; }
+                __syncwarp();
+                if (lane < rest) { sm.pend_pos[lane] = vp; sm.pend_slot[lane] = vs; }
+                np = rest;
+                __syncwarp();
             }
         }
-    }
-}
+    };
 
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_kd_query(const KdNav t, int q, const float* __restrict__ qpos,
-                                                                   const uint32_t* __restrict__ order,
-                                                                   const uint2* __restrict__ start_nodes, float r2,
-                                                                   int* counts, const long long* offsets, int* idx) {
-    __shared__ uint32_t pend[kWarpsPerBlock][64];
-    __shared__ uint2 stk[kWarpsPerBlock][kRootStack];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long w = blockIdx.x * (long long)kWarpsPerBlock + warp;
-    const long long first = w * kQueriesPerWarp;
-    if (first >= q) return;
-    const long long last = first + kQueriesPerWarp < q ? first + kQueriesPerWarp : q;
-    VisitCounts vc{0u, 0u, 0u};
-    for (long long slot = first; slot < last; ++slot) {
-        const long long j = order[slot];
-        const F3 p = f3(qpos[3 * j], qpos[3 * j + 1], qpos[3 * j + 2]);
-        const long long off = offsets ? offsets[j] : 0;
-        int n = 0, np = 0;
-        auto flush = [&](int cnt, const uint32_t* list) {
-            if (idx)
-                for (int k = lane; k < cnt; k += 32) idx[off + n + k] = (int)__ldg(&t.id[list[k]]);
-            n += cnt;
-        };
-        kd_query(t, p, r2, start_nodes[j], pend[warp], stk[warp], np, 0u, vc, flush);
-        if (np > 0) flush(np, pend[warp]);
-        __syncwarp();
-        if (lane == 0) counts[j] = n;
-    }
-}
-
-// Query ordering: each query descends the tree's near sides to `level` (cells of
-// n >> level photons); a counting sort by cell puts neighbouring queries in the same
-// warp, which keeps the union of a warp's tree paths close to one query's path.
-// The same descent also finds where the reference's traversal for this query first
-// branches: the shallowest node on the near path with (q[axis] - split)^2 < r^2.  Above
-// it the traversal only follows near sides and tests no median photon, so starting
-// there visits exactly the same photons.  start_nodes[i] = (node, first position).
-__global__ void k_query_cells(const KdNav t, const float* __restrict__ qpos, int stride, long long nq,
-                              const unsigned long long* __restrict__ nq_dev, int level,
-                              float r2, uint32_t* __restrict__ keys, uint32_t* __restrict__ counts,
-                              uint2* __restrict__ start_nodes) {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
-    if (i >= nq) return;
-    F3 q = f3(qpos[stride * i], qpos[stride * i + 1], qpos[stride * i + 2]);
-    uint32_t e = 1;
-    long long st = 0, c = t.n;
-    uint2 start = make_uint2(0u, 0u);
-    bool found = false;
-    int l = 0;
-    for (; l < level || !found; ++l) {
-        if (c <= kBucket) {                       // reached a bucket without branching
-            if (!found) { start = make_uint2(e, (uint32_t)st); found = true; }
-            break;
+    // The candidate chunks of one expansion step: lane j holds chunk j's box (blo, bhi;
+    // .w = first position, count) and bm names the chunks that met the group box.  First
+    // each candidate's mask of the group's queries whose sphere meets its box (kept by
+    // lane j), then the photon tests chunk by chunk, the next chunk's photons loaded
+    // while the current one's are tested; the queries of a chunk are tested two at a
+    // time into a per-photon mask of accepting queries.
+    auto chunks = [&](unsigned bm, float4 blo, float4 bhi) {
+        uint32_t my_qm = 0;
+        while (bm) {
+            const int j = __ffs(bm) - 1;
+            bm &= bm - 1u;
+            const float4 lo = make_float4(__shfl_sync(kFull, blo.x, j), __shfl_sync(kFull, blo.y, j),
+                                          __shfl_sync(kFull, blo.z, j), 0.0f);
+            const float4 hi = make_float4(__shfl_sync(kFull, bhi.x, j), __shfl_sync(kFull, bhi.y, j),
+                                          __shfl_sync(kFull, bhi.z, j), 0.0f);
+            const unsigned qm = __ballot_sync(kFull, in && !box_outside(q, lo, hi, r2));
+            if (lane == j) my_qm = qm;
         }
-        uint2 nd = __ldg(&t.nodes[e]);
-        uint32_t ax = nd.x & 0x60000000u;
-        float split = __uint_as_float(nd.y);
-        float qa = ax == 0 ? q.x : (ax == 0x20000000u ? q.y : q.z);
-        float d = qa - split;
-        if (!found && d * d < r2) { start = make_uint2(e, (uint32_t)st); found = true; }
-        long long half = c >> 1, odd = c & 1;
-        if (d < 0) { e = 2 * e; }
-        else { e = 2 * e + 1; st += half + odd; }
-        c = half;
-        if (l + 1 >= level && found) { ++l; break; }
+        unsigned cm = __ballot_sync(kFull, my_qm != 0u);
+        if (!cm) return;
+        int j = __ffs(cm) - 1;
+        uint32_t start = __shfl_sync(kFull, __float_as_uint(blo.w), j);
+        uint32_t cnt = __shfl_sync(kFull, __float_as_uint(bhi.w), j);
+        float4 pp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if ((uint32_t)lane < cnt) pp = __ldg(&t.pos[start + lane]);
+        for (;;) {
+            const uint32_t qm = __shfl_sync(kFull, my_qm, j);
+            cm &= cm - 1u;
+            int jn = 0;
+            uint32_t sn = 0, cn = 0;
+            float4 pn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (cm) {
+                jn = __ffs(cm) - 1;
+                sn = __shfl_sync(kFull, __float_as_uint(blo.w), jn);
+                cn = __shfl_sync(kFull, __float_as_uint(bhi.w), jn);
+                if ((uint32_t)lane < cn) pn = __ldg(&t.pos[sn + lane]);
+            }
+            ++n_chunks;
+            n_tests += cnt * (unsigned)__popc(qm);
+            uint32_t am = 0, qq = qm;
+            while (qq) {
+                const int s0 = __ffs(qq) - 1;
+                qq &= qq - 1u;
+                const int s1 = qq ? __ffs(qq) - 1 : s0;
+                qq &= qq - 1u;
+                const float4 a = sm.qp[s0], b = sm.qp[s1];
+                if (in_radius(xyz(a), pp.x, pp.y, pp.z, r2)) am |= 1u << s0;
+                if (in_radius(xyz(b), pp.x, pp.y, pp.z, r2)) am |= 1u << s1;
+            }
+            if ((uint32_t)lane >= cnt) am = 0u;
+            emit(am, start + (uint32_t)lane);
+            if (!cm) break;
+            j = jn; start = sn; cnt = cn; pp = pn;
+        }
+    };
+
+    const int lc = t.lc;
+    const float4 rlo = __ldg(&t.lo[1]), rhi = __ldg(&t.hi[1]);
+    // Sub-groups.  Consecutive queries of the Morton order can straddle a jump of the
+    // curve, and a group holding two distant clusters would walk every chunk between
+    // them.  A range is therefore split at its largest gap between consecutive queries
+    // when the two parts' boxes, grown by 4 radii, have less than half the surface of the
+    // whole range's; the parts are traversed one after another.
+    const float grow = 4.0f * sqrtf(r2);
+    int a = 0;
+    while (a < nslots) {
+        int b = nslots;
+        warp_box(lane >= a && lane < b, q, glo, ghi);
+        while (b - a >= 4) {
+            const F3 qp = f3(__shfl_up_sync(kFull, q.x, 1), __shfl_up_sync(kFull, q.y, 1), __shfl_up_sync(kFull, q.z, 1));
+            const float gap = (lane > a && lane < b) ? length_sq(q - qp) : -1.0f;
+            const int c = warp_argmax(gap);
+            float4 llo, lhi, rlo2, rhi2;
+            warp_box(lane >= a && lane < c, q, llo, lhi);
+            warp_box(lane >= c && lane < b, q, rlo2, rhi2);
+            if (!(box_surface(llo, lhi, grow) + box_surface(rlo2, rhi2, grow) < 0.5f * box_surface(glo, ghi, grow)))
+                break;
+            b = c;
+            glo = llo;
+            ghi = lhi;
+        }
+        in = lane >= a && lane < b;
+        ++n_boxes;
+        if (!gap_outside(glo, ghi, rlo, rhi, r2)) {
+        if (lc == 0) {
+            chunks(1u, rlo, rhi);
+        } else {
+            if (lane == 0) sm.stk[0] = 1u;
+            __syncwarp();
+            int sp = 1;
+            while (sp > 0) {
+                --sp;
+                const uint32_t e = sm.stk[sp];
+                __syncwarp();
+                const int L = 31 - __clz(e);
+                const int k = (lc - L) < E ? (lc - L) : E;
+                const uint32_t m = 1u << k;
+                const uint32_t ce = (e << k) + (uint32_t)lane;
+                bool keep = false;
+                float4 blo = make_float4(0.0f, 0.0f, 0.0f, 0.0f), bhi = blo;
+                if ((uint32_t)lane < m) {
+                    blo = __ldg(&t.lo[ce]);
+                    bhi = __ldg(&t.hi[ce]);
+                    keep = !gap_outside(glo, ghi, blo, bhi, r2);
+                }
+                n_boxes += m;
+                const unsigned bm = __ballot_sync(kFull, keep);
+                if (L + k == lc) {
+                    chunks(bm, blo, bhi);
+                } else {
+                    const int add = __popc(bm);
+                    if (sp + add > kRootStack) {   // cannot happen (bound above); flagged, not silent
+                        if (lane == 0 && err) atomicOr(err, 1);
+                        break;
+                    }
+                    if (keep) sm.stk[sp + __popc(bm & lt)] = ce;
+                    sp += add;
+                    __syncwarp();
+                }
+            }
+        }
+        }
+        a = b;
     }
-    // cell key at `level` (continue the near descent if the start was found early)
-    uint32_t ek = e;
-    int lk = l;
-    long long ck = c;
-    while (lk < level) {
-        if (ck <= 1) break;
-        uint2 nd = __ldg(&t.nodes[ek]);
-        uint32_t ax = nd.x & 0x60000000u;
-        float split = __uint_as_float(nd.y);
-        float qa = ax == 0 ? q.x : (ax == 0x20000000u ? q.y : q.z);
-        ek = 2 * ek + ((qa - split) < 0 ? 0u : 1u);
-        ck >>= 1;
-        ++lk;
+    if (np > 0) {
+        __syncwarp();
+        sink.flush(sm, lane, np);
+        n_acc += (unsigned)np;
     }
-    while (lk < level) { ek = 2 * ek; ++lk; }
-    if (lk > level) ek >>= (lk - level);
-    uint32_t key = ek - (1u << level);
-    keys[i] = key;
-    start_nodes[i] = start;
-    atomicAdd(&counts[key], 1u);
+    __syncwarp();
+    sink.finish(sm, lane, active, qi);
+    if (counters && lane == 0) {
+        atomicAdd(&counters[0], (unsigned long long)n_acc);
+        atomicAdd(&counters[1], (unsigned long long)n_tests);
+        atomicAdd(&counters[2], (unsigned long long)n_chunks);
+        atomicAdd(&counters[3], (unsigned long long)n_boxes);
+    }
 }
 
 // Exclusive scan of m counters in one CTA of 1024 threads (m up to a few million).
@@ -509,7 +494,7 @@ __global__ void __launch_bounds__(1024) k_scan_counts(uint32_t* counts, long lon
         uint32_t incl = sum;
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            uint32_t y = __shfl_up_sync(kFull, incl, o);
             if (lane >= o) incl += y;
         }
         if (lane == 31) warp_sums[wid] = incl;
@@ -517,7 +502,7 @@ __global__ void __launch_bounds__(1024) k_scan_counts(uint32_t* counts, long lon
         if (wid == 0) {
             uint32_t w = warp_sums[lane], wi = w;
             for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+                uint32_t y = __shfl_up_sync(kFull, wi, o);
                 if (lane >= o) wi += y;
             }
             warp_sums[lane] = wi - w;
@@ -547,7 +532,7 @@ __global__ void __launch_bounds__(1024) k_scan_tile(uint32_t* counts, long long 
     uint32_t incl = sum;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        uint32_t y = __shfl_up_sync(kFull, incl, o);
         if (lane >= o) incl += y;
     }
     if (lane == 31) warp_sums[wid] = incl;
@@ -555,7 +540,7 @@ __global__ void __launch_bounds__(1024) k_scan_tile(uint32_t* counts, long long 
     if (wid == 0) {
         uint32_t w = warp_sums[lane], wi = w;
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            uint32_t y = __shfl_up_sync(kFull, wi, o);
             if (lane >= o) wi += y;
         }
         warp_sums[lane] = wi - w;
@@ -574,127 +559,288 @@ __global__ void k_scan_tile_add(uint32_t* counts, long long m, const uint32_t* _
     if (i < m) counts[i] += tile_offsets[i / kScanTile];
 }
 
-__global__ void k_scatter_queries(const uint32_t* __restrict__ keys, long long nq,
-                                  const unsigned long long* __restrict__ nq_dev, uint32_t* __restrict__ cursor,
-                                  uint32_t* __restrict__ order) {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+// Query order: a stable LSD radix sort of the queries' 30-bit Morton codes (10 bits per
+// axis over the queries' bounding box), three passes of 10-bit digits.  Consecutive
+// queries of the sorted order are then close in space whatever the photon density (an
+// order by KD cell is not: a cell of a sparsely lit region holds hundreds of queries).
+constexpr int kRsBits = 10, kRsBins = 1 << kRsBits, kRsThreads = 256, kRsWarps = kRsThreads / 32;
+constexpr int kRsPerWarp = 256;                        // keys a warp ranks per tile
+constexpr long long kRsTile = kRsWarps * kRsPerWarp;   // keys per block
+
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__device__ __forceinline__ uint32_t cell10(float v) {
+    return v > 0.0f ? (v < 1023.0f ? (uint32_t)v : 1023u) : 0u;   // NaN -> 0
+}
+
+__global__ void k_query_keys(const float* __restrict__ qpos, int stride, long long nq,
+                             const unsigned long long* __restrict__ nq_dev, QueryFrame f, uint32_t* __restrict__ keys,
+                             uint32_t* __restrict__ vals) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
     if (i >= nq) return;
-    uint32_t pos = atomicAdd(&cursor[keys[i]], 1u);
-    order[pos] = (uint32_t)i;
+    const float* q = qpos + (long long)stride * i;
+    const uint32_t cx = cell10((q[0] - f.lo[0]) * f.scale[0]);
+    const uint32_t cy = cell10((q[1] - f.lo[1]) * f.scale[1]);
+    const uint32_t cz = cell10((q[2] - f.lo[2]) * f.scale[2]);
+    keys[i] = spread10(cx) | (spread10(cy) << 1) | (spread10(cz) << 2);
+    vals[i] = (uint32_t)i;
 }
 
-// Node bounding boxes, bottom-up: a warp per node on the lowest boxed level reduces
-// its contiguous photon range; each upper node unites its children and its median.
-__global__ void k_leaf_boxes(const KdNav t, int level, float4* lo, float4* hi) {
+// Per-block digit counts, digit-major (hist[d * blocks + b]), so that one exclusive scan
+// of the whole array gives every (digit, block) its first output position.
+__global__ void __launch_bounds__(kRsThreads) k_rs_hist(const uint32_t* __restrict__ keys, long long nq,
+                                                        const unsigned long long* __restrict__ nq_dev, int shift,
+                                                        uint32_t* __restrict__ hist) {
+    __shared__ uint32_t cnt[kRsBins];
+    for (int d = threadIdx.x; d < kRsBins; d += kRsThreads) cnt[d] = 0;
+    __syncthreads();
+    if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
+    const long long base = (long long)blockIdx.x * kRsTile;
+    for (int k = threadIdx.x; k < kRsTile; k += kRsThreads) {
+        const long long i = base + k;
+        if (i < nq) atomicAdd(&cnt[(keys[i] >> shift) & (kRsBins - 1)], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRsBins; d += kRsThreads) hist[(long long)d * gridDim.x + blockIdx.x] = cnt[d];
+}
+
+// Stable scatter of one block's tile: warp w ranks the keys [w * 256, (w + 1) * 256) of
+// the tile in order (per-warp digit counts, a prefix over the warps per digit on top of
+// the block's scanned offsets, then ranks by __match_any_sync round by round).
+__global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t* __restrict__ keys_in,
+                                                           const uint32_t* __restrict__ vals_in,
+                                                           uint32_t* __restrict__ keys_out,
+                                                           uint32_t* __restrict__ vals_out, long long nq,
+                                                           const unsigned long long* __restrict__ nq_dev, int shift,
+                                                           const uint32_t* __restrict__ offsets) {
+    __shared__ uint32_t wc[kRsWarps][kRsBins];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int k = threadIdx.x; k < kRsWarps * kRsBins; k += kRsThreads) (&wc[0][0])[k] = 0;
+    __syncthreads();
+    if (nq_dev) nq = (long long)min(*nq_dev, (unsigned long long)nq);
+    const long long wbase = (long long)blockIdx.x * kRsTile + (long long)warp * kRsPerWarp;
+    for (int r = 0; r < kRsPerWarp / 32; ++r) {
+        const long long i = wbase + r * 32 + lane;
+        const bool valid = i < nq;
+        const uint32_t d = valid ? (keys_in[i] >> shift) & (kRsBins - 1) : 0xffffffffu;
+        const unsigned peers = __match_any_sync(kFull, d);
+        if (valid && (peers & lt) == 0u) wc[warp][d] += (uint32_t)__popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRsBins; d += kRsThreads) {
+        uint32_t run = offsets[(long long)d * gridDim.x + blockIdx.x];
+        for (int w = 0; w < kRsWarps; ++w) {
+            const uint32_t c = wc[w][d];
+            wc[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (int r = 0; r < kRsPerWarp / 32; ++r) {
+        const long long i = wbase + r * 32 + lane;
+        const bool valid = i < nq;
+        uint32_t key = 0, val = 0, d = 0xffffffffu;
+        if (valid) {
+            key = keys_in[i];
+            val = vals_in[i];
+            d = (key >> shift) & (kRsBins - 1);
+        }
+        const unsigned peers = __match_any_sync(kFull, d);
+        uint32_t pos = 0;
+        if (valid) pos = wc[warp][d] + (uint32_t)__popc(peers & lt);
+        __syncwarp();
+        if (valid) {
+            keys_out[pos] = key;
+            vals_out[pos] = val;
+            if ((peers & lt) == 0u) wc[warp][d] += (uint32_t)__popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
+// Chunk boxes: one warp per chunk reduces its (at most 32) photons' coordinates.
+__global__ void k_chunk_boxes(const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ z,
+                              long long n, int lc, float4* __restrict__ lo, float4* __restrict__ hi) {
     const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    const long long first = 1LL << level;
-    if (w >= first) return;
-    const long long e = first + w;
-    const long long c = t.n >> level;
-    const long long s = kd_node_start(e, level, t.n);
+    const long long m = 1LL << lc;
+    if (w >= m) return;
+    const long long e = m + w;
+    const long long s = kd_node_start(e, lc, n);
+    const long long end = (w + 1 < m) ? kd_node_start(e + 1, lc, n) : n;
+    const long long c = end - s;   // <= 32: the node's range plus at most one median
     float mnx = INFINITY, mny = INFINITY, mnz = INFINITY, mxx = -INFINITY, mxy = -INFINITY, mxz = -INFINITY;
-    for (long long i = lane; i < c; i += 32) {
-        float x = t.x[s + i], y = t.y[s + i], z = t.z[s + i];
-        mnx = fminf(mnx, x); mny = fminf(mny, y); mnz = fminf(mnz, z);
-        mxx = fmaxf(mxx, x); mxy = fmaxf(mxy, y); mxz = fmaxf(mxz, z);
+    if (lane < c) {
+        mnx = mxx = x[s + lane];
+        mny = mxy = y[s + lane];
+        mnz = mxz = z[s + lane];
     }
+#pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o)); mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
-        mnz = fminf(mnz, __shfl_xor_sync(0xffffffffu, mnz, o)); mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
-        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o)); mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
+        mnx = fminf(mnx, __shfl_xor_sync(kFull, mnx, o)); mny = fminf(mny, __shfl_xor_sync(kFull, mny, o));
+        mnz = fminf(mnz, __shfl_xor_sync(kFull, mnz, o)); mxx = fmaxf(mxx, __shfl_xor_sync(kFull, mxx, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(kFull, mxy, o)); mxz = fmaxf(mxz, __shfl_xor_sync(kFull, mxz, o));
     }
-    if (lane == 0) { lo[e] = make_float4(mnx, mny, mnz, 0.0f); hi[e] = make_float4(mxx, mxy, mxz, 0.0f); }
+    if (lane == 0) {
+        lo[e] = make_float4(mnx, mny, mnz, __uint_as_float((uint32_t)s));
+        hi[e] = make_float4(mxx, mxy, mxz, __uint_as_float((uint32_t)c));
+    }
 }
 
-__global__ void k_parent_boxes(const KdNav t, int level, float4* lo, float4* hi) {
+// Boxes of the nodes on one level: the union of their children's.
+__device__ __forceinline__ void unite_children(float4* lo, float4* hi, long long e) {
+    const float4 a = lo[2 * e], b = lo[2 * e + 1], c = hi[2 * e], d = hi[2 * e + 1];
+    lo[e] = make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
+    hi[e] = make_float4(fmaxf(c.x, d.x), fmaxf(c.y, d.y), fmaxf(c.z, d.z), 0.0f);
+}
+__global__ void k_level_boxes(int level, float4* lo, float4* hi) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long first = 1LL << level;
-    if (i >= first) return;
-    const long long e = first + i;
-    float4 a = lo[2 * e], b = lo[2 * e + 1], c = hi[2 * e], d = hi[2 * e + 1];
-    float4 l = make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
-    float4 h = make_float4(fmaxf(c.x, d.x), fmaxf(c.y, d.y), fmaxf(c.z, d.z), 0.0f);
-    const long long cnt = t.n >> level;
-    if (cnt & 1) {
-        const long long p = kd_node_start(e, level, t.n) + (cnt >> 1);
-        l.x = fminf(l.x, t.x[p]); l.y = fminf(l.y, t.y[p]); l.z = fminf(l.z, t.z[p]);
-        h.x = fmaxf(h.x, t.x[p]); h.y = fmaxf(h.y, t.y[p]); h.z = fmaxf(h.z, t.z[p]);
+    if (i < (1LL << level)) unite_children(lo, hi, (1LL << level) + i);
+}
+// levels [0, top] in one CTA, bottom-up
+constexpr int kTopLevels = 11;
+__global__ void __launch_bounds__(1024) k_top_boxes(int top, float4* lo, float4* hi) {
+    for (int l = top; l >= 0; --l) {
+        for (long long i = threadIdx.x; i < (1LL << l); i += blockDim.x) unite_children(lo, hi, (1LL << l) + i);
+        __syncthreads();
     }
-    lo[e] = l;
-    hi[e] = h;
 }
 
-// Photon records gathered into tree order, so the gather reads them contiguously.
+// Photon records gathered into tree order, so the gather reads them contiguously
+// (positions only when ph.dir is null).
 __global__ void k_tree_records(PhotonBuf ph, const uint32_t* __restrict__ id, long long n, TreePhotons tp) {
-    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (p >= n) return;
-    uint32_t i = id[p];
+    const uint32_t i = id[p];
     tp.t0[p] = ph.pos[i];
-    tp.t1[p] = ph.dir[i];
-    tp.t2[p] = ph.tp[i];
+    if (ph.dir) {
+        tp.t1[p] = ph.dir[i];
+        tp.t2[p] = ph.tp[i];
+    }
 }
 
-KdNav nav_of(const KdTree& tr) {
-    return KdNav{tr.nodes, tr.x, tr.y, tr.z, tr.id, tr.box_lo, tr.box_hi, tr.box_lo ? tr.box_levels : 0, tr.n};
+ChunkTree chunk_tree(const KdTree& tree, const float4* t0) {
+    return ChunkTree{tree.box_lo, tree.box_hi, t0, (tree.n > 0 && tree.box_lo) ? tree.box_levels - 1 : -1};
+}
+
+// Launch shapes: (resident blocks per SM, queries per group, levels per expansion step).
+struct Shape { int mb, g, e; };
+constexpr Shape kShapes[] = {{2, 32, 5}, {3, 32, 5}, {4, 32, 5}, {3, 32, 4}, {4, 32, 4}, {3, 16, 5}, {4, 16, 4}, {4, 16, 5}};
+constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
+constexpr int kDefaultShape = 1;
+
+template <int MB, int G, int E, class Sink>
+void launch_shape(const ChunkTree& t, const float* qpos, int qstride, const uint32_t* order, long long nq,
+                  const unsigned long long* nq_dev, const int* skip, float r2, const Sink& sink,
+                  unsigned long long* counters, int* err, cudaStream_t s) {
+    const long long warps = (nq + G - 1) / G;
+    k_gather<MB, G, E, Sink><<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
+        t, qpos, qstride, order, nq, nq_dev, skip, r2, sink, counters, err);
+}
+
+template <class Sink>
+void launch_variant(int v, const ChunkTree& t, const float* qpos, int qstride, const uint32_t* order, long long nq,
+                    const unsigned long long* nq_dev, const int* skip, float r2, const Sink& sink,
+                    unsigned long long* counters, int* err, cudaStream_t s) {
+    switch (v) {
+    case 0: launch_shape<2, 32, 5>(t, qpos, qstride, order, nq, nq_dev, skip, r2, sink, counters, err, s); break;
+    case 2: launch_shape<4, 32, 5>(t, qpos, qstride, order, nq, nq_dev, skip, r2, sink, counters, err, s); break;
+    case 3: launch_shape<3, 32, 4>(t, qpos, qstride, order, nq, nq_dev, skip, r2, sink, counters, err, s); break;
+    case 4: launch_shape<4, 32, 4>(t, qpos, qstride, order, nq, nq_dev, skip, r2, sink, counters, err, s); break;
+    case 5: launch_shape<3, 16, 5>(t, qpos, qstride, order, nq, nq_dev, skip, r2, sink, counters, err, s); break;
+    case 6: launch_shape<4, 16, 4>(t, qpos, qstride, order, nq, nq_dev, skip, r2, sink, counters, err, s); break;
+    case 7: launch_shape<4, 16, 5>(t, qpos, qstride, order, nq, nq_dev, skip, r2, sink, counters, err, s); break;
+    default: launch_shape<3, 32, 5>(t, qpos, qstride, order, nq, nq_dev, skip, r2, sink, counters, err, s); break;
+    }
 }
 
 }  // namespace
 
-int kd_box_levels(long long n) {
-    // boxes for every level whose nodes hold more than half a bucket: the bucket level
-    // (nodes of at most kBucket photons) and everything above it
-    if (n <= 0) return 0;
+int kd_chunk_level(long long n) {
+    if (n <= 0) return -1;
     int l = 0;
-    while ((n >> l) > kBucket) ++l;
-    return l + 1;
+    while ((n >> l) > kChunkNode) ++l;
+    return l;
 }
+
+int kd_box_levels(long long n) { return n > 0 ? kd_chunk_level(n) + 1 : 0; }
 
 void launch_kd_boxes(const KdTree& tree, cudaStream_t s, int* launches) {
     if (tree.n <= 0 || !tree.box_lo) return;
-    KdNav t = nav_of(tree);
-    const int lb = tree.box_levels - 1;
-    const long long nodes = 1LL << lb;
-    k_leaf_boxes<<<(unsigned)((nodes * 32 + 255) / 256), 256, 0, s>>>(t, lb, tree.box_lo, tree.box_hi);
+    const int lc = tree.box_levels - 1;
+    const long long chunks = 1LL << lc;
+    k_chunk_boxes<<<(unsigned)((chunks * 32 + 255) / 256), 256, 0, s>>>(tree.x, tree.y, tree.z, tree.n, lc,
+                                                                        tree.box_lo, tree.box_hi);
     int nl = 1;
-    for (int l = lb - 1; l >= 0; --l) {
-        const long long cnt = 1LL << l;
-        k_parent_boxes<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(t, l, tree.box_lo, tree.box_hi);
+    int l = lc - 1;
+    for (; l > kTopLevels; --l) {
+        k_level_boxes<<<(unsigned)(((1LL << l) + 255) / 256), 256, 0, s>>>(l, tree.box_lo, tree.box_hi);
+        ++nl;
+    }
+    if (l >= 0) {
+        k_top_boxes<<<1, 1024, 0, s>>>(l, tree.box_lo, tree.box_hi);
         ++nl;
     }
     if (launches) *launches += nl;
 }
 
-int query_order_level(long long nq, const KdTree& tree) {
-    if (tree.n < 64 || nq <= 0) return 0;
-    int lq = 0;
-    while ((nq >> (lq + 1)) >= 16) ++lq;
-    int lmax = tree.levels - 5;      // cells keep at least 32 photons
-    if (lq > lmax) lq = lmax;
-    if (lq > 24) lq = 24;
-    return lq < 0 ? 0 : lq;
+namespace {
+long long rs_blocks(long long nq) { return (nq + kRsTile - 1) / kRsTile; }
+}  // namespace
+
+size_t query_order_scratch_bytes(long long nq) {
+    const long long n = nq > 0 ? nq : 1;
+    const long long m = rs_blocks(n) * kRsBins;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    return 3 * al(4 * (size_t)n) + al(4 * (size_t)m) + al(4 * scan_scratch_words(m));
 }
 
-size_t query_order_scratch_bytes(long long nq, const KdTree& tree) {
-    int lq = query_order_level(nq, tree);
-    return 4 * (size_t)(nq > 0 ? nq : 1) + 4 * ((size_t)1 << lq) + 4 * scan_scratch_words(1LL << lq) + 512;
+QueryFrame query_frame(const float lo[3], const float hi[3]) {
+    QueryFrame f;
+    for (int k = 0; k < 3; ++k) {
+        const float ext = hi[k] - lo[k];
+        f.lo[k] = lo[k];
+        f.scale[k] = ext > 0.0f ? 1023.99f / ext : 0.0f;
+    }
+    return f;
 }
 
-void launch_query_order(const KdTree& tree, const float* qpos, int stride, long long nq, float r2, void* scratch,
-                        uint32_t* order, uint2* start_nodes, int* launches, cudaStream_t s,
-                        const unsigned long long* nq_dev) {
+void launch_query_order(const float* qpos, int stride, long long nq, const QueryFrame& frame, void* scratch,
+                        uint32_t* order, int* launches, cudaStream_t s, const unsigned long long* nq_dev) {
     if (nq <= 0) return;
-    int lq = query_order_level(nq, tree);
-    uint32_t* keys = (uint32_t*)scratch;
-    uint32_t* counts = keys + ((nq + 63) & ~63LL);
-    long long m = 1LL << lq;
-    cudaMemsetAsync(counts, 0, 4 * (size_t)m, s);
-    unsigned g = (unsigned)((nq + 255) / 256);
-    k_query_cells<<<g, 256, 0, s>>>(nav_of(tree), qpos, stride, nq, nq_dev, lq, r2, keys, counts, start_nodes);
-    launch_scan_counts(counts, m, counts + ((m + 63) & ~63LL), s);
-    k_scatter_queries<<<g, 256, 0, s>>>(keys, nq, nq_dev, counts, order);
-    if (launches) *launches += m > 4 * kScanTile ? 5 : 3;
+    const long long B = rs_blocks(nq), m = B * kRsBins;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    char* p = (char*)scratch;
+    uint32_t* keys_a = (uint32_t*)p; p += al(4 * (size_t)nq);
+    uint32_t* keys_b = (uint32_t*)p; p += al(4 * (size_t)nq);
+    uint32_t* vals_a = (uint32_t*)p; p += al(4 * (size_t)nq);
+    uint32_t* hist = (uint32_t*)p; p += al(4 * (size_t)m);
+    uint32_t* tiles = (uint32_t*)p;
+    k_query_keys<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(qpos, stride, nq, nq_dev, frame, keys_a, vals_a);
+    int nl = 1;
+    // passes: a -> (keys_b, order), (keys_b, order) -> (keys_a, vals_a), (keys_a, vals_a) -> (keys_b, order)
+    const uint32_t* kin[3] = {keys_a, keys_b, keys_a};
+    const uint32_t* vin[3] = {vals_a, order, vals_a};
+    uint32_t* kout[3] = {keys_b, keys_a, keys_b};
+    uint32_t* vout[3] = {order, vals_a, order};
+    for (int pass = 0; pass < 3; ++pass) {
+        k_rs_hist<<<(unsigned)B, kRsThreads, 0, s>>>(kin[pass], nq, nq_dev, pass * kRsBits, hist);
+        launch_scan_counts(hist, m, tiles, s);
+        k_rs_scatter<<<(unsigned)B, kRsThreads, 0, s>>>(kin[pass], vin[pass], kout[pass], vout[pass], nq, nq_dev,
+                                                         pass * kRsBits, hist);
+        nl += 2 + (m > 4 * kScanTile ? 3 : 1);
+    }
+    if (launches) *launches += nl;
 }
 
 size_t scan_scratch_words(long long m) { return (size_t)(m / kScanTile + 2); }
@@ -713,63 +859,34 @@ void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaS
     k_tree_records<<<(unsigned)((tree.n + 255) / 256), 256, 0, s>>>(ph, tree.id, tree.n, tp);
 }
 
-template <int MB, int QPW, int E>
-void launch_gather_t(const VMParams& p, const KdNav& nav, QueryBuf qb, const uint32_t* order,
-                     const uint2* start_nodes, long long nq, MergeBuf mb, unsigned long long* counters,
-                     cudaStream_t s, const unsigned long long* nq_dev, const int* skip) {
-    const long long warps = (nq + QPW - 1) / QPW;
-    k_gather<MB, QPW, E><<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
-        p, nav, qb, order, start_nodes, nq, mb, counters, nq_dev, skip);
-}
-
-unsigned merge_grid() {
-    static thread_local unsigned g = 0;
-    if (!g) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_merge, kMergeThreads, 0);
-        g = (unsigned)(sms * (per_sm > 0 ? per_sm : 1));
-    }
-    return g;
-}
-
-int gather_variants() { return 8; }
+int gather_variants() { return kNumShapes; }
+int gather_default_variant() { return kDefaultShape; }
 
 const char* gather_variant_name(int v) {
-    static const char* names[8] = {
-        "blocks/SM>=2, 8 queries/warp, 5-level steps", "blocks/SM>=2, 16 queries/warp, 5-level steps",
-        "blocks/SM>=3, 8 queries/warp, 5-level steps", "blocks/SM>=3, 16 queries/warp, 5-level steps",
-        "blocks/SM>=4, 8 queries/warp, 5-level steps", "blocks/SM>=4, 16 queries/warp, 5-level steps",
-        "blocks/SM>=3, 8 queries/warp, 4-level steps", "blocks/SM>=4, 8 queries/warp, 4-level steps"};
-    return (v >= 0 && v < 8) ? names[v] : "?";
+    static const char* names[kNumShapes] = {
+        "blocks/SM>=2, 32 queries/group, 5-level steps", "blocks/SM>=3, 32 queries/group, 5-level steps",
+        "blocks/SM>=4, 32 queries/group, 5-level steps", "blocks/SM>=3, 32 queries/group, 4-level steps",
+        "blocks/SM>=4, 32 queries/group, 4-level steps", "blocks/SM>=3, 16 queries/group, 5-level steps",
+        "blocks/SM>=4, 16 queries/group, 4-level steps", "blocks/SM>=4, 16 queries/group, 5-level steps"};
+    return (v >= 0 && v < kNumShapes) ? names[v] : "?";
 }
 
 void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
-                   const uint2* start_nodes, long long nq, double* accum, unsigned long long* counters, MergeBuf mb,
-                   cudaStream_t s, int variant, const unsigned long long* nq_dev, const int* skip) {
-    if (nq <= 0) return;
-    const KdNav nav = nav_of(tree);
-    cudaMemsetAsync(mb.count, 0, sizeof(unsigned long long), s);
-    switch (variant) {
-    case 0: launch_gather_t<2, 8, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 1: launch_gather_t<2, 16, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 2: launch_gather_t<3, 8, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 4: launch_gather_t<4, 8, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 5: launch_gather_t<4, 16, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 6: launch_gather_t<3, 8, 4>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    case 7: launch_gather_t<4, 8, 4>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    default: launch_gather_t<3, 16, 5>(p, nav, qb, order, start_nodes, nq, mb, counters, s, nq_dev, skip); break;
-    }
-    k_merge<<<merge_grid(), kMergeThreads, 0, s>>>(p, tp, qb, tree.id, mb, accum, skip);
+                   long long nq, double* accum, unsigned long long* counters, cudaStream_t s, int variant,
+                   const unsigned long long* nq_dev, const int* skip) {
+    if (nq <= 0 || tree.n <= 0) return;
+    const EvalSink sink{p, qb, tp, tree.id, accum};
+    launch_variant(variant, chunk_tree(tree, tp.t0), reinterpret_cast<const float*>(qb.q0), 4, order, nq, nq_dev,
+                   skip, p.radius_sqr, sink, counters, p.error + ERR_GATHER, s);
 }
 
-void launch_kd_query(const KdTree& tree, int q, const float* qpos, const uint32_t* order, const uint2* start_nodes,
-                     float r2, int* counts, const long long* offsets, int* idx, cudaStream_t s) {
-    if (q <= 0) return;
-    long long warps = (q + kQueriesPerWarp - 1) / kQueriesPerWarp;
-    k_kd_query<<<(unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
-        nav_of(tree), q, qpos, order, start_nodes, r2, counts, offsets, idx);
+void launch_gather_sets(const KdTree& tree, const float4* t0, const float* qpos, int qstride, const uint32_t* order,
+                        long long nq, float r2, int* counts, const long long* offsets, int* cursor, int* idx,
+                        int variant, unsigned long long* counters, int* err, cudaStream_t s) {
+    if (nq <= 0 || tree.n <= 0) return;
+    const SetSink sink{tree.id, counts, offsets, cursor, idx};
+    launch_variant(variant, chunk_tree(tree, t0), qpos, qstride, order, nq, nullptr, nullptr, r2, sink, counters, err,
+                   s);
 }
 
 }  // namespace rc

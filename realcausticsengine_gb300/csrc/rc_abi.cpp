@@ -82,18 +82,12 @@ struct DeviceState {
     DevBuf<float4> tp0, tp1, box_lo, box_hi;
     DevBuf<float2> tp2;
     DevBuf<uint32_t> qorder;
-    DevBuf<uint2> qstart;
     DevBuf<unsigned char> qscratch;
     DevBuf<double> accum;
     DevBuf<float> image;          // FP32 mean for readback
     // light-path processing order (launch_light_order) and its scratch
     DevBuf<uint32_t> path_order;
     DevBuf<unsigned char> order_scratch;
-    // photon-query merge pairs between the gather's traversal and its merge evaluation
-    DevBuf<uint2> merges;
-    DevBuf<unsigned long long> merge_count;
-    unsigned long long last_merges = 0;
-    long long async_mcap = 0;
     // learned emission proposal
     std::unique_ptr<MlpStore> mlp;
     DevBuf<float4> prop, train_pos, train_dir;
@@ -106,7 +100,7 @@ struct DeviceState {
     // asynchronous iterations (graph replay): fixed capacities, launch shapes and a
     // per-iteration overflow flag; the instantiated graph is updated in place
     long long async_pcap = 0, async_qcap = 0;
-    int async_lvar = 0, async_cvar = 0, async_gvar = 3;
+    int async_lvar = 0, async_cvar = 0, async_gvar = 1;
     DevBuf<int> async_flags;
     cudaGraphExec_t graph_exec = nullptr;
     unsigned long long last_photons = 0, last_queries = 0;
@@ -128,13 +122,11 @@ struct DeviceState {
         world_mesh.release(); mesh_root.release(); lights.release(); cdf.release(); materials.release();
         ph_tp.release(); ph_path.release(); counters.release(); errors.release();
         kd_nodes.release(); kd_x.release(); kd_y.release(); kd_z.release(); kd_id.release(); kd_scratch.release();
-        tp0.release(); tp1.release(); tp2.release(); qorder.release(); qstart.release(); qscratch.release();
+        tp0.release(); tp1.release(); tp2.release(); qorder.release(); qscratch.release();
         box_lo.release(); box_hi.release();
         accum.release();
         image.release();
-        merges.release(); merge_count.release();
         path_order.release(); order_scratch.release();
-        last_merges = 0;
         mlp.reset();
         prop.release(); train_pos.release(); train_dir.release(); contrib.release(); train_wsum.release();
         prop_table.release();
@@ -436,6 +428,14 @@ int prepare() {
     return RC_OK;
 }
 
+// Frame of the merge queries' Morton order: the scene's bounding box (every camera
+// vertex lies on a scene surface).
+QueryFrame scene_query_frame(const HostScene& sc) {
+    const float lo[3] = {sc.bounds.mn.x, sc.bounds.mn.y, sc.bounds.mn.z};
+    const float hi[3] = {sc.bounds.mx.x, sc.bounds.mx.y, sc.bounds.mx.z};
+    return query_frame(lo, hi);
+}
+
 int check_errors() {
     int h[ERR_COUNT];
     RC_CUDA(cudaMemcpy(h, ctx().dev.errors.p, sizeof(h), cudaMemcpyDeviceToHost));
@@ -443,6 +443,7 @@ int check_errors() {
     if (h[ERR_MATERIAL]) { ctx().err = "triangle material index out of range"; return RC_E_INVALID; }
     if (h[ERR_KD]) { ctx().err = "KD-tree build found inconsistent counts"; return RC_E_INVALID; }
     if (h[ERR_MLP]) { ctx().err = "tensor-core pipeline wait timed out in the MLP"; return RC_E_CUDA; }
+    if (h[ERR_GATHER]) { ctx().err = "gather traversal stack overflow"; return RC_E_CAPACITY; }
     return RC_OK;
 }
 
@@ -802,36 +803,28 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     if (r) return r;
     QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, (long long)d.q0.n, d.counters.p + 1};
     RC_CUDA(d.qorder.reserve(std::max<unsigned long long>(nq, 1)));
-    RC_CUDA(d.qstart.reserve(std::max<unsigned long long>(nq, 1)));
-    RC_CUDA(d.qscratch.reserve(query_order_scratch_bytes((long long)nq, tree)));
+    RC_CUDA(d.qscratch.reserve(query_order_scratch_bytes((long long)nq)));
     RC_CUDA(cudaEventRecord(d.ev[6], s));
     int qlaunch = 0;
-    launch_query_order(tree, reinterpret_cast<const float*>(d.q0.p), 4, (long long)nq, p.radius_sqr, d.qscratch.p,
-                       d.qorder.p, d.qstart.p, &qlaunch, s);
-    // merge pairs: room for the last iteration's count + 1/4; before any count, 16 per
-    // query (the water pool merges 6.9 per query; an overflow only re-runs the gather)
-    long long mcap = std::max<long long>((long long)d.merges.n, d.last_merges
-                                                                   ? (long long)(d.last_merges + d.last_merges / 4) + 65536
-                                                                   : 16 * (long long)nq + 65536);
-    RC_CUDA(d.merges.reserve(mcap));
-    RC_CUDA(d.merge_count.reserve(1));
-    int variant = 3;
+    launch_query_order(reinterpret_cast<const float*>(d.q0.p), 4, (long long)nq, scene_query_frame(sc), d.qscratch.p,
+                       d.qorder.p, &qlaunch, s);
+    int variant = gather_default_variant();
     if (cfg().autotune && nq > 0) {
-        const MergeBuf mb{d.merges.p, (long long)d.merges.n, d.merge_count.p, nullptr};
         const int cls = 63 - __builtin_clzll((unsigned long long)nq);
         if (g_tune.gather[cls].load() < 0) {
             // time every launch shape on this iteration's queries into a scratch image
             // (warm-up launch first: the first launch of a shape loads its code)
             RC_CUDA(d.tune_accum.reserve(std::max<long long>(3 * npix, 1)));
             float best = 1e30f;
-            int best_v = 3;
+            int best_v = variant;
             for (int v = 0; v < gather_variants(); ++v) {
-                launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.tune_accum.p, nullptr, mb, s, v);
+                launch_gather(p, tree, tph, qb, d.qorder.p, (long long)nq, d.tune_accum.p, nullptr, s, v);
                 RC_CUDA(cudaEventRecord(d.evm[0], s));
-                launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.tune_accum.p, nullptr, mb, s, v);
+                launch_gather(p, tree, tph, qb, d.qorder.p, (long long)nq, d.tune_accum.p, nullptr, s, v);
                 RC_CUDA(cudaEventRecord(d.evm[1], s));
                 RC_CUDA(cudaEventSynchronize(d.evm[1]));
                 const float ms = ms_between(d.evm[0], d.evm[1]);
+                if (cfg().verbose) std::printf("{\"gather_shape\": %d, \"ms\": %.4f}\n", v, ms);
                 if (ms < best) { best = ms; best_v = v; }
             }
             g_tune.gather[cls] = best_v;
@@ -841,27 +834,17 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         }
         variant = g_tune.gather[cls].load();
     }
-    unsigned long long gc[4] = {0, 0, 0, 0}, nmerge = 0;
-    for (int attempt = 0; attempt < 3; ++attempt) {
-        // the merge evaluation does nothing when the pairs overflowed, so the gather can
-        // simply run again with a larger buffer
-        RC_CUDA(d.merges.reserve(mcap));
-        const MergeBuf mb{d.merges.p, (long long)d.merges.n, d.merge_count.p, nullptr};
-        RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
-        RC_CUDA(cudaEventRecord(d.evg[0], s));
-        launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, (long long)nq, d.accum.p, d.counters.p + 2, mb, s,
-                      variant);
-        RC_CUDA(cudaEventRecord(d.evg[1], s));
-        RC_CUDA(cudaGetLastError());
-        RC_CUDA(cudaEventRecord(d.ev[7], s));
-        RC_CUDA(cudaMemcpyAsync(gc, d.counters.p + 2, sizeof(gc), cudaMemcpyDeviceToHost, s));
-        RC_CUDA(cudaMemcpyAsync(&nmerge, d.merge_count.p, sizeof(nmerge), cudaMemcpyDeviceToHost, s));
-        RC_CUDA(cudaStreamSynchronize(s));
-        if ((long long)nmerge <= (long long)d.merges.n) break;
-        mcap = (long long)(nmerge + nmerge / 8) + 65536;
-        if (attempt == 2) { ctx().err = "merge pair buffer overflow"; return RC_E_CAPACITY; }
-    }
-    d.last_merges = nmerge;
+    unsigned long long gc[4] = {0, 0, 0, 0};
+    RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
+    RC_CUDA(cudaEventRecord(d.evg[0], s));
+    launch_gather(p, tree, tph, qb, d.qorder.p, (long long)nq, d.accum.p, d.counters.p + 2, s, variant);
+    RC_CUDA(cudaEventRecord(d.evg[1], s));
+    RC_CUDA(cudaGetLastError());
+    RC_CUDA(cudaEventRecord(d.ev[7], s));
+    RC_CUDA(cudaMemcpyAsync(gc, d.counters.p + 2, sizeof(gc), cudaMemcpyDeviceToHost, s));
+    RC_CUDA(cudaStreamSynchronize(s));
+    r = check_errors();
+    if (r) return r;
     if (train) {
         RC_CUDA(cudaEventRecord(d.evm[0], s));
         r = proposal_train(sc, p);
@@ -881,7 +864,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     st[2] = (double)nq;
     st[3] = (double)gc[0];   // accepted photon-query pairs
     st[14] = (double)gc[1];  // photon tests
-    st[15] = (double)gc[2];  // buckets visited (per warp)
+    st[15] = (double)gc[2];  // photon chunks tested (per group)
     d.last_nodes = (double)gc[3];
     st[4] = t_light;
     st[5] = ms_between(d.ev[2], d.ev[3]);
@@ -892,16 +875,16 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     st[10] = d.iterations_done;
     st[11] = sc.scene_radius;
     st[12] = std::sqrt(p.radius_sqr);
-    st[13] = kd_launches + 4 + qlaunch;
+    st[13] = kd_launches + 3 + qlaunch;
     d.acc_gather_ms += ms_between(d.evg[0], d.evg[1]);   // the gather kernel alone
     // gather algorithmic bytes: each photon record read once (40 B), each query record
-    // read once (80 B), each query's FP64 RGB pixel read and written once (48 B)
-    d.acc_gather_bytes += 40.0 * (double)nph + 80.0 * (double)nq + 48.0 * (double)nq;
+    // read once (64 B), each pixel's FP64 RGB sum read and written once (48 B)
+    d.acc_gather_bytes += 40.0 * (double)nph + 64.0 * (double)nq + 48.0 * (double)npix;
     d.acc_launches += st[13];
     d.acc_iters += 1;
     if (cfg().verbose)
         std::printf("{\"iteration\": %d, \"light_paths\": %lld, \"photons\": %llu, \"queries\": %llu, "
-                    "\"merged\": %llu, \"tests\": %llu, \"buckets\": %llu, \"nodes\": %llu, "
+                    "\"merged\": %llu, \"tests\": %llu, \"chunks\": %llu, \"boxes\": %llu, "
                     "\"light_ms\": %.3f, \"kd_ms\": %.3f, \"camera_ms\": %.3f, \"gather_ms\": %.3f}\n",
                     it, p.num_light_paths, nph, nq, gc[0], gc[1], gc[2], gc[3], st[4], st[5], st[6], st[7]);
     return RC_OK;
@@ -936,11 +919,6 @@ int async_setup(const HostScene& sc) {
     };
     d.async_pcap = std::min<long long>(capacity(d.last_photons), (1ll << 28) - 1);   // 28-bit photon index
     d.async_qcap = capacity(d.last_queries);
-    // merge pairs vary more between iterations than photons and queries: 1/8 margin
-    d.async_mcap = tight ? (long long)std::max<unsigned long long>(d.last_merges, 1)
-                         : (long long)(d.last_merges + d.last_merges / 8) + 65536;
-    RC_CUDA(d.merges.reserve(d.async_mcap));
-    RC_CUDA(d.merge_count.reserve(1));
     RC_CUDA(d.ph_pos.reserve(d.async_pcap)); RC_CUDA(d.ph_dir.reserve(d.async_pcap));
     RC_CUDA(d.ph_tp.reserve(d.async_pcap)); RC_CUDA(d.ph_path.reserve(d.async_pcap));
     {
@@ -957,17 +935,14 @@ int async_setup(const HostScene& sc) {
     RC_CUDA(d.tp0.reserve(n)); RC_CUDA(d.tp1.reserve(n)); RC_CUDA(d.tp2.reserve(n));
     const int bl = kd_box_levels(n);
     if (bl > 0) { RC_CUDA(d.box_lo.reserve((size_t)1 << bl)); RC_CUDA(d.box_hi.reserve((size_t)1 << bl)); }
-    KdTree t{};
-    t.n = n;
-    t.levels = n > 0 ? 63 - __builtin_clzll((unsigned long long)n) : 0;
-    RC_CUDA(d.qorder.reserve(d.async_qcap)); RC_CUDA(d.qstart.reserve(d.async_qcap));
-    RC_CUDA(d.qscratch.reserve(query_order_scratch_bytes(d.async_qcap, t)));
+    RC_CUDA(d.qorder.reserve(d.async_qcap));
+    RC_CUDA(d.qscratch.reserve(query_order_scratch_bytes(d.async_qcap)));
     RC_CUDA(d.accum.reserve(3 * npix));
     auto var = [](int v, int dflt) { return v >= 0 ? v : dflt; };
     d.async_lvar = var(g_tune.light[size_class(cfg().photons_per_iter > 0 ? cfg().photons_per_iter : npix)].load(), 0);
     d.async_cvar = var(g_tune.camera[size_class(npix)].load(), 0);
-    d.async_gvar = var(g_tune.gather[size_class((long long)d.last_queries)].load(), 3);
-    if (!cfg().autotune) d.async_lvar = d.async_cvar = 0, d.async_gvar = 3;
+    d.async_gvar = var(g_tune.gather[size_class((long long)d.last_queries)].load(), gather_default_variant());
+    if (!cfg().autotune) d.async_lvar = d.async_cvar = 0, d.async_gvar = gather_default_variant();
     return RC_OK;
 }
 
@@ -1020,13 +995,12 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     RC_CUDA(cudaStreamWaitEvent(s, d.join, 0));
     launch_check_counts(d.counters.p, pc, d.counters.p + 1, qc, flag, s);
     RC_CUDA(record(d.ev[6], s));
-    launch_query_order(tree, reinterpret_cast<const float*>(d.q0.p), 4, qc, p.radius_sqr, d.qscratch.p, d.qorder.p,
-                       d.qstart.p, nullptr, s, d.counters.p + 1);
+    launch_query_order(reinterpret_cast<const float*>(d.q0.p), 4, qc, scene_query_frame(sc), d.qscratch.p, d.qorder.p,
+                       nullptr, s, d.counters.p + 1);
     RC_CUDA(cudaMemsetAsync(d.counters.p + 2, 0, 4 * sizeof(unsigned long long), s));
     RC_CUDA(record(d.evg[0], s));
-    const MergeBuf mb{d.merges.p, d.async_mcap, d.merge_count.p, flag};
-    launch_gather(p, tree, tph, qb, d.qorder.p, d.qstart.p, qc, d.accum.p, d.counters.p + 2, mb, s, d.async_gvar,
-                  d.counters.p + 1, flag);
+    launch_gather(p, tree, tph, qb, d.qorder.p, qc, d.accum.p, d.counters.p + 2, s, d.async_gvar, d.counters.p + 1,
+                  flag);
     RC_CUDA(record(d.evg[1], s));
     RC_CUDA(record(d.ev[7], s));
     return RC_OK;
@@ -1134,7 +1108,8 @@ int render_iterations(HostScene& sc, int iterations) {
     st[12] = std::sqrt(p.radius_sqr);
     const double gms = ms_between(d.evg[0], d.evg[1]);
     d.acc_gather_ms += gms * n_async;    // the last replay's gather time stands for each
-    d.acc_gather_bytes += (40.0 * (double)cnt[0] + 128.0 * (double)cnt[1]) * n_async;
+    d.acc_gather_bytes += (40.0 * (double)cnt[0] + 64.0 * (double)cnt[1] +
+                           48.0 * (double)sc.camera.width * sc.camera.height) * n_async;
     d.acc_iters += n_async;
     d.acc_async += n_async;
     d.acc_launches += (d.stats[13] + 2.0) * n_async;   // an eager iteration's kernels + pad + check
@@ -1684,6 +1659,38 @@ int rc_proposal_state(long long n, float* prop4, float* contrib) {
     return RC_OK;
 }
 
+int rc_camera_queries(int iteration, float* out, long long cap, long long* count) {
+    int r = prepare();
+    if (r) return r;
+    if (iteration < 0 || (cap > 0 && !out)) { ctx().err = "bad query output"; return RC_E_INVALID; }
+    HostScene& sc = *ctx().scene;
+    DeviceState& d = ctx().dev;
+    cudaStream_t s = d.stream;
+    VMParams p = make_params(sc, iteration);
+    const long long npix = (long long)sc.camera.width * sc.camera.height;
+    long long qcap = std::max<long long>(npix * 2, 1024);
+    unsigned long long nq = 0;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        RC_CUDA(d.q0.reserve(qcap)); RC_CUDA(d.q1.reserve(qcap)); RC_CUDA(d.q2.reserve(qcap));
+        RC_CUDA(d.q3.reserve(qcap)); RC_CUDA(d.q4.reserve(qcap));
+        RC_CUDA(d.counters.reserve(8));
+        RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s));
+        QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, (long long)d.q0.n, d.counters.p + 1};
+        launch_camera_pass(p, qb, d.counters.p + 7, s);
+        RC_CUDA(cudaGetLastError());
+        RC_CUDA(cudaMemcpyAsync(&nq, d.counters.p + 1, sizeof(nq), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(cudaStreamSynchronize(s));
+        if ((long long)nq <= (long long)d.q0.n) break;
+        qcap = (long long)nq + 1024;
+    }
+    r = check_errors();
+    if (r) return r;
+    if (count) *count = (long long)nq;
+    const long long n = std::min<long long>((long long)nq, cap);
+    if (n > 0) RC_CUDA(cudaMemcpy(out, d.q0.p, 16 * (size_t)n, cudaMemcpyDeviceToHost));
+    return RC_OK;
+}
+
 int rc_light_photons(int iteration, float* out, long long cap, long long* count) {
     int r = prepare();
     if (r) return r;
@@ -1770,7 +1777,7 @@ int rc_trace_rays_full(int n, const float* origins, const float* directions, flo
 
 static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, DevBuf<uint2>& nodes, DevBuf<float>& x,
                          DevBuf<float>& y, DevBuf<float>& z, DevBuf<uint32_t>& id, DevBuf<unsigned char>& scratch,
-                         DevBuf<float4>& boxes, KdTree& tree, cudaStream_t s) {
+                         DevBuf<float4>& boxes, DevBuf<float4>& t0, KdTree& tree, cudaStream_t s) {
     DevBuf<int> err;
     RC_CUDA(err.reserve(1));
     RC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
@@ -1793,6 +1800,10 @@ static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, Dev
         tree.box_hi = boxes.p + ((size_t)1 << tree.box_levels);
         launch_kd_boxes(tree, s, nullptr);
         RC_CUDA(cudaGetLastError());
+        RC_CUDA(t0.reserve(std::max(n, 1)));
+        launch_tree_records(PhotonBuf{pos.p, nullptr, nullptr, nullptr, n, nullptr}, tree, TreePhotons{t0.p, nullptr, nullptr},
+                            s);
+        RC_CUDA(cudaGetLastError());
     }
     int h = 0;
     RC_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1802,29 +1813,43 @@ static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, Dev
     return RC_OK;
 }
 
-int rc_kd_query(int n, const float* positions, int q, const float* queries, float r2, int* counts, int* idx,
-                long long cap, long long* total) {
+int rc_gather_variants(void) { return gather_variants(); }
+
+int rc_gather_query(int variant, int n, const float* positions, int q, const float* queries, float r2, int* counts,
+                    int* idx, long long cap, long long* total) {
     if (n < 0 || q < 0 || (n > 0 && !positions) || (q > 0 && (!queries || !counts))) { ctx().err = "bad KD arrays"; return RC_E_INVALID; }
+    if (variant < -1 || variant >= gather_variants()) { ctx().err = "gather variant out of range"; return RC_E_INVALID; }
+    if (variant < 0) variant = gather_default_variant();
     cudaStream_t s = nullptr;
     RC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    DevBuf<float4> pos; DevBuf<uint2> nodes; DevBuf<float> x, y, z, qp; DevBuf<uint32_t> id;
-    DevBuf<unsigned char> scratch, osc; DevBuf<int> cnt, out; DevBuf<long long> off; DevBuf<uint32_t> ord;
-    DevBuf<uint2> qst;
+    DevBuf<float4> pos, boxes, t0; DevBuf<uint2> nodes; DevBuf<float> x, y, z, qp; DevBuf<uint32_t> id, ord;
+    DevBuf<unsigned char> scratch, osc; DevBuf<int> cnt, cur, out, err; DevBuf<long long> off;
     KdTree tree;
-    DevBuf<float4> boxes;
-    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, boxes, tree, s);
+    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, boxes, t0, tree, s);
+    if (!r && total) *total = 0;
     if (!r && q > 0) {
-        do {
-            RC_CUDA(qp.reserve(3 * (size_t)q)); RC_CUDA(cnt.reserve(q)); RC_CUDA(off.reserve(q));
+        r = [&]() -> int {
+            RC_CUDA(qp.reserve(3 * (size_t)q)); RC_CUDA(cnt.reserve(q)); RC_CUDA(cur.reserve(q)); RC_CUDA(off.reserve(q));
+            RC_CUDA(err.reserve(1)); RC_CUDA(ord.reserve(q));
+            RC_CUDA(osc.reserve(query_order_scratch_bytes(q)));
             RC_CUDA(cudaMemcpyAsync(qp.p, queries, 12 * (size_t)q, cudaMemcpyHostToDevice, s));
-            RC_CUDA(ord.reserve(q));
-            RC_CUDA(qst.reserve(q));
-            RC_CUDA(osc.reserve(query_order_scratch_bytes(q, tree)));
-            launch_query_order(tree, qp.p, 3, q, r2, osc.p, ord.p, qst.p, nullptr, s);
-            launch_kd_query(tree, q, qp.p, ord.p, qst.p, r2, cnt.p, nullptr, nullptr, s);
+            RC_CUDA(cudaMemsetAsync(cnt.p, 0, 4 * (size_t)q, s));
+            RC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (int j = 0; j < q; ++j)
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = std::min(lo[k], queries[3 * j + k]);
+                    hi[k] = std::max(hi[k], queries[3 * j + k]);
+                }
+            launch_query_order(qp.p, 3, q, query_frame(lo, hi), osc.p, ord.p, nullptr, s);
+            launch_gather_sets(tree, t0.p, qp.p, 3, ord.p, q, r2, cnt.p, nullptr, nullptr, nullptr, variant, nullptr,
+                               err.p, s);
             RC_CUDA(cudaGetLastError());
+            int h = 0;
             RC_CUDA(cudaMemcpyAsync(counts, cnt.p, 4 * (size_t)q, cudaMemcpyDeviceToHost, s));
+            RC_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
             RC_CUDA(cudaStreamSynchronize(s));
+            if (h) { ctx().err = "gather traversal stack overflow"; return RC_E_CAPACITY; }
             std::vector<long long> offs(q);
             long long t = 0;
             for (int j = 0; j < q; ++j) { offs[j] = t; t += counts[j]; }
@@ -1832,19 +1857,26 @@ int rc_kd_query(int n, const float* positions, int q, const float* queries, floa
             if (idx && t > 0 && t <= cap) {
                 RC_CUDA(out.reserve(t));
                 RC_CUDA(cudaMemcpyAsync(off.p, offs.data(), 8 * (size_t)q, cudaMemcpyHostToDevice, s));
-                launch_kd_query(tree, q, qp.p, ord.p, qst.p, r2, cnt.p, off.p, out.p, s);
+                RC_CUDA(cudaMemsetAsync(cur.p, 0, 4 * (size_t)q, s));
+                launch_gather_sets(tree, t0.p, qp.p, 3, ord.p, q, r2, nullptr, off.p, cur.p, out.p, variant, nullptr,
+                                   err.p, s);
                 RC_CUDA(cudaGetLastError());
                 RC_CUDA(cudaMemcpyAsync(idx, out.p, 4 * (size_t)t, cudaMemcpyDeviceToHost, s));
                 RC_CUDA(cudaStreamSynchronize(s));
             }
-        } while (0);
-    } else if (!r && total) {
-        *total = 0;
+            return RC_OK;
+        }();
     }
     pos.release(); nodes.release(); x.release(); y.release(); z.release(); id.release(); scratch.release();
-    cnt.release(); out.release(); off.release(); qp.release(); ord.release(); osc.release(); boxes.release(); qst.release();
+    cnt.release(); cur.release(); out.release(); off.release(); qp.release(); ord.release(); osc.release();
+    boxes.release(); t0.release(); err.release();
     cudaStreamDestroy(s);
     return r;
+}
+
+int rc_kd_query(int n, const float* positions, int q, const float* queries, float r2, int* counts, int* idx,
+                long long cap, long long* total) {
+    return rc_gather_query(-1, n, positions, q, queries, r2, counts, idx, cap, total);
 }
 
 int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes_out, long long cap, long long* num_nodes) {
@@ -1853,8 +1885,8 @@ int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes_out, long l
     RC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     DevBuf<float4> pos; DevBuf<uint2> nodes; DevBuf<float> x, y, z; DevBuf<uint32_t> id; DevBuf<unsigned char> scratch;
     KdTree tree;
-    DevBuf<float4> boxes;
-    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, boxes, tree, s);
+    DevBuf<float4> boxes, t0;
+    int r = kd_build_host(n, positions, pos, nodes, x, y, z, id, scratch, boxes, t0, tree, s);
     if (!r) {
         long long nn = kd_node_array_len(n);
         if (num_nodes) *num_nodes = nn;
@@ -1866,7 +1898,7 @@ int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes_out, long l
         }
     }
     pos.release(); nodes.release(); x.release(); y.release(); z.release(); id.release(); scratch.release();
-    boxes.release();
+    boxes.release(); t0.release();
     cudaStreamDestroy(s);
     return r;
 }

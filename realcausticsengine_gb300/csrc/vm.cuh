@@ -48,17 +48,6 @@ struct TreePhotons {
     float2* t2;
 };
 
-// Photon-query merge pairs, written by the gather's traversal and read by its merge
-// evaluation: pairs[i] = (query index, tree position).  *count may exceed cap (the
-// pairs beyond cap are dropped and the evaluation does nothing; *overflow, when given,
-// is set so that the iteration is rendered again).
-struct MergeBuf {
-    uint2* pairs;
-    long long cap;
-    unsigned long long* count;
-    int* overflow;
-};
-
 struct LightsView {
     const DevLight* lights;
     const float* cdf;      // n + 1 entries
@@ -91,7 +80,8 @@ struct VMParams {
 };
 
 // error flag slots
-enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_KD = 4, ERR_MLP = 5, ERR_COUNT = 8 };
+enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_KD = 4, ERR_MLP = 5,
+       ERR_GATHER = 6, ERR_COUNT = 8 };
 
 // Metropolis light pass (RC_SAMPLER_HYBRID / RC_SAMPLER_PSSMLT), `chains` chains in one
 // launch; stats[0] = visible large steps, stats[1] = large steps (HYBRID: light paths).
@@ -128,38 +118,52 @@ void launch_check_counts(const unsigned long long* photons, long long photon_cap
                          long long query_cap, int* flag, cudaStream_t s);
 void launch_trace_rays(const SceneView& s, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st);
+// Photon records in tree order (tp.t0/t1/t2 from ph.pos/dir/tp; only t0 when ph.dir is null).
 void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaStream_t s);
-// Node bounding boxes used by the gather to prune exactly: levels [0, kd_box_levels(n)),
-// arrays of 2^kd_box_levels(n) float4 each.
+// Node bounding boxes used by the gather to prune exactly: the photons in tree order
+// are cut into 2^Lc chunks of at most 32 (Lc = kd_chunk_level(n), the shallowest level
+// whose nodes hold at most 31 photons: a chunk is such a node's range plus the median
+// photon that may follow it); the chunk boxes carry their first position and count in
+// .w, every node above has the union of its children's.  Levels [0, kd_box_levels(n)),
+// arrays of 2^kd_box_levels(n) float4 each, filled from the tree's x/y/z.
+int kd_chunk_level(long long n);
 int kd_box_levels(long long n);
 void launch_kd_boxes(const KdTree& tree, cudaStream_t s, int* launches);
-// Spatial order of queries (positions at qpos + stride*i): order[] receives query
-// indices grouped by KD cell.  scratch: query_order_scratch_bytes(nq, tree).
-size_t query_order_scratch_bytes(long long nq, const KdTree& tree);
-void launch_query_order(const KdTree& tree, const float* qpos, int stride, long long nq, float r2, void* scratch,
-                        uint32_t* order, uint2* start_nodes, int* launches, cudaStream_t s,
-                        const unsigned long long* nq_dev = nullptr);
-// start_nodes[i]: the node where query i's traversal first branches (from launch_query_order).
-// counters (optional, 4 u64 accumulated): accepted photon-query pairs, photon tests
-// (lanes x staged photons), buckets visited, inner nodes visited
-// `variant` picks the gather's launch shape (see gather_variant_name); 3 is the default
-// the autotuner starts from.
-// With nq_dev the query count is read on the device (bounded by num_queries, the
-// capacity the grid is sized for) and a non-zero *skip makes the launch a no-op.
-// Two kernels: the traversal writes the accepted photon-query pairs to `mb`, then the
-// merge evaluation (BSDF, MIS weight, FP64 pixel sums) runs over the pairs.
+// Spatial order of queries (positions at qpos + stride*i): order[] receives the query
+// indices sorted by the 30-bit Morton code of their cell in a 1024^3 grid over the box
+// `frame` describes (query_frame(lo, hi); positions outside are clamped), by a stable
+// radix sort.  scratch: query_order_scratch_bytes(nq) bytes.
+struct QueryFrame { float lo[3], scale[3]; };
+QueryFrame query_frame(const float lo[3], const float hi[3]);
+size_t query_order_scratch_bytes(long long nq);
+void launch_query_order(const float* qpos, int stride, long long nq, const QueryFrame& frame, void* scratch,
+                        uint32_t* order, int* launches, cudaStream_t s, const unsigned long long* nq_dev = nullptr);
+// The gather: one fused kernel over groups of ordered queries (gather.cu).  Photon sets
+// are the reference's; each accepted photon's merge (BSDF, MIS weight, throughput) is
+// summed per query and added into the query's FP64 pixel.  `variant` picks the launch
+// shape (gather_variant_name).  counters (optional, 4 u64 accumulated): accepted
+// photon-query pairs, photon tests (chunk photons x overlapping queries), chunks
+// tested, boxes tested.  With nq_dev the query count is read on the device (bounded by
+// num_queries, the capacity the grid is sized for) and a non-zero *skip makes the
+// launch a no-op.  Needs the boxes (launch_kd_boxes) and the tree-order records.
 void launch_gather(const VMParams& p, const KdTree& tree, TreePhotons tp, QueryBuf qb, const uint32_t* order,
-                   const uint2* start_nodes, long long num_queries, double* accum, unsigned long long* counters,
-                   MergeBuf mb, cudaStream_t s, int variant = 3, const unsigned long long* nq_dev = nullptr,
-                   const int* skip = nullptr);
+                   long long num_queries, double* accum, unsigned long long* counters, cudaStream_t s, int variant,
+                   const unsigned long long* nq_dev = nullptr, const int* skip = nullptr);
+// Parity hook: the same kernel with a sink that records each query's photon ids
+// (tree.id of the accepted positions).  Without offsets it adds each query's count into
+// counts[] (zeroed by the caller); with offsets it writes the ids at offsets[q] +
+// cursor[q]++ (cursor zeroed by the caller).  t0: tree-order positions
+// (launch_tree_records); queries at qpos + qstride*i in the order `order`.  *err is set
+// if a traversal stack would overflow (cannot happen for n < 2^28).
+void launch_gather_sets(const KdTree& tree, const float4* t0, const float* qpos, int qstride, const uint32_t* order,
+                        long long nq, float r2, int* counts, const long long* offsets, int* cursor, int* idx,
+                        int variant, unsigned long long* counters, int* err, cudaStream_t s);
 int gather_variants();
+int gather_default_variant();
 // Launch shapes of the persistent light and camera passes (block size x traversal-stack
 // placement), chosen by the autotuner; 0 is the default.
 int pass_variants();
 const char* pass_variant_name(int v);
 const char* gather_variant_name(int v);
-// Radius query hook: counts (and, if idx != nullptr, ids at offsets) per query.
-void launch_kd_query(const KdTree& tree, int q, const float* qpos, const uint32_t* order, const uint2* start_nodes,
-                     float r2, int* counts, const long long* offsets, int* idx, cudaStream_t s);
 
 }  // namespace rc

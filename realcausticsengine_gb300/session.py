@@ -14,7 +14,7 @@ from .scene import InitArgs, Scene
 
 STAT_NAMES = ["light_paths", "photons", "queries", "merged", "light_ms", "kd_ms", "camera_ms", "gather_ms",
               "accum_ms", "device_ms", "iterations", "scene_radius", "radius", "launches", "photon_tests",
-              "buckets_visited"]
+              "chunks_tested"]
 
 
 class Context:
@@ -127,6 +127,14 @@ class Renderer:
               "rc_trace_rays_full")
         return out
 
+    def camera_queries(self, iteration: int) -> np.ndarray:
+        """Merge queries of one camera pass: (n, 4) float32 [position xyz, camera dVM]."""
+        n = C.c_longlong()
+        check(self.L.rc_camera_queries(int(iteration), None, 0, C.byref(n)), "rc_camera_queries")
+        out = np.zeros((max(n.value, 1), 4), np.float32)
+        check(self.L.rc_camera_queries(int(iteration), out.ctypes.data, len(out), C.byref(n)), "rc_camera_queries")
+        return out[:n.value]
+
     def light_photons(self, iteration: int) -> np.ndarray:
         n = C.c_longlong()
         check(self.L.rc_light_photons(int(iteration), None, 0, C.byref(n)), "rc_light_photons")
@@ -149,22 +157,27 @@ class Renderer:
         self.L.rc_release()
 
 
-def kd_query(positions: np.ndarray, queries: np.ndarray, r2: float, with_indices: bool = True):
-    """GPU KD-tree radius query on caller-chosen photons: (counts, [index arrays])."""
+def kd_query(positions: np.ndarray, queries: np.ndarray, r2: float, with_indices: bool = True, variant: int = -1):
+    """Radius query on caller-chosen photons through the render's own gather kernel
+    (launch shape `variant`, -1 = default): (counts, [photon id arrays])."""
     L = lib()
     p = np.ascontiguousarray(positions, np.float32)
     q = np.ascontiguousarray(queries, np.float32)
     counts = np.zeros(len(q), np.int32)
     total = C.c_longlong()
-    check(L.rc_kd_query(len(p), p.ctypes.data, len(q), q.ctypes.data, C.c_float(r2), counts.ctypes.data, None, 0,
-                        C.byref(total)), "rc_kd_query")
+    check(L.rc_gather_query(int(variant), len(p), p.ctypes.data, len(q), q.ctypes.data, C.c_float(r2),
+                            counts.ctypes.data, None, 0, C.byref(total)), "rc_gather_query")
     if not with_indices:
         return counts, None
     idx = np.zeros(max(total.value, 1), np.int32)
-    check(L.rc_kd_query(len(p), p.ctypes.data, len(q), q.ctypes.data, C.c_float(r2), counts.ctypes.data,
-                        idx.ctypes.data, len(idx), C.byref(total)), "rc_kd_query")
+    check(L.rc_gather_query(int(variant), len(p), p.ctypes.data, len(q), q.ctypes.data, C.c_float(r2),
+                            counts.ctypes.data, idx.ctypes.data, len(idx), C.byref(total)), "rc_gather_query")
     offs = np.concatenate([[0], np.cumsum(counts)])
     return counts, [idx[offs[j]:offs[j + 1]] for j in range(len(q))]
+
+
+def gather_variants() -> int:
+    return int(lib().rc_gather_variants())
 
 
 def kd_build_nodes(positions: np.ndarray) -> np.ndarray:

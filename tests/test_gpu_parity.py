@@ -203,7 +203,9 @@ def _rel_rmse(a, b):
 def test_render_vs_oracle_same_samples(orc):
     """Same seed and iterations: GPU FP32 against oracle FP32 and FP64.  Both use the
     same primary samples, so differences come from rounding only (plus paths that
-    drift after a transcendental differs by an ulp): relative RMSE < 3%."""
+    drift after a transcendental differs by an ulp): relative RMSE < 1e-4 (measured
+    ~2e-6 against FP32, ~1e-7 against FP64).  A photon missed or counted twice by the
+    gather moves the image by far more."""
     sc = scenes.test_scene(48, 36, subdiv=2)
     paths, seed, iters = 30000, 9, 3
     r = Renderer(sc, max_path_length=6, photons_per_iter=paths, seed=seed)
@@ -219,14 +221,14 @@ def test_render_vs_oracle_same_samples(orc):
         ref = acc / iters
         rel = _rel_rmse(img, ref)
         print(f"FP{prec}: rel RMSE {rel:.3e}, mean ratio {img.mean() / ref.mean():.5f}")
-        assert rel < 0.03
+        assert rel < 1e-4
 
 
 @pytest.mark.parametrize("rough", [False, True])
 def test_dispersion_vs_oracle_same_samples(orc, rough):
     """Per-channel IOR dispersion (material 'R', spread 0.05) on a smooth or rough glass
     sphere: GPU FP32 against the oracle's restatement with the same samples (channel
-    choice included): relative RMSE < 3%; and energy: the dispersive image's mean stays
+    choice included): relative RMSE < 1e-4 (measured ~6e-7 smooth, ~1e-6 rough); and energy: the dispersive image's mean stays
     within 5% of the same scene without dispersion (a 0.05 IOR spread moves the caustic,
     not the energy, up to Fresnel changes)."""
     sc = scenes.test_scene(48, 36, subdiv=2, rough_glass=rough, dispersion=0.05)
@@ -241,7 +243,7 @@ def test_dispersion_vs_oracle_same_samples(orc, rough):
     ref = acc / iters
     rel = _rel_rmse(img, ref)
     print(f"dispersion rough={rough}: rel RMSE {rel:.3e}")
-    assert rel < 0.03
+    assert rel < 1e-4
     plain = scenes.test_scene(48, 36, subdiv=2, rough_glass=rough)
     r = Renderer(plain, max_path_length=6, photons_per_iter=200000, seed=seed)
     r.render(6)
