@@ -105,11 +105,24 @@ class Ranks:
             self.dist = None
 
 
-class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+def nvsmi_id(lib) -> str:
+    """nvidia-smi's name for the GPU this process runs on: the PCI bus id of the current
+    CUDA device (nvidia-smi numbers GPUs physically and ignores CUDA_VISIBLE_DEVICES, so
+    a CUDA index would name another GPU whenever the visible list does not start at 0),
+    with the domain widened to the 8 hex digits nvidia-smi prints."""
+    buf = C.create_string_buffer(64)
+    if lib.rc_device_bus_id(buf, 64) != 0:
+        raise RuntimeError("rc_device_bus_id failed")
+    dom, rest = buf.value.decode().split(":", 1)
+    return f"{int(dom, 16):08X}:{rest.upper()}"
 
-    def __init__(self, gpu_index: int):
-        self.gpu = gpu_index
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region (read-only
+    queries of the GPU named by `gpu`, a PCI bus id)."""
+
+    def __init__(self, gpu: str):
+        self.gpu = gpu
         self.proc = None
         self.path = Path(tempfile.mkdtemp()) / "clocks.csv"
 
@@ -248,7 +261,7 @@ def run_ours(args):
     r.render(args.warmup)
     dev = np.zeros(4, np.float64)
     ranks.barrier()
-    with ClockSampler(local) as clk:
+    with ClockSampler(nvsmi_id(lib)) as clk:
         t0 = time.perf_counter()
         # synchronises the library's stream before its first event and after its last
         _native.check(lib.rc_render_timed(args.steps, dev.ctypes.data), "rc_render_timed")

@@ -21,8 +21,11 @@
  *     rays, KD-tree radius query on given photons) that tests use to compare the
  *     GPU kernels with the reference algorithms.
  *
- * All functions are synchronous, not re-entrant (one global scene, as the reference),
- * and return 0 on success or a negative RC_E* code.  No torch types cross this ABI.
+ * All functions are synchronous and return 0 on success or a negative RC_E* code.
+ * A thread that binds no context shares the process's default context, which holds one
+ * scene as the reference's global `scene` does; threads that bind their own contexts
+ * (rc_context_*) hold one scene each and may call concurrently.  No torch types cross
+ * this ABI.
  */
 #ifndef REALCAUSTICS_H
 #define REALCAUSTICS_H
@@ -291,10 +294,25 @@ int rc_gather_query(int variant, int n, const float* positions, int q, const flo
                     int* counts, int* idx, long long cap, long long* total);
 int rc_gather_variants(void);
 
+/* PCI bus id ("domain:bus:device.function") of the CUDA device the calling thread
+ * uses, for tools that address GPUs by bus id (nvidia-smi numbers GPUs physically and
+ * ignores CUDA_VISIBLE_DEVICES).  len >= 13. */
+int rc_device_bus_id(char* out, int len);
+
 /* The GPU-built tree in the reference's node format (8-byte KDTreeNode, heap order,
  * root at 1, src/KD_Tree.h:13-32) for n photon positions; returns the node count in
  * *num_nodes and copies up to cap nodes as (index word, split bits) pairs. */
 int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes, long long cap, long long* num_nodes);
+
+/* Tensor-core self-checks (no counterpart in the reference).  rc_tc_gemm_selftest:
+ * D (128 x N, FP32) = A (128 x K, BF16 bits, row-major) * B (N x K, BF16 bits,
+ * row-major)^T by the tcgen05 primitive the MLP kernels use (K, N multiples of 16,
+ * K <= 128, N <= 256).  rc_tc_wait_selftest: a kernel that allocates TMEM and waits,
+ * `tries` polls at most (1 to 65536), on an mbarrier that nothing completes; the
+ * bounded wait must expire, free the TMEM and return RC_E_TIMEOUT, leaving the context
+ * usable. */
+int rc_tc_gemm_selftest(int K, int N, const unsigned short* A, const unsigned short* B, float* D);
+int rc_tc_wait_selftest(unsigned tries);
 
 /* KD-tree build that allocates no GPU memory, for callers that cannot allocate at
  * the point they need a photon tree (a host application that hands this library only
@@ -305,10 +323,10 @@ int rc_kd_build_nodes(int n, const float* positions, unsigned* nodes, long long 
  * for n), x/y/z/ids = n entries each (photons in tree order).  Working memory is one
  * fixed array inside the library (held by every device that loads it), so n is
  * limited to 524288 photons (RC_E_CAPACITY beyond).  The first call on a device looks
- * up that array's address and should come before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race.  Runs on `stream` (a cudaStream_t, NULL
- * = legacy default stream) and synchronises it before returning; on error the message
- * is in rc_kd_noalloc_last_error(). */
+ * up that array's address.  Calls share the array: calls that overlap on the GPU race.
+ * Runs on `stream` (a cudaStream_t, NULL = legacy default stream) and synchronises it
+ * before returning, so it must not be called while that stream is being captured;
+ * on error the message is in rc_kd_noalloc_last_error(). */
 int rc_kd_build_noalloc(const float* positions4, long long n, unsigned* nodes, long long node_cap,
                         float* x, float* y, float* z, unsigned* ids, void* stream);
 const char* rc_kd_noalloc_last_error(void);

@@ -48,6 +48,9 @@ def lib() -> C.CDLL:
     L.rc_gather_query.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_void_p,
                                   C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_gather_variants.argtypes = []
+    L.rc_device_bus_id.argtypes = [C.c_char_p, C.c_int]
+    L.rc_tc_gemm_selftest.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.rc_tc_wait_selftest.argtypes = [C.c_uint]
     L.rc_camera_queries.argtypes = [C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_kd_build_nodes.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_render_timed.argtypes = [C.c_int, C.c_void_p]
@@ -82,4 +85,5 @@ EXPORTS = ["init", "main", "rc_default_config", "rc_set_config", "rc_prepare", "
            "rc_kd_noalloc_last_error", "rc_proposal_state", "rc_render_debug",
            "rc_save_state", "rc_load_state", "rc_scene_dump", "rc_prepare_stats",
            "rc_context_create", "rc_context_bind", "rc_context_destroy", "rc_gather_query",
-           "rc_gather_variants", "rc_camera_queries"]
+           "rc_gather_variants", "rc_camera_queries", "rc_device_bus_id", "rc_tc_gemm_selftest",
+           "rc_tc_wait_selftest"]

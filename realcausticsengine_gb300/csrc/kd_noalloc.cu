@@ -11,12 +11,12 @@
 // The array (`g_kd_scratch`) is a file-scope __device__ object: every GPU that loads
 // the library holds it until the process exits.  Host code cannot use its name as a
 // device address, so the first call on each device, with that device current, looks
-// the address up with cudaGetSymbolAddress and caches it.  Because that lookup may
-// initialise the module, make the first call on a device before any stream capture.
-// All calls share the array and it keeps the previous call's contents; the build
-// clears every part it reads before using it.  Calls whose work overlaps on the GPU
-// (concurrent streams, or threads sharing a device) race on the array and must be
-// serialised by the caller.
+// the address up with cudaGetSymbolAddress and caches it.  Every call reads an error
+// flag back and synchronises its stream before returning, so no call may be issued
+// while that stream is being captured into a CUDA graph.  All calls share the array
+// and it keeps the previous call's contents; the build clears every part it reads
+// before using it.  Calls whose work overlaps on the GPU (concurrent streams, or
+// threads sharing a device) race on the array and must be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -79,6 +79,9 @@ extern "C" int rc_kd_build_noalloc(const float* positions4, long long n, unsigne
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int* err = g_error_ptr[dev];
+    // a launch error left by an earlier, unrelated call would otherwise be reported as
+    // this call's
+    (void)cudaGetLastError();
     if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return fail(RC_E_CUDA, "cudaMemsetAsync failed");
     KdTree tree;
     tree.nodes = reinterpret_cast<uint2*>(nodes);

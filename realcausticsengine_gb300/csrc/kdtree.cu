@@ -15,6 +15,7 @@
 // sort along x, y and z (key, then local index), then stable splits of the three
 // lists per level, writing nodes and final order.
 #include "kdtree.cuh"
+#include "dev_once.h"
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -755,10 +756,10 @@ int kd_build(const float4* pos4, long long n, KdTree& tree, void* scratch, size_
         nl++;
     }
     size_t smem = SmemLayout::total;
-    // once per process: later builds may be recorded into a CUDA graph, and contexts on
+    // once per device: later builds may be recorded into a CUDA graph, and contexts on
     // several threads build concurrently
-    static std::once_flag attr_set;
-    std::call_once(attr_set, [&] { cudaFuncSetAttribute(k_smem_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
+    static std::once_flag attr_set[kOnceDevices];
+    once_per_device(attr_set, [&] { cudaFuncSetAttribute(k_smem_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
     k_smem_build<<<(unsigned)(1LL << l0), kSmemThreads, smem, stream>>>(B, cur, l0, n, tree.nodes);
     nl++;
     if (launches) *launches = nl;

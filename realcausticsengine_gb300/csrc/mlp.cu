@@ -4,6 +4,7 @@
 #include "proposal.cuh"
 #include "tc_gemm.cuh"
 #include "rng.cuh"
+#include "dev_once.h"
 
 #include <algorithm>
 #include <cmath>
@@ -736,8 +737,8 @@ int mlp_forward_batch(const MlpParams& p, MlpBatch& b, cudaStream_t s, int* err)
     if (b.n <= 0) return 0;
     BatchIO io{b.pos, b.out};
     const size_t smem = SmemFwd::total;
-    static std::once_flag attr;   // once per process (contexts on several threads launch)
-    std::call_once(attr, [&] { cudaFuncSetAttribute(k_mlp_forward<BatchIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
+    static std::once_flag attr[kOnceDevices];   // once per device (contexts on several threads launch)
+    once_per_device(attr, [&] { cudaFuncSetAttribute(k_mlp_forward<BatchIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
     const long long tiles = (b.n + 127) / 128;
     const int grid = (int)(tiles < forward_blocks() ? tiles : forward_blocks());
     k_mlp_forward<BatchIO><<<grid, 128, smem, s>>>(p, io, b.n, err);
@@ -748,8 +749,8 @@ int mlp_proposal(const MlpParams& p, const ProposalCtx& c, long long n, float4* 
     if (n <= 0) return 0;
     ProposalIO io{c, prop};
     const size_t smem = SmemFwd::total;
-    static std::once_flag attr;   // once per process (contexts on several threads launch)
-    std::call_once(attr, [&] { cudaFuncSetAttribute(k_mlp_forward<ProposalIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
+    static std::once_flag attr[kOnceDevices];   // once per device (contexts on several threads launch)
+    once_per_device(attr, [&] { cudaFuncSetAttribute(k_mlp_forward<ProposalIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
     const long long tiles = (n + 127) / 128;
     const int grid = (int)(tiles < forward_blocks() ? tiles : forward_blocks());
     k_mlp_forward<ProposalIO><<<grid, 128, smem, s>>>(p, io, n, err);
@@ -761,8 +762,8 @@ int mlp_proposal_table(const MlpParams& p, const ProposalCtx& c, int res, float*
     if (n <= 0) return 0;
     TableIO io{c, res, cells};
     const size_t smem = SmemFwd::total;
-    static std::once_flag attr;   // once per process (contexts on several threads launch)
-    std::call_once(attr, [&] { cudaFuncSetAttribute(k_mlp_forward<TableIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
+    static std::once_flag attr[kOnceDevices];   // once per device (contexts on several threads launch)
+    once_per_device(attr, [&] { cudaFuncSetAttribute(k_mlp_forward<TableIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
     const long long tiles = (n + 127) / 128;
     const int grid = (int)(tiles < forward_blocks() ? tiles : forward_blocks());
     k_mlp_forward<TableIO><<<grid, 128, smem, s>>>(p, io, n, err);
@@ -786,8 +787,8 @@ int mlp_train_step(MlpParams& p, MlpBatch& b, const float4* pos4, const float4* 
                    cudaStream_t s, int* err) {
     if (n <= 0) return 0;
     const size_t smem = SmemTrain::total;
-    static std::once_flag attr;   // once per process (contexts on several threads launch)
-    std::call_once(attr, [&] { cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
+    static std::once_flag attr[kOnceDevices];   // once per device (contexts on several threads launch)
+    once_per_device(attr, [&] { cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
     const int total = (int)mlp_param_floats();
     const int tiles = (n + 127) / 128;
     const int grid = std::min(std::min(tiles, sm_count()), b.part_rows);

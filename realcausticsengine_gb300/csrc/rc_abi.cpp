@@ -1815,6 +1815,14 @@ static int kd_build_host(int n, const float* positions, DevBuf<float4>& pos, Dev
 
 int rc_gather_variants(void) { return gather_variants(); }
 
+int rc_device_bus_id(char* out, int len) {
+    if (!out || len < 13) { ctx().err = "bus id buffer too small"; return RC_E_INVALID; }
+    int dev = 0;
+    RC_CUDA(cudaGetDevice(&dev));
+    RC_CUDA(cudaDeviceGetPCIBusId(out, len, dev));
+    return RC_OK;
+}
+
 int rc_gather_query(int variant, int n, const float* positions, int q, const float* queries, float r2, int* counts,
                     int* idx, long long cap, long long* total) {
     if (n < 0 || q < 0 || (n > 0 && !positions) || (q > 0 && (!queries || !counts))) { ctx().err = "bad KD arrays"; return RC_E_INVALID; }

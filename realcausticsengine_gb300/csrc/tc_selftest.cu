@@ -60,8 +60,48 @@ __global__ void __launch_bounds__(128) k_tc_selftest(const __nv_bfloat16* __rest
     if (warp == 0) tc::tmem_dealloc(d_tmem, 256);
 }
 
+// The timeout path of the bounded mbarrier wait that every tcgen05 kernel here uses:
+// TMEM is allocated as in those kernels, no MMA is issued and nothing ever arrives on
+// the barrier, so the wait must give up after `tries` polls, record the expiry and free
+// the TMEM, leaving the context usable.
+__global__ void __launch_bounds__(128) k_wait_selftest(uint32_t tries, int* err) {
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    if (warp == 0) tc::tmem_alloc(&tmem_base, 32);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t d_tmem = tmem_base;
+    const bool ok = tc::mbar_wait(&mbar, 0, tries);
+    if (!ok && tid == 0) atomicOr(err, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(d_tmem, 32);
+}
+
 }  // namespace
 }  // namespace rc
+
+// Test hook: a bounded mbarrier wait that nothing completes, `tries` polls long (1 to
+// 2^16).  Returns RC_E_TIMEOUT when the wait expired as it must (RC_OK would mean the
+// barrier completed without an arrival).  No counterpart in the reference.
+extern "C" int rc_tc_wait_selftest(unsigned tries) {
+    if (tries < 1 || tries > (1u << 16)) return RC_E_INVALID;
+    int* dErr = nullptr;
+    if (cudaMalloc(&dErr, sizeof(int)) != cudaSuccess) return RC_E_CUDA;
+    int rc = RC_OK;
+    cudaMemset(dErr, 0, sizeof(int));
+    rc::k_wait_selftest<<<1, 128>>>(tries, dErr);
+    cudaError_t e = cudaDeviceSynchronize();
+    int h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, dErr, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = RC_E_CUDA;
+    else if (h) rc = RC_E_TIMEOUT;
+    cudaFree(dErr);
+    return rc;
+}
 
 // Test hook: D (128 x N, FP32) = A (128 x K, BF16 bits, row-major) * B (N x K, BF16
 // bits, row-major)^T on the tensor cores.  K in {16, 32, ..., 128}, N in {16, ..., 256}

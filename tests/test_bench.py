@@ -48,7 +48,12 @@ class FakeLib:
             out[0], out[1], out[2], out[3] = self.DEVICE_MS, self.GATHER_MS, self.GATHER_BYTES, self.LAUNCHES
             return 0
 
+        def bus_id(buf, n):
+            C.memmove(buf, b"0000:1b:00.0\0", 13)
+            return 0
+
         self.rc_render_timed = _Fn(timed)
+        self.rc_device_bus_id = _Fn(bus_id)
         for name in ("rc_default_config", "rc_set_config", "rc_prepare", "rc_render", "rc_read_image",
                      "rc_release"):
             setattr(self, name, record(name))
@@ -175,3 +180,10 @@ def test_reference_arm_other_ranks_do_no_work(monkeypatch, capsys):
     monkeypatch.setattr(bench, "cpu_baseline", lambda **kw: pytest.fail("rank 1 ran the CPU baseline"))
     bench.run_reference(bench.parse_args(["--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0"]))
     assert capsys.readouterr().out == ""
+
+
+def test_clock_sampler_names_the_gpu_by_bus_id():
+    """nvidia-smi numbers GPUs physically: the sampler must name the CUDA device the
+    process runs on by its PCI bus id, in nvidia-smi's 8-digit-domain form."""
+    import bench
+    assert bench.nvsmi_id(FakeLib()) == "00000000:1B:00.0"

@@ -36,3 +36,18 @@ def test_tc_gemm_matches_host(K, N):
     want = a @ b.T
     scale = np.abs(a) @ np.abs(b).T
     assert np.all(np.abs(D - want) <= 1e-5 * scale + 1e-6), np.abs(D - want).max()
+
+
+def test_bounded_wait_expires_and_context_survives():
+    """A bounded mbarrier wait that nothing completes (no MMA in flight) must expire,
+    free its TMEM and report RC_E_TIMEOUT; the next tensor-core launch must work."""
+    lib = _native.lib()
+    assert lib.rc_tc_wait_selftest(2048) == -6
+    assert lib.rc_tc_wait_selftest(1) == -6
+    rng = np.random.default_rng(5)
+    A = to_bf16_bits(rng.normal(size=(128, 16)))
+    B = to_bf16_bits(rng.normal(size=(16, 16)))
+    D = np.zeros((128, 16), np.float32)
+    assert lib.rc_tc_gemm_selftest(16, 16, A.ctypes.data, B.ctypes.data, D.ctypes.data) == 0
+    want = bf16_bits_to_f32(A).astype(np.float64) @ bf16_bits_to_f32(B).astype(np.float64).T
+    assert np.abs(D - want).max() < 1e-3

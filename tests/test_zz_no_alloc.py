@@ -60,6 +60,25 @@ def test_noalloc_kd_build_matches_allocating_entry_point():
         assert (x == pos[ids, 0]).all() and (y == pos[ids, 1]).all() and (z == pos[ids, 2]).all()
 
 
+def test_noalloc_small_counts_match_allocating_entry_point():
+    """The early returns and the smallest scratch layouts: no photons, one, two, three,
+    and a count just above one on-chip subtree (1025)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    rng = np.random.default_rng(7)
+    for n in (0, 1, 2, 1025, 3):
+        pos = np.stack([rng.permutation(np.linspace(-1, 1, max(n, 1), dtype=np.float32))[:n] for _ in range(3)], 1)
+        pos = pos.reshape(n, 3)
+        nodes, x, y, z, ids = _call_noalloc(torch, pos)
+        if n == 0:
+            continue
+        want = kd_build_nodes(pos)
+        assert (nodes[: len(want)] == want).all(), f"node arrays differ for n={n}"
+        assert (np.sort(ids) == np.arange(n, dtype=np.uint32)).all()
+        assert (x == pos[ids, 0]).all() and (y == pos[ids, 1]).all() and (z == pos[ids, 2]).all()
+
+
 def test_noalloc_rejects_counts_beyond_fixed_scratch():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
