@@ -471,9 +471,10 @@ def run_batch(args):
     line = {"metric": METRIC, "value": total_paths / (t2 - t1), "unit": METRIC, "n_gpus": 1,
             "steps": args.steps, "warmup": 0, "ms_per_step": (t2 - t1) * 1000.0 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"batch of {args.batch} scenes: height fields of log-uniform [1k, 2M] triangles, "
-                                   "IOR U(1.3,1.8), roughness U(0,0.1), 1-4 area lights, log-uniform [256k, 8M] "
-                                   "photons/iter, 512x512", "total_triangles": tris, "host_threads": T,
+            "config": {"workload": f"batch of {args.batch} scenes: displaced glass spheres (vertex noise amplitude "
+                                   "U(0,0.2)) of log-uniform [1k, 2M] triangles, IOR U(1.3,1.8), roughness U(0,0.1), "
+                                   "over a diffuse plane, 1-4 point/area lights, log-uniform [256k, 8M] photons/iter, "
+                                   "512x512", "total_triangles": tris, "host_threads": T,
                        "contexts": len(batch)},
             "e2e": {"value": total_paths / (t3 - t0), "unit": METRIC, "wall_s": t3 - t0,
                     "load_s": t1 - t0, "render_s": t2 - t1, "read_s": t3 - t2},

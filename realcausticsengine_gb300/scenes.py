@@ -286,29 +286,81 @@ def gem_cluster(width=3840, height=2160, n_gems=2000, groups=1, seed=0, dispersi
                  name="gem_cluster")
 
 
+def geodesic_sphere(freq: int):
+    """Unit sphere from the icosahedron with every face cut into freq^2 triangles
+    (20 freq^2 in all), vertices shared between faces."""
+    V0, _, F0 = icosphere(0, 1.0)
+    V0 = V0.astype(np.float64)
+    V0 /= np.linalg.norm(V0, axis=1, keepdims=True)
+    i, j = np.meshgrid(np.arange(freq + 1), np.arange(freq + 1), indexing="ij")
+    keep = i + j <= freq
+    i, j = i[keep], j[keep]
+    index = -np.ones((freq + 1, freq + 1), np.int64)
+    index[i, j] = np.arange(len(i))
+    # the triangles of one face in local (i, j) grid indices
+    ti, tj = np.meshgrid(np.arange(freq), np.arange(freq), indexing="ij")
+    up = ti + tj < freq
+    down = ti + tj < freq - 1
+    local = np.concatenate([
+        np.stack([index[ti[up], tj[up]], index[ti[up] + 1, tj[up]], index[ti[up], tj[up] + 1]], 1),
+        np.stack([index[ti[down] + 1, tj[down]], index[ti[down] + 1, tj[down] + 1], index[ti[down], tj[down] + 1]], 1)])
+    Vs, Fs = [], []
+    for f, (a_, b_, c_) in enumerate(F0):
+        A, B, C = V0[a_], V0[b_], V0[c_]
+        P = (A[None] * (freq - i - j)[:, None] + B[None] * i[:, None] + C[None] * j[:, None]) / freq
+        Vs.append(P / np.linalg.norm(P, axis=1, keepdims=True))
+        Fs.append(local + f * len(i))
+    V = np.concatenate(Vs)
+    F = np.concatenate(Fs)
+    # weld the copies of edge and corner vertices
+    key = np.round(V * 1e7).astype(np.int64)
+    _, first, inv = np.unique(key, axis=0, return_index=True, return_inverse=True)
+    return V[first], inv.reshape(-1)[F]
+
+
+def displaced_glass_sphere(rng, tris: float, amplitude: float, radius: float = 1.0):
+    """Geodesic sphere of about `tris` triangles whose vertices move along the normal by
+    amplitude x a smooth noise in [-1, 1] (a sum of 6 random sinusoids of the unit
+    position); smooth normals from the displaced faces."""
+    freq = max(2, int(round(np.sqrt(tris / 20.0))))
+    U, F = geodesic_sphere(freq)
+    k = rng.normal(size=(6, 3)) * rng.uniform(2.0, 6.0, (6, 1))
+    ph = rng.uniform(0, 2 * np.pi, 6)
+    noise = np.sin(U @ k.T + ph).sum(1)
+    noise /= max(np.abs(noise).max(), 1e-12)
+    V = U * (radius * (1.0 + amplitude * noise))[:, None]
+    fn = np.cross(V[F[:, 1]] - V[F[:, 0]], V[F[:, 2]] - V[F[:, 0]])
+    N = np.zeros_like(V)
+    for c in range(3):
+        np.add.at(N, F[:, c], fn)
+    return V.astype(np.float32), _normals_i16(N), F.astype(np.uint32)
+
+
 def batch_scene(seed: int, width=512, height=512):
-    """One scene of the 64-scene batch: a refracting height field of log-uniform
-    [1k, 2M] triangles, IOR U(1.3, 1.8), roughness U(0, 0.1), over a diffuse floor, lit
-    by 1-4 area lights; photons per iteration log-uniform [256k, 8M].
-    Returns (scene, photons_per_iter)."""
+    """One scene of the 64-scene batch: a displaced glass sphere (vertex noise amplitude
+    U(0, 0.2)) of log-uniform [1k, 2M] triangles, IOR U(1.3, 1.8), roughness U(0, 0.1),
+    over a diffuse plane, lit by 1-4 lights, each a point or an area light; photons per
+    iteration log-uniform [256k, 8M], 512x512.  Returns (scene, photons_per_iter)."""
     rng = np.random.default_rng(1000 + seed)
     tris = float(np.exp(rng.uniform(np.log(1e3), np.log(2e6))))
-    grid = max(4, int(round(np.sqrt(tris / 2.0))) + 1)
     photons = int(np.exp(rng.uniform(np.log(256 * 1024), np.log(8 * 1024 * 1024))))
-    mats = [Material("R", color=(1, 1, 1), ior=float(rng.uniform(1.3, 1.8)), roughness=float(rng.uniform(0.0, 0.1))),
+    roughness = float(rng.uniform(0.0, 0.1))
+    mats = [Material("R", color=(1, 1, 1), ior=float(rng.uniform(1.3, 1.8)), roughness=roughness),
             Material("P", color=(0.8, 0.8, 0.8), roughness=1.0, specular=0.0)]
-    Vw, Nw, Fw = water_heightfield(grid, size=6.0, waves=16, seed=seed)
-    Vf, Nf, Ff = plane(6.0, -1.0)
-    meshes = [_mesh(Vw, Nw, Fw, 0), _mesh(Vf, Nf, Ff, 1)]
+    Vs, Ns, Fs = displaced_glass_sphere(rng, tris, float(rng.uniform(0.0, 0.2)))
+    Vp, Np, Fp = plane(8.0, 0.0)
+    meshes = [_mesh(Vs, Ns, Fs, 0, translate(0.0, 0.0, 1.4)), _mesh(Vp, Np, Fp, 1)]
     lights = []
     for i in range(int(rng.integers(1, 5))):
-        w = float(rng.uniform(0.5, 2.0))
-        lights.append(Light("A", color=tuple(float(c) for c in rng.uniform(0.6, 1.0, 3)),
-                            position=(float(rng.uniform(-1.5, 1.5)), float(rng.uniform(-1.5, 1.5)),
-                                      float(rng.uniform(3.0, 5.0))),
-                            width=w, height=w, power=float(rng.uniform(10.0, 30.0))))
-    cam = look_at_camera(width, height, (0.0, -4.5, 3.5), (0.0, 0.0, -1.0), (0, 0, 1), 50.0)
-    sc = Scene(meshes, mats, lights, cam, samples=4, base_radius=0.002, radius_reduction=0.75, name=f"batch{seed}")
+        col = tuple(float(c) for c in rng.uniform(0.6, 1.0, 3))
+        pos = (float(rng.uniform(-1.5, 1.5)), float(rng.uniform(-1.5, 1.5)), float(rng.uniform(4.0, 6.0)))
+        if rng.uniform() < 0.5:
+            lights.append(Light("P", color=col, position=pos, power=float(rng.uniform(15.0, 40.0))))
+        else:
+            w = float(rng.uniform(0.5, 2.0))
+            lights.append(Light("A", color=col, position=pos, width=w, height=w, power=float(rng.uniform(10.0, 30.0))))
+    cam = look_at_camera(width, height, (0.0, -5.0, 4.0), (0.0, 0.0, 0.6), (0, 0, 1), 45.0)
+    sc = Scene(meshes, mats, lights, cam, samples=4, base_radius=0.004, radius_reduction=0.75, name=f"batch{seed}")
     return sc, photons
 
 
