@@ -372,58 +372,73 @@ def same_config_anchor(cpu: dict | None, width: int = 960, height: int = 540, st
     return res
 
 
-def learned_equal_time(args, iters: int = 16, ref_iters: int = 48):
-    """Learned-guided vs plain vertex merging on the same workload, per-pixel RMSE of the
-    FP64-accumulated image against a reference image, as a function of device time.
+def learned_equal_time(args, iters: int = 16, ref_iters: int = 256, ref_scale: int = 8):
+    """Learned-guided vs plain vertex merging on the same workload: per-pixel RMSE of the
+    FP64-accumulated image against two reference images, as a function of device time.
 
-    Reference: plain, `ref_iters` iterations, independent light and camera seeds.  Plain
-    and learned share their seeds (camera paths identical between them, not with the
-    reference); learned trains on iterations 0..7 (64 Adam steps each, lr 1e-3) and
-    guides from iteration 1.  Reports both curves' end points, the learned RMSE at the
-    plain run's total device time, and the device-time ratio to reach the plain run's
-    final RMSE (None when the learned run does not reach it in `iters` iterations)."""
+      full         reference: plain, `ref_iters` iterations, independent light and camera
+                   seeds (its variance ~1/16 of a 16-iteration render's): the whole
+                   image error, camera-side noise (pixel jitter, camera paths through the
+                   rough water) included.
+      photon_side  reference: plain with the same camera seed and iterations as the
+                   compared renders (the same camera paths and merge queries) and
+                   `ref_scale` x the light paths per iteration: the error of the photon
+                   side of the estimator alone, the part an emission proposal can change.
+
+    Plain and learned share their camera seed.  The learned render trains on
+    iterations 0..7 (32 Adam steps each, lr 1e-3) and guides from iteration 1, with the
+    workload's light paths per iteration and with half of them (the same number of
+    stored photons as plain, since guided paths store about twice as many).  Reports the
+    end points, and the device-time ratio at which each learned curve reaches plain's
+    final error (None when it does not within `iters` iterations)."""
     from realcausticsengine_gb300 import scenes
     from realcausticsengine_gb300.session import Renderer
 
     sc = scenes.water_pool(args.width, args.height, grid=args.grid, samples=ref_iters)
 
-    def run(n, seed, camera_seed, learned, ref=None):
-        r = Renderer(sc, max_path_length=MAX_PATH, photons_per_iter=args.photons, seed=seed, camera_seed=camera_seed,
-                     learned_proposal=learned, train_iterations=8, train_steps=64, learning_rate=1e-3)
+    def run(n, seed, camera_seed, learned, refs=(), paths=None):
+        r = Renderer(sc, max_path_length=MAX_PATH, photons_per_iter=paths or args.photons, seed=seed,
+                     camera_seed=camera_seed, learned_proposal=learned, train_iterations=8, train_steps=32,
+                     learning_rate=1e-3)
         r.prepare()
-        t, curve = 0.0, []
+        if not refs:
+            r.render(n)
+            img = r.image().astype(np.float64)
+            r.release()
+            return img, None
+        t, curves = 0.0, [[] for _ in refs]
         for _ in range(n):
             r.render(1)
             t += r.stats()["device_ms"]
-            if ref is not None:
-                img = r.image().astype(np.float64)
-                curve.append((t, float(np.sqrt(((img - ref) ** 2).mean()))))
-        img = r.image().astype(np.float64)
+            img = r.image().astype(np.float64)
+            for c, ref in zip(curves, refs):
+                c.append((t, float(np.sqrt(((img - ref) ** 2).mean()))))
         r.release()
-        return img, curve
+        return img, curves
 
-    ref, _ = run(ref_iters, 1001, 1002, False)
-    _, plain = run(iters, 7, 8, False, ref)
-    _, learned = run(iters, 7, 8, True, ref)
-    t_plain, e_plain = plain[-1]
+    ref_full, _ = run(ref_iters, 1001, 1002, False)
+    ref_cam, _ = run(iters, 1001, 8, False, paths=ref_scale * args.photons)
+    _, (plain_full, plain_cam) = run(iters, 7, 8, False, (ref_full, ref_cam))
 
-    def at_time(curve, t):
-        prev = None
-        for tc_, e in curve:
-            if tc_ > t:
-                return prev
-            prev = e
-        return prev
+    def reach(curve, target):
+        return next((t for t, e in curve if e <= target), None)
 
-    reach = next((tc_ for tc_, e in learned if e <= e_plain), None)
-    return {"workload": "same as the line's config; reference image: plain, "
-                        f"{ref_iters} iterations, independent seeds, FP64 accumulation",
-            "iterations": iters, "plain_rmse": e_plain, "plain_device_ms": t_plain,
-            "learned_rmse": learned[-1][1], "learned_device_ms": learned[-1][0],
-            "learned_rmse_at_plain_time": at_time(learned, t_plain),
-            "time_ratio_to_plain_rmse": (reach / t_plain) if reach is not None else None,
-            "curve_plain": [(round(a, 2), round(b, 6)) for a, b in plain],
-            "curve_learned": [(round(a, 2), round(b, 6)) for a, b in learned]}
+    out = {"workload": "same as the line's config", "iterations": iters,
+           "references": {"full": f"plain, {ref_iters} iterations, independent light and camera seeds",
+                          "photon_side": f"plain, same camera seed and iterations, {ref_scale}x light paths"},
+           "plain": {"device_ms": plain_full[-1][0], "rmse_full": plain_full[-1][1], "rmse_photon_side": plain_cam[-1][1]}}
+    for label, paths in (("learned", args.photons), ("learned_half_paths", args.photons // 2)):
+        _, (lf, lc) = run(iters, 7, 8, True, (ref_full, ref_cam), paths)
+        rf, rc = reach(lf, plain_full[-1][1]), reach(lc, plain_cam[-1][1])
+        out[label] = {"light_paths_per_iter": paths, "device_ms": lf[-1][0], "rmse_full": lf[-1][1],
+                      "rmse_photon_side": lc[-1][1],
+                      "time_ratio_full": rf / plain_full[-1][0] if rf is not None else None,
+                      "time_ratio_photon_side": rc / plain_cam[-1][0] if rc is not None else None,
+                      "curve_full": [(round(a, 2), round(b, 6)) for a, b in lf]}
+    out["plain"]["curve_full"] = [(round(a, 2), round(b, 6)) for a, b in plain_full]
+    ratios = [out[k]["time_ratio_full"] for k in ("learned", "learned_half_paths") if out[k]["time_ratio_full"]]
+    out["time_ratio_to_plain_rmse"] = min(ratios) if ratios else None
+    return out
 
 
 def run_batch(args):

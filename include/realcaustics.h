@@ -244,11 +244,12 @@ int rc_load_state(const char* path);
  * init() got debug_test 2-4. */
 int rc_render_debug(int mode);
 
-/* Learned-proposal state of the last rendered iteration (no counterpart in the
- * reference): for the first n light paths, prop4 = [direction xyz, p_light / q] (zeros
- * before the network has been trained once) and contrib = the sum over the path's
- * merges of the squared luminance each adds to its pixel (recorded during training
- * iterations only).  Either output may be NULL. */
+/* Learned-proposal state (no counterpart in the reference): for the first n light
+ * paths of the last rendered iteration, prop4 = [direction xyz, p_light / q] as drawn
+ * with those paths' samples from the network's current 32 x 32-cell table (the draw the
+ * light pass makes; zeros before the network has been trained once), and contrib = the
+ * sum over the path's merges of the squared luminance each adds to its pixel (recorded
+ * during training iterations only).  Either output may be NULL. */
 int rc_proposal_state(long long n, float* prop4, float* contrib);
 
 /* ---- parity hooks (device kernels on caller-chosen inputs) ---- */

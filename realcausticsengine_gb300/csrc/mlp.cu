@@ -206,73 +206,6 @@ struct BatchIO {
 };
 
 // ----------------------------------------------------------------------------- proposal
-struct ProposalIO {
-    struct State {
-        int light;
-        float u3, u4, xi;
-    };
-    ProposalCtx c;
-    float4* prop;
-    __device__ __forceinline__ void input(long long row, bool valid, float* x, State& st) const {
-        if (!valid) {
-#pragma unroll
-            for (int i = 0; i < kMlpIn; ++i) x[i] = 0.0f;
-            return;
-        }
-        PathRng g;
-        g.init(c.seed, (uint64_t)row, c.iteration, STREAM_LIGHT);
-        const U4 b0 = g.block(0), b1 = g.block(1);
-        const LightSample ls = light_position(c.lights, u01(b0.a), u01(b0.b), u01(b0.c));
-        st.light = ls.idx;
-        st.u3 = u01(b0.d);
-        st.u4 = u01(b1.a);
-        st.xi = u01(b1.b);
-        encode((ls.o.x - c.bmin[0]) * c.binv[0], (ls.o.y - c.bmin[1]) * c.binv[1], (ls.o.z - c.bmin[2]) * c.binv[2], x);
-    }
-    __device__ __forceinline__ void output(long long row, bool valid, const float* o, const State& st) const {
-        if (!valid) return;
-        const DevLight& l = c.lights.lights[st.light];
-        if (l.type == LIGHT_SUN) { prop[row] = make_float4(l.fz[0], l.fz[1], l.fz[2], 1.0f); return; }
-        // mixture over the 80 outputs with static indexing only (keeps them in registers)
-        float mxl = -INFINITY;
-#pragma unroll
-        for (int k = 0; k < kMlpLobes; ++k) mxl = fmaxf(mxl, o[5 * k]);
-        float e[kMlpLobes], sum = 0.0f;
-#pragma unroll
-        for (int k = 0; k < kMlpLobes; ++k) { e[k] = __expf(o[5 * k] - mxl); sum += e[k]; }
-        F3 w;
-        if (st.xi < kMlpDefensive) {
-            w = light_direction(l, st.u3, st.u4);
-        } else {
-            const float t = (st.xi - kMlpDefensive) / (1.0f - kMlpDefensive) * sum;
-            float cum = 0.0f, kap = 1.0f;
-            F3 mu = f3(0.0f, 0.0f, 1.0f);
-            bool chosen = false;
-#pragma unroll
-            for (int k = 0; k < kMlpLobes; ++k) {
-                cum += e[k];
-                if (!chosen && (t < cum || k == kMlpLobes - 1)) {
-                    chosen = true;
-                    const float x = o[5 * k + 1], y = o[5 * k + 2], z = o[5 * k + 3];
-                    const float len = fmaxf(sqrtf(x * x + y * y + z * z), 1e-6f);
-                    mu = f3(x / len, y / len, z / len);
-                    kap = kappa_of(o[5 * k + 4]);
-                }
-            }
-            w = sample_vmf(mu, kap, st.u3, st.u4);
-        }
-        const float pl = light_direction_pdf(l, w);
-        float S = 0.0f;
-#pragma unroll
-        for (int k = 0; k < kMlpLobes; ++k) {
-            const float x = o[5 * k + 1], y = o[5 * k + 2], z = o[5 * k + 3];
-            const float rl = rsqrtf(fmaxf(x * x + y * y + z * z, 1e-12f));
-            S += e[k] * vmf_pdf_fast(kappa_of(o[5 * k + 4]), (x * w.x + y * w.y + z * w.z) * rl);
-        }
-        const float q = kMlpDefensive * pl + (1.0f - kMlpDefensive) * (S / sum);
-        prop[row] = make_float4(w.x, w.y, w.z, (pl > 0.0f && q > 0.0f) ? pl / q : 0.0f);
-    }
-};
 
 // The tabulated proposal (proposal.cuh): one row per (light, cell); the cell centre's
 // position in, the mixture (cumulative lobe weights, unit means, concentrations) out.
@@ -745,15 +678,39 @@ int mlp_forward_batch(const MlpParams& p, MlpBatch& b, cudaStream_t s, int* err)
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int mlp_proposal(const MlpParams& p, const ProposalCtx& c, long long n, float4* prop, cudaStream_t s, int* err) {
+// Per light path, the tabulated proposal's direction and weight p_light / q, from the
+// path's own Philox samples: light and area coordinates from block 0 (a, b, c), the
+// direction samples the plain path uses (block 0 d, block 1 a) and a sample the plain
+// path leaves unused (block 1 b) for the mixture component.  Paths are taken in
+// `order` (when given), so that neighbouring threads read the same table cells.
+__global__ void k_table_proposal(const ProposalCtx c, const float* __restrict__ cells, int res, long long n,
+                                 const uint32_t* __restrict__ order, float4* __restrict__ prop) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const long long i = order ? (long long)__ldg(&order[t]) : t;
+    PathRng g;
+    g.init(c.seed, (uint64_t)i, c.iteration, STREAM_LIGHT);
+    const U4 b0 = g.block(0), b1 = g.block(1);
+    const LightSample ls = light_position(c.lights, u01(b0.a), u01(b0.b), u01(b0.c));
+    const DevLight& l = c.lights.lights[ls.idx];
+    if (l.type == LIGHT_SUN) { prop[i] = make_float4(l.fz[0], l.fz[1], l.fz[2], 1.0f); return; }
+    F3 w;
+    const float ratio = table_direction(ProposalTable{cells, res}, l, ls.idx, u01(b0.b), u01(b0.c), u01(b0.d),
+                                        u01(b1.a), u01(b1.b), w);
+    prop[i] = make_float4(w.x, w.y, w.z, ratio);
+}
+
+int mlp_proposal(const MlpParams& p, const ProposalCtx& c, int res, float* cells, long long n, float4* prop,
+                 cudaStream_t s, int* err) {
     if (n <= 0) return 0;
-    ProposalIO io{c, prop};
-    const size_t smem = SmemFwd::total;
-    static std::once_flag attr[kOnceDevices];   // once per device (contexts on several threads launch)
-    once_per_device(attr, [&] { cudaFuncSetAttribute(k_mlp_forward<ProposalIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
-    const long long tiles = (n + 127) / 128;
-    const int grid = (int)(tiles < forward_blocks() ? tiles : forward_blocks());
-    k_mlp_forward<ProposalIO><<<grid, 128, smem, s>>>(p, io, n, err);
+    if (mlp_proposal_table(p, c, res, cells, s, err)) return -1;
+    return mlp_proposal_draw(c, res, cells, n, nullptr, prop, s);
+}
+
+int mlp_proposal_draw(const ProposalCtx& c, int res, const float* cells, long long n, const uint32_t* order,
+                      float4* prop, cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_table_proposal<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c, cells, res, n, order, prop);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

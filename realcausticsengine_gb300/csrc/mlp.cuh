@@ -80,10 +80,20 @@ struct ProposalCtx {
 };
 
 size_t mlp_param_floats();
-int mlp_proposal(const MlpParams& p, const ProposalCtx& c, long long n, float4* prop, cudaStream_t s, int* err);
-// The tabulated proposal for the Metropolis samplers (proposal.cuh): the mixture at the
-// centres of res x res cells per light, written to cells (lights x res x res x 80 floats).
+// The tabulated proposal (proposal.cuh): the mixture at the centres of res x res cells
+// per light, written to cells (lights x res x res x 80 floats) by the tensor-core forward
+// kernel.  The Metropolis samplers draw from it directly.
 int mlp_proposal_table(const MlpParams& p, const ProposalCtx& c, int res, float* cells, cudaStream_t s, int* err);
+// Emission of n uniformly sampled light paths from the same tabulated proposal: the
+// table (into cells), then per path prop[i] = (direction, p_light / q) drawn with the
+// path's own samples; the light pass, the light-path order and the training collection
+// read prop.
+int mlp_proposal(const MlpParams& p, const ProposalCtx& c, int res, float* cells, long long n, float4* prop,
+                 cudaStream_t s, int* err);
+// The per-path draw alone, from a table already in cells, over the paths in `order`
+// (nullptr: index order).
+int mlp_proposal_draw(const ProposalCtx& c, int res, const float* cells, long long n, const uint32_t* order,
+                      float4* prop, cudaStream_t s);
 // Training samples from the light paths that contributed to the image (contrib > 0,
 // contrib = the gather's per-path sum of squared per-merge luminance):
 // pos4 = (normalised emission position, p_light(dir)), dir4 = (dir, sqrt(contrib)),

@@ -535,11 +535,16 @@ int proposal_before(const HostScene& sc, VMParams& p, bool train) {
         RC_CUDA(d.train_count.reserve(1)); RC_CUDA(d.train_wsum.reserve(1));
     }
     if (d.mlp_rounds > 0) {
-        RC_CUDA(d.prop.reserve(std::max<long long>(n, 1)));
-        if (mlp_proposal(d.mlp->p, proposal_ctx(sc, p), n, d.prop.p, s, d.errors.p + ERR_MLP)) {
-            ctx().err = "proposal launch failed"; return RC_E_CUDA;
+        // the network on every light's 32 x 32 area cells (tensor cores); the light pass
+        // draws each path's emission from that table
+        RC_CUDA(d.prop_table.reserve((size_t)sc.lights.size() * kProposalRes * kProposalRes * kProposalCellFloats));
+        if (mlp_proposal_table(d.mlp->p, proposal_ctx(sc, p), kProposalRes, d.prop_table.p, s, d.errors.p + ERR_MLP)) {
+            ctx().err = "proposal table launch failed"; return RC_E_CUDA;
         }
-        p.proposal = d.prop.p;
+        // (the draw itself follows the light-path order, render_iteration)
+        p.proposal_table = d.prop_table.p;
+        p.proposal_table_res = kProposalRes;
+        RC_CUDA(d.prop.reserve(std::max<long long>(n, 1)));
     }
     if (train) {
         RC_CUDA(d.contrib.reserve(std::max<long long>(n, 1)));
@@ -674,6 +679,17 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             RC_CUDA(d.order_scratch.reserve(light_order_scratch_bytes(p.num_light_paths)));
             launch_light_order(p, d.order_scratch.p, d.path_order.p, s);
             p.path_order = d.path_order.p;
+        }
+        if (learned && p.proposal_table) {
+            // every path's emission drawn from the network's table, in the light-path
+            // order (neighbouring threads read the same cells); the light pass and the
+            // training collection read the draws
+            if (mlp_proposal_draw(proposal_ctx(sc, p), kProposalRes, p.proposal_table, p.num_light_paths, p.path_order,
+                                  d.prop.p, s)) {
+                ctx().err = "proposal draw launch failed"; return RC_E_CUDA;
+            }
+            p.proposal = d.prop.p;
+            p.proposal_table = nullptr;
         }
         int lvar = 0;
         if (sampler == RC_SAMPLER_UNIFORM && cfg().autotune) {
@@ -1648,8 +1664,21 @@ int rc_proposal_state(long long n, float* prop4, float* contrib) {
     DeviceState& d = ctx().dev;
     if (prop4) {
         std::memset(prop4, 0, sizeof(float) * 4 * (size_t)n);
-        const long long m = std::min<long long>(n, (long long)d.prop.n);
-        if (d.mlp_rounds > 0 && m > 0) RC_CUDA(cudaMemcpy(prop4, d.prop.p, sizeof(float4) * m, cudaMemcpyDeviceToHost));
+        if (d.mlp && d.mlp_rounds > 0 && n > 0 && ctx().scene && d.iterations_done > 0) {
+            // the last rendered iteration's draws, recomputed from the network's table with
+            // the paths' own samples (the light pass draws the same ones)
+            const HostScene& sc = *ctx().scene;
+            const VMParams p = make_params(sc, d.iterations_done - 1);
+            const long long m = std::min<long long>(n, p.num_light_paths);
+            RC_CUDA(d.prop.reserve(std::max<long long>(m, 1)));
+            RC_CUDA(d.prop_table.reserve((size_t)sc.lights.size() * kProposalRes * kProposalRes * kProposalCellFloats));
+            if (mlp_proposal(d.mlp->p, proposal_ctx(sc, p), kProposalRes, d.prop_table.p, m, d.prop.p, d.stream,
+                             d.errors.p + ERR_MLP)) {
+                ctx().err = "proposal launch failed"; return RC_E_CUDA;
+            }
+            RC_CUDA(cudaMemcpyAsync(prop4, d.prop.p, sizeof(float4) * m, cudaMemcpyDeviceToHost, d.stream));
+            RC_CUDA(cudaStreamSynchronize(d.stream));
+        }
     }
     if (contrib) {
         std::memset(contrib, 0, sizeof(float) * (size_t)n);

@@ -120,7 +120,13 @@ __global__ void k_light_keys(const VMParams P, uint32_t* __restrict__ keys, uint
     g.init(P.seed, (uint64_t)i, P.iteration, STREAM_LIGHT);
     const U4 b0 = g.block(0), b1 = g.block(1);
     float u[4] = {u01(b0.b), u01(b0.c), u01(b0.d), u01(b1.a)};
-    if (P.proposal) {
+    if (P.proposal_table) {
+        // emission about to be drawn from the tabulated proposal (mlp_proposal, in this
+        // order): area cell, mixture component sample and the first direction sample, so
+        // that a warp's lanes read the same table cells and lobes
+        u[2] = u01(b1.b);
+        u[3] = u01(b0.d);
+    } else if (P.proposal) {
         // the learned proposal gives the direction: its octahedral coordinates instead
         const float4 pr = __ldg(&P.proposal[i]);
         const float l1 = fabsf(pr.x) + fabsf(pr.y) + fabsf(pr.z);
