@@ -238,10 +238,13 @@ int rc_save_state(const char* path);
 int rc_load_state(const char* path);
 
 /* Debug view of the reference's debug_test modes (src/Debug_scene.cpp, dispatched by
- * src/main.cpp:172-180): mode 2 shading normals, 3 front/back facing, 4 Fresnel
- * reflectance with the IOR of Debug_stuff::specular.  One unjittered primary ray per
- * pixel; replaces the image (rc_read_image returns it).  main() runs the same view when
- * init() got debug_test 2-4. */
+ * src/main.cpp:172-186): mode 2 shading normals, 3 front/back facing, 4 Fresnel
+ * reflectance with the IOR of Debug_stuff::specular (one unjittered primary ray per
+ * pixel; replaces the image, which rc_read_image returns); mode 5 the boxes of every
+ * mesh BVH as OBJ files, one per mesh and depth, named "<dir>bvh<sep>Mesh_<k>_<depth>.obj"
+ * after the EXR path's directory <dir> and separator <sep> ("D:\bvh\Mesh_..." by
+ * default, as src/Debug_scene.cpp:284-320; the directory must exist), with no image
+ * (host only: needs no GPU).  main() runs the same view when init() got debug_test 2-5. */
 int rc_render_debug(int mode);
 
 /* Learned-proposal state (no counterpart in the reference): for the first n light

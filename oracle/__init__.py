@@ -102,5 +102,6 @@ def reference() -> C.CDLL | None:
         lib.ref_world_bvh.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         lib.ref_layout.argtypes = [C.c_void_p]
         lib.ref_debug.argtypes = [C.c_int, C.c_void_p]
+        lib.ref_debug_bvh.argtypes = []
         _ref = lib
     return _ref

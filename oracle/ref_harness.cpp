@@ -321,6 +321,15 @@ int ref_debug(int mode, float* rgb)
     return 0;
 }
 
+// Vertex_Merging::run_debug_bvh (src/Debug_scene.cpp:284-320): OBJ files of the mesh
+// BVH boxes, one per depth, written by the reference into the working directory.
+int ref_debug_bvh()
+{
+    if (!scene) return -1;
+    scene->integrator.run_debug_bvh();
+    return 0;
+}
+
 int ref_release()
 {
     delete scene;

@@ -603,6 +603,75 @@ int autotune_variants(int nvariants, Run&& run, const char* what, long long size
 
 int size_class(long long n) { return n > 0 ? 63 - __builtin_clzll((unsigned long long)n) : 0; }
 
+// Debug view 5 (Vertex_Merging::run_debug_bvh, src/Debug_scene.cpp:284-320): for every
+// mesh of every world leaf, in world-node order, one OBJ file per depth of the mesh's
+// BVH, "<dir>bvh<sep>Mesh_<k>_<depth>.obj" (k counts the meshes written, from 1; <dir>
+// and <sep> from the EXR path, the reference's "D:\bvh\" by default), holding the boxes
+// of that depth's nodes: 8 vertices and 6 quads each, numbered per file
+// (write_bvh / write_bounding_box, src/Debug_scene.cpp:217-262), numbers printed as an
+// ostream prints a float (%g).  The reference also walks inner world nodes as if they
+// were leaves (their child words read as a mesh range, past the end of the mesh list
+// when the world BVH has inner nodes); only leaves are walked here.
+int debug_bvh_obj(HostScene& sc) {
+    const std::string exr = cfg().exr_path;
+    const size_t cut = exr.find_last_of("/\\");
+    const std::string dir = cut == std::string::npos ? std::string() : exr.substr(0, cut + 1);
+    const char sep = cut == std::string::npos ? '\\' : exr[cut];
+    const std::string prefix = dir + "bvh" + sep + "Mesh_";
+    const std::vector<BvhNode>& wn = sc.world.nodes;
+    int written = 0;
+    for (size_t w = 0; w < wn.size(); ++w) {
+        if (!(wn[w].w0 & 0x80000000u)) continue;
+        const uint32_t cnt = wn[w].w0 & 0x7fffffffu;
+        for (uint32_t k = 0; k < cnt; ++k) {
+            const int mesh = sc.world.index[wn[w].w1 + 1 + k];
+            HostMesh& hm = sc.meshes[mesh];
+            if (hm.bvh.nodes.empty()) build_mesh_bvh(hm);   // the device built this scene's meshes
+            const std::vector<BvhNode>& nodes = hm.bvh.nodes;
+            // depth of every node (root 1), children after their parent in the array
+            std::vector<int> depth(nodes.size(), 0);
+            int max_depth = 0;
+            std::vector<std::pair<int, int>> stack{{0, 1}};
+            std::vector<int> order;   // pre-order: the reference's write_bvh recursion
+            while (!stack.empty()) {
+                const auto [i, dpt] = stack.back();
+                stack.pop_back();
+                depth[i] = dpt;
+                order.push_back(i);
+                if (nodes[i].w0 & 0x80000000u) { max_depth = std::max(max_depth, dpt); continue; }
+                stack.push_back({(int)nodes[i].w1, dpt + 1});
+                stack.push_back({(int)nodes[i].w0, dpt + 1});
+            }
+            ++written;
+            std::vector<FILE*> files((size_t)max_depth, nullptr);
+            for (int dpt = 1; dpt <= max_depth; ++dpt) {
+                const std::string name = prefix + std::to_string(written) + "_" + std::to_string(dpt) + ".obj";
+                files[dpt - 1] = std::fopen(name.c_str(), "w");
+                if (!files[dpt - 1]) {
+                    for (FILE* f : files) if (f) std::fclose(f);
+                    ctx().err = "cannot write " + name;
+                    return RC_E_IO;
+                }
+            }
+            std::vector<int> base((size_t)max_depth, 0);
+            for (int i : order) {
+                FILE* f = files[depth[i] - 1];
+                const Box& b = nodes[i].box;
+                const float cx[2] = {b.mx.x, b.mn.x}, cy[2] = {b.mx.y, b.mn.y}, cz[2] = {b.mx.z, b.mn.z};
+                for (int v = 0; v < 8; ++v)
+                    std::fprintf(f, "v %g %g %g\n", (double)cx[v >> 2], (double)cy[(v >> 1) & 1], (double)cz[v & 1]);
+                static const int quad[6][4] = {{1, 5, 7, 3}, {4, 3, 7, 8}, {8, 7, 5, 6}, {6, 2, 4, 8}, {2, 1, 3, 4}, {6, 5, 1, 2}};
+                const int o = base[depth[i] - 1];
+                for (const auto& q : quad)
+                    std::fprintf(f, "f %d/ %d/ %d/ %d/\n", q[0] + o, q[1] + o, q[2] + o, q[3] + o);
+                base[depth[i] - 1] += 8;
+            }
+            for (FILE* f : files) std::fclose(f);
+        }
+    }
+    return RC_OK;
+}
+
 // One progressive iteration with host round trips (counts read back, buffers grown on
 // overflow).  redo_iteration >= 0 renders that iteration index again without counting
 // it (an iteration an asynchronous replay had to skip).
@@ -1435,21 +1504,23 @@ void init(int samples, float base_radius, float radius_reduction, long long* mes
 
 int main(void) {
     if (!ctx().scene) { ctx().err = "main: no scene (init was not called or failed: " + ctx().err + ")"; return RC_E_NO_SCENE; }
-    int r = prepare();
+    // src/main.cpp:170-186: 1 = vertex merging, 2-4 = debug views (one pass, no
+    // averaging), 5 = the mesh BVHs' boxes as OBJ files (host only, no image)
+    const int mode = ctx().scene->debug_test;
+    int r = mode == 5 ? prepare_host() : prepare();
     if (!r) {
-        // src/main.cpp:170-186: 1 = vertex merging, 2-4 = debug views (one pass, no
-        // averaging), 5 = BVH dump to OBJ files (not provided here)
-        const int mode = ctx().scene->debug_test;
         if (mode == 1) {
             r = render_iterations(*ctx().scene, ctx().scene->samples);
         } else if (mode >= 2 && mode <= 4) {
             r = render_debug(*ctx().scene, mode);
+        } else if (mode == 5) {
+            r = debug_bvh_obj(*ctx().scene);
         } else {
-            ctx().err = "debug_test must be 1 (render) or 2-4 (debug views); 5 (BVH OBJ dump) is not provided";
+            ctx().err = "debug_test must be 1 (render), 2-4 (debug views) or 5 (BVH boxes as OBJ files)";
             r = RC_E_UNSUPPORTED;
         }
     }
-    if (!r && cfg().write_exr) {
+    if (!r && cfg().write_exr && mode != 5) {
         int w = ctx().scene->camera.width, h = ctx().scene->camera.height;
         std::vector<float> img(3 * (size_t)w * h);
         r = read_image(img.data(), w, h);
@@ -1615,6 +1686,11 @@ int rc_save_state(const char* path) { return save_state(path); }
 int rc_load_state(const char* path) { return load_state(path); }
 
 int rc_render_debug(int mode) {
+    if (mode == 5) {
+        int r = prepare_host();
+        if (r) return r;
+        return debug_bvh_obj(*ctx().scene);
+    }
     int r = prepare();
     if (r) return r;
     return render_debug(*ctx().scene, mode);

@@ -114,3 +114,58 @@ def test_material_index_out_of_range_rejected_at_init():
     with pytest.raises(RuntimeError, match="material index"):
         Renderer(sc)
     _native.lib().rc_release()
+
+
+def _bvh_obj_files(root):
+    return {p.name: p.read_bytes() for p in sorted(root.iterdir()) if p.name.startswith("D:\\bvh\\Mesh_")}
+
+
+def _single_mesh(sc):
+    sc.meshes = sc.meshes[:1]
+    return sc
+
+
+@pytest.mark.parametrize("maker", [lambda: _single_mesh(scenes.glass_sphere_point(16, 16, subdiv=3)),
+                                   lambda: _single_mesh(scenes.water_pool(16, 16, grid=40)),
+                                   lambda: _single_mesh(scenes.gem_cluster(16, 16, n_gems=60))])
+def test_debug_bvh_obj_matches_reference(ref, in_tmpdir, maker):
+    """Debug view 5 (Vertex_Merging::run_debug_bvh): the OBJ files of the mesh BVHs' boxes,
+    one per mesh and depth, byte for byte the reference's (host only: no GPU needed).
+    Single-mesh scenes: with inner world nodes the reference reads past its mesh list and
+    crashes (it walks every world node as a leaf); the library walks the leaves only."""
+    sc = maker()
+    args = InitArgs(sc)
+    args.call(ref.init)
+    assert ref.ref_prepare(None) == 0
+    assert ref.ref_debug_bvh() == 0
+    ref.ref_release()
+    want = _bvh_obj_files(in_tmpdir)
+    assert want
+    for name in want:
+        (in_tmpdir / name).unlink()
+    lib = _native.lib()
+    r = Renderer(sc)
+    assert lib.rc_render_debug(5) == 0, lib.rc_last_error()
+    r.release()
+    got = _bvh_obj_files(in_tmpdir)
+    assert sorted(got) == sorted(want)
+    for name in want:
+        assert got[name] == want[name], name
+
+
+def test_main_debug_bvh_writes_obj_files_and_no_image(tmp_path):
+    """init(debug_test=5) + main(): the BVH boxes as OBJ files beside the configured EXR
+    path (in its "bvh" directory), no image, no GPU needed."""
+    sc = _single_mesh(scenes.glass_sphere_point(16, 16, subdiv=2))
+    lib = _native.lib()
+    cfg = abi.RcConfig()
+    lib.rc_default_config(C.byref(cfg))
+    cfg.exr_path = str(tmp_path / "out.exr").encode()
+    assert lib.rc_set_config(C.byref(cfg)) == 0
+    (tmp_path / "bvh").mkdir()
+    InitArgs(sc, debug_test=5).call(lib.init)
+    assert lib.main() == 0, lib.rc_last_error()
+    names = sorted(p.name for p in (tmp_path / "bvh").iterdir())
+    assert names and names[0] == "Mesh_1_1.obj" and not (tmp_path / "out.exr").exists()
+    first = (tmp_path / "bvh" / "Mesh_1_1.obj").read_text().splitlines()
+    assert len(first) == 14 and first[0].startswith("v ") and first[8] == "f 1/ 5/ 7/ 3/"

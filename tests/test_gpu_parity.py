@@ -395,7 +395,7 @@ def test_main_runs_debug_view(tmp_path):
     InitArgs(sc, debug_test=2).call(L.init)
     assert L.main() == 0, L.rc_last_error()
     assert (tmp_path / "dbg.exr").stat().st_size > 32 * 24 * 12
-    InitArgs(sc, debug_test=5).call(L.init)
+    InitArgs(sc, debug_test=6).call(L.init)
     assert L.main() != 0 and b"debug_test" in L.rc_last_error()
 
 
