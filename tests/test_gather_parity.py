@@ -115,14 +115,19 @@ def test_water_pool_iteration_vs_oracle(orc):
     ph = r.light_photons(0)
     qs = r.camera_queries(0)
     r.render(1)
-    radius = r.stats()["radius"]
+    st = r.stats()
     r.release()
     pos = np.ascontiguousarray(ph[:, :3])
     qpos = np.ascontiguousarray(qs[:, :3])
     assert len(pos) > 5_000_000 and len(qpos) > 2_000_000
-    r2 = float(np.float32(radius) * np.float32(radius))
+    assert int(st["photons"]) == len(pos) and int(st["queries"]) == len(qpos)
+    # the reported radius is the double square root of the render's FP32 r^2: squaring it
+    # in double and rounding to FP32 gives that r^2 back exactly
+    r2 = float(np.float32(st["radius"] ** 2))
     base, _ = kd_query(pos, qpos, r2, with_indices=False)
     assert base.mean() > 2.0                        # the workload merges several photons per query
+    # the render's own gather (merge evaluation sink) accepted exactly these pairs
+    assert int(base.sum()) == int(st["merged"])
     for v in range(gather_variants()):
         counts, _ = kd_query(pos, qpos, r2, with_indices=False, variant=v)
         assert (counts == base).all(), f"shape {v} differs from the default on {int((counts != base).sum())} queries"
