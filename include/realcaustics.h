@@ -274,6 +274,11 @@ int rc_trace_rays_full(int n, const float* origins, const float* directions, flo
  * (u32 bits), 0].  *count receives the number stored (may exceed cap). */
 int rc_light_photons(int iteration, float* out, long long cap, long long* count);
 
+/* rc_light_photons with the light pass in launch shape `shape` (0 .. 5: the persistent
+ * pass's block/register shapes, 5 = the wavefront pass), for comparing them; the
+ * photons of every shape are the same, only their storage order differs. */
+int rc_light_photons_shape(int shape, int iteration, float* out, long long cap, long long* count);
+
 /* One camera pass (iteration `iteration`, current config) on the GPU; copies the merge
  * queries it writes (one per non-delta camera vertex, Vertex_Merging.cpp:309-362), in
  * storage order, as 4 floats each: [position xyz, camera dVM].  *count receives the

@@ -49,6 +49,7 @@ def lib() -> C.CDLL:
                                   C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_gather_variants.argtypes = []
     L.rc_device_bus_id.argtypes = [C.c_char_p, C.c_int]
+    L.rc_light_photons_shape.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_tc_gemm_selftest.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.rc_tc_wait_selftest.argtypes = [C.c_uint]
     L.rc_camera_queries.argtypes = [C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
@@ -86,4 +87,4 @@ EXPORTS = ["init", "main", "rc_default_config", "rc_set_config", "rc_prepare", "
            "rc_save_state", "rc_load_state", "rc_scene_dump", "rc_prepare_stats",
            "rc_context_create", "rc_context_bind", "rc_context_destroy", "rc_gather_query",
            "rc_gather_variants", "rc_camera_queries", "rc_device_bus_id", "rc_tc_gemm_selftest",
-           "rc_tc_wait_selftest"]
+           "rc_tc_wait_selftest", "rc_light_photons_shape"]

@@ -88,6 +88,7 @@ struct DeviceState {
     // light-path processing order (launch_light_order) and its scratch
     DevBuf<uint32_t> path_order;
     DevBuf<unsigned char> order_scratch;
+    DevBuf<unsigned char> wf_scratch;   // wavefront light pass: path state and queues
     // learned emission proposal
     std::unique_ptr<MlpStore> mlp;
     DevBuf<float4> prop, train_pos, train_dir;
@@ -126,7 +127,7 @@ struct DeviceState {
         box_lo.release(); box_hi.release();
         accum.release();
         image.release();
-        path_order.release(); order_scratch.release();
+        path_order.release(); order_scratch.release(); wf_scratch.release();
         mlp.reset();
         prop.release(); train_pos.release(); train_dir.release(); contrib.release(); train_wsum.release();
         prop_table.release();
@@ -593,6 +594,7 @@ int autotune_variants(int nvariants, Run&& run, const char* what, long long size
         cudaEventRecord(d.evm[1], d.stream);
         cudaEventSynchronize(d.evm[1]);
         const float ms = ms_between(d.evm[0], d.evm[1]);
+        if (cfg().verbose) std::printf("{\"autotune_shape\": \"%s\", \"variant\": %d, \"ms\": %.3f}\n", what, v, ms);
         if (ms < best) { best = ms; best_v = v; }
     }
     if (cfg().verbose)
@@ -602,6 +604,19 @@ int autotune_variants(int nvariants, Run&& run, const char* what, long long size
 }
 
 int size_class(long long n) { return n > 0 ? 63 - __builtin_clzll((unsigned long long)n) : 0; }
+
+// The light pass in launch shape v: the persistent pass's shapes, or (v ==
+// pass_variants()) the wavefront pass with its path state in the context's scratch.
+int light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s, int v) {
+    DeviceState& d = ctx().dev;
+    if (v == pass_variants()) {
+        RC_CUDA(d.wf_scratch.reserve(light_wavefront_scratch_bytes(p.num_light_paths)));
+        launch_light_wavefront(p, ph, d.wf_scratch.p, s);
+        return RC_OK;
+    }
+    launch_light_pass(p, ph, d.counters.p + 6, s, v);
+    return RC_OK;
+}
 
 // Debug view 5 (Vertex_Merging::run_debug_bvh, src/Debug_scene.cpp:284-320): for every
 // mesh of every world leaf, in world-node order, one OBJ file per depth of the mesh's
@@ -678,6 +693,7 @@ int debug_bvh_obj(HostScene& sc) {
 int render_iteration(HostScene& sc, int redo_iteration = -1) {
     DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
+    int r0 = RC_OK;
     const int it = redo_iteration >= 0 ? redo_iteration : d.iterations_done;
     VMParams p = make_params(sc, it);
     // With a Metropolis sampler and the learned proposal, the first train_iterations
@@ -764,15 +780,18 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         if (sampler == RC_SAMPLER_UNIFORM && cfg().autotune) {
             std::atomic<int>& slot = g_tune.light[size_class(p.num_light_paths)];
             if (slot.load() < 0)
-                slot = autotune_variants(pass_variants(), [&](int v) {
+                slot = autotune_variants(pass_variants() + 1, [&](int v) {
                     cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s);
-                    launch_light_pass(p, ph, d.counters.p + 6, s, v);
+                    light_pass(p, ph, s, v);
                 }, "light pass", p.num_light_paths);
             lvar = slot.load();
             RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         }
         if (cam_side && attempt == 0) RC_CUDA(cudaEventRecord(d.fork, s));
-        if (sampler == RC_SAMPLER_UNIFORM) launch_light_pass(p, ph, d.counters.p + 6, s, lvar);
+        if (sampler == RC_SAMPLER_UNIFORM) {
+            r0 = light_pass(p, ph, s, lvar);
+            if (r0) return r0;
+        }
         else launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaEventRecord(d.ev[1], s));
@@ -1028,6 +1047,10 @@ int async_setup(const HostScene& sc) {
     d.async_cvar = var(g_tune.camera[size_class(npix)].load(), 0);
     d.async_gvar = var(g_tune.gather[size_class((long long)d.last_queries)].load(), gather_default_variant());
     if (!cfg().autotune) d.async_lvar = d.async_cvar = 0, d.async_gvar = gather_default_variant();
+    if (d.async_lvar == pass_variants()) {   // the wavefront pass's state: reserved before any capture
+        const long long paths = cfg().photons_per_iter > 0 ? cfg().photons_per_iter : npix;
+        RC_CUDA(d.wf_scratch.reserve(light_wavefront_scratch_bytes(paths)));
+    }
     return RC_OK;
 }
 
@@ -1035,6 +1058,7 @@ int async_setup(const HostScene& sc) {
 int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
+    int r0 = RC_OK;
     VMParams p = make_params(sc, it);
     const long long pc = d.async_pcap, qc = d.async_qcap;
     RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
@@ -1047,7 +1071,8 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     RC_CUDA(record(d.ev[0], s));
     launch_light_order(p, d.order_scratch.p, d.path_order.p, s);
     p.path_order = d.path_order.p;
-    launch_light_pass(p, ph, d.counters.p + 6, s, d.async_lvar);
+    r0 = light_pass(p, ph, s, d.async_lvar);
+    if (r0) return r0;
     RC_CUDA(record(d.ev[1], s));
     RC_CUDA(record(d.ev[4], d.side));
     launch_camera_pass(p, qb, d.counters.p + 7, d.side, d.async_cvar);
@@ -1797,9 +1822,14 @@ int rc_camera_queries(int iteration, float* out, long long cap, long long* count
 }
 
 int rc_light_photons(int iteration, float* out, long long cap, long long* count) {
+    return rc_light_photons_shape(0, iteration, out, cap, count);
+}
+
+int rc_light_photons_shape(int shape, int iteration, float* out, long long cap, long long* count) {
     int r = prepare();
     if (r) return r;
     if (iteration < 0 || (cap > 0 && !out)) { ctx().err = "bad photon output"; return RC_E_INVALID; }
+    if (shape < 0 || shape > pass_variants()) { ctx().err = "light pass shape out of range"; return RC_E_INVALID; }
     HostScene& sc = *ctx().scene;
     DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;
@@ -1812,7 +1842,8 @@ int rc_light_photons(int iteration, float* out, long long cap, long long* count)
         RC_CUDA(d.counters.reserve(8));
         RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, (long long)d.ph_pos.n, d.counters.p};
-        launch_light_pass(p, ph, d.counters.p + 6, s);
+        r = light_pass(p, ph, s, shape);
+        if (r) return r;
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaMemcpyAsync(&nph, d.counters.p, sizeof(nph), cudaMemcpyDeviceToHost, s));
         RC_CUDA(cudaStreamSynchronize(s));

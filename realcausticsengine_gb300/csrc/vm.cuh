@@ -160,8 +160,14 @@ void launch_gather_sets(const KdTree& tree, const float4* t0, const float* qpos,
                         int variant, unsigned long long* counters, int* err, cudaStream_t s);
 int gather_variants();
 int gather_default_variant();
+// Wavefront light pass: the same paths and photons as launch_light_pass, one bounce of
+// every live path per round, split into a closest-hit kernel and a shading kernel with
+// path state and queues in `scratch` (light_wavefront_scratch_bytes(num_light_paths)).
+size_t light_wavefront_scratch_bytes(long long n);
+void launch_light_wavefront(const VMParams& p, PhotonBuf ph, void* scratch, cudaStream_t s);
 // Launch shapes of the persistent light and camera passes (block size x traversal-stack
-// placement), chosen by the autotuner; 0 is the default.
+// placement), chosen by the autotuner; 0 is the default.  The light pass has one more:
+// pass_variants() is the wavefront pass.
 int pass_variants();
 const char* pass_variant_name(int v);
 const char* gather_variant_name(int v);

@@ -59,13 +59,19 @@ __device__ __forceinline__ bool light_path_start(const VMParams& P, long long pi
     return true;
 }
 
-// One bounce of Vertex_Merging::trace_light_path (src/Vertex_Merging.cpp:140-194);
-// returns false when the path ends.
+// One bounce of Vertex_Merging::trace_light_path (src/Vertex_Merging.cpp:140-194), in
+// two halves: the closest hit of the path's next segment (false: the path ends), then
+// the shading at that hit - photon store, BSDF sample, Russian roulette, dVM update -
+// which returns false when the path ends.  The persistent pass runs both per bounce,
+// the wavefront pass runs them in separate kernels.
 template <class Stack>
-__device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& ph, LightPath& s, Stack& stack) {
-    F3 ro = s.o + s.d * kRayEps;
-    HitRec h;
-    if (!scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK, stack)) return false;
+__device__ __forceinline__ bool light_path_trace(const VMParams& P, const LightPath& s, HitRec& h, Stack& stack) {
+    const F3 ro = s.o + s.d * kRayEps;
+    return scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK, stack);
+}
+
+__device__ __forceinline__ bool light_path_shade(const VMParams& P, PhotonBuf& ph, LightPath& s, const HitRec& h) {
+    const F3 ro = s.o + s.d * kRayEps;
     Isect is;
     fill_isect(P.scene, h, ro, s.d, is);
     if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); return false; }
@@ -105,6 +111,109 @@ __device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& 
     else s.dVM = (smp.cos_out / smp.fwd) * (1.0f + smp.rev * s.dVM);
     s.len++;
     return true;
+}
+
+template <class Stack>
+__device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& ph, LightPath& s, Stack& stack) {
+    HitRec h;
+    if (!light_path_trace(P, s, h, stack)) return false;
+    return light_path_shade(P, ph, s, h);
+}
+
+// Wavefront light pass: the same paths, bounces and photons as the persistent pass,
+// with each bounce split over two kernels that every queued path passes through: a
+// trace kernel (the closest hit only, so it keeps few registers and every lane holds a
+// live ray) and a shade kernel that appends the paths that continue to the next queue.
+// Path state between the kernels, per slot (slot = position in the light-path order):
+//   o4 = origin | dVM, d4 = direction | tp.r, t2 = tp.gb,
+//   m4 = path index, length, diffuse bounces, last event | (dispersion channel + 1) << 8,
+//   hit = t, u, v, triangle slot (-1: the path ends).
+struct WfState {
+    float4* o4; float4* d4; float2* t2; int4* m4; float4* hit;
+    uint32_t* queue[2];
+    unsigned long long* count;   // [2] queue lengths
+};
+
+__device__ __forceinline__ void wf_store(const WfState& W, uint32_t slot, const LightPath& s) {
+    W.o4[slot] = make_float4(s.o.x, s.o.y, s.o.z, s.dVM);
+    W.d4[slot] = make_float4(s.d.x, s.d.y, s.d.z, s.tp.x);
+    W.t2[slot] = make_float2(s.tp.y, s.tp.z);
+    W.m4[slot] = make_int4((int)(uint32_t)s.idx, s.len, s.diffuse, (s.last & 0xff) | ((s.channel + 1) << 8));
+}
+
+__device__ __forceinline__ void wf_load(const VMParams& P, const WfState& W, uint32_t slot, LightPath& s) {
+    const float4 o = W.o4[slot], d = W.d4[slot];
+    const float2 t = W.t2[slot];
+    const int4 m = W.m4[slot];
+    s.o = f3(o.x, o.y, o.z); s.dVM = o.w;
+    s.d = f3(d.x, d.y, d.z);
+    s.tp = f3(d.w, t.x, t.y);
+    s.idx = (long long)(uint32_t)m.x;
+    s.len = m.y; s.diffuse = m.z;
+    s.last = m.w & 0xff;
+    s.channel = (m.w >> 8) - 1;
+    s.rng.init(P.seed, (uint64_t)s.idx, P.iteration, STREAM_LIGHT);
+}
+
+__device__ __forceinline__ void wf_push(const WfState& W, int q, uint32_t slot) {
+    W.queue[q][warp_append(&W.count[q])] = slot;
+}
+
+__global__ void k_wf_start(const VMParams P, WfState W) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= P.num_light_paths) return;
+    const long long pidx = P.path_order ? (long long)__ldg(&P.path_order[i]) : i;
+    LightPath s;
+    if (!light_path_start(P, pidx, s)) return;
+    wf_store(W, (uint32_t)i, s);
+    wf_push(W, 0, (uint32_t)i);
+}
+
+template <int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) k_wf_trace(const VMParams P, WfState W, int q) {
+    const unsigned long long n = W.count[q];
+    CallStack stk;
+    for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < n;
+         j += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t slot = W.queue[q][j];
+        const float4 o = W.o4[slot], d = W.d4[slot];
+        LightPath s;
+        s.o = f3(o.x, o.y, o.z);
+        s.d = f3(d.x, d.y, d.z);
+        HitRec h;
+        if (!light_path_trace(P, s, h, stk)) h.slot = -1;
+        W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.slot));
+    }
+}
+
+// The paths still queued after the last wavefront round, each taken through all of its
+// remaining bounces by one thread (few paths remain; one launch instead of a round per
+// bounce, each of which waits for its longest traversal).
+__global__ void __launch_bounds__(128, 8) k_wf_finish(const VMParams P, PhotonBuf ph, WfState W, int q) {
+    const unsigned long long n = W.count[q];
+    CallStack stk;
+    for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < n;
+         j += (unsigned long long)gridDim.x * blockDim.x) {
+        LightPath s;
+        wf_load(P, W, W.queue[q][j], s);
+        while (light_path_bounce(P, ph, s, stk)) {}
+    }
+}
+
+__global__ void __launch_bounds__(128) k_wf_shade(const VMParams P, PhotonBuf ph, WfState W, int q) {
+    const unsigned long long n = W.count[q];
+    for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < n;
+         j += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t slot = W.queue[q][j];
+        const float4 hv = W.hit[slot];
+        HitRec h{hv.x, hv.y, hv.z, __float_as_int(hv.w)};
+        if (h.slot < 0) continue;
+        LightPath s;
+        wf_load(P, W, slot, s);
+        if (!light_path_shade(P, ph, s, h)) continue;
+        wf_store(W, slot, s);
+        wf_push(W, q ^ 1, slot);
+    }
 }
 
 // Light-path order: 4D Morton key of a path's emission samples (the same Philox draws
@@ -401,6 +510,46 @@ void launch_light_order(const VMParams& p, void* scratch, uint32_t* order, cudaS
     k_light_scatter<<<g, 256, 0, s>>>(keys, n, counts, order);
 }
 
+size_t light_wavefront_scratch_bytes(long long n) {
+    const size_t m = (size_t)(n > 0 ? n : 1);
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    return al(16 * m) * 4 + al(8 * m) + al(16 * m) + 2 * al(4 * m) + 256;
+}
+
+void launch_light_wavefront(const VMParams& p, PhotonBuf ph, void* scratch, cudaStream_t s) {
+    const long long n = p.num_light_paths;
+    if (n <= 0) return;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    char* c = static_cast<char*>(scratch);
+    WfState W;
+    W.o4 = (float4*)c; c += al(16 * (size_t)n);
+    W.d4 = (float4*)c; c += al(16 * (size_t)n);
+    W.m4 = (int4*)c; c += al(16 * (size_t)n);
+    W.hit = (float4*)c; c += al(16 * (size_t)n);
+    W.t2 = (float2*)c; c += al(8 * (size_t)n);
+    W.queue[0] = (uint32_t*)c; c += al(4 * (size_t)n);
+    W.queue[1] = (uint32_t*)c; c += al(4 * (size_t)n);
+    W.count = (unsigned long long*)c;
+    cudaMemsetAsync(W.count, 0, 2 * sizeof(unsigned long long), s);
+    k_wf_start<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, W);
+    static thread_local unsigned trace_grid = 0, shade_grid = 0, finish_grid = 0;
+    if (!trace_grid) {
+        trace_grid = persistent_grid(k_wf_trace<8>, 128, 0, 1LL << 40);
+        shade_grid = persistent_grid(k_wf_shade, 128, 0, 1LL << 40);
+        finish_grid = persistent_grid(k_wf_finish, 128, 0, 1LL << 40);
+    }
+    // a bounce per round for the first kWavefrontRounds bounces (most paths end by then),
+    // then one launch finishes the rest
+    constexpr int kWavefrontRounds = 4;
+    int q = 0;
+    for (int b = 0; b < kWavefrontRounds; ++b, q ^= 1) {
+        k_wf_trace<8><<<trace_grid, 128, 0, s>>>(p, W, q);
+        cudaMemsetAsync(W.count + (q ^ 1), 0, sizeof(unsigned long long), s);
+        k_wf_shade<<<shade_grid, 128, 0, s>>>(p, ph, W, q);
+    }
+    k_wf_finish<<<finish_grid, 128, 0, s>>>(p, ph, W, q);
+}
+
 int pass_variants() { return 5; }
 
 const char* pass_variant_name(int v) {
@@ -409,6 +558,7 @@ const char* pass_variant_name(int v) {
                                    "128 threads, >= 8 blocks/SM (<= 64 registers)",
                                    "128 threads, >= 5 blocks/SM (<= 102 registers)",
                                    "128 threads, >= 10 blocks/SM (<= 51 registers)"};
+    if (v == 5) return "wavefront: closest-hit and shading kernels per bounce";
     return (v >= 0 && v < 5) ? names[v] : "?";
 }
 

@@ -135,6 +135,15 @@ class Renderer:
         check(self.L.rc_camera_queries(int(iteration), out.ctypes.data, len(out), C.byref(n)), "rc_camera_queries")
         return out[:n.value]
 
+    def light_photons_shape(self, shape: int, iteration: int) -> np.ndarray:
+        """Photons of one light pass in launch shape `shape` (5: the wavefront pass)."""
+        n = C.c_longlong()
+        check(self.L.rc_light_photons_shape(shape, int(iteration), None, 0, C.byref(n)), "rc_light_photons_shape")
+        out = np.zeros((max(n.value, 1), 12), np.float32)
+        check(self.L.rc_light_photons_shape(shape, int(iteration), out.ctypes.data, len(out), C.byref(n)),
+              "rc_light_photons_shape")
+        return out[:n.value]
+
     def light_photons(self, iteration: int) -> np.ndarray:
         n = C.c_longlong()
         check(self.L.rc_light_photons(int(iteration), None, 0, C.byref(n)), "rc_light_photons")

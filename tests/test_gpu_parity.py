@@ -451,3 +451,30 @@ def test_hybrid_with_learned_proposal_runs():
     st = {}
     hyb = _render_mean(sc, 1, 4096, 12, paths=200000, seed=11, learned=True, stats=st)
     assert st["accum_ms"] > 0.0 and hyb > 0.0
+
+
+@pytest.mark.parametrize("name", ["test_scene", "water"])
+def test_light_pass_shapes_store_the_same_photons(name):
+    """Every launch shape of the light pass - the persistent pass's block/register shapes
+    and the wavefront pass (closest-hit and shading kernels per bounce) - stores the same
+    photon records bit for bit (same counter-based samples, same arithmetic); only their
+    storage order differs."""
+    if name == "test_scene":
+        sc, paths = scenes.test_scene(32, 24, subdiv=2), 60000
+    else:
+        sc, paths = scenes.water_pool(96, 54, grid=512), 1 << 20
+    r = Renderer(sc, max_path_length=8, photons_per_iter=paths, seed=5)
+    r.prepare()
+    shapes = [r.light_photons_shape(v, 2) for v in range(6)]
+    r.release()
+
+    def canonical(ph):
+        words = np.ascontiguousarray(ph).view(np.uint32)
+        order = np.lexsort(words.T[::-1])
+        return words[order]
+
+    want = canonical(shapes[0])
+    assert len(want) > 1000
+    for v in range(1, 6):
+        got = canonical(shapes[v])
+        assert got.shape == want.shape and (got == want).all(), f"shape {v} differs"
