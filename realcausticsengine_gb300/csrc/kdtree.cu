@@ -6,8 +6,9 @@
 //   hist x4   8-bit radix select of the rank-count/2 key along the node's axis (the
 //             leading digits the node's box fixes are skipped)
 //   partition photons below / equal / above the median key to their halves
-// A CTA covers kChunk consecutive positions; because nodes on these levels hold more
-// than kChunk photons, a chunk meets at most two nodes (and one ancestor median
+// A CTA covers T x kItems consecutive positions (T = 256 threads on levels whose nodes
+// hold more than 2048 photons, else 128); because nodes on these levels hold more
+// than that many photons, a chunk meets at most two nodes (and one ancestor median
 // between them), so histograms and counters stay in shared memory and only their
 // totals go to global memory.
 // From the first level with at most kSmemSeg photons per node, one CTA per node
@@ -25,9 +26,9 @@ namespace rc {
 namespace {
 
 constexpr int kSmemSeg = 1024;      // largest node finished in shared memory (~66 KB: 3 CTAs per SM)
-constexpr int kChunk = 1024;        // positions per CTA in the global passes (<= kSmemSeg)
-constexpr int kThreads = 128;
-constexpr int kItems = kChunk / kThreads;
+constexpr int kItems = 8;           // positions per thread in the global passes
+constexpr int kThreads = 128;       // CTA size of the global passes (kThreads x kItems <= kSmemSeg)
+constexpr int kWideThreads = 256;   // CTA size on levels whose nodes hold more than its positions
 constexpr int kSmemThreads = 256;
 constexpr float kSplitBias = 1.175494e-38f;   // src/KD_Tree.cpp:150
 
@@ -97,7 +98,7 @@ struct ChunkNodes {
     long long eA, sA, eB, sB, c;
 };
 
-__device__ __forceinline__ void chunk_nodes(long long a, int level, long long n, ChunkNodes& cn) {
+__device__ __forceinline__ void chunk_nodes(long long a, long long chunk, int level, long long n, ChunkNodes& cn) {
     long long c = n >> level;
     long long s;
     long long e = locate(a, level, n, &s);
@@ -105,7 +106,7 @@ __device__ __forceinline__ void chunk_nodes(long long a, int level, long long n,
     cn.eA = e; cn.sA = s; cn.c = c;
     long long endA = s + c;
     cn.eB = 0; cn.sB = -1;
-    if (endA < a + kChunk && endA < n) {
+    if (endA < a + chunk && endA < n) {
         long long s2;
         long long e2 = locate(endA, level, n, &s2);
         if (e2 == 0 && endA + 1 < n) e2 = locate(endA + 1, level, n, &s2);
@@ -132,11 +133,12 @@ __global__ void k_level_init(int level, long long first, long long count, int* n
     s.first = 0;
 }
 
-__global__ void __launch_bounds__(kThreads) k_bbox(Buffers B, int cur, int level, long long n, long long first, int* nbox) {
+template <int T>
+__global__ void __launch_bounds__(T) k_bbox(Buffers B, int cur, int level, long long n, long long first, int* nbox) {
     __shared__ ChunkNodes cn;
     __shared__ int sb[2][6];
-    long long a = blockIdx.x * (long long)kChunk;
-    if (threadIdx.x == 0) chunk_nodes(a, level, n, cn);
+    long long a = blockIdx.x * (long long)(T * kItems);
+    if (threadIdx.x == 0) chunk_nodes(a, T * kItems, level, n, cn);
     if (threadIdx.x < 12) sb[threadIdx.x / 6][threadIdx.x % 6] = (threadIdx.x % 6) < 3 ? 0x7fffffff : (int)0x80000000;
     __syncthreads();
     int mn[2][3], mx[2][3];
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(kThreads) k_bbox(Buffers B, int cur, int level
     const Side S = side(B, cur);
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {   // loads of all rounds in flight together
-        long long i = a + it * kThreads + threadIdx.x;
+        long long i = a + it * T + threadIdx.x;
         wh[it] = i < n ? which(i, cn) : -1;
         const long long j = wh[it] >= 0 ? i : a;
         px[it] = S.x[j]; py[it] = S.y[j]; pz[it] = S.z[j];
@@ -213,16 +215,17 @@ __device__ __forceinline__ float coord(const Side& S, long long i, int axis) {
     return axis == 0 ? S.x[i] : (axis == 1 ? S.y[i] : S.z[i]);
 }
 
-__global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level, long long n, long long first,
+template <int T>
+__global__ void __launch_bounds__(T) k_hist(Buffers B, int cur, int level, long long n, long long first,
                                                    const NodeSel* sel, uint32_t* hist, int pass) {
     __shared__ ChunkNodes cn;
     __shared__ uint32_t sh[2][256];
     __shared__ uint32_t pre[2];
     __shared__ int ax[2];
     __shared__ bool live[2];   // the node's digit for this pass is not fixed by its box
-    long long a = blockIdx.x * (long long)kChunk;
+    long long a = blockIdx.x * (long long)(T * kItems);
     if (threadIdx.x == 0) {
-        chunk_nodes(a, level, n, cn);
+        chunk_nodes(a, T * kItems, level, n, cn);
         const NodeSel* sa = sel + (cn.eA - first);
         ax[0] = sa->axis; pre[0] = sa->prefix; live[0] = pass >= sa->first;
         live[1] = false;
@@ -231,7 +234,7 @@ __global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level
             ax[1] = sb->axis; pre[1] = sb->prefix; live[1] = pass >= sb->first;
         }
     }
-    for (int k = threadIdx.x; k < 512; k += kThreads) (&sh[0][0])[k] = 0;
+    for (int k = threadIdx.x; k < 512; k += T) (&sh[0][0])[k] = 0;
     __syncthreads();
     if (!live[0] && !live[1]) return;
     const int shift = 24 - 8 * pass;
@@ -241,7 +244,7 @@ __global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level
     const Side S = side(B, cur);
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
-        long long i = a + it * kThreads + threadIdx.x;
+        long long i = a + it * T + threadIdx.x;
         const int w = i < n ? which(i, cn) : -1;
         wh[it] = w >= 0 && live[w] ? w : -1;
         val[it] = wh[it] >= 0 ? coord(S, i, ax[wh[it]]) : 0.0f;
@@ -262,7 +265,7 @@ __global__ void __launch_bounds__(kThreads) k_hist(Buffers B, int cur, int level
             atomicAdd(&(&sh[0][0])[slot], (uint32_t)__popc(peers));
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < 512; k += kThreads) {
+    for (int k = threadIdx.x; k < 512; k += T) {
         int q = k >> 8;
         uint32_t v = (&sh[0][0])[k];
         long long e = q == 0 ? cn.eA : cn.eB;
@@ -318,16 +321,17 @@ __global__ void k_select(long long count, long long first, int level, long long 
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int level, long long n, long long first,
+template <int T>
+__global__ void __launch_bounds__(T) k_partition(Buffers B, int cur, int level, long long n, long long first,
                                                         NodeSel* sel, uint2* nodes, int* err) {
     __shared__ ChunkNodes cn;
     __shared__ int ax[2], krem[2], eq[2];
     __shared__ uint32_t med[2];
     __shared__ int base[6];
-    __shared__ int woff[kItems][kThreads / 32][6];
-    long long a = blockIdx.x * (long long)kChunk;
+    __shared__ int woff[kItems][T / 32][6];
+    long long a = blockIdx.x * (long long)(T * kItems);
     if (threadIdx.x == 0) {
-        chunk_nodes(a, level, n, cn);
+        chunk_nodes(a, T * kItems, level, n, cn);
         NodeSel s = sel[cn.eA - first];
         ax[0] = s.axis; krem[0] = s.krem; eq[0] = s.eq; med[0] = s.prefix;
         if (cn.eB) {
@@ -337,7 +341,7 @@ __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int 
     }
     __syncthreads();
     const int dst = cur ^ 1;
-    // coalesced rounds of kThreads consecutive positions; the rank of a photon in its
+    // coalesced rounds of T consecutive positions; the rank of a photon in its
     // class (node A/B x below/equal/above) follows position order inside the CTA:
     // ballots within a warp, then per-(round, warp) offsets
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -350,7 +354,7 @@ __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int 
     const Side S = side(B, cur), D = side(B, dst);
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
-        const long long i = a + it * kThreads + threadIdx.x;
+        const long long i = a + it * T + threadIdx.x;
         const long long j = i < n ? i : a;
         px[it] = S.x[j]; py[it] = S.y[j]; pz[it] = S.z[j]; pid[it] = S.id[j];
         cls[it] = i < n ? which(i, cn) : -2;
@@ -378,7 +382,7 @@ __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int 
         const int q = threadIdx.x;
         int run = 0;
         for (int it = 0; it < kItems; ++it)
-            for (int w = 0; w < kThreads / 32; ++w) {
+            for (int w = 0; w < T / 32; ++w) {
                 const int v = woff[it][w][q];
                 woff[it][w][q] = run;
                 run += v;
@@ -391,7 +395,7 @@ __global__ void __launch_bounds__(kThreads) k_partition(Buffers B, int cur, int 
     const long long k = c >> 1, odd = c & 1;
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
-        long long i = a + it * kThreads + threadIdx.x;
+        long long i = a + it * T + threadIdx.x;
         int q = cls[it];
         if (q == -2) continue;
         const float xv = px[it], yv = py[it], zv = pz[it];
@@ -732,21 +736,29 @@ int kd_build(const float4* pos4, long long n, KdTree& tree, void* scratch, size_
     nl++;
     if (l0 > 0) cudaMemsetAsync(hist, 0, 1024 * (size_t)maxnodes, stream);
     int cur = 0;
-    const unsigned chunks = (unsigned)((n + kChunk - 1) / kChunk);
     for (int l = 0; l < l0; ++l) {
         long long first = 1LL << l, count = 1LL << l;
         unsigned g = (unsigned)((count + 255) / 256);
+        // half as many CTAs, each twice as wide, while a wide chunk still meets at most
+        // two nodes: the passes' per-CTA fixed cost (chunk location, shared-memory
+        // reduction) is paid half as often
+        const bool wide = (n >> l) > (long long)kWideThreads * kItems;
+        const long long span = (long long)(wide ? kWideThreads : kThreads) * kItems;
+        const unsigned chunks = (unsigned)((n + span - 1) / span);
         k_level_init<<<g, 256, 0, stream>>>(l, first, count, nbox, sel, n);
-        k_bbox<<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, nbox);
+        if (wide) k_bbox<kWideThreads><<<chunks, kWideThreads, 0, stream>>>(B, cur, l, n, first, nbox);
+        else k_bbox<kThreads><<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, nbox);
         k_axis<<<g, 256, 0, stream>>>(count, nbox, sel);
         nl += 3;
         for (int pass = 0; pass < 4; ++pass) {
-            k_hist<<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, sel, hist, pass);
+            if (wide) k_hist<kWideThreads><<<chunks, kWideThreads, 0, stream>>>(B, cur, l, n, first, sel, hist, pass);
+            else k_hist<kThreads><<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, sel, hist, pass);
             k_select<<<(unsigned)((count + 7) / 8), 256, 0, stream>>>(count, first, l, n, sel, hist, pass, tree.nodes,
                                                                        err);
             nl += 2;
         }
-        k_partition<<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, sel, tree.nodes, err);
+        if (wide) k_partition<kWideThreads><<<chunks, kWideThreads, 0, stream>>>(B, cur, l, n, first, sel, tree.nodes, err);
+        else k_partition<kThreads><<<chunks, kThreads, 0, stream>>>(B, cur, l, n, first, sel, tree.nodes, err);
         nl++;
         cur ^= 1;
     }
