@@ -334,7 +334,7 @@ def run_ours(args):
         "clocks": clk.summary(),
         "phase_ms_per_step": {k: st[k] for k in ("light_ms", "kd_ms", "camera_ms", "gather_ms")},
         "phase_note": "event windows of the last iteration; the camera pass runs on a second stream "
-                      "beside the light pass and the KD build, its window opening with the light pass",
+                      "beside the light pass's last launch and the KD build, its window opening there",
         "wall_s": wall,
     }
     if not args.no_learned:

@@ -43,6 +43,7 @@ def lib() -> C.CDLL:
     L.rc_get_stats.argtypes = [C.c_void_p, C.c_int]
     L.rc_trace_rays.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
     L.rc_trace_rays_full.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
+    L.rc_trace_rays_shape.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_int]
     L.rc_kd_query.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
                               C.c_longlong, C.POINTER(C.c_longlong)]
     L.rc_gather_query.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_void_p,
@@ -81,7 +82,7 @@ def check(rc: int, what: str = "") -> None:
 
 EXPORTS = ["init", "main", "rc_default_config", "rc_set_config", "rc_prepare", "rc_prepare_host",
            "rc_host_mesh_bvh", "rc_host_world_bvh", "rc_render", "rc_read_image", "rc_release",
-           "rc_last_error", "rc_get_stats", "rc_trace_rays", "rc_trace_rays_full", "rc_kd_query",
+           "rc_last_error", "rc_get_stats", "rc_trace_rays", "rc_trace_rays_full", "rc_trace_rays_shape", "rc_kd_query",
            "rc_kd_build_nodes", "rc_light_photons", "rc_render_timed", "rc_kd_build_noalloc",
            "rc_kd_noalloc_last_error", "rc_proposal_state", "rc_render_debug",
            "rc_save_state", "rc_load_state", "rc_scene_dump", "rc_prepare_stats",

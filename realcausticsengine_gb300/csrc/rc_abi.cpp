@@ -607,14 +607,17 @@ int size_class(long long n) { return n > 0 ? 63 - __builtin_clzll((unsigned long
 
 // The light pass in launch shape v: the persistent pass's shapes, or (v ==
 // pass_variants()) the wavefront pass with its path state in the context's scratch.
-int light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s, int v) {
+// `tail`, if given, is recorded where the pass stops filling the GPU: before the
+// wavefront pass's last launch, after a persistent pass.
+int light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s, int v, cudaEvent_t tail = nullptr) {
     DeviceState& d = ctx().dev;
     if (v == pass_variants()) {
         RC_CUDA(d.wf_scratch.reserve(light_wavefront_scratch_bytes(p.num_light_paths)));
-        launch_light_wavefront(p, ph, d.wf_scratch.p, s);
+        launch_light_wavefront(p, ph, d.wf_scratch.p, s, tail);
         return RC_OK;
     }
     launch_light_pass(p, ph, d.counters.p + 6, s, v);
+    if (tail) RC_CUDA(cudaEventRecord(tail, s));
     return RC_OK;
 }
 
@@ -787,15 +790,16 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             lvar = slot.load();
             RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         }
-        if (cam_side && attempt == 0) RC_CUDA(cudaEventRecord(d.fork, s));
+        // the camera pass forks where the light pass stops filling the GPU
+        const bool fork = cam_side && attempt == 0;
         if (sampler == RC_SAMPLER_UNIFORM) {
-            r0 = light_pass(p, ph, s, lvar);
+            r0 = light_pass(p, ph, s, lvar, fork ? d.fork : nullptr);
             if (r0) return r0;
         }
         else launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaEventRecord(d.ev[1], s));
-        if (cam_side && attempt == 0) {
+        if (fork) {
             // (its count is read at the join: a read into pageable memory would wait here)
             RC_CUDA(cudaStreamWaitEvent(d.side, d.fork, 0));
             RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), d.side));
@@ -1064,16 +1068,15 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
     PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, pc, d.counters.p};
     QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qc, d.counters.p + 1};
-    // the camera pass on a branch of its own beside the light pass and the KD build
-    // (it reads nothing they write), joined before the count check
-    RC_CUDA(cudaEventRecord(d.fork, s));
-    RC_CUDA(cudaStreamWaitEvent(d.side, d.fork, 0));
+    // the camera pass on a branch of its own beside the light pass's tail and the KD
+    // build (it reads nothing they write), joined before the count check
     RC_CUDA(record(d.ev[0], s));
     launch_light_order(p, d.order_scratch.p, d.path_order.p, s);
     p.path_order = d.path_order.p;
-    r0 = light_pass(p, ph, s, d.async_lvar);
-    if (r0) return r0;
+    r0 = light_pass(p, ph, s, d.async_lvar, d.fork);   // the camera branch forks where
+    if (r0) return r0;                                  // the light pass stops filling the GPU
     RC_CUDA(record(d.ev[1], s));
+    RC_CUDA(cudaStreamWaitEvent(d.side, d.fork, 0));
     RC_CUDA(record(d.ev[4], d.side));
     launch_camera_pass(p, qb, d.counters.p + 7, d.side, d.async_cvar);
     RC_CUDA(record(d.ev[5], d.side));
@@ -1894,6 +1897,11 @@ int rc_trace_rays(int n, const float* origins, const float* directions, float tm
 }
 
 int rc_trace_rays_full(int n, const float* origins, const float* directions, float tmin, float* out) {
+    return rc_trace_rays_shape(n, origins, directions, tmin, out, 0);
+}
+
+int rc_trace_rays_shape(int n, const float* origins, const float* directions, float tmin, float* out, int shape) {
+    if (shape != 0 && shape != 1) { ctx().err = "traversal shape must be 0 or 1"; return RC_E_INVALID; }
     int r = prepare();
     if (r) return r;
     if (n < 0 || (n > 0 && (!origins || !directions || !out))) { ctx().err = "bad ray arrays"; return RC_E_INVALID; }
@@ -1903,7 +1911,7 @@ int rc_trace_rays_full(int n, const float* origins, const float* directions, flo
     RC_CUDA(o.reserve(3 * (size_t)n)); RC_CUDA(d.reserve(3 * (size_t)n)); RC_CUDA(f.reserve(16 * (size_t)n));
     RC_CUDA(cudaMemcpyAsync(o.p, origins, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
     RC_CUDA(cudaMemcpyAsync(d.p, directions, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
-    launch_trace_rays(ctx().dev.view, n, o.p, d.p, tmin, f.p, nullptr, ctx().dev.errors.p, s);
+    launch_trace_rays(ctx().dev.view, n, o.p, d.p, tmin, f.p, nullptr, ctx().dev.errors.p, s, shape);
     RC_CUDA(cudaGetLastError());
     RC_CUDA(cudaMemcpyAsync(out, f.p, 64 * (size_t)n, cudaMemcpyDeviceToHost, s));
     RC_CUDA(cudaStreamSynchronize(s));

@@ -5,7 +5,10 @@
 // (src/mesh.cpp:70-105) -> CacheBVHNode_mesh::hit (src/BVH/BVH_mesh.cpp:265-283) ->
 // aabb::hit (src/aabb.cpp:6-41) and Triangle::hit (src/Triangle.cpp:20-88):
 //  * stack DFS, right child pushed before left, so the left subtree is visited first;
-//  * every box is tested against the current closest distance of its own level;
+//  * every box is tested against the current closest distance of its own level (the
+//    warp-stepped mesh traversal tests both children's boxes at their parent and keeps
+//    the right one's entry distance on the stack: mesh_traverse_steps says why that is
+//    the same test);
 //  * a world leaf starts a fresh record (distance = inf) and, if any of its meshes is
 //    hit, OVERWRITES the running result - so the answer is the last hit world leaf's
 //    closest triangle, exactly as the reference returns it;
@@ -50,6 +53,14 @@ struct LocalStack {
     __device__ __forceinline__ int& operator[](int i) { return s[i]; }
 };
 struct CallStack {};
+// WarpStepStack: the tag of the warp-stepped traversal (mesh_traverse_steps), for
+// kernels whose lanes all trace at once; its per-traversal stack holds node index and
+// box entry distance (float bits) per entry.
+struct WarpStepStack {};
+struct LocalPairStack {
+    int2 s[kStackSize];
+    __device__ __forceinline__ int2& operator[](int i) { return s[i]; }
+};
 
 struct HitRec {
     float t, u, v;
@@ -75,6 +86,29 @@ __device__ __forceinline__ bool box_hit(float4 lo, float4 hi, F3 o, F3 inv, floa
     tmax = t1 < tmax ? t1 : tmax;
     if (tmax < tmin) return false;
     return true;
+}
+
+// box_hit in two parts: the same slab arithmetic, with the box's entry distance n
+// (tmin and the three near-slab distances, NaNs skipped, as box_hit folds them) kept.
+// box_hit's early exits never change its answer (the interval only narrows), so it
+// equals !(far < near) over all three slabs: box_entry returns exactly box_hit(tmax),
+// and for any tmax' <= tmax, box_hit(tmax') == box_entry(tmax) && !(tmax' < n).
+__device__ __forceinline__ bool box_entry(float4 lo, float4 hi, F3 o, F3 inv, float tmin, float tmax, float& n) {
+    float a = tmin, b = tmax;
+    float t0 = (lo.x - o.x) * inv.x, t1 = (hi.x - o.x) * inv.x;
+    if (inv.x < 0) { float s = t0; t0 = t1; t1 = s; }
+    a = t0 > a ? t0 : a;
+    b = t1 < b ? t1 : b;
+    t0 = (lo.y - o.y) * inv.y; t1 = (hi.y - o.y) * inv.y;
+    if (inv.y < 0) { float s = t0; t0 = t1; t1 = s; }
+    a = t0 > a ? t0 : a;
+    b = t1 < b ? t1 : b;
+    t0 = (lo.z - o.z) * inv.z; t1 = (hi.z - o.z) * inv.z;
+    if (inv.z < 0) { float s = t0; t0 = t1; t1 = s; }
+    a = t0 > a ? t0 : a;
+    b = t1 < b ? t1 : b;
+    n = a;
+    return !(b < a);
 }
 
 // Möller-Trumbore as src/Triangle.cpp:44-66 computes it.
@@ -138,6 +172,73 @@ __device__ __forceinline__ bool mesh_traverse_impl(const SceneView& s, int mesh,
     return true;
 }
 
+// Mesh::hit (src/mesh.cpp:70-105) visits nodes in left-first DFS order and tests each
+// box when it is popped, against the running distance then.  Here an inner node tests
+// both children's boxes at once (two independent loads in flight): the left child is
+// the node the reference pops next, with the same distance, so its test is the
+// reference's; the right child is popped only after the left subtree, when the
+// distance may have shrunk.  The distance never grows, so a right box that fails now
+// fails then too (box_hit is monotone in tmax) and is not pushed; one that passes is
+// pushed with its entry distance n, and at its pop the reference's test is
+// !(distance < n) (box_entry).  Same nodes, same triangles, same order.
+template <class Stack>
+__device__ __forceinline__ bool mesh_traverse_steps(const SceneView& s, int mesh, F3 o, F3 d, F3 inv, float tmin,
+                                                   HitRec& rec, bool& any, int* overflow, Stack& stack) {
+    // the lanes that arrive together step together: one node per lane per round, the
+    // round ending in a vote, so that a warp's lanes meet again after every node
+    const unsigned lanes = __activemask();
+    const int root = __ldg(&s.mesh_root[mesh]);
+    float4 lo = __ldg(&s.nodes[2 * root]);
+    float4 hi = __ldg(&s.nodes[2 * root + 1]);
+    float n;
+    bool active = box_entry(lo, hi, o, inv, tmin, rec.t, n);
+    int sp = 0;
+    bool ok = true;
+    while (__any_sync(lanes, active)) {
+        if (!active) continue;
+        const uint32_t w0 = __float_as_uint(lo.w), w1 = __float_as_uint(hi.w);
+        bool descend = false;
+        if (!(w0 & 0x80000000u)) {
+            const float4 llo = __ldg(&s.nodes[2 * w0]), lhi = __ldg(&s.nodes[2 * w0 + 1]);
+            const float4 rlo = __ldg(&s.nodes[2 * w1]), rhi = __ldg(&s.nodes[2 * w1 + 1]);
+            float nl, nr;
+            const bool hl = box_entry(llo, lhi, o, inv, tmin, rec.t, nl);
+            const bool hr = box_entry(rlo, rhi, o, inv, tmin, rec.t, nr);
+            if (hl && hr) {
+                if (sp < kStackSize) stack[sp++] = make_int2((int)w1, __float_as_int(nr));
+                else { *overflow = 1; ok = false; active = false; continue; }
+            }
+            descend = hl || hr;
+            lo = hl ? llo : rlo;
+            hi = hl ? lhi : rhi;
+        } else {
+            const int cnt = (int)(w0 & 0x7fffffffu);
+            for (int k = 0; k < cnt; ++k) {
+                const int slot = (int)w1 + k;
+                float t, u, v;
+                if (tri_hit(s, slot, o, d, tmin, rec.t, t, u, v)) {
+                    rec.t = t; rec.u = u; rec.v = v; rec.slot = slot;
+                    any = true;
+                }
+            }
+        }
+        if (!descend) {
+            // pop pending right children until one whose box the current distance reaches
+            int next = -1;
+            while (sp > 0 && next < 0) {
+                const int2 e = stack[--sp];
+                if (!(rec.t < __int_as_float(e.y))) next = e.x;
+            }
+            active = next >= 0;
+            if (active) {
+                lo = __ldg(&s.nodes[2 * next]);
+                hi = __ldg(&s.nodes[2 * next + 1]);
+            }
+        }
+    }
+    return ok;
+}
+
 template <class Stack>
 __device__ __forceinline__ bool mesh_traverse(const SceneView& s, int mesh, F3 o, F3 d, F3 inv, float tmin,
                                               HitRec& rec, bool& any, int* overflow, Stack& stack) {
@@ -149,6 +250,13 @@ __device__ __forceinline__ bool mesh_traverse<CallStack>(const SceneView& s, int
                                                          CallStack&) {
     LocalStack st;
     return mesh_traverse_impl(s, mesh, o, d, inv, tmin, rec, any, overflow, st);
+}
+template <>
+__device__ __forceinline__ bool mesh_traverse<WarpStepStack>(const SceneView& s, int mesh, F3 o, F3 d, F3 inv,
+                                                             float tmin, HitRec& rec, bool& any, int* overflow,
+                                                             WarpStepStack&) {
+    LocalPairStack st;
+    return mesh_traverse_steps(s, mesh, o, d, inv, tmin, rec, any, overflow, st);
 }
 
 // Scene::hit.  `out` is the reported record (t = inf when nothing was hit).  `stack`

@@ -116,8 +116,9 @@ void launch_pad_photons(float4* pos, const unsigned long long* count, long long 
                         cudaStream_t s);
 void launch_check_counts(const unsigned long long* photons, long long photon_cap, const unsigned long long* queries,
                          long long query_cap, int* flag, cudaStream_t s);
+// shape 0: the persistent passes' traversal; 1: the wavefront pass's warp-stepped one.
 void launch_trace_rays(const SceneView& s, int n, const float* o, const float* d, float tmin, float* out_full,
-                       unsigned* out_words, int* err, cudaStream_t st);
+                       unsigned* out_words, int* err, cudaStream_t st, int shape = 0);
 // Photon records in tree order (tp.t0/t1/t2 from ph.pos/dir/tp; only t0 when ph.dir is null).
 void launch_tree_records(PhotonBuf ph, const KdTree& tree, TreePhotons tp, cudaStream_t s);
 // Node bounding boxes used by the gather to prune exactly: the photons in tree order
@@ -163,8 +164,11 @@ int gather_default_variant();
 // Wavefront light pass: the same paths and photons as launch_light_pass, one bounce of
 // every live path per round, split into a closest-hit kernel and a shading kernel with
 // path state and queues in `scratch` (light_wavefront_scratch_bytes(num_light_paths)).
+// `tail`, if given, is recorded on s before the last launch (the few paths left after the
+// rounds, which leaves most SMs idle): work that waits on it fills them.
 size_t light_wavefront_scratch_bytes(long long n);
-void launch_light_wavefront(const VMParams& p, PhotonBuf ph, void* scratch, cudaStream_t s);
+void launch_light_wavefront(const VMParams& p, PhotonBuf ph, void* scratch, cudaStream_t s,
+                            cudaEvent_t tail = nullptr);
 // Launch shapes of the persistent light and camera passes (block size x traversal-stack
 // placement), chosen by the autotuner; 0 is the default.  The light pass has one more:
 // pass_variants() is the wavefront pass.

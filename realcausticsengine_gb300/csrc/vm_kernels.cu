@@ -172,7 +172,7 @@ __global__ void k_wf_start(const VMParams P, WfState W) {
 template <int kMinBlocks>
 __global__ void __launch_bounds__(128, kMinBlocks) k_wf_trace(const VMParams P, WfState W, int q) {
     const unsigned long long n = W.count[q];
-    CallStack stk;
+    WarpStepStack stk;   // the lanes of a warp trace together here: step them together
     for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < n;
          j += (unsigned long long)gridDim.x * blockDim.x) {
         const uint32_t slot = W.queue[q][j];
@@ -411,6 +411,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_camera_pass_persistent(c
     }
 }
 
+// Stack: CallStack (the reference-order pop-and-test traversal of the persistent passes)
+// or WarpStepStack (the warp-stepped traversal of the wavefront pass).
+template <class Stack>
 __global__ void k_trace_rays(const SceneView S, int n, const float* __restrict__ o, const float* __restrict__ d,
                              float tmin, float* out_full, unsigned* out_words, int* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -418,7 +421,8 @@ __global__ void k_trace_rays(const SceneView S, int n, const float* __restrict__
     F3 ro = f3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
     F3 rd = f3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
     HitRec h;
-    bool hit = scene_hit(S, ro, rd, tmin, h, err);
+    Stack stk;
+    bool hit = scene_hit(S, ro, rd, tmin, h, err, stk);
     Isect is;
     if (hit) fill_isect(S, h, ro, rd, is);
     if (out_words) {
@@ -516,7 +520,7 @@ size_t light_wavefront_scratch_bytes(long long n) {
     return al(16 * m) * 4 + al(8 * m) + al(16 * m) + 2 * al(4 * m) + 256;
 }
 
-void launch_light_wavefront(const VMParams& p, PhotonBuf ph, void* scratch, cudaStream_t s) {
+void launch_light_wavefront(const VMParams& p, PhotonBuf ph, void* scratch, cudaStream_t s, cudaEvent_t tail) {
     const long long n = p.num_light_paths;
     if (n <= 0) return;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
@@ -547,6 +551,7 @@ void launch_light_wavefront(const VMParams& p, PhotonBuf ph, void* scratch, cuda
         cudaMemsetAsync(W.count + (q ^ 1), 0, sizeof(unsigned long long), s);
         k_wf_shade<<<shade_grid, 128, 0, s>>>(p, ph, W, q);
     }
+    if (tail) cudaEventRecord(tail, s);
     k_wf_finish<<<finish_grid, 128, 0, s>>>(p, ph, W, q);
 }
 
@@ -669,9 +674,12 @@ void launch_check_counts(const unsigned long long* photons, long long photon_cap
 }
 
 void launch_trace_rays(const SceneView& sv, int n, const float* o, const float* d, float tmin, float* out_full,
-                       unsigned* out_words, int* err, cudaStream_t st) {
+                       unsigned* out_words, int* err, cudaStream_t st, int shape) {
     if (n <= 0) return;
-    k_trace_rays<<<(n + 127) / 128, 128, 0, st>>>(sv, n, o, d, tmin, out_full, out_words, err);
+    if (shape == 1)
+        k_trace_rays<WarpStepStack><<<(n + 127) / 128, 128, 0, st>>>(sv, n, o, d, tmin, out_full, out_words, err);
+    else
+        k_trace_rays<CallStack><<<(n + 127) / 128, 128, 0, st>>>(sv, n, o, d, tmin, out_full, out_words, err);
 }
 
 }  // namespace rc

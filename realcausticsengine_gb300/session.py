@@ -118,13 +118,15 @@ class Renderer:
         check(self.L.rc_get_stats(a.ctypes.data, 16), "rc_get_stats")
         return dict(zip(STAT_NAMES, a.tolist()))
 
-    def trace(self, origins: np.ndarray, dirs: np.ndarray, tmin: float = 0.001) -> np.ndarray:
+    def trace(self, origins: np.ndarray, dirs: np.ndarray, tmin: float = 0.001, shape: int = 0) -> np.ndarray:
+        """Closest hits (n, 16) through traversal `shape`: 0 the persistent passes',
+        1 the wavefront pass's warp-stepped one."""
         o = np.ascontiguousarray(origins, np.float32)
         d = np.ascontiguousarray(dirs, np.float32)
         n = len(o)
         out = np.zeros((n, 16), np.float32)
-        check(self.L.rc_trace_rays_full(n, o.ctypes.data, d.ctypes.data, C.c_float(tmin), out.ctypes.data),
-              "rc_trace_rays_full")
+        check(self.L.rc_trace_rays_shape(n, o.ctypes.data, d.ctypes.data, C.c_float(tmin), out.ctypes.data,
+                                         int(shape)), "rc_trace_rays_shape")
         return out
 
     def camera_queries(self, iteration: int) -> np.ndarray:

@@ -46,10 +46,11 @@ def _random_rays(rng, n, lo=-4.0, hi=4.0, zlo=0.2, zhi=5.0, aim=None):
 def test_closest_hits_golden(golden):
     sc = scenes.test_scene(48, 36, subdiv=2, samples=2)
     r = Renderer(sc)
-    got = r.trace(golden["ray_o"], golden["ray_d"])
+    got = [r.trace(golden["ray_o"], golden["ray_d"], shape=k) for k in (0, 1)]
     want = golden["ray_hits"]
     r.release()
-    assert (got[:, :15].view(np.uint32) == want[:, :15].view(np.uint32)).all()
+    for g in got:   # both traversals: the persistent passes' and the warp-stepped one
+        assert (g[:, :15].view(np.uint32) == want[:, :15].view(np.uint32)).all()
 
 
 @pytest.mark.parametrize("name", ["test_scene", "sun_scene", "glass_sphere", "water"])
@@ -68,13 +69,14 @@ def test_closest_hits_vs_oracle(orc, name):
     if name == "water":
         o[:, 2] = rng.uniform(-1.4, 3.0, n)
     r = Renderer(sc)
-    got = r.trace(o, d)
+    got = [r.trace(o, d, shape=k) for k in (0, 1)]
     r.release()
     _oracle_scene(orc, sc)
     want = _oracle_trace(orc, o, d)
     assert want[:, 0].sum() > n * 0.3
-    mism = (got.view(np.uint32) != want.view(np.uint32)).any(1)
-    assert not mism.any(), f"{int(mism.sum())} of {n} rays differ"
+    for k, g in enumerate(got):
+        mism = (g.view(np.uint32) != want.view(np.uint32)).any(1)
+        assert not mism.any(), f"traversal {k}: {int(mism.sum())} of {n} rays differ"
 
 
 @pytest.mark.parametrize("k", range(5))

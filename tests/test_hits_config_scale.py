@@ -3,7 +3,7 @@ restatement of Scene::hit (src/Scene.cpp:154-189, world leaves src/BVH/BVH_world
 Möller-Trumbore src/Triangle.cpp:20-88), which is pinned to the compiled reference.
 
 The GPU path builds the mesh BVHs on the device (word-for-word the host build) and
-traverses them; the oracle builds its own host BVH.  Every field of every ray's hit
+traverses them with both of its traversals; the oracle builds its own host BVH.  Every field of every ray's hit
 record must match: t, u, v, Ng, Ns, position, front face, material, triangle id.
 """
 import ctypes as C
@@ -31,16 +31,19 @@ def _rays(rng, n, lo, hi, zlo, zhi, aim_lo, aim_hi, aim_z):
 
 
 def _compare(orc, sc, o, d, min_hit_frac):
+    """Both GPU traversals (0: the persistent passes', 1: the wavefront pass's
+    warp-stepped one) against the oracle."""
     r = Renderer(sc)
-    got = r.trace(o, d)
+    got = [r.trace(o, d, shape=k) for k in (0, 1)]
     r.release()
     InitArgs(sc).call(orc.oracle_init)
     assert orc.oracle_prepare(None) == 0
     want = np.zeros((len(o), 16), np.float32)
     orc.oracle_trace(len(o), o.ctypes.data, d.ctypes.data, C.c_float(0.001), want.ctypes.data, 32)
     assert want[:, 0].mean() > min_hit_frac
-    mism = (got.view(np.uint32) != want.view(np.uint32)).any(1)
-    assert not mism.any(), f"{int(mism.sum())} of {len(o)} rays differ"
+    for k, g in enumerate(got):
+        mism = (g.view(np.uint32) != want.view(np.uint32)).any(1)
+        assert not mism.any(), f"traversal {k}: {int(mism.sum())} of {len(o)} rays differ"
 
 
 def test_hits_water_pool_full_grid(orc):
