@@ -187,6 +187,24 @@ rc_context* rc_context_create(void);
 int rc_context_bind(rc_context* ctx);
 int rc_context_destroy(rc_context* ctx);
 
+/* Batch render (no counterpart in the reference, which renders one scene per call to
+ * main(): src/Vertex_Merging.cpp:367-379 is its per-scene iteration loop).  Renders
+ * `iterations` more progressive iterations of each of the n scenes held by ctxs[0..n-1]
+ * (distinct contexts, each with a scene from init() and the uniform sampler without the
+ * learned proposal) as one launch set per iteration: one persistent light pass over all
+ * scenes' light paths, one persistent camera pass over all scenes' pixels, and each
+ * scene's light-path order, KD build, query order and gather as parallel branches of the
+ * same CUDA graph, which is captured, updated in place and replayed per iteration.  A
+ * scene that has rendered no iteration yet renders its first one alone first (it fixes
+ * the photon and query capacities of the graph); an iteration whose counts outgrow
+ * them is rendered again alone at the end.  Each scene's image equals what rc_render on
+ * its own context gives (the same samples; FP64 sums in another order).  Synchronous; the
+ * contexts must not be in use on other threads meanwhile.  Errors are reported through
+ * the calling thread's context.  out (NULL or 6 doubles): [0] device ms of the batch
+ * iterations, [1] batch iterations, [2] kernel launches in them, [3] iterations rendered
+ * again, [4] / [5] light / camera pass ms of the last batch iteration. */
+int rc_batch_render(rc_context* const* ctxs, int n, int iterations, double* out);
+
 /* Timing of the last rc_prepare: out[0] = mesh BVH build ms (host or device, uploads
  * included), out[1] = 1 if the device built the mesh BVHs, out[2] = world BVH + light
  * + material conversion + remaining uploads ms, out[3] = mesh BVH nodes, out[4] = device

@@ -1058,29 +1058,25 @@ int async_setup(const HostScene& sc) {
     return RC_OK;
 }
 
-// Enqueue iteration `it` (no host synchronisation); `flag` receives the overflow flag.
-int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
+// The two ends of an asynchronous iteration (no host synchronisation), shared by the
+// single-scene replay and the batch (batch_render).  async_head, on s: the iteration's
+// photon and query counters reset, the light-path order.
+int async_head(VMParams& p, cudaStream_t s) {
     DeviceState& d = ctx().dev;
-    cudaStream_t s = d.stream;
-    int r0 = RC_OK;
-    VMParams p = make_params(sc, it);
-    const long long pc = d.async_pcap, qc = d.async_qcap;
     RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long) * 2, s));
-    PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, pc, d.counters.p};
-    QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qc, d.counters.p + 1};
-    // the camera pass on a branch of its own beside the light pass's tail and the KD
-    // build (it reads nothing they write), joined before the count check
     RC_CUDA(record(d.ev[0], s));
     launch_light_order(p, d.order_scratch.p, d.path_order.p, s);
     p.path_order = d.path_order.p;
-    r0 = light_pass(p, ph, s, d.async_lvar, d.fork);   // the camera branch forks where
-    if (r0) return r0;                                  // the light pass stops filling the GPU
-    RC_CUDA(record(d.ev[1], s));
-    RC_CUDA(cudaStreamWaitEvent(d.side, d.fork, 0));
-    RC_CUDA(record(d.ev[4], d.side));
-    launch_camera_pass(p, qb, d.counters.p + 7, d.side, d.async_cvar);
-    RC_CUDA(record(d.ev[5], d.side));
-    RC_CUDA(cudaEventRecord(d.join, d.side));
+    return RC_OK;
+}
+
+// async_tail, on s after the light pass: the photon capacity padded, the KD tree and its
+// boxes, the tree-order records; then, once the camera pass has recorded `camera_done`,
+// the count check (`flag` = 1 on an overflow), the query order and the gather.
+int async_tail(HostScene& sc, const VMParams& p, cudaStream_t s, cudaEvent_t camera_done, int* flag) {
+    DeviceState& d = ctx().dev;
+    const long long pc = d.async_pcap, qc = d.async_qcap;
+    QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qc, d.counters.p + 1};
     // pads one scene extent (plus four base radii) beyond the scene's +x face: outside
     // every merge radius, and close enough that the KD build's largest-extent rule
     // separates them from the stored photons along x within a few levels
@@ -1105,7 +1101,7 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     }
     launch_tree_records(PhotonBuf{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, pc, d.counters.p}, tree, tph, s);
     RC_CUDA(record(d.ev[3], s));
-    RC_CUDA(cudaStreamWaitEvent(s, d.join, 0));
+    RC_CUDA(cudaStreamWaitEvent(s, camera_done, 0));
     launch_check_counts(d.counters.p, pc, d.counters.p + 1, qc, flag, s);
     RC_CUDA(record(d.ev[6], s));
     launch_query_order(reinterpret_cast<const float*>(d.q0.p), 4, qc, scene_query_frame(sc), d.qscratch.p, d.qorder.p,
@@ -1117,6 +1113,29 @@ int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
     RC_CUDA(record(d.evg[1], s));
     RC_CUDA(record(d.ev[7], s));
     return RC_OK;
+}
+
+// Enqueue iteration `it` (no host synchronisation); `flag` receives the overflow flag.
+int enqueue_async_iteration(HostScene& sc, int it, int* flag) {
+    DeviceState& d = ctx().dev;
+    cudaStream_t s = d.stream;
+    VMParams p = make_params(sc, it);
+    const long long pc = d.async_pcap, qc = d.async_qcap;
+    PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, pc, d.counters.p};
+    QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, qc, d.counters.p + 1};
+    int r = async_head(p, s);
+    if (r) return r;
+    // the camera pass on a branch of its own beside the light pass's tail and the KD
+    // build (it reads nothing they write), joined before the count check
+    r = light_pass(p, ph, s, d.async_lvar, d.fork);   // the camera branch forks where
+    if (r) return r;                                   // the light pass stops filling the GPU
+    RC_CUDA(record(d.ev[1], s));
+    RC_CUDA(cudaStreamWaitEvent(d.side, d.fork, 0));
+    RC_CUDA(record(d.ev[4], d.side));
+    launch_camera_pass(p, qb, d.counters.p + 7, d.side, d.async_cvar);
+    RC_CUDA(record(d.ev[5], d.side));
+    RC_CUDA(cudaEventRecord(d.join, d.side));
+    return async_tail(sc, p, s, d.join, flag);
 }
 
 // Capture iteration `it` as a graph, update the instantiated graph with it (or
@@ -1154,6 +1173,66 @@ int launch_async_iteration(HostScene& sc, int it, int* flag) {
     RC_CUDA(cudaGetLastError());
     return RC_OK;
 }
+
+// After n_async asynchronous iterations from first_it were enqueued: their overflow
+// flags read back (synchronising the context's stream), the statistics of the last one,
+// every flagged iteration rendered again with host round trips, and the capacities sized
+// again if any overflowed.  `windows`: the light and camera passes' event windows
+// belong to this scene (not in a batch, whose passes cover every scene at once).
+int async_finish(HostScene& sc, int first_it, int n_async, bool windows) {
+    DeviceState& d = ctx().dev;
+    int r = RC_OK;
+    std::vector<int> flags(n_async, 0);
+    RC_CUDA(cudaMemcpyAsync(flags.data(), d.async_flags.p, sizeof(int) * n_async, cudaMemcpyDeviceToHost, d.stream));
+    RC_CUDA(cudaStreamSynchronize(d.stream));
+    r = check_errors();
+    if (r) return r;
+    // stats of the last replayed iteration
+    unsigned long long cnt[6] = {0, 0, 0, 0, 0, 0};
+    RC_CUDA(cudaMemcpy(cnt, d.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
+    VMParams p = make_params(sc, d.iterations_done - 1);
+    double* st = d.stats;
+    st[0] = (double)p.num_light_paths;
+    st[1] = (double)cnt[0];
+    st[2] = (double)cnt[1];
+    st[3] = (double)cnt[2];
+    st[14] = (double)cnt[3];
+    st[15] = (double)cnt[4];
+    st[4] = windows ? ms_between(d.ev[0], d.ev[1]) : 0.0;
+    st[5] = ms_between(d.ev[2], d.ev[3]);
+    st[6] = windows ? ms_between(d.ev[4], d.ev[5]) : 0.0;
+    st[7] = ms_between(d.ev[6], d.ev[7]);
+    st[8] = 0.0;
+    st[9] = windows ? overlapped_ms(d) + st[7] : ms_between(d.ev[2], d.ev[7]);
+    st[10] = d.iterations_done;
+    st[11] = sc.scene_radius;
+    st[12] = std::sqrt(p.radius_sqr);
+    const double gms = ms_between(d.evg[0], d.evg[1]);
+    d.acc_gather_ms += gms * n_async;    // the last replay's gather time stands for each
+    d.acc_gather_bytes += (40.0 * (double)cnt[0] + 64.0 * (double)cnt[1] +
+                           48.0 * (double)sc.camera.width * sc.camera.height) * n_async;
+    d.acc_iters += n_async;
+    d.acc_async += n_async;
+    d.acc_launches += (d.stats[13] + 2.0) * n_async;   // an eager iteration's kernels + pad + check
+    bool regrow = false;
+    for (int k = 0; k < n_async; ++k) {
+        if (!flags[k]) continue;
+        regrow = true;
+        r = render_iteration(sc, first_it + k);   // the skipped iteration, with round trips
+        if (r) return r;
+    }
+    if (regrow) {
+        // counts outgrew the capacities: size them again from the last measured counts
+        if (d.graph_exec) { cudaGraphExecDestroy(d.graph_exec); d.graph_exec = nullptr; }
+        r = async_setup(sc);
+        if (r) return r;
+    }
+    if (cfg().verbose)
+        std::printf("{\"replayed_iterations\": %d, \"redone\": %d, \"photon_capacity\": %lld, \"query_capacity\": %lld}\n",
+                    n_async, (int)std::count(flags.begin(), flags.end(), 1), d.async_pcap, d.async_qcap);
+    return RC_OK;
+}
+
 
 // `iterations` progressive iterations: the first with host round trips, the rest
 // replayed asynchronously when eligible; overflowed iterations are rendered again.
@@ -1194,54 +1273,311 @@ int render_iterations(HostScene& sc, int iterations) {
         if (r) return r;
         d.iterations_done++;
     }
-    std::vector<int> flags(n_async, 0);
-    RC_CUDA(cudaMemcpyAsync(flags.data(), d.async_flags.p, sizeof(int) * n_async, cudaMemcpyDeviceToHost, d.stream));
-    RC_CUDA(cudaStreamSynchronize(d.stream));
-    r = check_errors();
-    if (r) return r;
-    // stats of the last replayed iteration
-    unsigned long long cnt[6] = {0, 0, 0, 0, 0, 0};
-    RC_CUDA(cudaMemcpy(cnt, d.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
-    VMParams p = make_params(sc, d.iterations_done - 1);
-    double* st = d.stats;
-    st[0] = (double)p.num_light_paths;
-    st[1] = (double)cnt[0];
-    st[2] = (double)cnt[1];
-    st[3] = (double)cnt[2];
-    st[14] = (double)cnt[3];
-    st[15] = (double)cnt[4];
-    st[4] = ms_between(d.ev[0], d.ev[1]);
-    st[5] = ms_between(d.ev[2], d.ev[3]);
-    st[6] = ms_between(d.ev[4], d.ev[5]);
-    st[7] = ms_between(d.ev[6], d.ev[7]);
-    st[8] = 0.0;
-    st[9] = overlapped_ms(d) + st[7];
-    st[10] = d.iterations_done;
-    st[11] = sc.scene_radius;
-    st[12] = std::sqrt(p.radius_sqr);
-    const double gms = ms_between(d.evg[0], d.evg[1]);
-    d.acc_gather_ms += gms * n_async;    // the last replay's gather time stands for each
-    d.acc_gather_bytes += (40.0 * (double)cnt[0] + 64.0 * (double)cnt[1] +
-                           48.0 * (double)sc.camera.width * sc.camera.height) * n_async;
-    d.acc_iters += n_async;
-    d.acc_async += n_async;
-    d.acc_launches += (d.stats[13] + 2.0) * n_async;   // an eager iteration's kernels + pad + check
-    bool regrow = false;
-    for (int k = 0; k < n_async; ++k) {
-        if (!flags[k]) continue;
-        regrow = true;
-        r = render_iteration(sc, first_it + k);   // the skipped iteration, with round trips
-        if (r) return r;
+    return async_finish(sc, first_it, n_async, true);
+}
+
+// ---------------------------------------------------------------- batch of scenes
+// Several resident scenes (one context each) rendered as one launch set per iteration:
+// one persistent light pass over every scene's light paths and one persistent camera
+// pass over every scene's pixels (scene index found per work item), and per scene its
+// light-path order, KD build, query order and gather on a branch of its own; the whole
+// iteration is captured as one CUDA graph, updated in place and replayed per iteration.
+// Capacities are each scene's asynchronous ones (async_setup: fixed from a first
+// iteration with host round trips), so the graph holds no host round trip, whatever
+// an iteration's length; overflowed iterations are rendered again afterwards.
+
+// Launch shapes of the batch passes, tuned on the first batch (-1: untuned).
+std::atomic<int> g_batch_light{-1}, g_batch_camera{-1};
+
+struct BatchRun {
+    cudaStream_t main = nullptr, side = nullptr;
+    std::vector<cudaStream_t> branch;
+    cudaEvent_t start = nullptr, light = nullptr, camera = nullptr, join = nullptr, t0 = nullptr, t1 = nullptr;
+    cudaEvent_t light_start = nullptr, light_end = nullptr, camera_start = nullptr, camera_end = nullptr;
+    DevBuf<BatchScene> scenes;          // per graph iteration: its scenes' entries, end to end
+    DevBuf<long long> prefix;           // per graph iteration: path prefix (m + 1), pixel prefix (m + 1)
+    DevBuf<unsigned long long> next;    // [0] next light path, [1] next pixel
+    cudaGraphExec_t exec = nullptr;
+    ~BatchRun() {
+        if (exec) cudaGraphExecDestroy(exec);
+        scenes.release(); prefix.release(); next.release();
+        for (cudaEvent_t e : {start, light, camera, join, t0, t1, light_start, light_end, camera_start, camera_end})
+            if (e) cudaEventDestroy(e);
+        for (cudaStream_t b : branch) if (b) cudaStreamDestroy(b);
+        if (side) cudaStreamDestroy(side);
+        if (main) cudaStreamDestroy(main);
     }
-    if (regrow) {
-        // counts outgrew the capacities: size them again from the last measured counts
-        if (d.graph_exec) { cudaGraphExecDestroy(d.graph_exec); d.graph_exec = nullptr; }
-        r = async_setup(sc);
-        if (r) return r;
+};
+
+struct BindGuard {
+    Context* prev = t_bound;
+    ~BindGuard() { t_bound = prev; }
+};
+
+int batch_render(Context* const* cs, int n, int iterations, double* out) {
+    BindGuard guard;
+    Context* caller = &ctx();
+    caller->err.clear();
+    auto fail = [&](int code, const std::string& msg) { caller->err = msg; return code; };
+    auto scene_fail = [&](int i, int code) {
+        caller->err = "batch scene " + std::to_string(i) + ": " + cs[i]->err;
+        return code;
+    };
+    // 1. every scene prepared, with its asynchronous capacities (a first iteration with
+    //    host round trips where none has been rendered yet)
+    std::vector<int> remaining(n, iterations), first_it(n, 0), pcap_was(n, 0);
+    for (int i = 0; i < n; ++i) {
+        if (!cs[i]) return fail(RC_E_INVALID, "rc_batch_render: null context " + std::to_string(i));
+        for (int k = 0; k < i; ++k)
+            if (cs[k] == cs[i]) return fail(RC_E_INVALID, "rc_batch_render: context " + std::to_string(i) + " repeated");
     }
-    if (cfg().verbose)
-        std::printf("{\"replayed_iterations\": %d, \"redone\": %d, \"photon_capacity\": %lld, \"query_capacity\": %lld}\n",
-                    n_async, (int)std::count(flags.begin(), flags.end(), 1), d.async_pcap, d.async_qcap);
+    for (int i = 0; i < n; ++i) {
+        t_bound = cs[i];
+        if (!ctx().scene) return fail(RC_E_NO_SCENE, "rc_batch_render: scene " + std::to_string(i) + " has no scene");
+        if (cfg().sampler != RC_SAMPLER_UNIFORM || cfg().learned_proposal)
+            return fail(RC_E_INVALID, "rc_batch_render: scene " + std::to_string(i) +
+                                          " uses a Metropolis sampler or the learned proposal (uniform sampler only)");
+    }
+    for (int i = 0; i < n; ++i) {
+        t_bound = cs[i];
+        int r = prepare();
+        if (r) return scene_fail(i, r);
+        HostScene& sc = *ctx().scene;
+        DeviceState& d = ctx().dev;
+        pcap_was[i] = d.async_pcap < 0 ? -1 : 0;
+        if (d.async_pcap <= 0) {
+            if (d.iterations_done == 0 && remaining[i] > 0) {
+                r = render_iteration(sc);
+                if (r) return scene_fail(i, r);
+                remaining[i]--;
+            }
+            if (d.iterations_done > 0) {
+                r = async_setup(sc);
+                if (r) return scene_fail(i, r);
+            } else {
+                remaining[i] = 0;
+            }
+        }
+        if (remaining[i] > 0) {
+            // an eager iteration's side-stream camera pass (error return) may still write
+            // the query buffers the graph's camera pass writes
+            if (cudaStreamSynchronize(d.side) != cudaSuccess || cudaStreamSynchronize(d.stream) != cudaSuccess)
+                return fail(RC_E_CUDA, std::string("rc_batch_render: ") + cudaGetErrorString(cudaGetLastError()));
+            if (d.async_flags.reserve(remaining[i]) != cudaSuccess) return fail(RC_E_CUDA, "batch flag allocation failed");
+        }
+        first_it[i] = d.iterations_done;
+    }
+    const int K = n > 0 ? *std::max_element(remaining.begin(), remaining.end()) : 0;
+    t_bound = caller;
+    if (out) for (int k = 0; k < 6; ++k) out[k] = 0.0;
+    if (K <= 0) return RC_OK;
+    // 2. per graph iteration: the scenes still rendering, their entries and prefixes
+    std::vector<std::vector<int>> active(K);
+    std::vector<BatchScene> entries;
+    std::vector<long long> prefix;
+    std::vector<size_t> entry_at(K), prefix_at(K);
+    std::vector<long long> total_paths(K), total_pixels(K);
+    for (int j = 0; j < K; ++j) {
+        for (int i = 0; i < n; ++i) if (remaining[i] > j) active[j].push_back(i);
+        entry_at[j] = entries.size();
+        prefix_at[j] = prefix.size();
+        const int m = (int)active[j].size();
+        prefix.resize(prefix.size() + 2 * (m + 1));
+        long long* pp = prefix.data() + prefix_at[j];
+        long long* px = pp + m + 1;
+        pp[0] = px[0] = 0;
+        for (int a = 0; a < m; ++a) {
+            const int i = active[j][a];
+            t_bound = cs[i];
+            DeviceState& d = ctx().dev;
+            BatchScene b{};
+            b.p = make_params(*ctx().scene, first_it[i] + j);
+            b.p.path_order = d.path_order.p;
+            b.ph = PhotonBuf{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, d.async_pcap, d.counters.p};
+            b.qb = QueryBuf{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, d.async_qcap, d.counters.p + 1};
+            entries.push_back(b);
+            pp[a + 1] = pp[a] + b.p.num_light_paths;
+            px[a + 1] = px[a] + (long long)b.p.camera.width * b.p.camera.height;
+        }
+        total_paths[j] = pp[m];
+        total_pixels[j] = px[m];
+    }
+    t_bound = caller;
+    BatchRun B;
+    RC_CUDA(B.scenes.reserve(entries.size()));
+    RC_CUDA(B.prefix.reserve(prefix.size()));
+    RC_CUDA(B.next.reserve(2));
+    RC_CUDA(cudaMemcpy(B.scenes.p, entries.data(), entries.size() * sizeof(BatchScene), cudaMemcpyHostToDevice));
+    RC_CUDA(cudaMemcpy(B.prefix.p, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice));
+    RC_CUDA(cudaStreamCreateWithFlags(&B.main, cudaStreamNonBlocking));
+    RC_CUDA(cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking));
+    B.branch.assign(n, nullptr);
+    for (int i = 0; i < n; ++i) RC_CUDA(cudaStreamCreateWithFlags(&B.branch[i], cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&B.start, &B.light, &B.camera, &B.join})
+        RC_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (cudaEvent_t* e : {&B.t0, &B.t1, &B.light_start, &B.light_end, &B.camera_start, &B.camera_end})
+        RC_CUDA(cudaEventCreate(e));
+    // 3. launch shapes of the batch passes, timed once per process on the first
+    //    iteration's scenes (warm-up launch, then a timed one; the graph resets every
+    //    counter the passes append to)
+    if (g_batch_light.load() < 0 || g_batch_camera.load() < 0) {
+        const int m = (int)active[0].size();
+        const BatchScene* sc0 = B.scenes.p + entry_at[0];
+        const long long* pp = B.prefix.p + prefix_at[0];
+        for (int a = 0; a < m; ++a) {
+            t_bound = cs[active[0][a]];
+            VMParams p = entries[entry_at[0] + a].p;
+            launch_light_order(p, ctx().dev.order_scratch.p, ctx().dev.path_order.p, B.main);
+        }
+        t_bound = caller;
+        auto reset = [&](int which) {
+            for (int a = 0; a < m; ++a)
+                cudaMemsetAsync(cs[active[0][a]]->dev.counters.p + which, 0, sizeof(unsigned long long), B.main);
+        };
+        auto tune = [&](auto&& run) {
+            float best = 1e30f;
+            int best_v = 0;
+            for (int v = 0; v < pass_variants(); ++v) {
+                run(v);
+                cudaEventRecord(B.t0, B.main);
+                run(v);
+                cudaEventRecord(B.t1, B.main);
+                cudaEventSynchronize(B.t1);
+                const float ms = ms_between(B.t0, B.t1);
+                if (ms < best) { best = ms; best_v = v; }
+            }
+            return best_v;
+        };
+        g_batch_light = tune([&](int v) {
+            reset(0);
+            launch_light_pass_batch(sc0, pp, m, total_paths[0], B.next.p, B.main, v);
+        });
+        g_batch_camera = tune([&](int v) {
+            reset(1);
+            launch_camera_pass_batch(sc0, pp + m + 1, m, total_pixels[0], B.next.p + 1, B.main, v);
+        });
+        RC_CUDA(cudaStreamSynchronize(B.main));
+        RC_CUDA(cudaGetLastError());
+        if (caller->cfg_set && caller->cfg.verbose)
+            std::printf("{\"autotune\": \"batch passes\", \"light\": %d, \"camera\": %d}\n", g_batch_light.load(),
+                        g_batch_camera.load());
+    }
+    const int lvar = g_batch_light.load(), cvar = g_batch_camera.load();
+    // 4. one graph per iteration: captured, the executable graph updated in place (or
+    //    instantiated) and launched
+    double kernels = 0;
+    RC_CUDA(cudaEventRecord(B.t0, B.main));
+    for (int j = 0; j < K; ++j) {
+        const int m = (int)active[j].size();
+        RC_CUDA(cudaStreamBeginCapture(B.main, cudaStreamCaptureModeRelaxed));
+        int r = RC_OK;
+        auto enqueue = [&]() -> int {
+            RC_CUDA(cudaEventRecord(B.start, B.main));
+            for (int a = 0; a < m; ++a) {
+                const int i = active[j][a];
+                t_bound = cs[i];
+                VMParams p = entries[entry_at[j] + a].p;
+                RC_CUDA(cudaStreamWaitEvent(B.branch[i], B.start, 0));
+                int rr = async_head(p, B.branch[i]);
+                if (rr) return scene_fail(i, rr);
+                RC_CUDA(cudaEventRecord(B.join, B.branch[i]));
+                RC_CUDA(cudaStreamWaitEvent(B.main, B.join, 0));
+            }
+            t_bound = caller;
+            RC_CUDA(record(B.light_start, B.main));
+            launch_light_pass_batch(B.scenes.p + entry_at[j], B.prefix.p + prefix_at[j], m, total_paths[j], B.next.p,
+                                    B.main, lvar);
+            RC_CUDA(record(B.light_end, B.main));
+            RC_CUDA(cudaEventRecord(B.light, B.main));
+            RC_CUDA(cudaStreamWaitEvent(B.side, B.light, 0));
+            RC_CUDA(record(B.camera_start, B.side));
+            launch_camera_pass_batch(B.scenes.p + entry_at[j], B.prefix.p + prefix_at[j] + m + 1, m, total_pixels[j],
+                                     B.next.p + 1, B.side, cvar);
+            RC_CUDA(record(B.camera_end, B.side));
+            RC_CUDA(cudaEventRecord(B.camera, B.side));
+            for (int a = 0; a < m; ++a) {
+                const int i = active[j][a];
+                t_bound = cs[i];
+                RC_CUDA(cudaStreamWaitEvent(B.branch[i], B.light, 0));
+                int rr = async_tail(*ctx().scene, entries[entry_at[j] + a].p, B.branch[i], B.camera,
+                                    ctx().dev.async_flags.p + j);
+                if (rr) return scene_fail(i, rr);
+                RC_CUDA(cudaEventRecord(B.join, B.branch[i]));
+                RC_CUDA(cudaStreamWaitEvent(B.main, B.join, 0));
+            }
+            t_bound = caller;
+            RC_CUDA(cudaStreamWaitEvent(B.main, B.camera, 0));
+            return RC_OK;
+        };
+        r = enqueue();
+        Context* at = t_bound;
+        t_bound = caller;
+        if (r && caller->err.empty())
+            caller->err = "batch graph capture: " + (at && at != caller ? at->err : std::string("failed"));
+        const cudaError_t le = cudaGetLastError();
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(B.main, &graph);
+        if (r) { if (graph) cudaGraphDestroy(graph); return r; }
+        if (le != cudaSuccess || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return fail(RC_E_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(le != cudaSuccess ? le : e));
+        }
+        {
+            size_t nodes = 0;
+            cudaGraphGetNodes(graph, nullptr, &nodes);
+            std::vector<cudaGraphNode_t> list(nodes);
+            if (nodes) cudaGraphGetNodes(graph, list.data(), &nodes);
+            for (cudaGraphNode_t g : list) {
+                cudaGraphNodeType t;
+                if (cudaGraphNodeGetType(g, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) kernels += 1;
+            }
+        }
+        if (B.exec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(B.exec, graph, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(B.exec);
+                B.exec = nullptr;
+            }
+        }
+        if (!B.exec) {
+            const cudaError_t ie = cudaGraphInstantiate(&B.exec, graph, 0);
+            if (ie != cudaSuccess) {
+                cudaGraphDestroy(graph);
+                return fail(RC_E_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(ie));
+            }
+        }
+        cudaGraphDestroy(graph);
+        RC_CUDA(cudaGraphLaunch(B.exec, B.main));
+    }
+    RC_CUDA(cudaEventRecord(B.t1, B.main));
+    RC_CUDA(cudaStreamSynchronize(B.main));
+    const double batch_ms = ms_between(B.t0, B.t1);
+    // 5. per scene: flags, statistics of its last iteration, overflowed iterations again
+    int redone = 0;
+    for (int i = 0; i < n; ++i) {
+        if (remaining[i] <= 0) continue;
+        t_bound = cs[i];
+        DeviceState& d = ctx().dev;
+        d.iterations_done += remaining[i];
+        d.acc_gather_ms = d.acc_gather_bytes = d.acc_launches = 0;
+        d.acc_iters = d.acc_async = 0;
+        std::vector<int> fl(remaining[i], 0);
+        RC_CUDA(cudaMemcpy(fl.data(), d.async_flags.p, sizeof(int) * remaining[i], cudaMemcpyDeviceToHost));
+        redone += (int)std::count(fl.begin(), fl.end(), 1);
+        const int r = async_finish(*ctx().scene, first_it[i], remaining[i], false);
+        if (r) return scene_fail(i, r);
+        if (pcap_was[i] < 0) d.async_pcap = -1;   // single-scene renders keep their round trips
+    }
+    t_bound = caller;
+    if (out) {
+        out[0] = batch_ms;
+        out[1] = K;
+        out[2] = kernels;
+        out[3] = redone;
+        out[4] = ms_between(B.light_start, B.light_end);
+        out[5] = ms_between(B.camera_start, B.camera_end);
+    }
     return RC_OK;
 }
 
@@ -1722,6 +2058,11 @@ int rc_render_debug(int mode) {
     int r = prepare();
     if (r) return r;
     return render_debug(*ctx().scene, mode);
+}
+
+int rc_batch_render(rc_context* const* ctxs, int n, int iterations, double* out) {
+    if (!ctxs || n < 1 || iterations < 0) { ctx().err = "rc_batch_render: bad arguments"; return RC_E_INVALID; }
+    return batch_render(reinterpret_cast<Context* const*>(ctxs), n, iterations, out);
 }
 
 int rc_render_timed(int iterations, double* out) {

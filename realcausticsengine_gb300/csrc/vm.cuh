@@ -79,6 +79,14 @@ struct VMParams {
     const uint32_t* path_order;    // light-path processing order (launch_light_order; nullptr: index order)
 };
 
+// One scene of a batch render (launch_light_pass_batch / launch_camera_pass_batch):
+// its iteration parameters and the buffers its passes append to.
+struct BatchScene {
+    VMParams p;
+    PhotonBuf ph;
+    QueryBuf qb;
+};
+
 // error flag slots
 enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERFLOW = 3, ERR_KD = 4, ERR_MLP = 5,
        ERR_GATHER = 6, ERR_COUNT = 8 };
@@ -103,6 +111,15 @@ void launch_scan_counts(uint32_t* counts, long long m, uint32_t* tile_scratch, c
 // next_path: device counter for the persistent kernel (nullptr: one thread per path)
 void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant = 0);
 void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s, int variant = 0);
+// The persistent light and camera passes over n resident scenes in one launch each:
+// scenes[i] (device memory) holds scene i's parameters and buffers, path_prefix
+// (pixel_prefix) n + 1 device words with the first work index of each scene and the
+// total at [n].  A scene's photons (queries) are the ones its own pass stores, in
+// another order.  variant: the launch shapes of the single-scene passes (0-4).
+void launch_light_pass_batch(const BatchScene* scenes, const long long* path_prefix, int n, long long total_paths,
+                             unsigned long long* next_path, cudaStream_t s, int variant = 0);
+void launch_camera_pass_batch(const BatchScene* scenes, const long long* pixel_prefix, int n, long long total_pixels,
+                              unsigned long long* next_pixel, cudaStream_t s, int variant = 0);
 // Debug view `mode` (2 normals, 3 facing, 4 materials with IOR `ior`) added into the
 // FP64 image accumulation.
 void launch_debug_view(const VMParams& p, int mode, float ior, double* accum, cudaStream_t s);

@@ -8,9 +8,13 @@ namespace rc {
 
 namespace {
 
-// Warp-aggregated append: one atomic per converged group of lanes.
+// Warp-aggregated append: one atomic per converged group of lanes.  kGrouped: the
+// lanes may append to different counters (the batch passes, where a warp's lanes can
+// hold paths of several scenes): one atomic per group of lanes sharing a counter.
+template <bool kGrouped = false>
 __device__ __forceinline__ unsigned long long warp_append(unsigned long long* counter) {
     unsigned m = __activemask();
+    if (kGrouped) m = __match_any_sync(m, (unsigned long long)counter);
     int lane = threadIdx.x & 31;
     int leader = __ffs(m) - 1;
     unsigned lower = m & ((1u << lane) - 1u);
@@ -70,7 +74,9 @@ __device__ __forceinline__ bool light_path_trace(const VMParams& P, const LightP
     return scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK, stack);
 }
 
-__device__ __forceinline__ bool light_path_shade(const VMParams& P, PhotonBuf& ph, LightPath& s, const HitRec& h) {
+template <bool kGrouped = false>
+__device__ __forceinline__ bool light_path_shade(const VMParams& P, const PhotonBuf& ph, LightPath& s,
+                                                 const HitRec& h) {
     const F3 ro = s.o + s.d * kRayEps;
     Isect is;
     fill_isect(P.scene, h, ro, s.d, is);
@@ -84,7 +90,7 @@ __device__ __forceinline__ bool light_path_shade(const VMParams& P, PhotonBuf& p
     s.dVM /= fabsf(b.cos_theta_in());
     bool stored = false;
     if (!b.is_delta() && (s.last & EV_GLOSSY)) {
-        unsigned long long slot = warp_append(ph.count);
+        unsigned long long slot = warp_append<kGrouped>(ph.count);
         if (slot < (unsigned long long)ph.capacity) {
             ph.pos[slot] = make_float4(is.pos.x, is.pos.y, is.pos.z, s.dVM);
             ph.dir[slot] = make_float4(-is.dir.x, -is.dir.y, -is.dir.z, s.tp.x);
@@ -113,11 +119,12 @@ __device__ __forceinline__ bool light_path_shade(const VMParams& P, PhotonBuf& p
     return true;
 }
 
-template <class Stack>
-__device__ __forceinline__ bool light_path_bounce(const VMParams& P, PhotonBuf& ph, LightPath& s, Stack& stack) {
+template <bool kGrouped = false, class Stack>
+__device__ __forceinline__ bool light_path_bounce(const VMParams& P, const PhotonBuf& ph, LightPath& s,
+                                                  Stack& stack) {
     HitRec h;
     if (!light_path_trace(P, s, h, stack)) return false;
-    return light_path_shade(P, ph, s, h);
+    return light_path_shade<kGrouped>(P, ph, s, h);
 }
 
 // Wavefront light pass: the same paths, bounces and photons as the persistent pass,
@@ -338,8 +345,9 @@ __device__ __forceinline__ bool camera_path_start(const VMParams& P, long long p
     return true;
 }
 
-template <class Stack>
-__device__ __forceinline__ bool camera_path_bounce(const VMParams& P, QueryBuf& qb, CameraPath& s, Stack& stack) {
+template <bool kGrouped = false, class Stack>
+__device__ __forceinline__ bool camera_path_bounce(const VMParams& P, const QueryBuf& qb, CameraPath& s,
+                                                   Stack& stack) {
     F3 ro = s.o + s.d * kRayEps;
     HitRec h;
     if (!scene_hit(P.scene, ro, s.d, kRayEps, h, P.error + ERR_STACK, stack)) return false;
@@ -354,7 +362,7 @@ __device__ __forceinline__ bool camera_path_bounce(const VMParams& P, QueryBuf& 
     if (!b.valid()) return false;
     s.dVM /= fabsf(b.cos_theta_in());
     if (!b.is_delta()) {
-        unsigned long long slot = warp_append(qb.count);
+        unsigned long long slot = warp_append<kGrouped>(qb.count);
         if (slot < (unsigned long long)qb.capacity) {
             F3 w = s.tp * P.vm_norm;
             qb.q0[slot] = make_float4(is.pos.x, is.pos.y, is.pos.z, s.dVM);
@@ -408,6 +416,88 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_camera_pass_persistent(c
         }
         if (!__any_sync(0xffffffffu, alive)) break;
         if (alive) alive = camera_path_bounce(P, qb, s, stk);
+    }
+}
+
+// Batch passes: the persistent light and camera passes over the paths (pixels) of
+// several resident scenes in one launch.  Work index g runs over the scenes' paths laid
+// end to end (prefix[i] = first index of scene i, prefix[n] = total); a lane that takes
+// index g finds its scene by binary search and runs that scene's path with the scene's
+// own parameters and buffers (read from global memory: every lane of a warp that holds
+// paths of one scene reads the same words).  Each path's samples, bounces and photons
+// are those of the scene's own pass.
+__device__ __forceinline__ int batch_scene_of(const long long* __restrict__ prefix, int n, long long g) {
+    int lo = 0, hi = n - 1;   // the last scene whose range starts at or before g
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&prefix[mid]) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int kBlock, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_light_pass_batch(const BatchScene* __restrict__ B,
+                                                                         const long long* __restrict__ prefix, int n,
+                                                                         unsigned long long* __restrict__ next_path) {
+    CallStack stk;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long total = (unsigned long long)__ldg(&prefix[n]);
+    LightPath s;
+    int sid = 0;
+    bool alive = false;
+    bool pool_left = true;
+    while (true) {
+        const unsigned need = __ballot_sync(0xffffffffu, !alive);
+        if (need && pool_left && (__popc(need) >= kRefillLanes || need == 0xffffffffu)) {
+            unsigned long long base = 0;
+            if (lane == __ffs(need) - 1) base = atomicAdd(next_path, (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
+            if (!alive) {
+                const unsigned long long mine = base + __popc(need & ((1u << lane) - 1u));
+                if (mine < total) {
+                    sid = batch_scene_of(prefix, n, (long long)mine);
+                    const VMParams& P = B[sid].p;
+                    const long long local = (long long)mine - __ldg(&prefix[sid]);
+                    alive = light_path_start(P, P.path_order ? (long long)__ldg(&P.path_order[local]) : local, s);
+                }
+            }
+            if (base + __popc(need) >= total) pool_left = false;
+        }
+        if (!__any_sync(0xffffffffu, alive)) break;
+        if (alive) alive = light_path_bounce<true>(B[sid].p, B[sid].ph, s, stk);
+    }
+}
+
+template <int kBlock, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_camera_pass_batch(const BatchScene* __restrict__ B,
+                                                                          const long long* __restrict__ prefix, int n,
+                                                                          unsigned long long* __restrict__ next_pixel) {
+    CallStack stk;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long total = (unsigned long long)__ldg(&prefix[n]);
+    CameraPath s;
+    int sid = 0;
+    bool alive = false;
+    bool pool_left = true;
+    while (true) {
+        unsigned need = __ballot_sync(0xffffffffu, !alive);
+        while (need && pool_left && (__popc(need) >= kRefillLanes || need == 0xffffffffu)) {
+            unsigned long long base = 0;
+            if (lane == __ffs(need) - 1) base = atomicAdd(next_pixel, (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
+            if (!alive) {
+                const unsigned long long mine = base + __popc(need & ((1u << lane) - 1u));
+                if (mine < total) {
+                    sid = batch_scene_of(prefix, n, (long long)mine);
+                    alive = camera_path_start(B[sid].p, (long long)mine - __ldg(&prefix[sid]), s);
+                }
+            }
+            if (base + __popc(need) >= total) pool_left = false;
+            need = __ballot_sync(0xffffffffu, !alive);
+        }
+        if (!__any_sync(0xffffffffu, alive)) break;
+        if (alive) alive = camera_path_bounce<true>(B[sid].p, B[sid].qb, s, stk);
     }
 }
 
@@ -494,6 +584,32 @@ void launch_camera_t(const VMParams& p, QueryBuf qb, unsigned long long* next_pi
     }
     cudaMemsetAsync(next_pixel, 0, sizeof(unsigned long long), s);
     k_camera_pass_persistent<B, MB><<<grid_cache, B, 0, s>>>(p, qb, next_pixel);
+}
+
+template <int B, int MB>
+void launch_light_batch_t(const BatchScene* scenes, const long long* prefix, int n, long long total,
+                          unsigned long long* next, cudaStream_t s) {
+    static thread_local unsigned grid_cache = 0;
+    static thread_local long long grid_for = -1;
+    if (grid_for != total) {
+        grid_cache = persistent_grid(k_light_pass_batch<B, MB>, B, 0, total);
+        grid_for = total;
+    }
+    cudaMemsetAsync(next, 0, sizeof(unsigned long long), s);
+    k_light_pass_batch<B, MB><<<grid_cache, B, 0, s>>>(scenes, prefix, n, next);
+}
+
+template <int B, int MB>
+void launch_camera_batch_t(const BatchScene* scenes, const long long* prefix, int n, long long total,
+                           unsigned long long* next, cudaStream_t s) {
+    static thread_local unsigned grid_cache = 0;
+    static thread_local long long grid_for = -1;
+    if (grid_for != total) {
+        grid_cache = persistent_grid(k_camera_pass_batch<B, MB>, B, 0, total);
+        grid_for = total;
+    }
+    cudaMemsetAsync(next, 0, sizeof(unsigned long long), s);
+    k_camera_pass_batch<B, MB><<<grid_cache, B, 0, s>>>(scenes, prefix, n, next);
 }
 
 }  // namespace
@@ -590,6 +706,30 @@ void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next
     case 3: launch_camera_t<128, 5>(p, qb, next_pixel, s); break;
     case 4: launch_camera_t<128, 10>(p, qb, next_pixel, s); break;
     default: launch_camera_t<256, 3>(p, qb, next_pixel, s); break;
+    }
+}
+
+void launch_light_pass_batch(const BatchScene* scenes, const long long* path_prefix, int n, long long total_paths,
+                             unsigned long long* next_path, cudaStream_t s, int variant) {
+    if (n <= 0 || total_paths <= 0 || !next_path) return;
+    switch (variant) {
+    case 1: launch_light_batch_t<128, 7>(scenes, path_prefix, n, total_paths, next_path, s); break;
+    case 2: launch_light_batch_t<128, 8>(scenes, path_prefix, n, total_paths, next_path, s); break;
+    case 3: launch_light_batch_t<128, 5>(scenes, path_prefix, n, total_paths, next_path, s); break;
+    case 4: launch_light_batch_t<128, 10>(scenes, path_prefix, n, total_paths, next_path, s); break;
+    default: launch_light_batch_t<256, 3>(scenes, path_prefix, n, total_paths, next_path, s); break;
+    }
+}
+
+void launch_camera_pass_batch(const BatchScene* scenes, const long long* pixel_prefix, int n, long long total_pixels,
+                              unsigned long long* next_pixel, cudaStream_t s, int variant) {
+    if (n <= 0 || total_pixels <= 0 || !next_pixel) return;
+    switch (variant) {
+    case 1: launch_camera_batch_t<128, 7>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
+    case 2: launch_camera_batch_t<128, 8>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
+    case 3: launch_camera_batch_t<128, 5>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
+    case 4: launch_camera_batch_t<128, 10>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
+    default: launch_camera_batch_t<256, 3>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
     }
 }
 

@@ -49,6 +49,18 @@ class Context:
             self.handle = None
 
 
+def batch_render(contexts, iterations: int) -> np.ndarray:
+    """rc_batch_render: `iterations` more iterations of every scene held by `contexts`
+    (Context objects, each with a scene loaded while it was bound) as one launch set per
+    iteration.  Returns the call's timing record (device ms, batch iterations, kernel
+    launches, iterations rendered again, light and camera pass ms of the last one)."""
+    L = lib()
+    handles = (C.c_void_p * len(contexts))(*[c.handle for c in contexts])
+    out = np.zeros(6, np.float64)
+    check(L.rc_batch_render(handles, len(contexts), iterations, out.ctypes.data), "rc_batch_render")
+    return out
+
+
 class Renderer:
     """One scene loaded into the library (the library holds one scene at a time,
     like the reference's global `scene`)."""
