@@ -286,10 +286,11 @@ int rc_trace_rays(int n, const float* origins, const float* directions, float tm
  * oracle): [hit, t, u, v, Ng xyz, Ns xyz, position xyz, front_face, material, tri]. */
 int rc_trace_rays_full(int n, const float* origins, const float* directions, float tmin, float* out);
 
-/* rc_trace_rays_full through a chosen traversal: 0 the persistent passes' (pop a node,
- * test its box), 1 the wavefront pass's (a warp's lanes step one node at a time
- * together, both children's boxes tested at the parent).  Both visit the reference's
- * nodes in its order and return its hits.  RC_E_INVALID for any other shape. */
+/* rc_trace_rays_full through a chosen traversal: 0 the persistent passes' (one lane per
+ * ray, both children's boxes tested at the parent), 1 the wavefront pass's (the same
+ * tests, a warp's lanes stepping one node at a time together), 2 the reference's own
+ * form (pop a node, test its box).  All visit the reference's nodes in its order and
+ * return its hits.  RC_E_INVALID for any other shape. */
 int rc_trace_rays_shape(int n, const float* origins, const float* directions, float tmin, float* out, int shape);
 
 /* One light pass (iteration `iteration`, current config) on the GPU; copies the stored

@@ -2242,7 +2242,7 @@ int rc_trace_rays_full(int n, const float* origins, const float* directions, flo
 }
 
 int rc_trace_rays_shape(int n, const float* origins, const float* directions, float tmin, float* out, int shape) {
-    if (shape != 0 && shape != 1) { ctx().err = "traversal shape must be 0 or 1"; return RC_E_INVALID; }
+    if (shape < 0 || shape > 2) { ctx().err = "traversal shape must be 0, 1 or 2"; return RC_E_INVALID; }
     int r = prepare();
     if (r) return r;
     if (n < 0 || (n > 0 && (!origins || !directions || !out))) { ctx().err = "bad ray arrays"; return RC_E_INVALID; }

@@ -133,7 +133,8 @@ void launch_pad_photons(float4* pos, const unsigned long long* count, long long 
                         cudaStream_t s);
 void launch_check_counts(const unsigned long long* photons, long long photon_cap, const unsigned long long* queries,
                          long long query_cap, int* flag, cudaStream_t s);
-// shape 0: the persistent passes' traversal; 1: the wavefront pass's warp-stepped one.
+// shape 0: the persistent passes' traversal; 1: the wavefront pass's warp-stepped one;
+// 2: pop-and-test (the reference's form).
 void launch_trace_rays(const SceneView& s, int n, const float* o, const float* d, float tmin, float* out_full,
                        unsigned* out_words, int* err, cudaStream_t st, int shape = 0);
 // Photon records in tree order (tp.t0/t1/t2 from ph.pos/dir/tp; only t0 when ph.dir is null).

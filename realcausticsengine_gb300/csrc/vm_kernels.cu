@@ -501,8 +501,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_camera_pass_batch(const 
     }
 }
 
-// Stack: CallStack (the reference-order pop-and-test traversal of the persistent passes)
-// or WarpStepStack (the warp-stepped traversal of the wavefront pass).
+// Stack: CallStack (the persistent passes' traversal: children tested at the parent),
+// WarpStepStack (the wavefront pass's warp-stepped one) or LocalStack (pop-and-test, the
+// reference's own form).
 template <class Stack>
 __global__ void k_trace_rays(const SceneView S, int n, const float* __restrict__ o, const float* __restrict__ d,
                              float tmin, float* out_full, unsigned* out_words, int* err) {
@@ -818,6 +819,8 @@ void launch_trace_rays(const SceneView& sv, int n, const float* o, const float* 
     if (n <= 0) return;
     if (shape == 1)
         k_trace_rays<WarpStepStack><<<(n + 127) / 128, 128, 0, st>>>(sv, n, o, d, tmin, out_full, out_words, err);
+    else if (shape == 2)
+        k_trace_rays<LocalStack><<<(n + 127) / 128, 128, 0, st>>>(sv, n, o, d, tmin, out_full, out_words, err);
     else
         k_trace_rays<CallStack><<<(n + 127) / 128, 128, 0, st>>>(sv, n, o, d, tmin, out_full, out_words, err);
 }

@@ -132,7 +132,7 @@ class Renderer:
 
     def trace(self, origins: np.ndarray, dirs: np.ndarray, tmin: float = 0.001, shape: int = 0) -> np.ndarray:
         """Closest hits (n, 16) through traversal `shape`: 0 the persistent passes',
-        1 the wavefront pass's warp-stepped one."""
+        1 the wavefront pass's warp-stepped one, 2 pop-and-test (the reference's form)."""
         o = np.ascontiguousarray(origins, np.float32)
         d = np.ascontiguousarray(dirs, np.float32)
         n = len(o)

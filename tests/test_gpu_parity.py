@@ -46,10 +46,10 @@ def _random_rays(rng, n, lo=-4.0, hi=4.0, zlo=0.2, zhi=5.0, aim=None):
 def test_closest_hits_golden(golden):
     sc = scenes.test_scene(48, 36, subdiv=2, samples=2)
     r = Renderer(sc)
-    got = [r.trace(golden["ray_o"], golden["ray_d"], shape=k) for k in (0, 1)]
+    got = [r.trace(golden["ray_o"], golden["ray_d"], shape=k) for k in (0, 1, 2)]
     want = golden["ray_hits"]
     r.release()
-    for g in got:   # both traversals: the persistent passes' and the warp-stepped one
+    for g in got:   # every traversal: the persistent passes', the warp-stepped one, pop-and-test
         assert (g[:, :15].view(np.uint32) == want[:, :15].view(np.uint32)).all()
 
 
@@ -69,7 +69,7 @@ def test_closest_hits_vs_oracle(orc, name):
     if name == "water":
         o[:, 2] = rng.uniform(-1.4, 3.0, n)
     r = Renderer(sc)
-    got = [r.trace(o, d, shape=k) for k in (0, 1)]
+    got = [r.trace(o, d, shape=k) for k in (0, 1, 2)]
     r.release()
     _oracle_scene(orc, sc)
     want = _oracle_trace(orc, o, d)

@@ -3,7 +3,7 @@ restatement of Scene::hit (src/Scene.cpp:154-189, world leaves src/BVH/BVH_world
 Möller-Trumbore src/Triangle.cpp:20-88), which is pinned to the compiled reference.
 
 The GPU path builds the mesh BVHs on the device (word-for-word the host build) and
-traverses them with both of its traversals; the oracle builds its own host BVH.  Every field of every ray's hit
+traverses them with each of its traversals; the oracle builds its own host BVH.  Every field of every ray's hit
 record must match: t, u, v, Ng, Ns, position, front face, material, triangle id.
 """
 import ctypes as C
@@ -31,10 +31,10 @@ def _rays(rng, n, lo, hi, zlo, zhi, aim_lo, aim_hi, aim_z):
 
 
 def _compare(orc, sc, o, d, min_hit_frac):
-    """Both GPU traversals (0: the persistent passes', 1: the wavefront pass's
-    warp-stepped one) against the oracle."""
+    """Every GPU traversal (0: the persistent passes', 1: the wavefront pass's
+    warp-stepped one, 2: pop-and-test) against the oracle."""
     r = Renderer(sc)
-    got = [r.trace(o, d, shape=k) for k in (0, 1)]
+    got = [r.trace(o, d, shape=k) for k in (0, 1, 2)]
     r.release()
     InitArgs(sc).call(orc.oracle_init)
     assert orc.oracle_prepare(None) == 0
