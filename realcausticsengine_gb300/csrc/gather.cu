@@ -172,7 +172,7 @@ struct EvalSink {
             st.fwo = (bs.kind == BSDF_K_PLASTIC_GGX || bs.kind == BSDF_K_PLASTIC_SMOOTH)
                          ? fresnel_reflectance(fabsf(bs.wo.z), bs.s) : 0.0f;
             st.dvm = dvm;
-            st.tp[0] = g.x; st.tp[1] = g.y; st.tp[2] = g.z;
+            st.tp[0] = g.x * P.merge_scale; st.tp[1] = g.y * P.merge_scale; st.tp[2] = g.z * P.merge_scale;
         }
         sm.g.acc[lane][0] = 0.0f; sm.g.acc[lane][1] = 0.0f; sm.g.acc[lane][2] = 0.0f;
     }

@@ -474,6 +474,7 @@ VMParams make_params(const HostScene& sc, int iteration) {
     float radius_sqr = radius * radius;
     p.radius_sqr = radius_sqr;
     p.vm_norm = 1.0f / (PI * radius_sqr * light_paths_count);
+    p.merge_scale = 1.0f;
     p.error = ctx().dev.errors.p;
     return p;
 }
@@ -731,19 +732,20 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         p.proposal_table = d.prop_table.p;
         p.proposal_table_res = kProposalRes;
     }
-    // With uniformly sampled light paths the camera pass reads nothing that the light
-    // pass writes (a Metropolis sampler scales vm_norm by the light pass's visibility).
-    // Once its launch shape is tuned it then runs on the side stream, issued right
-    // behind the light pass: its blocks take the SMs that the light pass's tail frees
-    // and run through the host's read-back of the photon count and the KD build's
-    // launches; it joins the main stream before the query order.  (With the learned
-    // proposal the network's inference ends before the fork and its training starts
-    // after the join: no tensor-core kernel runs beside it.)
+    // The camera pass reads nothing that the light pass writes (the Metropolis samplers'
+    // visibility factor, known only after the light pass, is applied by the gather).
+    // Once its launch shape is tuned it then runs on the side stream: with uniformly
+    // sampled light paths issued right behind the light pass, so that its blocks take
+    // the SMs that the light pass's tail frees and run through the host's read-back of
+    // the photon count and the KD build's launches; with a Metropolis sampler issued
+    // before the chains, whose one thread per chain leaves room on every SM.  It joins
+    // the main stream before the query order.  (With the learned proposal the network's
+    // inference ends before the fork and its training starts after the join: no
+    // tensor-core kernel runs beside it.)
     long long qcap = std::max<long long>((long long)d.q0.n, npix * 2);
     unsigned long long nq = 0;
     float t_cam = 0.0f;
-    const bool cam_side = sampler == RC_SAMPLER_UNIFORM &&
-                          (!cfg().autotune || g_tune.camera[size_class(npix)].load() >= 0);
+    const bool cam_side = !cfg().autotune || g_tune.camera[size_class(npix)].load() >= 0;
     const int cam_var = cfg().autotune ? std::max(g_tune.camera[size_class(npix)].load(), 0) : 0;
     if (cam_side) {
         RC_CUDA(d.q0.reserve(qcap)); RC_CUDA(d.q1.reserve(qcap)); RC_CUDA(d.q2.reserve(qcap));
@@ -796,7 +798,10 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             r0 = light_pass(p, ph, s, lvar, fork ? d.fork : nullptr);
             if (r0) return r0;
         }
-        else launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
+        else {
+            if (fork) RC_CUDA(cudaEventRecord(d.fork, s));
+            launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
+        }
         RC_CUDA(cudaGetLastError());
         RC_CUDA(cudaEventRecord(d.ev[1], s));
         if (fork) {
@@ -830,7 +835,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     if (sampler != RC_SAMPLER_UNIFORM) {
         // visibility normalisation of the Metropolis samplers (src/Vertex_Merging.cpp:277-282)
         const float vis = mlt[1] ? (float)mlt[0] / (float)mlt[1] : 0.0f;
-        p.vm_norm *= vis;
+        p.merge_scale = vis;
         d.stats_mlt_visible = vis;
     }
     // KD tree over the stored photons

@@ -68,6 +68,8 @@ struct VMParams {
     int max_path_length;
     float radius_sqr;
     float vm_norm;
+    float merge_scale;      // gather: factor on every merge (the Metropolis samplers' visible
+                            // fraction of large steps, known after the light pass; else 1)
     int* error;             // device flags: [0] stack overflow, [1] bad material
     const float4* proposal; // learned emission proposal per light path (nullptr: none)
     float* path_contrib;    // gather: per light path, sum over its merges of the squared

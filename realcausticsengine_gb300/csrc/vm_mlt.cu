@@ -44,70 +44,90 @@ constexpr int kPhotonBuf = kMltMaxLen + 2;
 
 struct PhotonRec { float4 pos, dir; float2 tp; };
 
-// Trace one light path driven by the primary samples u[0..kMltDims); photons go to
-// `out` (at most kPhotonBuf).  Russian roulette draws come from `rr` (the reference
-// takes them from its global stream).  Returns the number of photons.
-__device__ int trace_light_samples(const VMParams& P, const float* u, const PathRng& rr, int maxlen, PhotonRec* out) {
+// One light path driven by the primary samples u[0..kMltDims), split into its emission
+// (mlt_path_start: false when the emission carries nothing) and its segments
+// (mlt_path_bounce: one closest hit and its shading; false when the path ends), so that
+// a chain can advance its path one segment per loop iteration.  Photons go to `out` (at
+// most kPhotonBuf).  Russian-roulette draws come from `rr` (the reference takes them
+// from its global stream).
+struct MltPath {
     F3 o, d, tp;
+    float dVM;
+    int diffuse, last, len, channel, n;
+};
+
+__device__ __forceinline__ bool mlt_path_start(const VMParams& P, const float* u, MltPath& t) {
+    t.diffuse = 0; t.last = EV_DIFFUSE; t.len = 0; t.channel = -1; t.n = 0;
+    t.dVM = 0.0f;
     if (P.proposal_table) {
         const LightSample ls = light_position(P.lights, u[0], u[1], u[2]);
         const DevLight& l = P.lights.lights[ls.idx];
-        o = ls.o;
-        tp = ls.tp;
+        t.o = ls.o;
+        t.tp = ls.tp;
         if (l.type == LIGHT_SUN) {
-            d = light_direction(l, u[3], u[4]);
+            t.d = light_direction(l, u[3], u[4]);
         } else {
             const float ratio = table_direction(ProposalTable{P.proposal_table, P.proposal_table_res}, l, ls.idx, u[1],
-                                                u[2], u[3], u[4], u[kMltDims - 1], d);
-            if (!(ratio > 0.0f)) return 0;
-            tp = tp * ratio;
+                                                u[2], u[3], u[4], u[kMltDims - 1], t.d);
+            if (!(ratio > 0.0f)) return false;
+            t.tp = t.tp * ratio;
         }
     } else {
-        sample_light(P.lights, u[0], u[1], u[2], u[3], u[4], o, d, tp);
+        sample_light(P.lights, u[0], u[1], u[2], u[3], u[4], t.o, t.d, t.tp);
     }
-    int diffuse = 0, last = EV_DIFFUSE, n = 0, channel = -1;
-    float dVM = 0.0f;
-    for (int len = 0;; ++len) {
-        F3 ro = o + d * kRayEps;
-        HitRec h;
-        if (!scene_hit(P.scene, ro, d, kRayEps, h, P.error + ERR_STACK)) break;
-        Isect is;
-        fill_isect(P.scene, h, ro, d, is);
-        if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); break; }
-        const DevMaterial& mat = P.materials[is.material];
-        // dispersion channel from the Russian-roulette stream (outside the primary samples)
-        const float shift = mat.disp > 0.0f
-            ? dispersion_shift(mat, channel, tp, u01(rr.block(kChannelBlock + len).a)) : 0.0f;
-        Bsdf b;
-        b.init(mat, is.ns, is.dir, false, shift);
-        if (!b.valid()) break;
-        dVM /= fabsf(b.cos_theta_in());
-        bool stored = false;
-        if (!b.is_delta() && (last & EV_GLOSSY) && n < kPhotonBuf) {
-            out[n].pos = make_float4(is.pos.x, is.pos.y, is.pos.z, dVM);
-            out[n].dir = make_float4(-is.dir.x, -is.dir.y, -is.dir.z, tp.x);
-            out[n].tp = make_float2(tp.y, tp.z);
-            ++n;
-            stored = true;
-        }
-        if (len > maxlen || diffuse > kMaxDiffuse) break;
-        const float* s = u + 5 + 3 * len;
-        BsdfSample smp = b.sample(s[0], s[1], s[2], is.ng);
-        if (is_zero(smp.f)) break;
-        F3 f = smp.f;
-        if (len > kRRDepth) {
-            if (u01(rr.block(2 + len).a) > smp.cont) break;
-            f = div_each(f, smp.cont);
-        }
-        o = is.pos;
-        d = smp.wi;
-        if (smp.event & EV_DIFFUSE) diffuse++;
-        tp = tp * f;
-        last = smp.event;
-        if (!stored) dVM *= (smp.cos_out / smp.fwd) * smp.rev;
-        else dVM = (smp.cos_out / smp.fwd) * (1.0f + smp.rev * dVM);
+    return true;
+}
+
+__device__ __forceinline__ bool mlt_path_bounce(const VMParams& P, const float* u, const PathRng& rr, int maxlen,
+                                                MltPath& t, PhotonRec* out) {
+    const F3 ro = t.o + t.d * kRayEps;
+    HitRec h;
+    if (!scene_hit(P.scene, ro, t.d, kRayEps, h, P.error + ERR_STACK)) return false;
+    Isect is;
+    fill_isect(P.scene, h, ro, t.d, is);
+    if ((unsigned)is.material >= (unsigned)P.num_materials) { atomicOr(P.error + ERR_MATERIAL, 1); return false; }
+    const DevMaterial& mat = P.materials[is.material];
+    // dispersion channel from the Russian-roulette stream (outside the primary samples)
+    const float shift = mat.disp > 0.0f
+        ? dispersion_shift(mat, t.channel, t.tp, u01(rr.block(kChannelBlock + t.len).a)) : 0.0f;
+    Bsdf b;
+    b.init(mat, is.ns, is.dir, false, shift);
+    if (!b.valid()) return false;
+    t.dVM /= fabsf(b.cos_theta_in());
+    bool stored = false;
+    if (!b.is_delta() && (t.last & EV_GLOSSY) && t.n < kPhotonBuf) {
+        out[t.n].pos = make_float4(is.pos.x, is.pos.y, is.pos.z, t.dVM);
+        out[t.n].dir = make_float4(-is.dir.x, -is.dir.y, -is.dir.z, t.tp.x);
+        out[t.n].tp = make_float2(t.tp.y, t.tp.z);
+        ++t.n;
+        stored = true;
     }
-    return n;
+    if (t.len > maxlen || t.diffuse > kMaxDiffuse) return false;
+    const float* sv = u + 5 + 3 * t.len;
+    BsdfSample smp = b.sample(sv[0], sv[1], sv[2], is.ng);
+    if (is_zero(smp.f)) return false;
+    F3 f = smp.f;
+    if (t.len > kRRDepth) {
+        if (u01(rr.block(2 + t.len).a) > smp.cont) return false;
+        f = div_each(f, smp.cont);
+    }
+    t.o = is.pos;
+    t.d = smp.wi;
+    if (smp.event & EV_DIFFUSE) t.diffuse++;
+    t.tp = t.tp * f;
+    t.last = smp.event;
+    if (!stored) t.dVM *= (smp.cos_out / smp.fwd) * smp.rev;
+    else t.dVM = (smp.cos_out / smp.fwd) * (1.0f + smp.rev * t.dVM);
+    t.len++;
+    return true;
+}
+
+// The whole path; returns the number of photons.
+__device__ int trace_light_samples(const VMParams& P, const float* u, const PathRng& rr, int maxlen, PhotonRec* out) {
+    MltPath t;
+    if (!mlt_path_start(P, u, t)) return 0;
+    while (mlt_path_bounce(P, u, rr, maxlen, t, out)) {}
+    return t.n;
 }
 
 __device__ __forceinline__ void store_photons(PhotonBuf& ph, const PhotonRec* r, int n, float weight, uint32_t path) {
@@ -203,65 +223,107 @@ __global__ void __launch_bounds__(128) k_mlt_hybrid(const VMParams P, PhotonBuf 
     atomicAdd(&stats[1], (unsigned long long)(p1 - p0));
 }
 
+// PSSMLT, one chain per thread, advanced one path segment per loop iteration: lanes
+// whose proposal's path has ended wait until kSettleLanes lanes of the warp (or all
+// that still have steps) have, then settle their steps together (accept or reject,
+// dwell, the adaptive mutation size) and start their chains' next proposals, so that
+// the lanes of a warp neither wait for the warp's longest path at every step nor draw
+// their proposals' random numbers (dozens of Philox blocks) a few lanes at a time.
+// Each chain takes the same steps with the same random numbers in the same order as a
+// step-at-a-time loop: burn-in large steps t = 0 .. (first visible, at most 256) from
+// the chain's first path index, then one step per further path index.
+constexpr int kSettleLanes = 16;
+
 __global__ void __launch_bounds__(128) k_mlt_pss(const VMParams P, PhotonBuf ph, int chains, float p_large,
                                                  unsigned long long* __restrict__ stats) {
     const int chain = blockIdx.x * blockDim.x + threadIdx.x;
-    if (chain >= chains) return;
     const long long N = P.num_light_paths;
     const long long per = (N + chains - 1) / chains;
     const long long p0 = (long long)chain * per;
     const long long p1 = p0 + per < N ? p0 + per : N;
-    if (p0 >= p1) return;
+    // lanes without a chain stay in the loop (its votes take the whole warp), idle
+    bool alive = chain < chains && p0 < p1;
     const int maxlen = P.max_path_length < kMltMaxLen ? P.max_path_length : kMltMaxLen;
-    float cur[kMltDims], prop[kMltDims];
-    PhotonRec cur_ph[kPhotonBuf], tmp[kPhotonBuf];
+    // the current state and the proposal: sample vectors and photon lists, swapped on
+    // acceptance
+    float su[2][kMltDims];
+    PhotonRec sph[2][kPhotonBuf];
+    int ci = 0;                      // index of the current state
     int cur_n = 0;
     unsigned long long large = 0, large_visible = 0;
-    // burn-in: large steps until a visible state (bounded); they count as large steps
-    long long step = 0;
-    for (int t = 0; t < 256 && cur_n == 0; ++t) {
-        uniform_samples(P, p0, 16u + (uint32_t)t, cur);
-        PathRng rr;
-        rr.init(P.seed, ((uint64_t)p0 << 9) | (uint64_t)t, P.iteration, STREAM_MLT + 2u);
-        cur_n = trace_light_samples(P, cur, rr, maxlen, cur_ph);
-        ++large;
-        if (cur_n > 0) ++large_visible;
-    }
     float m = 1.0f;
     int accepted = 1, mutated = 0;
     float dwell = 1.0f;
-    for (long long p = p0 + 1; p < p1; ++p, ++step) {
-        PathRng g;
-        g.init(P.seed, (uint64_t)p, P.iteration, STREAM_MLT + 3u);
-        const bool is_large = u01(g.block(0).a) < p_large;
-        if (is_large) uniform_samples(P, p, 0u, prop);
-        else {
-            for (int k = 0; k < kMltDims; ++k) prop[k] = cur[k];
-            mutate(P, (uint64_t)p, m, prop);
-            ++mutated;
-        }
-        PathRng rr;
-        rr.init(P.seed, (uint64_t)p * 2u, P.iteration, STREAM_MLT + 1u);
-        const int n = trace_light_samples(P, prop, rr, maxlen, tmp);
-        if (is_large) { ++large; if (n > 0) ++large_visible; }
-        if (n > 0) {
-            if (cur_n > 0) store_photons(ph, cur_ph, cur_n, dwell, (uint32_t)p);
-            for (int k = 0; k < kMltDims; ++k) cur[k] = prop[k];
-            for (int k = 0; k < n; ++k) cur_ph[k] = tmp[k];
-            cur_n = n;
-            dwell = 1.0f;
-            if (!is_large) ++accepted;
-        } else {
-            dwell += 1.0f;
-        }
-        if (!is_large && mutated > 0) {
-            const float R = (float)accepted / (float)mutated;
-            m += (R - 0.234f) / (float)mutated;
-        }
+    int t = 0;                       // burn-in step (t < 256), then main steps
+    bool burn_in = true;
+    long long p = p0 + 1;
+    bool is_large = true;
+    PathRng rr;
+    MltPath path;
+    path.n = 0;
+    bool tracing = false;
+    if (alive) {
+        // first proposal: burn-in step 0
+        uniform_samples(P, p0, 16u, su[ci ^ 1]);
+        rr.init(P.seed, (uint64_t)p0 << 9, P.iteration, STREAM_MLT + 2u);
+        tracing = mlt_path_start(P, su[ci ^ 1], path);
+        if (!tracing) path.n = 0;
     }
-    if (cur_n > 0) store_photons(ph, cur_ph, cur_n, dwell, (uint32_t)p0);
-    atomicAdd(&stats[0], large_visible);
-    atomicAdd(&stats[1], large);
+    while (__any_sync(0xffffffffu, alive)) {
+        if (alive && tracing) tracing = mlt_path_bounce(P, su[ci ^ 1], rr, maxlen, path, sph[ci ^ 1]);
+        const unsigned waiting = __ballot_sync(0xffffffffu, alive && !tracing);
+        const unsigned live = __ballot_sync(0xffffffffu, alive);
+        if (!waiting || (__popc(waiting) < kSettleLanes && waiting != live)) continue;
+        if (!(alive && !tracing)) continue;
+        // the proposal's path has ended: settle its step
+        const int n = path.n;
+        if (burn_in) {
+            ++large;
+            if (n > 0) { ++large_visible; ci ^= 1; cur_n = n; burn_in = false; }
+            else if (++t == 256) { ci ^= 1; cur_n = 0; burn_in = false; }   // go on from the last state tried
+        } else {
+            if (is_large) { ++large; if (n > 0) ++large_visible; }
+            if (n > 0) {
+                if (cur_n > 0) store_photons(ph, sph[ci], cur_n, dwell, (uint32_t)p);
+                ci ^= 1;
+                cur_n = n;
+                dwell = 1.0f;
+                if (!is_large) ++accepted;
+            } else {
+                dwell += 1.0f;
+            }
+            if (!is_large && mutated > 0) {
+                const float R = (float)accepted / (float)mutated;
+                m += (R - 0.234f) / (float)mutated;
+            }
+            ++p;
+        }
+        // the next proposal
+        if (burn_in) {
+            uniform_samples(P, p0, 16u + (uint32_t)t, su[ci ^ 1]);
+            rr.init(P.seed, ((uint64_t)p0 << 9) | (uint64_t)t, P.iteration, STREAM_MLT + 2u);
+        } else {
+            if (p >= p1) {
+                alive = false;
+                if (cur_n > 0) store_photons(ph, sph[ci], cur_n, dwell, (uint32_t)p0);
+                atomicAdd(&stats[0], large_visible);
+                atomicAdd(&stats[1], large);
+                continue;
+            }
+            PathRng g;
+            g.init(P.seed, (uint64_t)p, P.iteration, STREAM_MLT + 3u);
+            is_large = u01(g.block(0).a) < p_large;
+            if (is_large) uniform_samples(P, p, 0u, su[ci ^ 1]);
+            else {
+                for (int k = 0; k < kMltDims; ++k) su[ci ^ 1][k] = su[ci][k];
+                mutate(P, (uint64_t)p, m, su[ci ^ 1]);
+                ++mutated;
+            }
+            rr.init(P.seed, (uint64_t)p * 2u, P.iteration, STREAM_MLT + 1u);
+        }
+        tracing = mlt_path_start(P, su[ci ^ 1], path);
+        if (!tracing) path.n = 0;
+    }
 }
 
 }  // namespace
