@@ -232,7 +232,9 @@ __global__ void __launch_bounds__(128) k_mlt_hybrid(const VMParams P, PhotonBuf 
 // Each chain takes the same steps with the same random numbers in the same order as a
 // step-at-a-time loop: burn-in large steps t = 0 .. (first visible, at most 256) from
 // the chain's first path index, then one step per further path index.
-constexpr int kSettleLanes = 16;
+// (gem cluster, 65,536 chains, 32M steps: 1, 4, 8, 16, 24 lanes -> 680, 681, 679, 700,
+// 779 ms per iteration)
+constexpr int kSettleLanes = 8;
 
 __global__ void __launch_bounds__(128) k_mlt_pss(const VMParams P, PhotonBuf ph, int chains, float p_large,
                                                  unsigned long long* __restrict__ stats) {
