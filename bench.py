@@ -53,6 +53,10 @@ PHOTON_BYTES, QUERY_BYTES, PIXEL_BYTES = 40, 64, 48
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) over algorithmic bytes of one
 # k_gather launch on the 960x540 / 4M-path water pool (profiles/k_gather_water_pool_960x540.md)
 GATHER_TRAFFIC_OVER_ALGORITHMIC = 1.161
+# SM issue efficiency of the persistent light pass from the same kind of capture
+# (profiles/k_light_pass_water_pool_960x540.md): issue-active cycles and thread
+# instructions per warp instruction
+LIGHT_ISSUE_ACTIVE_PCT, LIGHT_LANES_ACTIVE = 62.2, 10.3
 
 
 def dist_env():
@@ -333,6 +337,13 @@ def run_ours(args):
         "gpu_launches": int(dev[3]),
         "clocks": clk.summary(),
         "phase_ms_per_step": {k: st[k] for k in ("light_ms", "kd_ms", "camera_ms", "gather_ms")},
+        "light_pass": {
+            "paths_per_s": paths / (st["light_ms"] / 1000.0) if st["light_ms"] > 0 else None,
+            "rays_per_s": st["light_rays"] / (st["light_ms"] / 1000.0) if st["light_ms"] > 0 and st["light_rays"] else None,
+            "rays_per_path": st["light_rays"] / paths if st["light_rays"] else None,
+            # ncu on the 960x540 / 4M-path case (profiles/k_light_pass_water_pool_960x540.md)
+            "issue_active_pct_ncu": LIGHT_ISSUE_ACTIVE_PCT, "lanes_active_per_warp_instruction_ncu": LIGHT_LANES_ACTIVE,
+            "note": "window of the last iteration's light pass (the coherent path order included)"},
         "phase_note": "event windows of the last iteration; the camera pass runs on a second stream "
                       "beside the light pass's last launch and the KD build, its window opening there",
         "wall_s": wall,
@@ -372,12 +383,12 @@ def same_config_anchor(cpu: dict | None, width: int = 960, height: int = 540, st
     return res
 
 
-def learned_equal_time(args, iters: int = 16, ref_iters: int = 256, ref_scale: int = 8):
+def learned_equal_time(args, iters: int = 16, ref_iters: int = 512, ref_scale: int = 8):
     """Learned-guided vs plain vertex merging on the same workload: per-pixel RMSE of the
     FP64-accumulated image against two reference images, as a function of device time.
 
       full         reference: plain, `ref_iters` iterations, independent light and camera
-                   seeds (its variance ~1/16 of a 16-iteration render's): the whole
+                   seeds (its variance ~1/32 of a 16-iteration render's): the whole
                    image error, camera-side noise (pixel jitter, camera paths through the
                    rough water) included.
       photon_side  reference: plain with the same camera seed and iterations as the

@@ -236,7 +236,9 @@ const char* rc_last_error(void);
  * [8] accumulate ms, [9] total device ms, [10] iterations rendered so far,
  * [11] scene radius, [12] current merge radius, [13] kernel launches,
  * [14] photon-query distance tests in the gather, [15] photon chunks (of at most 32)
- * tested by the gather's query groups.
+ * tested by the gather's query groups, [16] closest-hit queries (rays) the light pass
+ * traced (persistent launch shapes; 0 for the wavefront pass, the Metropolis samplers
+ * and a batch render).
  * With the learned proposal, [8] is the proposal inference + training time.
  * With uniformly sampled light paths the camera pass runs on
  * a second stream beside the light pass and the KD build: its window [6] opens with the

@@ -108,7 +108,7 @@ struct DeviceState {
     int mlp_rounds = 0;          // training rounds done (the proposal is used after the first)
     double mlp_last_rows = 0;    // training samples collected in the last round
     int iterations_done = 0;
-    double stats[16] = {};
+    double stats[17] = {};
     double last_nodes = 0;
     float stats_mlt_visible = 0.0f;
     // accumulated over a timed render call
@@ -300,7 +300,7 @@ int upload_scene_rest(HostScene& sc, const std::vector<int>& mesh_root) {
         (r = upload(d.lights, sc.lights, s)) || (r = upload(d.cdf, sc.light_cdf, s)) ||
         (r = upload(d.materials, sc.materials, s)))
         return r;
-    RC_CUDA(d.counters.reserve(8));
+    RC_CUDA(d.counters.reserve(10));   // [8] closest-hit queries of the persistent light pass
     RC_CUDA(d.errors.reserve(ERR_COUNT));
     RC_CUDA(cudaMemsetAsync(d.errors.p, 0, sizeof(int) * ERR_COUNT, s));
     RC_CUDA(cudaStreamSynchronize(s));
@@ -614,10 +614,11 @@ int light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s, int v, cudaEvent
     DeviceState& d = ctx().dev;
     if (v == pass_variants()) {
         RC_CUDA(d.wf_scratch.reserve(light_wavefront_scratch_bytes(p.num_light_paths)));
+        RC_CUDA(cudaMemsetAsync(d.counters.p + 8, 0, sizeof(unsigned long long), s));   // (not counted)
         launch_light_wavefront(p, ph, d.wf_scratch.p, s, tail);
         return RC_OK;
     }
-    launch_light_pass(p, ph, d.counters.p + 6, s, v);
+    launch_light_pass(p, ph, d.counters.p + 6, s, v, d.counters.p + 8);
     if (tail) RC_CUDA(cudaEventRecord(tail, s));
     return RC_OK;
 }
@@ -718,7 +719,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     // counter based, so the re-trace produces the same photons)
     long long cap = (long long)d.ph_pos.n;
     if (cap < p.num_light_paths * 2) cap = p.num_light_paths * 2;
-    unsigned long long nph = 0;
+    unsigned long long nph = 0, rays = 0;
     unsigned long long mlt[2] = {0, 0};
     float t_light = 0.0f;
     if (tabulated) {
@@ -800,6 +801,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
         }
         else {
             if (fork) RC_CUDA(cudaEventRecord(d.fork, s));
+            RC_CUDA(cudaMemsetAsync(d.counters.p + 8, 0, sizeof(unsigned long long), s));   // (not counted)
             launch_mlt_pass(p, ph, sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s);
         }
         RC_CUDA(cudaGetLastError());
@@ -816,6 +818,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
             RC_CUDA(cudaEventRecord(d.join, d.side));
         }
         RC_CUDA(cudaMemcpyAsync(&nph, d.counters.p, sizeof(nph), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(cudaMemcpyAsync(&rays, d.counters.p + 8, sizeof(rays), cudaMemcpyDeviceToHost, s));
         if (sampler != RC_SAMPLER_UNIFORM)
             RC_CUDA(cudaMemcpyAsync(mlt, d.counters.p + 2, sizeof(mlt), cudaMemcpyDeviceToHost, s));
         RC_CUDA(cudaStreamSynchronize(s));
@@ -978,6 +981,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     st[3] = (double)gc[0];   // accepted photon-query pairs
     st[14] = (double)gc[1];  // photon tests
     st[15] = (double)gc[2];  // photon chunks tested (per group)
+    st[16] = (double)rays;   // closest-hit queries of the light pass (persistent shapes)
     d.last_nodes = (double)gc[3];
     st[4] = t_light;
     st[5] = ms_between(d.ev[2], d.ev[3]);
@@ -1193,7 +1197,7 @@ int async_finish(HostScene& sc, int first_it, int n_async, bool windows) {
     r = check_errors();
     if (r) return r;
     // stats of the last replayed iteration
-    unsigned long long cnt[6] = {0, 0, 0, 0, 0, 0};
+    unsigned long long cnt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     RC_CUDA(cudaMemcpy(cnt, d.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
     VMParams p = make_params(sc, d.iterations_done - 1);
     double* st = d.stats;
@@ -1203,6 +1207,7 @@ int async_finish(HostScene& sc, int first_it, int n_async, bool windows) {
     st[3] = (double)cnt[2];
     st[14] = (double)cnt[3];
     st[15] = (double)cnt[4];
+    st[16] = windows ? (double)cnt[8] : 0.0;
     st[4] = windows ? ms_between(d.ev[0], d.ev[1]) : 0.0;
     st[5] = ms_between(d.ev[2], d.ev[3]);
     st[6] = windows ? ms_between(d.ev[4], d.ev[5]) : 0.0;
@@ -2105,7 +2110,7 @@ const char* rc_last_error(void) { return ctx().err.c_str(); }
 
 int rc_get_stats(double* out, int n) {
     if (!out || n < 0) return RC_E_INVALID;
-    for (int i = 0; i < n && i < 16; ++i) out[i] = ctx().dev.stats[i];
+    for (int i = 0; i < n && i < 17; ++i) out[i] = ctx().dev.stats[i];
     return RC_OK;
 }
 
@@ -2152,7 +2157,7 @@ int rc_camera_queries(int iteration, float* out, long long cap, long long* count
     for (int attempt = 0; attempt < 3; ++attempt) {
         RC_CUDA(d.q0.reserve(qcap)); RC_CUDA(d.q1.reserve(qcap)); RC_CUDA(d.q2.reserve(qcap));
         RC_CUDA(d.q3.reserve(qcap)); RC_CUDA(d.q4.reserve(qcap));
-        RC_CUDA(d.counters.reserve(8));
+        RC_CUDA(d.counters.reserve(10));
         RC_CUDA(cudaMemsetAsync(d.counters.p + 1, 0, sizeof(unsigned long long), s));
         QueryBuf qb{d.q0.p, d.q1.p, d.q2.p, d.q3.p, d.q4.p, (long long)d.q0.n, d.counters.p + 1};
         launch_camera_pass(p, qb, d.counters.p + 7, s);
@@ -2188,7 +2193,7 @@ int rc_light_photons_shape(int shape, int iteration, float* out, long long cap, 
     for (int attempt = 0; attempt < 3; ++attempt) {
         RC_CUDA(d.ph_pos.reserve(pcap)); RC_CUDA(d.ph_dir.reserve(pcap));
         RC_CUDA(d.ph_tp.reserve(pcap)); RC_CUDA(d.ph_path.reserve(pcap));
-        RC_CUDA(d.counters.reserve(8));
+        RC_CUDA(d.counters.reserve(10));
         RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
         PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, (long long)d.ph_pos.n, d.counters.p};
         r = light_pass(p, ph, s, shape);

@@ -110,8 +110,10 @@ void launch_light_order(const VMParams& p, void* scratch, uint32_t* order, cudaS
 // with tile_scratch (scan_scratch_words(m) words) for the tile totals.
 size_t scan_scratch_words(long long m);
 void launch_scan_counts(uint32_t* counts, long long m, uint32_t* tile_scratch, cudaStream_t s);
-// next_path: device counter for the persistent kernel (nullptr: one thread per path)
-void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant = 0);
+// next_path: device counter for the persistent kernel (nullptr: one thread per path);
+// rays (optional): receives the number of closest-hit queries the pass traced.
+void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant = 0,
+                       unsigned long long* rays = nullptr);
 void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next_pixel, cudaStream_t s, int variant = 0);
 // The persistent light and camera passes over n resident scenes in one launch each:
 // scenes[i] (device memory) holds scene i's parameters and buffers, path_prefix

@@ -279,12 +279,14 @@ constexpr int kRefillLanes = 24;
 // allow); traversal stacks are per-traversal local-memory arrays.
 template <int kBlock, int kMinBlocks>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_light_pass_persistent(const VMParams P, PhotonBuf ph,
-                                                                               unsigned long long* __restrict__ next_path) {
+                                                                               unsigned long long* __restrict__ next_path,
+                                                                               unsigned long long* __restrict__ rays) {
     CallStack stk;
     const int lane = threadIdx.x & 31;
     LightPath s;
     bool alive = false;
     bool pool_left = true;
+    unsigned traced = 0;      // closest-hit queries of this lane (one per bounce)
     while (true) {
         // refill lanes without a path, once at least kRefillLanes are free (or none has
         // a path): lanes refilled together take consecutive, coherent paths (the order
@@ -305,8 +307,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_light_pass_persistent(co
             if (base + __popc(need) >= (unsigned long long)P.num_light_paths) pool_left = false;
         }
         if (!__any_sync(0xffffffffu, alive)) break;
-        if (alive) alive = light_path_bounce(P, ph, s, stk);
+        if (alive) { alive = light_path_bounce(P, ph, s, stk); ++traced; }
     }
+    const unsigned w = __reduce_add_sync(0xffffffffu, traced);
+    if (rays && lane == 0) atomicAdd(rays, (unsigned long long)w);
 }
 
 // Persistent camera pass with path regeneration (same scheme as the light pass).
@@ -561,7 +565,8 @@ unsigned persistent_grid(K kernel, int block, size_t smem, long long work_items)
 }
 
 template <int B, int MB>
-void launch_light_t(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s) {
+void launch_light_t(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, unsigned long long* rays,
+                    cudaStream_t s) {
     // per host thread: contexts on different threads launch concurrently
     static thread_local unsigned grid_cache = 0;
     static thread_local long long grid_for = -1;
@@ -570,7 +575,8 @@ void launch_light_t(const VMParams& p, PhotonBuf ph, unsigned long long* next_pa
         grid_for = p.num_light_paths;
     }
     cudaMemsetAsync(next_path, 0, sizeof(unsigned long long), s);
-    k_light_pass_persistent<B, MB><<<grid_cache, B, 0, s>>>(p, ph, next_path);
+    if (rays) cudaMemsetAsync(rays, 0, sizeof(unsigned long long), s);
+    k_light_pass_persistent<B, MB><<<grid_cache, B, 0, s>>>(p, ph, next_path, rays);
 }
 
 template <int B, int MB>
@@ -684,16 +690,17 @@ const char* pass_variant_name(int v) {
     return (v >= 0 && v < 5) ? names[v] : "?";
 }
 
-void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant) {
+void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant,
+                       unsigned long long* rays) {
     long long n = p.num_light_paths;
     if (n <= 0) return;
     if (!next_path) return;
     switch (variant) {
-    case 1: launch_light_t<128, 7>(p, ph, next_path, s); break;
-    case 2: launch_light_t<128, 8>(p, ph, next_path, s); break;
-    case 3: launch_light_t<128, 5>(p, ph, next_path, s); break;
-    case 4: launch_light_t<128, 10>(p, ph, next_path, s); break;
-    default: launch_light_t<256, 3>(p, ph, next_path, s); break;
+    case 1: launch_light_t<128, 7>(p, ph, next_path, rays, s); break;
+    case 2: launch_light_t<128, 8>(p, ph, next_path, rays, s); break;
+    case 3: launch_light_t<128, 5>(p, ph, next_path, rays, s); break;
+    case 4: launch_light_t<128, 10>(p, ph, next_path, rays, s); break;
+    default: launch_light_t<256, 3>(p, ph, next_path, rays, s); break;
     }
 }
 

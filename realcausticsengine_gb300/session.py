@@ -14,7 +14,7 @@ from .scene import InitArgs, Scene
 
 STAT_NAMES = ["light_paths", "photons", "queries", "merged", "light_ms", "kd_ms", "camera_ms", "gather_ms",
               "accum_ms", "device_ms", "iterations", "scene_radius", "radius", "launches", "photon_tests",
-              "chunks_tested"]
+              "chunks_tested", "light_rays"]
 
 
 class Context:
@@ -126,8 +126,8 @@ class Renderer:
         return out
 
     def stats(self) -> dict:
-        a = np.zeros(16, np.float64)
-        check(self.L.rc_get_stats(a.ctypes.data, 16), "rc_get_stats")
+        a = np.zeros(len(STAT_NAMES), np.float64)
+        check(self.L.rc_get_stats(a.ctypes.data, len(STAT_NAMES)), "rc_get_stats")
         return dict(zip(STAT_NAMES, a.tolist()))
 
     def trace(self, origins: np.ndarray, dirs: np.ndarray, tmin: float = 0.001, shape: int = 0) -> np.ndarray:

@@ -73,7 +73,7 @@ class FakeRenderer:
 
     def stats(self):
         return {"queries": 3.6e6, "photons": 7.6e6, "merged": 2.5e7, "light_ms": 13.7, "kd_ms": 6.2,
-                "camera_ms": 15.4, "gather_ms": 6.6}
+                "camera_ms": 15.4, "gather_ms": 6.6, "light_rays": 6.0e7}
 
     def release(self):
         pass
