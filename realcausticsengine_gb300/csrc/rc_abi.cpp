@@ -608,8 +608,8 @@ int size_class(long long n) { return n > 0 ? 63 - __builtin_clzll((unsigned long
 
 // The light pass in launch shape v: the persistent pass's shapes, or (v ==
 // pass_variants()) the wavefront pass with its path state in the context's scratch.
-// `tail`, if given, is recorded where the pass stops filling the GPU: before the
-// wavefront pass's last launch, after a persistent pass.
+// `tail`, if given, is recorded where work forked from it can fill the slots the pass
+// stops using: before the wavefront pass's last launch, before a persistent pass.
 int light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s, int v, cudaEvent_t tail = nullptr) {
     DeviceState& d = ctx().dev;
     if (v == pass_variants()) {
@@ -618,8 +618,11 @@ int light_pass(const VMParams& p, PhotonBuf ph, cudaStream_t s, int v, cudaEvent
         launch_light_wavefront(p, ph, d.wf_scratch.p, s, tail);
         return RC_OK;
     }
-    launch_light_pass(p, ph, d.counters.p + 6, s, v, d.counters.p + 8);
+    // (the persistent pass holds every block slot until its pool drains: work forked
+    // before it takes the slots its tail frees; measured 20.62 -> 20.53 ms per water-pool
+    // iteration against forking after it)
     if (tail) RC_CUDA(cudaEventRecord(tail, s));
+    launch_light_pass(p, ph, d.counters.p + 6, s, v, d.counters.p + 8);
     return RC_OK;
 }
 
