@@ -1306,6 +1306,7 @@ struct BatchRun {
     cudaStream_t main = nullptr, side = nullptr;
     std::vector<cudaStream_t> branch;
     cudaEvent_t start = nullptr, light = nullptr, camera = nullptr, join = nullptr, t0 = nullptr, t1 = nullptr;
+    cudaEvent_t cam_fork = nullptr;
     cudaEvent_t light_start = nullptr, light_end = nullptr, camera_start = nullptr, camera_end = nullptr;
     DevBuf<BatchScene> scenes;          // per graph iteration: its scenes' entries, end to end
     DevBuf<long long> prefix;           // per graph iteration: path prefix (m + 1), pixel prefix (m + 1)
@@ -1314,7 +1315,8 @@ struct BatchRun {
     ~BatchRun() {
         if (exec) cudaGraphExecDestroy(exec);
         scenes.release(); prefix.release(); next.release();
-        for (cudaEvent_t e : {start, light, camera, join, t0, t1, light_start, light_end, camera_start, camera_end})
+        for (cudaEvent_t e : {start, light, camera, join, cam_fork, t0, t1, light_start, light_end, camera_start,
+                              camera_end})
             if (e) cudaEventDestroy(e);
         for (cudaStream_t b : branch) if (b) cudaStreamDestroy(b);
         if (side) cudaStreamDestroy(side);
@@ -1426,7 +1428,7 @@ int batch_render(Context* const* cs, int n, int iterations, double* out) {
     RC_CUDA(cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking));
     B.branch.assign(n, nullptr);
     for (int i = 0; i < n; ++i) RC_CUDA(cudaStreamCreateWithFlags(&B.branch[i], cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&B.start, &B.light, &B.camera, &B.join})
+    for (cudaEvent_t* e : {&B.start, &B.light, &B.camera, &B.join, &B.cam_fork})
         RC_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (cudaEvent_t* e : {&B.t0, &B.t1, &B.light_start, &B.light_end, &B.camera_start, &B.camera_end})
         RC_CUDA(cudaEventCreate(e));
@@ -1497,12 +1499,15 @@ int batch_render(Context* const* cs, int n, int iterations, double* out) {
                 RC_CUDA(cudaStreamWaitEvent(B.main, B.join, 0));
             }
             t_bound = caller;
+            // the camera pass forks before the light pass: its blocks take the slots the
+            // persistent light pass's tail frees
+            RC_CUDA(cudaEventRecord(B.cam_fork, B.main));
             RC_CUDA(record(B.light_start, B.main));
             launch_light_pass_batch(B.scenes.p + entry_at[j], B.prefix.p + prefix_at[j], m, total_paths[j], B.next.p,
                                     B.main, lvar);
             RC_CUDA(record(B.light_end, B.main));
             RC_CUDA(cudaEventRecord(B.light, B.main));
-            RC_CUDA(cudaStreamWaitEvent(B.side, B.light, 0));
+            RC_CUDA(cudaStreamWaitEvent(B.side, B.cam_fork, 0));
             RC_CUDA(record(B.camera_start, B.side));
             launch_camera_pass_batch(B.scenes.p + entry_at[j], B.prefix.p + prefix_at[j] + m + 1, m, total_pixels[j],
                                      B.next.p + 1, B.side, cvar);
