@@ -180,7 +180,8 @@ __device__ __forceinline__ bool mesh_traverse_impl(const SceneView& s, int mesh,
 // pass, a warp's lanes stepping together) test both children's boxes at their parent
 // instead, with the same outcome (below).  Measured on the water pool (light pass per
 // iteration): pop-and-test (mesh_traverse_impl) 13.3 ms, children tested at the parent
-// 11.9 ms, four-wide records of grandchildren tested at the grandparent 14.7 ms.
+// 11.9 ms, the same with a warp's lanes stepping together (mesh_traverse_steps) 13.3
+// ms, four-wide records of grandchildren tested at the grandparent 14.7 ms.
 template <class Stack>
 __device__ __forceinline__ bool mesh_traverse_children(const SceneView& s, int mesh, F3 o, F3 d, F3 inv,
                                                        float tmin, HitRec& rec, bool& any, int* overflow,
