@@ -334,6 +334,7 @@ def run_ours(args):
                      "bytes_formula": "40 B x stored photons + 64 B x merge queries + 48 B x pixels",
                      "touched_bytes": touched,
                      "touched_frac": (touched / (gather_ms_mean / 1000.0) / 1e9) / peak if gather_ms_mean > 0 else 0.0},
+        "kd_roofline": kd_roofline(nph, st["kd_ms"], peak, peak_kind),
         "gpu_launches": int(dev[3]),
         "clocks": clk.summary(),
         "phase_ms_per_step": {k: st[k] for k in ("light_ms", "kd_ms", "camera_ms", "gather_ms")},
@@ -354,6 +355,24 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(cores=args.cpu_cores)
         line["same_config"] = same_config_anchor(line["cpu_baseline"])
     print(json.dumps(line), flush=True)
+
+
+def kd_roofline(nph: float, kd_ms: float, peak: float, peak_kind: str) -> dict:
+    """The KD build against the HBM roofline with the algorithmic bytes of a median-split
+    build over P photons: 12 P (positions read once) + 2 x 16 P per level over ceil(log2 P)
+    levels (x, y, z, id read and written) + 8 B per node of the 2^(floor(log2 P) + 1)-node
+    array.  kd_ms is the event window of the build, its boxes and the tree-order records,
+    with the camera pass running beside them on the other stream (so a lower bound on
+    the build's own rate)."""
+    import math
+    P = float(nph)
+    if P < 2 or kd_ms <= 0:
+        return None
+    b = 12.0 * P + 32.0 * P * math.ceil(math.log2(P)) + 8.0 * 2 ** (math.floor(math.log2(P)) + 1)
+    achieved = b / (kd_ms / 1000.0) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind, "algorithmic_bytes": b, "window_ms": kd_ms,
+            "bytes_formula": "12 P + 32 P ceil(log2 P) + 8 x 2^(floor(log2 P) + 1)"}
 
 
 def same_config_anchor(cpu: dict | None, width: int = 960, height: int = 540, steps: int = 8, warmup: int = 2):
