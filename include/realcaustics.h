@@ -301,6 +301,15 @@ int rc_trace_rays_shape(int n, const float* origins, const float* directions, fl
  * (u32 bits), 0].  *count receives the number stored (may exceed cap). */
 int rc_light_photons(int iteration, float* out, long long cap, long long* count);
 
+/* One Metropolis light pass (the configured sampler, iteration `iteration`); the stored
+ * photons as rc_light_photons writes them, large_steps (NULL or 2) = visible large
+ * steps, large steps.  PSSMLT variant 0: the render's chains, advanced one path segment
+ * per loop iteration; 1: the same chains one step at a time.  Both store the same
+ * photons (in another order) and count the same steps; HYBRID ignores the variant.  No
+ * counterpart in the reference (its sampler is src/Vertex_Merging.cpp:218-274). */
+int rc_mlt_photons(int variant, int iteration, float* out, long long cap, long long* count,
+                   unsigned long long* large_steps);
+
 /* rc_light_photons with the light pass in launch shape `shape` (0 .. 5: the persistent
  * pass's block/register shapes, 5 = the wavefront pass), for comparing them; the
  * photons of every shape are the same, only their storage order differs. */

@@ -71,6 +71,7 @@ def lib() -> C.CDLL:
     L.rc_context_bind.argtypes = [C.c_void_p]
     L.rc_context_destroy.argtypes = [C.c_void_p]
     L.rc_batch_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.rc_mlt_photons.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong), C.c_void_p]
     _lib = L
     return L
 
@@ -89,4 +90,5 @@ EXPORTS = ["init", "main", "rc_default_config", "rc_set_config", "rc_prepare", "
            "rc_save_state", "rc_load_state", "rc_scene_dump", "rc_prepare_stats",
            "rc_context_create", "rc_context_bind", "rc_context_destroy", "rc_gather_query",
            "rc_gather_variants", "rc_camera_queries", "rc_device_bus_id", "rc_tc_gemm_selftest",
-           "rc_tc_wait_selftest", "rc_light_photons_shape", "rc_batch_render"]
+           "rc_tc_wait_selftest", "rc_light_photons_shape", "rc_batch_render",
+           "rc_mlt_photons"]

@@ -2236,6 +2236,57 @@ int rc_light_photons_shape(int shape, int iteration, float* out, long long cap, 
     return RC_OK;
 }
 
+int rc_mlt_photons(int variant, int iteration, float* out, long long cap, long long* count,
+                   unsigned long long* large_steps) {
+    int r = prepare();
+    if (r) return r;
+    if (iteration < 0 || (cap > 0 && !out)) { ctx().err = "bad photon output"; return RC_E_INVALID; }
+    if (variant < 0 || variant >= mlt_variants()) { ctx().err = "Metropolis pass shape out of range"; return RC_E_INVALID; }
+    if (cfg().sampler == RC_SAMPLER_UNIFORM) { ctx().err = "the configuration has no Metropolis sampler"; return RC_E_INVALID; }
+    HostScene& sc = *ctx().scene;
+    DeviceState& d = ctx().dev;
+    cudaStream_t s = d.stream;
+    VMParams p = make_params(sc, iteration);
+    long long pcap = std::max<long long>(p.num_light_paths * 2, 1024);
+    unsigned long long nph = 0, st[2] = {0, 0};
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        RC_CUDA(d.ph_pos.reserve(pcap)); RC_CUDA(d.ph_dir.reserve(pcap));
+        RC_CUDA(d.ph_tp.reserve(pcap)); RC_CUDA(d.ph_path.reserve(pcap));
+        RC_CUDA(cudaMemsetAsync(d.counters.p, 0, sizeof(unsigned long long), s));
+        PhotonBuf ph{d.ph_pos.p, d.ph_dir.p, d.ph_tp.p, d.ph_path.p, (long long)d.ph_pos.n, d.counters.p};
+        launch_mlt_pass(p, ph, cfg().sampler, cfg().mlt_chains, cfg().large_step_prob, d.counters.p + 2, s, variant);
+        RC_CUDA(cudaGetLastError());
+        RC_CUDA(cudaMemcpyAsync(&nph, d.counters.p, sizeof(nph), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(cudaMemcpyAsync(st, d.counters.p + 2, sizeof(st), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(cudaStreamSynchronize(s));
+        if ((long long)nph <= (long long)d.ph_pos.n) break;
+        pcap = (long long)nph + 1024;
+    }
+    r = check_errors();
+    if (r) return r;
+    if (count) *count = (long long)nph;
+    if (large_steps) { large_steps[0] = st[0]; large_steps[1] = st[1]; }
+    long long n = std::min<long long>((long long)nph, cap);
+    if (n > 0) {
+        std::vector<float4> pos(n), dir(n);
+        std::vector<float2> tp(n);
+        std::vector<uint32_t> path(n);
+        RC_CUDA(cudaMemcpy(pos.data(), d.ph_pos.p, 16 * n, cudaMemcpyDeviceToHost));
+        RC_CUDA(cudaMemcpy(dir.data(), d.ph_dir.p, 16 * n, cudaMemcpyDeviceToHost));
+        RC_CUDA(cudaMemcpy(tp.data(), d.ph_tp.p, 8 * n, cudaMemcpyDeviceToHost));
+        RC_CUDA(cudaMemcpy(path.data(), d.ph_path.p, 4 * n, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < n; ++i) {
+            float* w = out + 12 * i;
+            w[0] = pos[i].x; w[1] = pos[i].y; w[2] = pos[i].z;
+            w[3] = dir[i].x; w[4] = dir[i].y; w[5] = dir[i].z;
+            w[6] = dir[i].w; w[7] = tp[i].x; w[8] = tp[i].y; w[9] = pos[i].w;
+            std::memcpy(&w[10], &path[i], 4);
+            w[11] = 0.0f;
+        }
+    }
+    return RC_OK;
+}
+
 int rc_trace_rays(int n, const float* origins, const float* directions, float tmin, unsigned* out) {
     int r = prepare();
     if (r) return r;

@@ -97,8 +97,11 @@ enum { ERR_STACK = 0, ERR_MATERIAL = 1, ERR_PHOTON_OVERFLOW = 2, ERR_QUERY_OVERF
 // launch; stats[0] = visible large steps, stats[1] = large steps (HYBRID: light paths).
 // The photons must be scaled by stats[0] / stats[1] (applied through VM_normalization).
 constexpr int kMltMaxPathLength = 12;
+// variant (PSSMLT only): 0 the chains advanced one path segment per loop iteration,
+// 1 one step at a time (the same photons and counts).
 void launch_mlt_pass(const VMParams& p, PhotonBuf ph, int sampler, int chains, float p_large,
-                     unsigned long long* stats, cudaStream_t s);
+                     unsigned long long* stats, cudaStream_t s, int variant = 0);
+int mlt_variants();
 // Processing order of the light paths (p.num_light_paths of them) for p.path_order:
 // indices sorted by the 4D Morton cell (32 per axis) of their own emission samples (area
 // u, v, direction u, v; with p.proposal, the proposed direction's octahedral coordinates

@@ -328,15 +328,83 @@ __global__ void __launch_bounds__(128) k_mlt_pss(const VMParams P, PhotonBuf ph,
     }
 }
 
+// PSSMLT one step at a time per chain: the sampler as defined (propose, trace the whole
+// path, accept or reject, adapt the mutation size), kept as a launch shape so that tests
+// can check that k_mlt_pss (the same chains advanced one path segment per loop
+// iteration) stores exactly its photons.
+__global__ void __launch_bounds__(128) k_mlt_pss_steps(const VMParams P, PhotonBuf ph, int chains, float p_large,
+                                                 unsigned long long* __restrict__ stats) {
+    const int chain = blockIdx.x * blockDim.x + threadIdx.x;
+    if (chain >= chains) return;
+    const long long N = P.num_light_paths;
+    const long long per = (N + chains - 1) / chains;
+    const long long p0 = (long long)chain * per;
+    const long long p1 = p0 + per < N ? p0 + per : N;
+    if (p0 >= p1) return;
+    const int maxlen = P.max_path_length < kMltMaxLen ? P.max_path_length : kMltMaxLen;
+    float cur[kMltDims], prop[kMltDims];
+    PhotonRec cur_ph[kPhotonBuf], tmp[kPhotonBuf];
+    int cur_n = 0;
+    unsigned long long large = 0, large_visible = 0;
+    // burn-in: large steps until a visible state (bounded); they count as large steps
+    long long step = 0;
+    for (int t = 0; t < 256 && cur_n == 0; ++t) {
+        uniform_samples(P, p0, 16u + (uint32_t)t, cur);
+        PathRng rr;
+        rr.init(P.seed, ((uint64_t)p0 << 9) | (uint64_t)t, P.iteration, STREAM_MLT + 2u);
+        cur_n = trace_light_samples(P, cur, rr, maxlen, cur_ph);
+        ++large;
+        if (cur_n > 0) ++large_visible;
+    }
+    float m = 1.0f;
+    int accepted = 1, mutated = 0;
+    float dwell = 1.0f;
+    for (long long p = p0 + 1; p < p1; ++p, ++step) {
+        PathRng g;
+        g.init(P.seed, (uint64_t)p, P.iteration, STREAM_MLT + 3u);
+        const bool is_large = u01(g.block(0).a) < p_large;
+        if (is_large) uniform_samples(P, p, 0u, prop);
+        else {
+            for (int k = 0; k < kMltDims; ++k) prop[k] = cur[k];
+            mutate(P, (uint64_t)p, m, prop);
+            ++mutated;
+        }
+        PathRng rr;
+        rr.init(P.seed, (uint64_t)p * 2u, P.iteration, STREAM_MLT + 1u);
+        const int n = trace_light_samples(P, prop, rr, maxlen, tmp);
+        if (is_large) { ++large; if (n > 0) ++large_visible; }
+        if (n > 0) {
+            if (cur_n > 0) store_photons(ph, cur_ph, cur_n, dwell, (uint32_t)p);
+            for (int k = 0; k < kMltDims; ++k) cur[k] = prop[k];
+            for (int k = 0; k < n; ++k) cur_ph[k] = tmp[k];
+            cur_n = n;
+            dwell = 1.0f;
+            if (!is_large) ++accepted;
+        } else {
+            dwell += 1.0f;
+        }
+        if (!is_large && mutated > 0) {
+            const float R = (float)accepted / (float)mutated;
+            m += (R - 0.234f) / (float)mutated;
+        }
+    }
+    if (cur_n > 0) store_photons(ph, cur_ph, cur_n, dwell, (uint32_t)p0);
+    atomicAdd(&stats[0], large_visible);
+    atomicAdd(&stats[1], large);
+}
+
 }  // namespace
 
+int mlt_variants() { return 2; }
+
 void launch_mlt_pass(const VMParams& p, PhotonBuf ph, int sampler, int chains, float p_large,
-                     unsigned long long* stats, cudaStream_t s) {
+                     unsigned long long* stats, cudaStream_t s, int variant) {
     if (p.num_light_paths <= 0 || chains <= 0) return;
     cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), s);
     const unsigned grid = (unsigned)((chains + 127) / 128);
-    if (sampler == RC_SAMPLER_PSSMLT) k_mlt_pss<<<grid, 128, 0, s>>>(p, ph, chains, p_large, stats);
-    else k_mlt_hybrid<<<grid, 128, 0, s>>>(p, ph, chains, stats);
+    if (sampler != RC_SAMPLER_PSSMLT) k_mlt_hybrid<<<grid, 128, 0, s>>>(p, ph, chains, stats);
+    else if (variant == 1) k_mlt_pss_steps<<<grid, 128, 0, s>>>(p, ph, chains, p_large, stats);
+    else k_mlt_pss<<<grid, 128, 0, s>>>(p, ph, chains, p_large, stats);
 }
 
 }  // namespace rc

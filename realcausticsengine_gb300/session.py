@@ -158,6 +158,18 @@ class Renderer:
               "rc_light_photons_shape")
         return out[:n.value]
 
+    def mlt_photons(self, variant: int, iteration: int):
+        """Photons of one Metropolis light pass (PSSMLT variant 0: the render's chains, one
+        path segment per loop iteration; 1: one step at a time) and its (visible large
+        steps, large steps)."""
+        n = C.c_longlong()
+        st = np.zeros(2, np.uint64)
+        check(self.L.rc_mlt_photons(variant, int(iteration), None, 0, C.byref(n), st.ctypes.data), "rc_mlt_photons")
+        out = np.zeros((max(n.value, 1), 12), np.float32)
+        check(self.L.rc_mlt_photons(variant, int(iteration), out.ctypes.data, len(out), C.byref(n), st.ctypes.data),
+              "rc_mlt_photons")
+        return out[:n.value], (int(st[0]), int(st[1]))
+
     def light_photons(self, iteration: int) -> np.ndarray:
         n = C.c_longlong()
         check(self.L.rc_light_photons(int(iteration), None, 0, C.byref(n)), "rc_light_photons")

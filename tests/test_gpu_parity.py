@@ -368,6 +368,36 @@ def test_pssmlt_is_consistent_with_plain_vm():
     assert abs(pss / plain - 1.0) < 0.05, (pss, plain)
 
 
+@pytest.mark.parametrize("name", ["test_scene", "gem_cluster"])
+def test_pssmlt_segment_chains_store_the_step_chains_photons(name):
+    """The render's PSSMLT chains (one path segment per loop iteration, finished steps
+    settled together) store the photons of the same chains run one step at a time (the
+    sampler as defined) bit for bit - positions, directions, dwell-weighted throughputs,
+    dVM, path indices - and count the same large steps; only the storage order differs."""
+    from realcausticsengine_gb300 import abi
+    if name == "test_scene":
+        sc, paths, chains = scenes.test_scene(32, 24, subdiv=2), 40000, 512
+    else:
+        sc, paths, chains = scenes.gem_cluster(64, 36), 1 << 18, 4096
+    r = Renderer(sc, max_path_length=8, photons_per_iter=paths, seed=9)
+    cfg = abi.RcConfig()
+    r.L.rc_default_config(C.byref(cfg))
+    cfg.max_path_length, cfg.photons_per_iter, cfg.seed, cfg.write_exr = 8, paths, 9, 0
+    cfg.sampler, cfg.mlt_chains = abi.SAMPLER_PSSMLT, chains
+    assert r.L.rc_set_config(C.byref(cfg)) == 0, r.L.rc_last_error()
+    (seg, seg_steps), (step, step_steps) = r.mlt_photons(0, 3), r.mlt_photons(1, 3)
+    r.release()
+
+    def canonical(ph):
+        words = np.ascontiguousarray(ph).view(np.uint32)
+        return words[np.lexsort(words.T[::-1])]
+
+    a, b = canonical(seg), canonical(step)
+    assert len(b) > 1000 and step_steps[1] >= chains
+    assert seg_steps == step_steps
+    assert a.shape == b.shape and (a == b).all()
+
+
 @pytest.mark.parametrize("mode", [2, 3, 4])
 def test_debug_views_match_reference(golden, mode):
     """debug_test 2-4 on the GPU (one primary ray per pixel corner, closest hit, colour by
