@@ -292,7 +292,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_light_pass_persistent(co
         // a path): lanes refilled together take consecutive, coherent paths (the order
         // sorts paths by their emission samples), so a warp keeps groups of coherent
         // paths together for several bounces (measured on the water pool: refilling at
-        // any free lane 14.2 ms, at 16 free 13.6, at 20-24 free 13.4, at 32 free 14.5)
+        // any free lane 14.2 ms, at 16 free 13.6, at 20-24 free 13.4, at 32 free 14.5;
+        // with the children tested at the parent, per iteration at 20 / 24 / 28 / 32
+        // free: 20.49 / 20.48 / 20.82 / 21.13 ms)
         const unsigned need = __ballot_sync(0xffffffffu, !alive);
         if (need && pool_left && (__popc(need) >= kRefillLanes || need == 0xffffffffu)) {
             unsigned long long base = 0;
