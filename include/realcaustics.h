@@ -311,7 +311,7 @@ int rc_mlt_photons(int variant, int iteration, float* out, long long cap, long l
                    unsigned long long* large_steps);
 
 /* rc_light_photons with the light pass in launch shape `shape` (0 .. 5: the persistent
- * pass's block/register shapes, 5 = the wavefront pass), for comparing them; the
+ * pass's block/register shapes, 6 = the wavefront pass), for comparing them; the
  * photons of every shape are the same, only their storage order differs. */
 int rc_light_photons_shape(int shape, int iteration, float* out, long long cap, long long* count);
 

@@ -680,16 +680,17 @@ void launch_light_wavefront(const VMParams& p, PhotonBuf ph, void* scratch, cuda
     k_wf_finish<<<finish_grid, 128, 0, s>>>(p, ph, W, q);
 }
 
-int pass_variants() { return 5; }
+int pass_variants() { return 6; }
 
 const char* pass_variant_name(int v) {
-    static const char* names[5] = {"256 threads, >= 3 blocks/SM (<= 85 registers)",
+    static const char* names[6] = {"256 threads, >= 3 blocks/SM (<= 85 registers)",
                                    "128 threads, >= 7 blocks/SM (<= 73 registers)",
                                    "128 threads, >= 8 blocks/SM (<= 64 registers)",
                                    "128 threads, >= 5 blocks/SM (<= 102 registers)",
-                                   "128 threads, >= 10 blocks/SM (<= 51 registers)"};
-    if (v == 5) return "wavefront: closest-hit and shading kernels per bounce";
-    return (v >= 0 && v < 5) ? names[v] : "?";
+                                   "128 threads, >= 10 blocks/SM (<= 51 registers)",
+                                   "128 threads, >= 9 blocks/SM (<= 56 registers)"};
+    if (v == 6) return "wavefront: closest-hit and shading kernels per bounce";
+    return (v >= 0 && v < 6) ? names[v] : "?";
 }
 
 void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next_path, cudaStream_t s, int variant,
@@ -702,6 +703,7 @@ void launch_light_pass(const VMParams& p, PhotonBuf ph, unsigned long long* next
     case 2: launch_light_t<128, 8>(p, ph, next_path, rays, s); break;
     case 3: launch_light_t<128, 5>(p, ph, next_path, rays, s); break;
     case 4: launch_light_t<128, 10>(p, ph, next_path, rays, s); break;
+    case 5: launch_light_t<128, 9>(p, ph, next_path, rays, s); break;
     default: launch_light_t<256, 3>(p, ph, next_path, rays, s); break;
     }
 }
@@ -715,6 +717,7 @@ void launch_camera_pass(const VMParams& p, QueryBuf qb, unsigned long long* next
     case 2: launch_camera_t<128, 8>(p, qb, next_pixel, s); break;
     case 3: launch_camera_t<128, 5>(p, qb, next_pixel, s); break;
     case 4: launch_camera_t<128, 10>(p, qb, next_pixel, s); break;
+    case 5: launch_camera_t<128, 9>(p, qb, next_pixel, s); break;
     default: launch_camera_t<256, 3>(p, qb, next_pixel, s); break;
     }
 }
@@ -727,6 +730,7 @@ void launch_light_pass_batch(const BatchScene* scenes, const long long* path_pre
     case 2: launch_light_batch_t<128, 8>(scenes, path_prefix, n, total_paths, next_path, s); break;
     case 3: launch_light_batch_t<128, 5>(scenes, path_prefix, n, total_paths, next_path, s); break;
     case 4: launch_light_batch_t<128, 10>(scenes, path_prefix, n, total_paths, next_path, s); break;
+    case 5: launch_light_batch_t<128, 9>(scenes, path_prefix, n, total_paths, next_path, s); break;
     default: launch_light_batch_t<256, 3>(scenes, path_prefix, n, total_paths, next_path, s); break;
     }
 }
@@ -739,6 +743,7 @@ void launch_camera_pass_batch(const BatchScene* scenes, const long long* pixel_p
     case 2: launch_camera_batch_t<128, 8>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
     case 3: launch_camera_batch_t<128, 5>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
     case 4: launch_camera_batch_t<128, 10>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
+    case 5: launch_camera_batch_t<128, 9>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
     default: launch_camera_batch_t<256, 3>(scenes, pixel_prefix, n, total_pixels, next_pixel, s); break;
     }
 }

@@ -150,7 +150,7 @@ class Renderer:
         return out[:n.value]
 
     def light_photons_shape(self, shape: int, iteration: int) -> np.ndarray:
-        """Photons of one light pass in launch shape `shape` (5: the wavefront pass)."""
+        """Photons of one light pass in launch shape `shape` (6: the wavefront pass)."""
         n = C.c_longlong()
         check(self.L.rc_light_photons_shape(shape, int(iteration), None, 0, C.byref(n)), "rc_light_photons_shape")
         out = np.zeros((max(n.value, 1), 12), np.float32)

@@ -497,7 +497,7 @@ def test_light_pass_shapes_store_the_same_photons(name):
         sc, paths = scenes.water_pool(96, 54, grid=512), 1 << 20
     r = Renderer(sc, max_path_length=8, photons_per_iter=paths, seed=5)
     r.prepare()
-    shapes = [r.light_photons_shape(v, 2) for v in range(6)]
+    shapes = [r.light_photons_shape(v, 2) for v in range(7)]
     r.release()
 
     def canonical(ph):
@@ -507,6 +507,6 @@ def test_light_pass_shapes_store_the_same_photons(name):
 
     want = canonical(shapes[0])
     assert len(want) > 1000
-    for v in range(1, 6):
+    for v in range(1, 7):
         got = canonical(shapes[v])
         assert got.shape == want.shape and (got == want).all(), f"shape {v} differs"
