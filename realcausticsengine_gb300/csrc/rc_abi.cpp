@@ -739,7 +739,7 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     // The camera pass reads nothing that the light pass writes (the Metropolis samplers'
     // visibility factor, known only after the light pass, is applied by the gather).
     // Once its launch shape is tuned it then runs on the side stream: with uniformly
-    // sampled light paths issued right behind the light pass, so that its blocks take
+    // sampled light paths issued right before the light pass, so that its blocks take
     // the SMs that the light pass's tail frees and run through the host's read-back of
     // the photon count and the KD build's launches; with a Metropolis sampler issued
     // before the chains, whose one thread per chain leaves room on every SM.  It joins
@@ -749,7 +749,12 @@ int render_iteration(HostScene& sc, int redo_iteration = -1) {
     long long qcap = std::max<long long>((long long)d.q0.n, npix * 2);
     unsigned long long nq = 0;
     float t_cam = 0.0f;
-    const bool cam_side = !cfg().autotune || g_tune.camera[size_class(npix)].load() >= 0;
+    // (Metropolis samplers: only when the chains are long enough for the camera pass to
+    // hide beside them - 512 steps per chain on the 4K gem cluster: 50 ms of camera pass
+    // hidden; 8 per chain at 960x540: 4.75 ms per iteration serial against 5.28 beside)
+    const bool mlt_long = (long long)cfg().mlt_chains * 64 <= p.num_light_paths;
+    const bool cam_side = (sampler == RC_SAMPLER_UNIFORM || mlt_long) &&
+                          (!cfg().autotune || g_tune.camera[size_class(npix)].load() >= 0);
     const int cam_var = cfg().autotune ? std::max(g_tune.camera[size_class(npix)].load(), 0) : 0;
     if (cam_side) {
         RC_CUDA(d.q0.reserve(qcap)); RC_CUDA(d.q1.reserve(qcap)); RC_CUDA(d.q2.reserve(qcap));
