@@ -1346,10 +1346,17 @@ int batch_render(Context* const* cs, int n, int iterations, double* out) {
     // 1. every scene prepared, with its asynchronous capacities (a first iteration with
     //    host round trips where none has been rendered yet)
     std::vector<int> remaining(n, iterations), first_it(n, 0), pcap_was(n, 0);
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < n; ++i)
         if (!cs[i]) return fail(RC_E_INVALID, "rc_batch_render: null context " + std::to_string(i));
-        for (int k = 0; k < i; ++k)
-            if (cs[k] == cs[i]) return fail(RC_E_INVALID, "rc_batch_render: context " + std::to_string(i) + " repeated");
+    {
+        std::vector<std::pair<const Context*, int>> seen(n);
+        for (int i = 0; i < n; ++i) seen[i] = {cs[i], i};
+        std::sort(seen.begin(), seen.end());
+        for (int i = 1; i < n; ++i)
+            if (seen[i].first == seen[i - 1].first)
+                return fail(RC_E_INVALID, "rc_batch_render: context " +
+                                              std::to_string(std::max(seen[i].second, seen[i - 1].second)) +
+                                              " repeated");
     }
     for (int i = 0; i < n; ++i) {
         t_bound = cs[i];
@@ -1431,8 +1438,12 @@ int batch_render(Context* const* cs, int n, int iterations, double* out) {
     RC_CUDA(cudaMemcpy(B.prefix.p, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice));
     RC_CUDA(cudaStreamCreateWithFlags(&B.main, cudaStreamNonBlocking));
     RC_CUDA(cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking));
-    B.branch.assign(n, nullptr);
-    for (int i = 0; i < n; ++i) RC_CUDA(cudaStreamCreateWithFlags(&B.branch[i], cudaStreamNonBlocking));
+    // one capture stream per scene branch, at most kBatchStreams (scenes beyond share them
+    // in turn: their branches then follow one another in the graph)
+    constexpr int kBatchStreams = 64;
+    B.branch.assign(std::min(n, kBatchStreams), nullptr);
+    for (cudaStream_t& b : B.branch) RC_CUDA(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking));
+    auto branch = [&](int i) { return B.branch[(size_t)i % B.branch.size()]; };
     for (cudaEvent_t* e : {&B.start, &B.light, &B.camera, &B.join, &B.cam_fork})
         RC_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (cudaEvent_t* e : {&B.t0, &B.t1, &B.light_start, &B.light_end, &B.camera_start, &B.camera_end})
@@ -1497,10 +1508,10 @@ int batch_render(Context* const* cs, int n, int iterations, double* out) {
                 const int i = active[j][a];
                 t_bound = cs[i];
                 VMParams p = entries[entry_at[j] + a].p;
-                RC_CUDA(cudaStreamWaitEvent(B.branch[i], B.start, 0));
-                int rr = async_head(p, B.branch[i]);
+                RC_CUDA(cudaStreamWaitEvent(branch(i), B.start, 0));
+                int rr = async_head(p, branch(i));
                 if (rr) return scene_fail(i, rr);
-                RC_CUDA(cudaEventRecord(B.join, B.branch[i]));
+                RC_CUDA(cudaEventRecord(B.join, branch(i)));
                 RC_CUDA(cudaStreamWaitEvent(B.main, B.join, 0));
             }
             t_bound = caller;
@@ -1521,11 +1532,11 @@ int batch_render(Context* const* cs, int n, int iterations, double* out) {
             for (int a = 0; a < m; ++a) {
                 const int i = active[j][a];
                 t_bound = cs[i];
-                RC_CUDA(cudaStreamWaitEvent(B.branch[i], B.light, 0));
-                int rr = async_tail(*ctx().scene, entries[entry_at[j] + a].p, B.branch[i], B.camera,
+                RC_CUDA(cudaStreamWaitEvent(branch(i), B.light, 0));
+                int rr = async_tail(*ctx().scene, entries[entry_at[j] + a].p, branch(i), B.camera,
                                     ctx().dev.async_flags.p + j);
                 if (rr) return scene_fail(i, rr);
-                RC_CUDA(cudaEventRecord(B.join, B.branch[i]));
+                RC_CUDA(cudaEventRecord(B.join, branch(i)));
                 RC_CUDA(cudaStreamWaitEvent(B.main, B.join, 0));
             }
             t_bound = caller;
