@@ -2254,11 +2254,11 @@ int rc_light_photons_shape(int shape, int iteration, float* out, long long cap, 
 
 int rc_mlt_photons(int variant, int iteration, float* out, long long cap, long long* count,
                    unsigned long long* large_steps) {
-    int r = prepare();
-    if (r) return r;
     if (iteration < 0 || (cap > 0 && !out)) { ctx().err = "bad photon output"; return RC_E_INVALID; }
     if (variant < 0 || variant >= mlt_variants()) { ctx().err = "Metropolis pass shape out of range"; return RC_E_INVALID; }
     if (cfg().sampler == RC_SAMPLER_UNIFORM) { ctx().err = "the configuration has no Metropolis sampler"; return RC_E_INVALID; }
+    int r = prepare();
+    if (r) return r;
     HostScene& sc = *ctx().scene;
     DeviceState& d = ctx().dev;
     cudaStream_t s = d.stream;

@@ -187,3 +187,13 @@ def test_clock_sampler_names_the_gpu_by_bus_id():
     process runs on by its PCI bus id, in nvidia-smi's 8-digit-domain form."""
     import bench
     assert bench.nvsmi_id(FakeLib()) == "00000000:1B:00.0"
+
+
+def test_kd_roofline_bytes():
+    """The KD build's algorithmic bytes: 12 P + 32 P ceil(log2 P) + 8 x 2^(floor(log2 P) + 1)."""
+    import bench
+    r = bench.kd_roofline(1 << 20, 2.0, 6000.0, "measured")
+    want = 12 * 2 ** 20 + 32 * 2 ** 20 * 20 + 8 * 2 ** 21
+    assert r["algorithmic_bytes"] == want
+    assert abs(r["achieved"] - want / 2e-3 / 1e9) < 1e-6 and abs(r["frac"] - r["achieved"] / 6000.0) < 1e-12
+    assert bench.kd_roofline(1, 1.0, 6000.0, "measured") is None

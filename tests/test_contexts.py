@@ -135,3 +135,28 @@ def test_unbound_threads_share_the_default_context():
 def _ctypes_float_p():
     import ctypes as C
     return C.POINTER(C.c_float)
+
+
+def test_parity_hooks_validate_shapes_before_device_work():
+    """The traversal and Metropolis parity hooks refuse an unknown shape, and the
+    Metropolis hook a configuration without a Metropolis sampler, before any device work."""
+    import ctypes as C
+    from realcausticsengine_gb300 import abi
+    lib = _native.lib()
+    r = Renderer(scenes.test_scene())
+    o = np.zeros((1, 3), np.float32)
+    out = np.zeros((1, 16), np.float32)
+    assert lib.rc_trace_rays_shape(1, o.ctypes.data, o.ctypes.data, C.c_float(0.001), out.ctypes.data, 3) != 0
+    assert b"shape" in lib.rc_last_error()
+    n = C.c_longlong()
+    assert lib.rc_mlt_photons(0, 0, None, 0, C.byref(n), None) != 0       # uniform sampler
+    assert b"Metropolis" in lib.rc_last_error()
+    cfg = abi.RcConfig()
+    lib.rc_default_config(C.byref(cfg))
+    cfg.sampler, cfg.write_exr = abi.SAMPLER_PSSMLT, 0
+    assert lib.rc_set_config(C.byref(cfg)) == 0
+    assert lib.rc_mlt_photons(2, 0, None, 0, C.byref(n), None) != 0       # variants 0 and 1 only
+    assert b"shape" in lib.rc_last_error()
+    lib.rc_default_config(C.byref(cfg))
+    assert lib.rc_set_config(C.byref(cfg)) == 0
+    r.release()
